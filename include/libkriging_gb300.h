@@ -1,0 +1,120 @@
+/*
+ * libkriging_gb300.h -- C ABI of the GB300-native libKriging likelihood path.
+ *
+ * The entry points mirror libKriging's own C ABI (bindings/Julia/jlibkriging/csrc/libkriging_c.h, implementation
+ * bindings/Julia/jlibkriging/csrc/libkriging_c.cpp) one for one, with the prefix lkg_ instead of lk_: same argument
+ * order, sizes and meaning (column-major double arrays, int status 0 / -1, thread-local last error), so a binding
+ * written against lk_* switches by renaming the symbols.  Entry points without a counterpart there say so.
+ *
+ * Everything computes on the GPU (sm_103a); there is no CPU fallback.  A call made without a usable CUDA device
+ * returns -1 (or NULL / NaN) with the CUDA error in lkg_get_last_error().
+ */
+#ifndef LIBKRIGING_GB300_H
+#define LIBKRIGING_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* libkriging_c.h:9 lk_get_last_error -- message of the last failed call on this thread. */
+const char* lkg_get_last_error(void);
+
+/* ---------------------------------------------------------------- Kriging ---------------------------------------- */
+/* noise_model: "none" (or NULL) or "nugget".  "heterogeneous" is rejected (not part of this path). */
+
+/* libkriging_c.h:18 lk_kriging_new */
+void* lkg_kriging_new(const char* kernel, const char* noise_model);
+/* libkriging_c.h:19-41 lk_kriging_new_fit (theta: one starting point of length theta_n, as there) */
+void* lkg_kriging_new_fit(const double* y, int n, const double* noise, int noise_n, const double* X, int nX, int d,
+                          const char* kernel, const char* noise_model, const char* regmodel, int normalize,
+                          const char* optim, const char* objective, const double* sigma2, int is_sigma2_estim,
+                          const double* theta, int theta_n, int is_theta_estim, const double* beta, int beta_n,
+                          int is_beta_estim, const double* nugget, int is_nugget_estim);
+/* libkriging_c.h:42 lk_kriging_delete */
+void lkg_kriging_delete(void* ptr);
+/* libkriging_c.h:45-56 lk_kriging_fit */
+int lkg_kriging_fit(void* ptr, const double* y, int n, const double* noise, int noise_n, const double* X, int nX,
+                    int d, const char* regmodel, int normalize, const char* optim, const char* objective);
+/* No counterpart in the reference C ABI (its C++ Kriging::fit takes Kriging::Parameters, Kriging.hpp:113-119):
+ * fit with parameters; theta is theta_rows x d column-major (one starting point per row). */
+int lkg_kriging_fit_params(void* ptr, const double* y, int n, const double* X, int nX, int d, const char* regmodel,
+                           int normalize, const char* optim, const char* objective, const double* sigma2,
+                           int is_sigma2_estim, const double* theta, int theta_rows, int is_theta_estim,
+                           const double* beta, int beta_n, int is_beta_estim, const double* nugget,
+                           int is_nugget_estim);
+/* libkriging_c.h:58-69 lk_kriging_predict (return_deriv is rejected) */
+int lkg_kriging_predict(void* ptr, const double* X_n, int m, int d, int return_stdev, int return_cov,
+                        int return_deriv, double* mean_out, double* stdev_out, double* cov_out, double* mean_deriv_out,
+                        double* stdev_deriv_out);
+/* libkriging_c.h:102 lk_kriging_summary */
+const char* lkg_kriging_summary(void* ptr);
+/* libkriging_c.h:104-111 lk_kriging_log_likelihood_fun (return_hess is rejected; hess_out untouched) */
+int lkg_kriging_log_likelihood_fun(void* ptr, const double* theta, int theta_n, int return_grad, int return_hess,
+                                   double* ll_out, double* grad_out, double* hess_out);
+/* libkriging_c.h:126 lk_kriging_log_likelihood */
+double lkg_kriging_log_likelihood(void* ptr);
+/* No counterpart in the reference: k candidates (k x theta_n column-major) evaluated in one batched GPU pass;
+ * ll_out[k], grad_out k x theta_n column-major. */
+int lkg_kriging_log_likelihood_fun_batch(void* ptr, const double* thetas, int k, int theta_n, int return_grad,
+                                         double* ll_out, double* grad_out);
+/* No counterpart in the reference: logLikelihoodFun(..., bench=true) writing the per-stage timings (ms, CUDA events)
+ * as "key<TAB>value<LF>" lines; keys are the reference's Bench keys (src/lib/KrigingImpl.cpp:96-124). */
+int lkg_kriging_log_likelihood_fun_bench(void* ptr, const double* theta, int theta_n, int return_grad, double* ll_out,
+                                         double* grad_out, char* bench_out, int bench_cap);
+
+/* getters, libkriging_c.h:141-166 */
+const char* lkg_kriging_kernel(void* ptr);
+const char* lkg_kriging_optim(void* ptr);
+const char* lkg_kriging_objective(void* ptr);
+int lkg_kriging_is_normalize(void* ptr);
+const char* lkg_kriging_regmodel(void* ptr);
+int lkg_kriging_get_X(void* ptr, double* out, int* n, int* d);
+int lkg_kriging_get_centerX(void* ptr, double* out, int* d);
+int lkg_kriging_get_scaleX(void* ptr, double* out, int* d);
+int lkg_kriging_get_y(void* ptr, double* out, int* n);
+double lkg_kriging_get_centerY(void* ptr);
+double lkg_kriging_get_scaleY(void* ptr);
+int lkg_kriging_get_T(void* ptr, double* out, int* n, int* d);
+int lkg_kriging_get_M(void* ptr, double* out, int* n, int* d);
+int lkg_kriging_get_z(void* ptr, double* out, int* n);
+int lkg_kriging_get_beta(void* ptr, double* out, int* n);
+int lkg_kriging_is_beta_estim(void* ptr);
+int lkg_kriging_get_theta(void* ptr, double* out, int* n);
+int lkg_kriging_is_theta_estim(void* ptr);
+double lkg_kriging_get_sigma2(void* ptr);
+int lkg_kriging_is_sigma2_estim(void* ptr);
+const char* lkg_kriging_noise_model(void* ptr);
+double lkg_kriging_get_nugget(void* ptr);
+int lkg_kriging_is_nugget_estim(void* ptr);
+
+/* ------------------------------------------------------- numerical / optimiser settings --------------------------- */
+/* LinearAlgebra::set_num_nugget / get_num_nugget (src/lib/LinearAlgebra.cpp:35-41) */
+void lkg_set_num_nugget(double nugget);
+double lkg_get_num_nugget(void);
+/* LinearAlgebra::check_chol_rcond (src/lib/LinearAlgebra.cpp:53-55) */
+void lkg_check_chol_rcond(int check);
+/* LinearAlgebra::set_chol_warning (src/lib/LinearAlgebra.cpp:47-49) */
+void lkg_set_chol_warning(int warn);
+/* Optim setters (src/lib/Optim.cpp:44-139) */
+void lkg_optim_use_reparametrize(int r);
+void lkg_optim_set_theta_lower_factor(double f);
+void lkg_optim_set_theta_upper_factor(double f);
+void lkg_optim_use_variogram_bounds_heuristic(int v);
+void lkg_optim_set_log_level(int l);
+void lkg_optim_set_max_iteration(int m);
+void lkg_optim_set_gradient_tolerance(double t);
+void lkg_optim_set_objective_rel_tolerance(double t);
+void lkg_optim_set_max_restart(int m);
+
+/* ------------------------------------------------------------- diagnostics ---------------------------------------- */
+/* No counterpart in the reference: name of CUDA device 0, or NULL without a device. */
+const char* lkg_device_name(void);
+/* No counterpart in the reference: measured FP64 FMA throughput (TFLOP/s) of this GPU, the roofline denominator of
+ * the FP64 kernels (the DFMA pipe; FP64 mma.sync is slower on GB300). */
+int lkg_probe_fp64_peak(double* tflops_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LIBKRIGING_GB300_H */

@@ -1,0 +1,12 @@
+"""libkriging_gb300 -- GB300-native (sm_103a) libKriging likelihood path.
+
+Drop-in for pylibkriging's ``Kriging`` on the likelihood path: covariance build, blocked FP64 Cholesky and
+triangular solves, concentrated log-likelihood with its one-pass adjoint theta-gradient, the L-BFGS-B fit
+(multistart evaluations batched into single GPU launches) and predict.  All compute goes through the C ABI of
+``include/libkriging_gb300.h``.
+"""
+from ._lib import LibKrigingError, header_symbols, load
+from .kriging import Kriging, Optim, check_chol_rcond, get_num_nugget, set_num_nugget
+
+__all__ = ["Kriging", "Optim", "set_num_nugget", "get_num_nugget", "check_chol_rcond", "LibKrigingError", "load",
+           "header_symbols"]

@@ -1,0 +1,403 @@
+// capi.cpp -- extern "C" boundary (include/libkriging_gb300.h).
+//
+// Same conventions as libKriging's C ABI (bindings/Julia/jlibkriging/csrc/libkriging_c.cpp:16-41): opaque handles,
+// column-major double arrays, 0 / -1 status, thread_local last error; NULL / NaN returns for pointer / double
+// functions on error.
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <sstream>
+#include <string>
+
+#include "../../include/libkriging_gb300.h"
+#include "config.hpp"
+#include "kriging.hpp"
+
+using lkg::Kriging;
+using lkg::Mat;
+
+static thread_local std::string g_last_error;
+
+#define CATCH_RETURN                \
+  catch (const std::exception& e) { \
+    g_last_error = e.what();        \
+    return -1;                      \
+  }
+#define CATCH_RETURN_NULL           \
+  catch (const std::exception& e) { \
+    g_last_error = e.what();        \
+    return nullptr;                 \
+  }
+#define CATCH_RETURN_NAN                             \
+  catch (const std::exception& e) {                  \
+    g_last_error = e.what();                         \
+    return std::numeric_limits<double>::quiet_NaN(); \
+  }
+
+namespace {
+
+Kriging::NoiseModel parse_noise_model(const char* s) {
+  if (!s || std::string(s) == "none") return Kriging::NoiseModel::None;
+  if (std::string(s) == "nugget") return Kriging::NoiseModel::Nugget;
+  if (std::string(s) == "heterogeneous")
+    throw std::invalid_argument("noise_model 'heterogeneous' is not supported by the GPU build");
+  throw std::runtime_error(std::string("Unknown noise_model: ") + s);
+}
+
+Kriging* K(void* p) {
+  if (!p) throw std::invalid_argument("null Kriging handle");
+  return static_cast<Kriging*>(p);
+}
+
+Mat mat_of(const double* p, int rows, int cols) {
+  Mat m;
+  m.rows = rows;
+  m.cols = cols;
+  m.v.assign(p, p + (size_t)rows * cols);
+  return m;
+}
+
+lkg::Parameters make_params(const double* sigma2, int is_sigma2_estim, const double* theta, int theta_rows, int d,
+                            int is_theta_estim, const double* beta, int beta_n, int is_beta_estim,
+                            const double* nugget, int is_nugget_estim) {
+  lkg::Parameters P;
+  if (sigma2) P.sigma2 = *sigma2;
+  P.is_sigma2_estim = is_sigma2_estim != 0;
+  if (theta && theta_rows > 0) P.theta = mat_of(theta, theta_rows, d);
+  P.is_theta_estim = is_theta_estim != 0;
+  if (beta && beta_n > 0) P.beta = std::vector<double>(beta, beta + beta_n);
+  P.is_beta_estim = is_beta_estim != 0;
+  if (nugget) P.nugget = *nugget;
+  P.is_nugget_estim = is_nugget_estim != 0;
+  return P;
+}
+
+int copy_vec(const std::vector<double>& v, double* out, int* n) {
+  if (n) *n = (int)v.size();
+  if (out) std::memcpy(out, v.data(), sizeof(double) * v.size());
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* lkg_get_last_error(void) { return g_last_error.c_str(); }
+
+void* lkg_kriging_new(const char* kernel, const char* noise_model) {
+  try {
+    return new Kriging(kernel ? kernel : "matern3_2", parse_noise_model(noise_model));
+  }
+  CATCH_RETURN_NULL
+}
+
+void* lkg_kriging_new_fit(const double* y, int n, const double* noise, int noise_n, const double* X, int nX, int d,
+                          const char* kernel, const char* noise_model, const char* regmodel, int normalize,
+                          const char* optim, const char* objective, const double* sigma2, int is_sigma2_estim,
+                          const double* theta, int theta_n, int is_theta_estim, const double* beta, int beta_n,
+                          int is_beta_estim, const double* nugget, int is_nugget_estim) {
+  Kriging* kr = nullptr;
+  try {
+    if (noise && noise_n > 0) throw std::invalid_argument("per-observation noise is not supported by the GPU build");
+    if (n != nX) throw std::runtime_error("Dimension of new data should be the same");
+    kr = new Kriging(kernel ? kernel : "matern3_2", parse_noise_model(noise_model));
+    // theta: one starting point (1 x theta_n), as in the reference C ABI
+    lkg::Parameters P = make_params(sigma2, is_sigma2_estim, theta, (theta && theta_n > 0) ? 1 : 0, theta_n,
+                                    is_theta_estim, beta, beta_n, is_beta_estim, nugget, is_nugget_estim);
+    std::vector<double> yv(y, y + n);
+    kr->fit(yv, mat_of(X, nX, d), lkg::regmodel_from_string(regmodel ? regmodel : "constant"), normalize != 0,
+            optim ? optim : "BFGS", objective ? objective : "LL", P);
+    return kr;
+  } catch (const std::exception& e) {
+    g_last_error = e.what();
+    delete kr;
+    return nullptr;
+  }
+}
+
+void lkg_kriging_delete(void* ptr) { delete static_cast<Kriging*>(ptr); }
+
+int lkg_kriging_fit(void* ptr, const double* y, int n, const double* noise, int noise_n, const double* X, int nX,
+                    int d, const char* regmodel, int normalize, const char* optim, const char* objective) {
+  try {
+    if (noise && noise_n > 0) throw std::invalid_argument("per-observation noise is not supported by the GPU build");
+    if (n != nX) throw std::runtime_error("Dimension of new data should be the same");
+    std::vector<double> yv(y, y + n);
+    K(ptr)->fit(yv, mat_of(X, nX, d), lkg::regmodel_from_string(regmodel ? regmodel : "constant"), normalize != 0,
+                optim ? optim : "BFGS", objective ? objective : "LL", {});
+    return 0;
+  }
+  CATCH_RETURN
+}
+
+int lkg_kriging_fit_params(void* ptr, const double* y, int n, const double* X, int nX, int d, const char* regmodel,
+                           int normalize, const char* optim, const char* objective, const double* sigma2,
+                           int is_sigma2_estim, const double* theta, int theta_rows, int is_theta_estim,
+                           const double* beta, int beta_n, int is_beta_estim, const double* nugget,
+                           int is_nugget_estim) {
+  try {
+    if (n != nX) throw std::runtime_error("Dimension of new data should be the same");
+    lkg::Parameters P = make_params(sigma2, is_sigma2_estim, theta, theta_rows, d, is_theta_estim, beta, beta_n,
+                                    is_beta_estim, nugget, is_nugget_estim);
+    std::vector<double> yv(y, y + n);
+    K(ptr)->fit(yv, mat_of(X, nX, d), lkg::regmodel_from_string(regmodel ? regmodel : "constant"), normalize != 0,
+                optim ? optim : "BFGS", objective ? objective : "LL", P);
+    return 0;
+  }
+  CATCH_RETURN
+}
+
+int lkg_kriging_predict(void* ptr, const double* X_n, int m, int d, int return_stdev, int return_cov,
+                        int return_deriv, double* mean_out, double* stdev_out, double* cov_out, double* mean_deriv_out,
+                        double* stdev_deriv_out) {
+  try {
+    (void)mean_deriv_out;
+    (void)stdev_deriv_out;
+    auto [mean, sd, cov, md, sdd] = K(ptr)->predict(mat_of(X_n, m, d), return_stdev != 0, return_cov != 0,
+                                                    return_deriv != 0);
+    if (mean_out) std::memcpy(mean_out, mean.data(), sizeof(double) * mean.size());
+    if (stdev_out && return_stdev) std::memcpy(stdev_out, sd.data(), sizeof(double) * sd.size());
+    if (cov_out && return_cov) std::memcpy(cov_out, cov.v.data(), sizeof(double) * cov.v.size());
+    return 0;
+  }
+  CATCH_RETURN
+}
+
+const char* lkg_kriging_summary(void* ptr) {
+  try {
+    static thread_local std::string buf;
+    buf = K(ptr)->summary();
+    return buf.c_str();
+  }
+  CATCH_RETURN_NULL
+}
+
+int lkg_kriging_log_likelihood_fun(void* ptr, const double* theta, int theta_n, int return_grad, int return_hess,
+                                   double* ll_out, double* grad_out, double* hess_out) {
+  try {
+    (void)hess_out;
+    if (return_hess) throw std::invalid_argument("logLikelihoodFun: return_hess is not supported by the GPU build");
+    std::vector<double> g(theta, theta + theta_n);
+    auto [ll, grad] = K(ptr)->logLikelihoodFun(g, return_grad != 0, false);
+    if (ll_out) *ll_out = ll;
+    if (grad_out && return_grad) std::memcpy(grad_out, grad.data(), sizeof(double) * grad.size());
+    return 0;
+  }
+  CATCH_RETURN
+}
+
+int lkg_kriging_log_likelihood_fun_bench(void* ptr, const double* theta, int theta_n, int return_grad, double* ll_out,
+                                         double* grad_out, char* bench_out, int bench_cap) {
+  try {
+    std::vector<double> g(theta, theta + theta_n);
+    auto [ll, grad] = K(ptr)->logLikelihoodFun(g, return_grad != 0, true);
+    if (ll_out) *ll_out = ll;
+    if (grad_out && return_grad) std::memcpy(grad_out, grad.data(), sizeof(double) * grad.size());
+    if (bench_out && bench_cap > 0) {
+      std::ostringstream o;
+      o.precision(17);
+      for (auto& kv : K(ptr)->last_bench()) o << kv.first << "\t" << kv.second << "\n";
+      const std::string s = o.str();
+      std::strncpy(bench_out, s.c_str(), bench_cap - 1);
+      bench_out[bench_cap - 1] = 0;
+    }
+    return 0;
+  }
+  CATCH_RETURN
+}
+
+int lkg_kriging_log_likelihood_fun_batch(void* ptr, const double* thetas, int k, int theta_n, int return_grad,
+                                         double* ll_out, double* grad_out) {
+  try {
+    std::vector<double> ll, grad;
+    K(ptr)->logLikelihoodFunBatch(mat_of(thetas, k, theta_n), return_grad != 0, ll, grad);
+    if (ll_out) std::memcpy(ll_out, ll.data(), sizeof(double) * k);
+    if (grad_out && return_grad)  // grad is row-major per candidate -> column-major k x theta_n
+      for (int b = 0; b < k; ++b)
+        for (int j = 0; j < theta_n; ++j) grad_out[b + (size_t)j * k] = grad[(size_t)b * theta_n + j];
+    return 0;
+  }
+  CATCH_RETURN
+}
+
+double lkg_kriging_log_likelihood(void* ptr) {
+  try {
+    return K(ptr)->logLikelihood();
+  }
+  CATCH_RETURN_NAN
+}
+
+const char* lkg_kriging_kernel(void* ptr) {
+  try {
+    return K(ptr)->kernel().c_str();
+  }
+  CATCH_RETURN_NULL
+}
+const char* lkg_kriging_optim(void* ptr) {
+  try {
+    return K(ptr)->optim().c_str();
+  }
+  CATCH_RETURN_NULL
+}
+const char* lkg_kriging_objective(void* ptr) {
+  try {
+    return K(ptr)->objective().c_str();
+  }
+  CATCH_RETURN_NULL
+}
+int lkg_kriging_is_normalize(void* ptr) {
+  try {
+    return K(ptr)->is_normalize() ? 1 : 0;
+  }
+  CATCH_RETURN
+}
+const char* lkg_kriging_regmodel(void* ptr) {
+  try {
+    return lkg::regmodel_to_string(K(ptr)->regmodel());
+  }
+  CATCH_RETURN_NULL
+}
+int lkg_kriging_get_X(void* ptr, double* out, int* n, int* d) {
+  try {
+    Kriging* k = K(ptr);
+    if (n) *n = k->n();
+    if (d) *d = k->d();
+    if (out) {  // original scale (m_X * scaleX + centerX), as the reference getter returns m_X un-normalised
+      for (int j = 0; j < k->d(); ++j)
+        for (int i = 0; i < k->n(); ++i)
+          out[i + (size_t)j * k->n()] = k->X()[i + (size_t)j * k->n()] * k->scaleX()[j] + k->centerX()[j];
+    }
+    return 0;
+  }
+  CATCH_RETURN
+}
+int lkg_kriging_get_centerX(void* ptr, double* out, int* d) {
+  try {
+    return copy_vec(K(ptr)->centerX(), out, d);
+  }
+  CATCH_RETURN
+}
+int lkg_kriging_get_scaleX(void* ptr, double* out, int* d) {
+  try {
+    return copy_vec(K(ptr)->scaleX(), out, d);
+  }
+  CATCH_RETURN
+}
+int lkg_kriging_get_y(void* ptr, double* out, int* n) {
+  try {
+    Kriging* k = K(ptr);
+    if (n) *n = k->n();
+    if (out)
+      for (int i = 0; i < k->n(); ++i) out[i] = k->y()[i] * k->scaleY() + k->centerY();
+    return 0;
+  }
+  CATCH_RETURN
+}
+double lkg_kriging_get_centerY(void* ptr) {
+  try {
+    return K(ptr)->centerY();
+  }
+  CATCH_RETURN_NAN
+}
+double lkg_kriging_get_scaleY(void* ptr) {
+  try {
+    return K(ptr)->scaleY();
+  }
+  CATCH_RETURN_NAN
+}
+int lkg_kriging_get_T(void* ptr, double* out, int* n, int* d) {
+  try {
+    Mat T = K(ptr)->T();
+    if (n) *n = T.rows;
+    if (d) *d = T.cols;
+    if (out) std::memcpy(out, T.v.data(), sizeof(double) * T.v.size());
+    return 0;
+  }
+  CATCH_RETURN
+}
+int lkg_kriging_get_M(void* ptr, double* out, int* n, int* d) {
+  try {
+    Mat M = K(ptr)->M();
+    if (n) *n = M.rows;
+    if (d) *d = M.cols;
+    if (out) std::memcpy(out, M.v.data(), sizeof(double) * M.v.size());
+    return 0;
+  }
+  CATCH_RETURN
+}
+int lkg_kriging_get_z(void* ptr, double* out, int* n) {
+  try {
+    return copy_vec(K(ptr)->z(), out, n);
+  }
+  CATCH_RETURN
+}
+int lkg_kriging_get_beta(void* ptr, double* out, int* n) {
+  try {
+    return copy_vec(K(ptr)->beta(), out, n);
+  }
+  CATCH_RETURN
+}
+int lkg_kriging_is_beta_estim(void* ptr) {
+  try {
+    return K(ptr)->is_beta_estim() ? 1 : 0;
+  }
+  CATCH_RETURN
+}
+int lkg_kriging_get_theta(void* ptr, double* out, int* n) {
+  try {
+    return copy_vec(K(ptr)->theta(), out, n);
+  }
+  CATCH_RETURN
+}
+int lkg_kriging_is_theta_estim(void* ptr) {
+  try {
+    return K(ptr)->is_theta_estim() ? 1 : 0;
+  }
+  CATCH_RETURN
+}
+double lkg_kriging_get_sigma2(void* ptr) {
+  try {
+    return K(ptr)->sigma2();
+  }
+  CATCH_RETURN_NAN
+}
+int lkg_kriging_is_sigma2_estim(void* ptr) {
+  try {
+    return K(ptr)->is_sigma2_estim() ? 1 : 0;
+  }
+  CATCH_RETURN
+}
+const char* lkg_kriging_noise_model(void* ptr) {
+  try {
+    return K(ptr)->noise_model() == Kriging::NoiseModel::Nugget ? "nugget" : "none";
+  }
+  CATCH_RETURN_NULL
+}
+double lkg_kriging_get_nugget(void* ptr) {
+  try {
+    return K(ptr)->nugget();
+  }
+  CATCH_RETURN_NAN
+}
+int lkg_kriging_is_nugget_estim(void* ptr) {
+  try {
+    return K(ptr)->is_nugget_estim() ? 1 : 0;
+  }
+  CATCH_RETURN
+}
+
+void lkg_set_num_nugget(double nugget) { lkg::config().num_nugget = nugget; }
+double lkg_get_num_nugget(void) { return lkg::config().num_nugget; }
+void lkg_check_chol_rcond(int check) { lkg::config().chol_rcond_check = check != 0; }
+void lkg_set_chol_warning(int warn) { lkg::config().warn_chol = warn != 0; }
+void lkg_optim_use_reparametrize(int r) { lkg::config().reparametrize = r != 0; }
+void lkg_optim_set_theta_lower_factor(double f) { lkg::config().theta_lower_factor = f; }
+void lkg_optim_set_theta_upper_factor(double f) { lkg::config().theta_upper_factor = f; }
+void lkg_optim_use_variogram_bounds_heuristic(int v) { lkg::config().variogram_bounds_heuristic = v != 0; }
+void lkg_optim_set_log_level(int l) { lkg::config().log_level = l; }
+void lkg_optim_set_max_iteration(int m) { lkg::config().max_iteration = m; }
+void lkg_optim_set_gradient_tolerance(double t) { lkg::config().gradient_tolerance = t; }
+void lkg_optim_set_objective_rel_tolerance(double t) { lkg::config().objective_rel_tolerance = t; }
+void lkg_optim_set_max_restart(int m) { lkg::config().max_restart = m; }
+
+}  // extern "C"

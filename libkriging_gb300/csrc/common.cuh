@@ -1,0 +1,110 @@
+// common.cuh -- shared definitions for the GB300 likelihood kernels (sm_103a).
+//
+// Covariance functions restate libKriging src/lib/Covariance.cpp (same formulas, same operation order):
+//   gauss      Cov :24-36   DlnCovDtheta :38-50
+//   exp        Cov :65-75   DlnCovDtheta :77-88
+//   matern3_2  Cov :104-116 DlnCovDtheta :118-130
+//   matern5_2  Cov :149-161 DlnCovDtheta :163-179
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+
+namespace lkg {
+
+enum Kernel : int { KGAUSS = 0, KEXP = 1, KMATERN32 = 2, KMATERN52 = 3 };
+
+constexpr int MAX_D = 32;  // largest input dimension the fused kernels accept
+
+struct CudaError : std::runtime_error {
+  explicit CudaError(const std::string& s) : std::runtime_error(s) {}
+};
+
+inline void check_cuda(cudaError_t e, const char* what, const char* file, int line) {
+  if (e != cudaSuccess)
+    throw CudaError(std::string("CUDA error in ") + what + " (" + file + ":" + std::to_string(line) +
+                    "): " + cudaGetErrorString(e));
+}
+#define LKG_CUDA(x) ::lkg::check_cuda((x), #x, __FILE__, __LINE__)
+#define LKG_LAUNCH(what) ::lkg::check_cuda(cudaGetLastError(), what, __FILE__, __LINE__)
+
+// ---------------------------------------------------------------------------------------------------------------
+// device covariance functions.  dx is X_j - X_i (sign irrelevant for Cov and DlnCovDtheta), inv_theta = 1/theta is
+// NOT used for the value so that the rounding matches the reference's dx/theta division.
+// ---------------------------------------------------------------------------------------------------------------
+template <int K>
+__device__ __forceinline__ double cov_term(double dx, double th) {
+  if constexpr (K == KGAUSS) {
+    double v = dx / th;
+    return v * v;
+  } else if constexpr (K == KEXP) {
+    return fabs(dx / th);
+  } else if constexpr (K == KMATERN32) {
+    double t = sqrt(3.0) * fabs(dx / th);
+    return t - log1p(t);
+  } else {
+    double t = sqrt(5.0) * fabs(dx / th);
+    return t - log1p(t + (t * t) / 3.0);
+  }
+}
+
+template <int K>
+__device__ __forceinline__ double cov_from_sum(double s) {
+  if constexpr (K == KGAUSS)
+    return exp(-0.5 * s);
+  else
+    return exp(-s);
+}
+
+template <int K>
+__device__ __forceinline__ double dlncov_term(double dx, double th) {
+  if constexpr (K == KGAUSS) {
+    return (dx * dx) / (th * th * th);
+  } else if constexpr (K == KEXP) {
+    return fabs(dx) / (th * th);
+  } else if constexpr (K == KMATERN32) {
+    double t = sqrt(3.0) * fabs(dx / th);
+    return (t * t) / (1.0 + t) / th;
+  } else {
+    double t = sqrt(5.0) * fabs(dx / th);
+    double a = 1.0 + t;
+    double b = (t * t) / 3.0;
+    return (a * b) / (a + b) / th;
+  }
+}
+
+// dispatch a runtime kernel id to a template functor call
+template <typename F>
+inline void dispatch_kernel(int k, F&& f) {
+  switch (k) {
+    case KGAUSS: f.template operator()<KGAUSS>(); break;
+    case KEXP: f.template operator()<KEXP>(); break;
+    case KMATERN32: f.template operator()<KMATERN32>(); break;
+    case KMATERN52: f.template operator()<KMATERN52>(); break;
+    default: throw std::invalid_argument("Unsupported covariance kernel id " + std::to_string(k));
+  }
+}
+
+inline int kernel_from_name(const std::string& s) {
+  if (s == "gauss") return KGAUSS;
+  if (s == "exp") return KEXP;
+  if (s == "matern3_2") return KMATERN32;
+  if (s == "matern5_2") return KMATERN52;
+  throw std::invalid_argument("Unsupported covariance kernel: " + s);
+}
+
+inline const char* kernel_name(int k) {
+  switch (k) {
+    case KGAUSS: return "gauss";
+    case KEXP: return "exp";
+    case KMATERN32: return "matern3_2";
+    case KMATERN52: return "matern5_2";
+  }
+  return "?";
+}
+
+inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+}  // namespace lkg

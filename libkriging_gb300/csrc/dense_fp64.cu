@@ -1,0 +1,407 @@
+// dense_fp64.cu -- FP64 blocked Cholesky / triangular inverse / R^-1 / small-RHS solves (sm_103a).
+//
+// These replace the LAPACK calls of libKriging's populate_Model (src/lib/KrigingImpl.cpp:73-125):
+//   arma::chol (dpotrf)                 -> potrf_blocked   (right-looking, NB = 64 blocks)
+//   inv_sympd = solve(L', solve(L, I))  -> trtri_blocked + wtw_lower  (2n^3/3 flops instead of 2n^3)
+//   solve(trimatl(L), B), solve(trimatu(L'), B) -> trsm_lower_left[_t] (blocked, uses the diagonal-block inverses)
+#include "dense_fp64.cuh"
+
+namespace lkg {
+
+namespace {
+
+constexpr int TB = 64;   // tile edge
+constexpr int KC = 16;   // k-chunk staged through shared memory
+constexpr int NT = 256;  // threads per tile CTA (16 x 16, 4 x 4 accumulators each)
+
+struct TileSmem {
+  double a[KC][TB];
+  double b[KC][TB];
+};
+
+// acc += A(m0.., k) * B(k, n0..) over k in [0, K); A/B element (r,c) at p[r*sr + c*sc].
+__device__ __forceinline__ void tile_mma_fp64(int M, int N, int K, const double* __restrict__ Ap, int64_t asr,
+                                              int64_t asc, const double* __restrict__ Bp, int64_t bsr, int64_t bsc,
+                                              int m0, int n0, TileSmem& sm, double (&acc)[4][4]) {
+  const int t = threadIdx.x;
+  const int tm = t & 15, tn = t >> 4;
+  const bool a_mfast = (asr == 1);
+  const bool b_kfast = (bsr == 1);
+  for (int k0 = 0; k0 < K; k0 += KC) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int idx = t + NT * r;
+      int m, k;
+      if (a_mfast) {
+        m = idx & 63;
+        k = idx >> 6;
+      } else {
+        k = idx & 15;
+        m = idx >> 4;
+      }
+      const int gm = m0 + m, gk = k0 + k;
+      sm.a[k][m] = (gm < M && gk < K) ? Ap[(int64_t)gm * asr + (int64_t)gk * asc] : 0.0;
+      int n;
+      if (b_kfast) {
+        k = idx & 15;
+        n = idx >> 4;
+      } else {
+        n = idx & 63;
+        k = idx >> 6;
+      }
+      const int gn = n0 + n;
+      const int gk2 = k0 + k;
+      sm.b[k][n] = (gn < N && gk2 < K) ? Bp[(int64_t)gk2 * bsr + (int64_t)gn * bsc] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < KC; ++k) {
+      double av[4], bv[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) av[i] = sm.a[k][tm + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) bv[j] = sm.b[k][tn + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fma(av[i], bv[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+}
+
+__device__ __forceinline__ void tile_store(int M, int N, double alpha, double beta, double* C, int64_t ldc, int m0,
+                                           int n0, bool lower_only, const double (&acc)[4][4]) {
+  const int t = threadIdx.x;
+  const int tm = t & 15, tn = t >> 4;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int r = m0 + tm + 16 * i, c = n0 + tn + 16 * j;
+      if (r < M && c < N && (!lower_only || r >= c)) {
+        double* cp = C + r + (int64_t)c * ldc;
+        *cp = (beta == 0.0) ? alpha * acc[i][j] : fma(alpha, acc[i][j], beta * *cp);
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(NT) k_gemm_tiles(int M, int N, int K, double alpha, MatView A, MatView B,
+                                                   double beta, double* C, int64_t ldc, int64_t c_batch,
+                                                   bool lower_only) {
+  const int m0 = blockIdx.x * TB, n0 = blockIdx.y * TB;
+  if (lower_only && m0 + TB - 1 < n0) return;  // tile strictly above the diagonal
+  const int64_t b = blockIdx.z;
+  __shared__ TileSmem sm;
+  double acc[4][4] = {};
+  tile_mma_fp64(M, N, K, A.p + b * A.batch, A.sr, A.sc, B.p + b * B.batch, B.sr, B.sc, m0, n0, sm, acc);
+  tile_store(M, N, alpha, beta, C + b * c_batch, ldc, m0, n0, lower_only, acc);
+}
+
+// ---- diagonal block: Cholesky + inverse in shared memory (one CTA per batch entry) ----
+constexpr int DPAD = NB + 1;
+
+__global__ void __launch_bounds__(NT) k_potrf_diag(double* A, int64_t lda, int64_t mstride, int k0, int nb,
+                                                   double* Dinv, int64_t dinv_bstride, int blk, int* info) {
+  const int64_t b = blockIdx.z;
+  if (info[b] != 0) return;  // an earlier block of this matrix already failed
+  extern __shared__ double dsm[];
+  double* s = dsm;                 // [NB][DPAD]  s[i*DPAD + j] = L(i, j)
+  double* w = dsm + NB * DPAD;     // [NB][DPAD]  w[i*DPAD + j] = L^-1(i, j)
+  __shared__ int failed;
+  double* Ab = A + b * mstride + k0 + (int64_t)k0 * lda;
+  const int t = threadIdx.x;
+  if (t == 0) failed = 0;
+  for (int idx = t; idx < NB * NB; idx += NT) {
+    const int i = idx & 63, j = idx >> 6;
+    s[i * DPAD + j] = (i < nb && j < nb && i >= j) ? Ab[i + (int64_t)j * lda] : 0.0;
+    w[i * DPAD + j] = 0.0;
+  }
+  __syncthreads();
+  for (int j = 0; j < nb; ++j) {
+    if (t == 0) {
+      const double dj = s[j * DPAD + j];
+      if (!(dj > 0.0)) {  // non-positive or NaN pivot
+        failed = 1;
+        info[b] = k0 + j + 1;
+      } else {
+        s[j * DPAD + j] = sqrt(dj);
+      }
+    }
+    __syncthreads();
+    if (failed) return;
+    const double ljj = s[j * DPAD + j];
+    for (int i = j + 1 + t; i < nb; i += NT) s[i * DPAD + j] /= ljj;
+    __syncthreads();
+    // trailing update of columns c in (j, nb): 64 columns x 4 row groups
+    {
+      const int c = j + 1 + (t & 63);
+      if (c < nb) {
+        const double lcj = s[c * DPAD + j];
+        for (int i = c + (t >> 6); i < nb; i += 4) s[i * DPAD + c] -= s[i * DPAD + j] * lcj;
+      }
+    }
+    __syncthreads();
+  }
+  // inverse by row wavefront: w(i, c) = (delta_ic - sum_{k=c}^{i-1} L(i,k) w(k,c)) / L(i,i), 4 lanes per column
+  {
+    const int c = t >> 2, q = t & 3;
+    for (int i = 0; i < nb; ++i) {
+      double sum = 0.0;
+      if (c <= i && c < nb)
+        for (int k = c + q; k < i; k += 4) sum = fma(s[i * DPAD + k], w[k * DPAD + c], sum);
+      sum += __shfl_xor_sync(0xffffffffu, sum, 1);
+      sum += __shfl_xor_sync(0xffffffffu, sum, 2);
+      if (q == 0 && c <= i && c < nb) w[i * DPAD + c] = ((i == c ? 1.0 : 0.0) - sum) / s[i * DPAD + i];
+      __syncthreads();
+    }
+  }
+  double* Db = Dinv + b * dinv_bstride + (int64_t)blk * NB * NB;
+  for (int idx = t; idx < NB * NB; idx += NT) {
+    const int i = idx & 63, j = idx >> 6;
+    if (i < nb && j < nb && i >= j) Ab[i + (int64_t)j * lda] = s[i * DPAD + j];
+    Db[i + j * NB] = (i >= j) ? w[i * DPAD + j] : 0.0;  // zero above the diagonal and in the ragged padding
+  }
+}
+
+// ---- R^-1 = W^T W lower tiles, each tile with its own k range ----
+__global__ void __launch_bounds__(NT) k_wtw(const double* W, int64_t ldw, int64_t wstride, int n, double* C,
+                                            int64_t ldc, int64_t cstride) {
+  // linear lower-tile index -> (I, J), I >= J, ordered by I (heaviest tiles first)
+  const int64_t x = blockIdx.x;
+  int I = (int)((sqrt(8.0 * (double)x + 1.0) - 1.0) * 0.5);
+  while ((int64_t)(I + 1) * (I + 2) / 2 <= x) ++I;
+  while ((int64_t)I * (I + 1) / 2 > x) --I;
+  const int J = (int)(x - (int64_t)I * (I + 1) / 2);
+  const int64_t b = blockIdx.z;
+  const double* Wb = W + b * wstride;
+  const int r0 = I * TB, c0 = J * TB;
+  const int K = n - r0;
+  __shared__ TileSmem sm;
+  double acc[4][4] = {};
+  // A(m, kk) = W(r0 + kk, r0 + m) ; B(kk, c) = W(r0 + kk, c0 + c)
+  tile_mma_fp64(n - r0, n - c0, K, Wb + r0 + (int64_t)r0 * ldw, ldw, 1, Wb + r0 + (int64_t)c0 * ldw, 1, ldw, 0, 0,
+                sm, acc);
+  // store into C(r0.., c0..), lower triangle only on diagonal tiles
+  tile_store(n - r0, n - c0, 1.0, 0.0, C + b * cstride + r0 + (int64_t)c0 * ldc, ldc, 0, 0, I == J, acc);
+}
+
+// ---- small-RHS helpers ----
+// B_k (nb x r, ldb) <- D (nb x nb, lower, NB-strided) * B_k   (trans: D^T * B_k)
+__global__ void k_small_apply(const double* Dinv, int64_t dinv_bstride, int blk, double* B, int64_t ldb,
+                              int64_t bstride, int k0, int nb, int r, bool trans) {
+  const int64_t b = blockIdx.z;
+  const double* D = Dinv + b * dinv_bstride + (int64_t)blk * NB * NB;
+  double* Bk = B + b * bstride + k0;
+  extern __shared__ double xs[];  // nb * r
+  for (int idx = threadIdx.x; idx < nb * r; idx += blockDim.x) {
+    const int i = idx % nb, c = idx / nb;
+    xs[idx] = Bk[i + (int64_t)c * ldb];
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < nb * r; idx += blockDim.x) {
+    const int i = idx % nb, c = idx / nb;
+    double s = 0.0;
+    if (!trans) {
+      for (int k = 0; k <= i; ++k) s = fma(D[i + k * NB], xs[k + c * nb], s);
+    } else {
+      for (int k = i; k < nb; ++k) s = fma(D[k + i * NB], xs[k + c * nb], s);
+    }
+    Bk[i + (int64_t)c * ldb] = s;
+  }
+}
+
+// B(k0+nb+i, c) -= sum_kk L(k0+nb+i, k0+kk) X(kk, c)   thread per row
+__global__ void k_panel_update(const double* L, int64_t lda, int64_t mstride, double* B, int64_t ldb,
+                               int64_t bstride, int k0, int nb, int M, int r) {
+  const int64_t b = blockIdx.z;
+  extern __shared__ double xs[];  // nb * r
+  const double* Lb = L + b * mstride;
+  double* Bb = B + b * bstride;
+  for (int idx = threadIdx.x; idx < nb * r; idx += blockDim.x) {
+    const int i = idx % nb, c = idx / nb;
+    xs[idx] = Bb[k0 + i + (int64_t)c * ldb];
+  }
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= M) return;
+  const int row = k0 + nb + i;
+  double acc[8];
+  for (int c0 = 0; c0 < r; c0 += 8) {
+    const int rc = min(8, r - c0);
+#pragma unroll
+    for (int c = 0; c < 8; ++c) acc[c] = 0.0;
+    for (int kk = 0; kk < nb; ++kk) {
+      const double l = Lb[row + (int64_t)(k0 + kk) * lda];
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+        if (c < rc) acc[c] = fma(l, xs[kk + (c0 + c) * nb], acc[c]);
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+      if (c < rc) Bb[row + (int64_t)(c0 + c) * ldb] -= acc[c];
+  }
+}
+
+// B(j, c) -= sum_kk L(k0+kk, j) X(kk, c)  for j < k0; one warp per column j
+__global__ void k_panel_update_t(const double* L, int64_t lda, int64_t mstride, double* B, int64_t ldb,
+                                 int64_t bstride, int k0, int nb, int r) {
+  const int64_t b = blockIdx.z;
+  extern __shared__ double xs[];  // nb * r
+  const double* Lb = L + b * mstride;
+  double* Bb = B + b * bstride;
+  for (int idx = threadIdx.x; idx < nb * r; idx += blockDim.x) {
+    const int i = idx % nb, c = idx / nb;
+    xs[idx] = Bb[k0 + i + (int64_t)c * ldb];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (j >= k0) return;
+  for (int c = 0; c < r; ++c) {
+    double s = 0.0;
+    for (int kk = lane; kk < nb; kk += 32) s = fma(Lb[k0 + kk + (int64_t)j * lda], xs[kk + c * nb], s);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) Bb[j + (int64_t)c * ldb] -= s;
+  }
+}
+
+__global__ void k_copy_dinv_block(const double* Dinv, int64_t dinv_bstride, int blk, double* W, int64_t ldw,
+                                  int64_t wstride, int k0, int nb) {
+  const int64_t b = blockIdx.z;
+  const double* D = Dinv + b * dinv_bstride + (int64_t)blk * NB * NB;
+  double* Wb = W + b * wstride + k0 + (int64_t)k0 * ldw;
+  for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
+    const int i = idx % nb, j = idx / nb;
+    Wb[i + (int64_t)j * ldw] = D[i + j * NB];
+  }
+}
+
+bool g_diag_attr_set = false;
+
+}  // namespace
+
+void gemm_tiles(int M, int N, int K, double alpha, MatView A, MatView B, double beta, double* C, int64_t ldc,
+                int64_t c_batch, int batch, bool lower_only, cudaStream_t st) {
+  if (M <= 0 || N <= 0) return;
+  dim3 grid(ceil_div(M, TB), ceil_div(N, TB), batch);
+  k_gemm_tiles<<<grid, NT, 0, st>>>(M, N, K, alpha, A, B, beta, C, ldc, c_batch, lower_only);
+  LKG_LAUNCH("k_gemm_tiles");
+}
+
+void potrf_diag(double* A, int64_t lda, int64_t mstride, int k0, int nb, double* Dinv, int64_t dinv_bstride, int blk,
+                int* info, int batch, cudaStream_t st) {
+  const size_t smem = 2 * NB * DPAD * sizeof(double);
+  if (!g_diag_attr_set) {
+    LKG_CUDA(cudaFuncSetAttribute(k_potrf_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    g_diag_attr_set = true;
+  }
+  k_potrf_diag<<<dim3(1, 1, batch), NT, smem, st>>>(A, lda, mstride, k0, nb, Dinv, dinv_bstride, blk, info);
+  LKG_LAUNCH("k_potrf_diag");
+}
+
+void potrf_blocked(double* A, int64_t lda, int64_t mstride, int n, double* Dinv, int* info, int batch,
+                   cudaStream_t st) {
+  const int nblk = ceil_div(n, NB);
+  const int64_t dstride = (int64_t)nblk * NB * NB;
+  LKG_CUDA(cudaMemsetAsync(info, 0, sizeof(int) * batch, st));
+  for (int k = 0; k < nblk; ++k) {
+    const int k0 = k * NB, nb = std::min(NB, n - k0);
+    potrf_diag(A, lda, mstride, k0, nb, Dinv, dstride, k, info, batch, st);
+    const int M = n - k0 - nb;
+    if (M <= 0) continue;
+    double* A21 = A + (k0 + nb) + (int64_t)k0 * lda;
+    // L21 = A21 * Dinv_k^T   (in place: each CTA reads its whole row block before writing)
+    MatView a{A21, 1, lda, mstride};
+    MatView bt{Dinv + (int64_t)k * NB * NB, NB, 1, dstride};  // B(kk, c) = Dinv(c, kk)
+    gemm_tiles(M, nb, nb, 1.0, a, bt, 0.0, A21, lda, mstride, batch, false, st);
+    // A22 -= L21 L21^T (lower tiles)
+    MatView l21t{A21, lda, 1, mstride};  // B(kk, c) = L21(c, kk)
+    gemm_tiles(M, M, nb, -1.0, a, l21t, 1.0, A21 + (int64_t)nb * lda, lda, mstride, batch, true, st);
+  }
+}
+
+void trtri_blocked(const double* L, int64_t lda, int64_t mstride, int n, const double* Dinv, double* W, int64_t ldw,
+                   int64_t wstride, int batch, cudaStream_t st) {
+  const int nblk = ceil_div(n, NB);
+  const int64_t dstride = (int64_t)nblk * NB * NB;
+  for (int b = 0; b < batch; ++b)
+    LKG_CUDA(cudaMemset2DAsync(W + b * wstride, ldw * sizeof(double), 0, n * sizeof(double), n, st));
+  for (int k = 0; k < nblk; ++k) {
+    const int k0 = k * NB, nb = std::min(NB, n - k0);
+    k_copy_dinv_block<<<dim3(1, 1, batch), 256, 0, st>>>(Dinv, dstride, k, W, ldw, wstride, k0, nb);
+    LKG_LAUNCH("k_copy_dinv_block");
+    if (k0 > 0) {
+      // W(k0:k0+nb, 0:k0) = -Dinv_k * Acc(k0:k0+nb, 0:k0)   (in place per column tile)
+      MatView d{Dinv + (int64_t)k * NB * NB, 1, NB, dstride};
+      MatView acc{W + k0, 1, ldw, wstride};
+      gemm_tiles(nb, k0, nb, -1.0, d, acc, 0.0, W + k0, ldw, wstride, batch, false, st);
+    }
+    const int M2 = n - k0 - nb;
+    if (M2 > 0) {
+      // Acc(k0+nb:, 0:k0+nb) += L(k0+nb:, k0:k0+nb) * W(k0:k0+nb, 0:k0+nb)
+      MatView a{L + (k0 + nb) + (int64_t)k0 * lda, 1, lda, mstride};
+      MatView bw{W + k0, 1, ldw, wstride};
+      gemm_tiles(M2, k0 + nb, nb, 1.0, a, bw, 1.0, W + k0 + nb, ldw, wstride, batch, false, st);
+    }
+  }
+}
+
+void wtw_lower(const double* W, int64_t ldw, int64_t wstride, int n, double* C, int64_t ldc, int64_t cstride,
+               int batch, cudaStream_t st) {
+  const int nblk = ceil_div(n, TB);
+  const int64_t ntiles = (int64_t)nblk * (nblk + 1) / 2;
+  k_wtw<<<dim3((unsigned)ntiles, 1, batch), NT, 0, st>>>(W, ldw, wstride, n, C, ldc, cstride);
+  LKG_LAUNCH("k_wtw");
+}
+
+void trsm_lower_left(const double* L, int64_t lda, int64_t mstride, int n, const double* Dinv, double* B,
+                     int64_t ldb, int64_t bstride, int r, int batch, cudaStream_t st) {
+  const int nblk = ceil_div(n, NB);
+  const int64_t dstride = (int64_t)nblk * NB * NB;
+  if (r > 16 && batch != 1 && mstride == 0)
+    throw std::invalid_argument("trsm_lower_left: shared factor with many right-hand sides is not supported");
+  const size_t smem = sizeof(double) * NB * r;
+  for (int k = 0; k < nblk; ++k) {
+    const int k0 = k * NB, nb = std::min(NB, n - k0);
+    const int M = n - k0 - nb;
+    if (r > 16) {  // many right-hand sides: tile GEMMs (X_k = Dinv_k B_k in place per column tile, then update)
+      MatView d{Dinv + (int64_t)k * NB * NB, 1, NB, dstride};
+      MatView bk{B + k0, 1, ldb, bstride};
+      gemm_tiles(nb, r, nb, 1.0, d, bk, 0.0, B + k0, ldb, bstride, batch, false, st);
+      if (M > 0) {
+        MatView a{L + (k0 + nb) + (int64_t)k0 * lda, 1, lda, mstride};
+        gemm_tiles(M, r, nb, -1.0, a, bk, 1.0, B + k0 + nb, ldb, bstride, batch, false, st);
+      }
+      continue;
+    }
+    k_small_apply<<<dim3(1, 1, batch), 256, smem, st>>>(Dinv, dstride, k, B, ldb, bstride, k0, nb, r, false);
+    LKG_LAUNCH("k_small_apply");
+    if (M > 0) {
+      k_panel_update<<<dim3(ceil_div(M, 128), 1, batch), 128, smem, st>>>(L, lda, mstride, B, ldb, bstride, k0, nb, M,
+                                                                          r);
+      LKG_LAUNCH("k_panel_update");
+    }
+  }
+}
+
+void trsm_lower_left_t(const double* L, int64_t lda, int64_t mstride, int n, const double* Dinv, double* B,
+                       int64_t ldb, int64_t bstride, int r, int batch, cudaStream_t st) {
+  const int nblk = ceil_div(n, NB);
+  const int64_t dstride = (int64_t)nblk * NB * NB;
+  const size_t smem = sizeof(double) * NB * r;
+  for (int k = nblk - 1; k >= 0; --k) {
+    const int k0 = k * NB, nb = std::min(NB, n - k0);
+    k_small_apply<<<dim3(1, 1, batch), 256, smem, st>>>(Dinv, dstride, k, B, ldb, bstride, k0, nb, r, true);
+    LKG_LAUNCH("k_small_apply");
+    if (k0 > 0) {
+      k_panel_update_t<<<dim3(ceil_div(k0, 8), 1, batch), 256, smem, st>>>(L, lda, mstride, B, ldb, bstride, k0, nb,
+                                                                           r);
+      LKG_LAUNCH("k_panel_update_t");
+    }
+  }
+}
+
+}  // namespace lkg

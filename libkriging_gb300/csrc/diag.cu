@@ -1,0 +1,72 @@
+// diag.cu -- device diagnostics exported through the C ABI: device name and the FP64 FMA throughput probe that
+// serves as the roofline denominator of the FP64 kernels (MEASURED peaks of this machine cover HBM and bf16 only).
+#include <string>
+
+#include "../../include/libkriging_gb300.h"
+#include "common.cuh"
+
+namespace {
+
+constexpr int kProbeIters = 4096;
+
+// every thread runs 8 independent FMA chains and writes exactly one element of out (grid * block elements)
+__global__ void k_dfma_probe(double* out, double s) {
+  double a0 = threadIdx.x * 1e-3, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3, a4 = a0 + 4, a5 = a0 + 5, a6 = a0 + 6,
+         a7 = a0 + 7;
+  const double b = s, c = 1.0 - s;
+  for (int i = 0; i < kProbeIters; ++i) {
+    a0 = fma(a0, b, c);
+    a1 = fma(a1, b, c);
+    a2 = fma(a2, b, c);
+    a3 = fma(a3, b, c);
+    a4 = fma(a4, b, c);
+    a5 = fma(a5, b, c);
+    a6 = fma(a6, b, c);
+    a7 = fma(a7, b, c);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
+thread_local std::string g_name;
+
+}  // namespace
+
+extern "C" {
+
+const char* lkg_device_name(void) {
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, 0) != cudaSuccess) return nullptr;
+  g_name = prop.name;
+  return g_name.c_str();
+}
+
+int lkg_probe_fp64_peak(double* tflops_out) {
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0) != cudaSuccess) return -1;
+  const int blocks = sms * 8, threads = 256;
+  double* out = nullptr;
+  if (cudaMalloc(&out, sizeof(double) * blocks * threads) != cudaSuccess) return -1;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  for (int rep = 0; rep < 5; ++rep) {
+    cudaEventRecord(e0);
+    k_dfma_probe<<<blocks, threads>>>(out, 0.999);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0 && ms < best) best = ms;
+  }
+  const cudaError_t err = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (err != cudaSuccess) return -1;
+  const double flops = (double)blocks * threads * kProbeIters * 8 * 2;
+  if (tflops_out) *tflops_out = flops / (best * 1e-3) / 1e12;
+  return 0;
+}
+
+}  // extern "C"

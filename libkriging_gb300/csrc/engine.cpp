@@ -1,0 +1,420 @@
+// engine.cpp -- device-resident evaluation engine (host orchestration of the sm_103a kernels).
+//
+// Order of operations per evaluation follows KrigingImpl::populate_Model (src/lib/KrigingImpl.cpp:73-125):
+//   R = factor * C(X; theta), diag = 1 (+ numerical nugget on retry)      LinearAlgebra::cholCov  (:142-204)
+//   L = chol(R) with the rcond / nugget-retry rules                        safe_chol_lower_retry   (:68-98)
+//   [F* y*] = L \ [F y]; R* = chol(F*'F*); beta = R* \ (R*' \ F*'y*); E* = y* - F* beta; SSE = E*'E*
+// and, when a gradient is requested, the adjoint sums of compute_ll_grad_theta_vecs (KrigingImpl.cpp:855-885)
+// with x = L' \ E* and R^-1 = (L^-1)' L^-1.
+#include "engine.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+
+#include "common.cuh"
+#include "dense_fp64.cuh"
+#include "lik_kernels.cuh"
+
+namespace lkg {
+
+namespace {
+
+template <typename T>
+T env_or(const char* name, T def) {
+  const char* v = std::getenv(name);
+  if (!v) return def;
+  try {
+    if constexpr (std::is_same_v<T, int>) return std::stoi(v);
+    else if constexpr (std::is_same_v<T, double>) return std::stod(v);
+    else if constexpr (std::is_same_v<T, bool>) {
+      std::string s(v);
+      return s == "1" || s == "true" || s == "TRUE" || s == "True";
+    }
+  } catch (...) {
+  }
+  return def;
+}
+
+struct Timer {
+  cudaStream_t st;
+  std::map<std::string, double>* bench;
+  cudaEvent_t e0 = nullptr;
+  Timer(cudaStream_t s, std::map<std::string, double>* b) : st(s), bench(b) {
+    if (bench) {
+      LKG_CUDA(cudaEventCreate(&e0));
+      LKG_CUDA(cudaEventRecord(e0, st));
+    }
+  }
+  ~Timer() {
+    if (e0) cudaEventDestroy(e0);
+  }
+  void lap(const char* key) {
+    if (!bench) return;
+    cudaEvent_t e1;
+    LKG_CUDA(cudaEventCreate(&e1));
+    LKG_CUDA(cudaEventRecord(e1, st));
+    LKG_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    LKG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    (*bench)[key] += ms;
+    LKG_CUDA(cudaEventDestroy(e0));
+    e0 = e1;
+  }
+};
+
+template <typename P>
+void dalloc(P** p, size_t count) {
+  LKG_CUDA(cudaMalloc((void**)p, sizeof(P) * std::max<size_t>(count, 1)));
+}
+
+}  // namespace
+
+Config& config() {
+  static Config c = [] {
+    Config x;
+    x.reparametrize = env_or("LK_REPARAMETRIZE", true);
+    x.theta_lower_factor = env_or("LK_THETA_LOWER_FACTOR", 0.02);
+    x.theta_upper_factor = env_or("LK_THETA_UPPER_FACTOR", 10.0);
+    x.variogram_bounds_heuristic = env_or("LK_VARIOGRAM_BOUNDS_HEURISTIC", true);
+    x.log_level = env_or("LK_LOG_LEVEL", 0);
+    x.max_restart = env_or("LK_MAX_RESTART", 10);
+    x.max_iteration = env_or("LK_MAX_ITERATION", 20);
+    x.gradient_tolerance = env_or("LK_GRADIENT_TOLERANCE", 0.001);
+    x.objective_rel_tolerance = env_or("LK_OBJECTIVE_REL_TOLERANCE", 0.001);
+    return x;
+  }();
+  return c;
+}
+
+Engine::Engine(int kernel, int n, int d, int p, const double* X, const double* y, const double* F, int batch_cap)
+    : kernel_(kernel), n_(n), d_(d), p_(p), cap_(batch_cap) {
+  if (n < 1 || d < 1 || d > MAX_D || p < 0 || p > 64 || batch_cap < 1)
+    throw std::invalid_argument("Engine: unsupported sizes n=" + std::to_string(n) + " d=" + std::to_string(d) +
+                                " p=" + std::to_string(p));
+  LKG_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+  lda_ = ((int64_t)n + 7) / 8 * 8;  // 64-byte aligned columns
+  mstride_ = lda_ * n;
+  const int nblk = ceil_div(n, NB);
+  dstride_ = (int64_t)nblk * NB * NB;
+  fystride_ = (int64_t)n * (p + 1);
+  gram_stride_ = (p + 1) * (p + 1) + 1;
+  dalloc(&dX_, (size_t)n * d);
+  dalloc(&dY_, n);
+  dalloc(&dF_, (size_t)n * std::max(p, 1));
+  LKG_CUDA(cudaMemcpyAsync(dX_, X, sizeof(double) * n * d, cudaMemcpyHostToDevice, st_));
+  LKG_CUDA(cudaMemcpyAsync(dY_, y, sizeof(double) * n, cudaMemcpyHostToDevice, st_));
+  if (p > 0) LKG_CUDA(cudaMemcpyAsync(dF_, F, sizeof(double) * n * p, cudaMemcpyHostToDevice, st_));
+  dalloc(&dA_, (size_t)mstride_ * cap_);
+  dalloc(&dDinv_, (size_t)dstride_ * cap_);
+  dalloc(&dFY_, (size_t)fystride_ * cap_);
+  dalloc(&dEstar_, (size_t)n * cap_);
+  dalloc(&dxv_, (size_t)n * cap_);
+  dalloc(&dvec_, (size_t)n * cap_);
+  dalloc(&dcol_, (size_t)n * cap_);
+  dalloc(&dtheta_, (size_t)d * cap_);
+  dalloc(&dfactor_, cap_);
+  dalloc(&ddiag_, cap_);
+  dalloc(&dgram_, (size_t)gram_stride_ * cap_);
+  dalloc(&dbeta_, (size_t)std::max(p, 1) * cap_);
+  dalloc(&drstar_, (size_t)std::max(p * p, 1) * cap_);
+  dalloc(&dsse_, cap_);
+  dalloc(&dadj_, (size_t)adjoint_nacc(d) * cap_);
+  dalloc(&dinfo_, cap_);
+  dalloc(&dgls_info_, cap_);
+  LKG_CUDA(cudaStreamSynchronize(st_));
+}
+
+Engine::~Engine() {
+  for (double* p : {dX_, dY_, dF_, dA_, dDinv_, dW_, dRinv_, dFY_, dEstar_, dxv_, dtheta_, dfactor_, ddiag_, dgram_,
+                    dbeta_, drstar_, dsse_, dpart_, dadj_, dvec_, dcol_})
+    if (p) cudaFree(p);
+  if (dinfo_) cudaFree(dinfo_);
+  if (dgls_info_) cudaFree(dgls_info_);
+  if (st_) cudaStreamDestroy(st_);
+}
+
+void Engine::ensure_grad_buffers() {
+  if (dW_) return;
+  dalloc(&dW_, (size_t)mstride_ * cap_);
+  dalloc(&dRinv_, (size_t)mstride_ * cap_);
+  part_size_ = adjoint_partials_size(n_, d_, cap_);
+  dalloc(&dpart_, part_size_);
+}
+
+void Engine::solve_lower_inplace(int b, double* dB, int64_t ldb, int r) const {
+  trsm_lower_left(dA_ + (size_t)b * mstride_, lda_, mstride_, n_, dDinv_ + (size_t)b * dstride_, dB, ldb, 0, r, 1,
+                  st_);
+}
+
+// dtrcon('1', 'L', 'N') style estimate (LAPACK dlacn2 iteration of Hager / Higham) of rcond(L)^2 for every entry,
+// with the triangular solves of all entries batched into the same launches.
+void Engine::rcond_batch(int batch, std::vector<double>& rc2) {
+  const int n = n_;
+  std::vector<double> colsum((size_t)n * batch);
+  lower_colsum_abs(n, dA_, lda_, mstride_, dcol_, batch, st_);
+  LKG_CUDA(cudaMemcpyAsync(colsum.data(), dcol_, sizeof(double) * n * batch, cudaMemcpyDeviceToHost, st_));
+  LKG_CUDA(cudaStreamSynchronize(st_));
+  std::vector<double> anorm(batch, 0.0);
+  for (int b = 0; b < batch; ++b)
+    for (int j = 0; j < n; ++j) anorm[b] = std::max(anorm[b], colsum[(size_t)b * n + j]);
+
+  // per-entry state machine of dlacn2
+  struct St {
+    int phase = 0;  // 0: x=1/n pending kind1; 1: sign pending kind2; 2: e_j pending kind1; 3: altsgn kind1; 4 done
+    int iter = 0, j = 0;
+    double est = 0.0;
+    std::vector<double> xi;
+    bool first_done = false;
+  };
+  std::vector<St> S(batch);
+  std::vector<double> vec((size_t)n * batch);
+  auto set_x = [&](int b, int phase) {
+    double* x = vec.data() + (size_t)b * n;
+    if (phase == 0) {
+      for (int i = 0; i < n; ++i) x[i] = 1.0 / n;
+    } else if (phase == 1) {
+      for (int i = 0; i < n; ++i) x[i] = S[b].xi[i];
+    } else if (phase == 2) {
+      std::fill(x, x + n, 0.0);
+      x[S[b].j] = 1.0;
+    } else if (phase == 3) {
+      double altsgn = 1.0;
+      for (int i = 0; i < n; ++i) {
+        x[i] = altsgn * (1.0 + (n > 1 ? (double)i / (double)(n - 1) : 0.0));
+        altsgn = -altsgn;
+      }
+    }
+  };
+  for (int b = 0; b < batch; ++b) {
+    S[b].xi.assign(n, 0.0);
+    set_x(b, 0);
+    if (!(anorm[b] > 0.0)) S[b].phase = 4;
+  }
+  auto kind_of = [](int phase) { return phase == 1 ? 2 : 1; };
+  for (int round = 0; round < 64; ++round) {
+    bool any1 = false, any2 = false;
+    for (int b = 0; b < batch; ++b)
+      if (S[b].phase < 4) (kind_of(S[b].phase) == 1 ? any1 : any2) = true;
+    if (!any1 && !any2) break;
+    const int kind = any1 ? 1 : 2;
+    LKG_CUDA(cudaMemcpyAsync(dvec_, vec.data(), sizeof(double) * n * batch, cudaMemcpyHostToDevice, st_));
+    if (kind == 1)
+      trsm_lower_left(dA_, lda_, mstride_, n, dDinv_, dvec_, n, n, 1, batch, st_);
+    else
+      trsm_lower_left_t(dA_, lda_, mstride_, n, dDinv_, dvec_, n, n, 1, batch, st_);
+    std::vector<double> res((size_t)n * batch);
+    LKG_CUDA(cudaMemcpyAsync(res.data(), dvec_, sizeof(double) * n * batch, cudaMemcpyDeviceToHost, st_));
+    LKG_CUDA(cudaStreamSynchronize(st_));
+    for (int b = 0; b < batch; ++b) {
+      St& s = S[b];
+      if (s.phase >= 4 || kind_of(s.phase) != kind) continue;
+      const double* y = res.data() + (size_t)b * n;
+      double l1 = 0.0;
+      for (int i = 0; i < n; ++i) l1 += std::fabs(y[i]);
+      if (s.phase == 0) {
+        s.est = l1;
+        if (n == 1) {
+          s.phase = 4;
+          continue;
+        }
+        for (int i = 0; i < n; ++i) s.xi[i] = (y[i] >= 0.0) ? 1.0 : -1.0;
+        s.phase = 1;
+        s.iter = 2;
+        s.first_done = true;
+      } else if (s.phase == 1) {
+        int jlast = s.j;
+        int jm = 0;
+        for (int i = 1; i < n; ++i)
+          if (std::fabs(y[i]) > std::fabs(y[jm])) jm = i;
+        if (s.first_done) {
+          s.first_done = false;
+          s.j = jm;
+          s.phase = 2;
+        } else {
+          s.j = jm;
+          if (y[jlast] != std::fabs(y[jm]) && s.iter < 5) {
+            s.iter++;
+            s.phase = 2;
+          } else {
+            s.phase = 3;
+          }
+        }
+      } else if (s.phase == 2) {
+        const double estold = s.est;
+        s.est = l1;
+        bool same = true;
+        for (int i = 0; i < n && same; ++i) same = (((y[i] >= 0.0) ? 1.0 : -1.0) == s.xi[i]);
+        if (same || s.est <= estold) {
+          s.phase = 3;
+        } else {
+          for (int i = 0; i < n; ++i) s.xi[i] = (y[i] >= 0.0) ? 1.0 : -1.0;
+          s.phase = 1;
+        }
+      } else if (s.phase == 3) {
+        const double temp = 2.0 * l1 / (3.0 * n);
+        if (temp > s.est) s.est = temp;
+        s.phase = 4;
+      }
+      if (s.phase < 4) set_x(b, s.phase);
+    }
+  }
+  rc2.assign(batch, 0.0);
+  for (int b = 0; b < batch; ++b) {
+    double rc = 0.0;
+    if (anorm[b] > 0.0 && S[b].est > 0.0) rc = (1.0 / anorm[b]) / S[b].est;
+    rc2[b] = rc * rc;
+  }
+}
+
+void Engine::evaluate(int batch, const double* thetas, const double* factors, bool with_grad,
+                      std::vector<EvalOut>& out, std::map<std::string, double>* bench) {
+  if (batch < 1 || batch > cap_) throw std::invalid_argument("Engine::evaluate: batch out of range");
+  const Config& cfg = config();
+  const int n = n_, d = d_, p = p_;
+  out.assign(batch, EvalOut{});
+  Timer tm(st_, bench);
+  LKG_CUDA(cudaMemcpyAsync(dtheta_, thetas, sizeof(double) * d * batch, cudaMemcpyHostToDevice, st_));
+  LKG_CUDA(cudaMemcpyAsync(dfactor_, factors, sizeof(double) * batch, cudaMemcpyHostToDevice, st_));
+
+  // ---- R, L with the numerical-nugget retry rules (LinearAlgebra.cpp:68-98) ----
+  std::vector<double> diag(batch, 1.0);
+  std::vector<int> inc(batch, 0);
+  std::vector<char> dead(batch, 0);
+  std::vector<int> info(batch, 0);
+  std::vector<double> rc2(batch, -1.0);
+  for (int attempt = 0;; ++attempt) {
+    LKG_CUDA(cudaMemcpyAsync(ddiag_, diag.data(), sizeof(double) * batch, cudaMemcpyHostToDevice, st_));
+    cov_build_lower(kernel_, n, d, dX_, 0, dtheta_, dfactor_, ddiag_, dA_, lda_, mstride_, batch, st_);
+    potrf_blocked(dA_, lda_, mstride_, n, dDinv_, dinfo_, batch, st_);
+    LKG_CUDA(cudaMemcpyAsync(info.data(), dinfo_, sizeof(int) * batch, cudaMemcpyDeviceToHost, st_));
+    LKG_CUDA(cudaStreamSynchronize(st_));
+    if (cfg.chol_rcond_check) rcond_batch(batch, rc2);
+    bool retry = false;
+    for (int b = 0; b < batch; ++b) {
+      if (dead[b]) continue;
+      const bool ok = info[b] == 0;
+      const bool wrong = cfg.chol_rcond_check && ok && rc2[b] < cfg.min_rcond;
+      if (!ok || wrong) {
+        if (inc[b] > cfg.max_inc_choldiag) {
+          dead[b] = 1;
+          out[b].status = 1;
+          out[b].message = "[ERROR] Exceed max numerical nugget (" + std::to_string(inc[b]) + " x 1e" +
+                           std::to_string(std::log10(cfg.num_nugget)) + ") added to force chol matrix";
+        } else if (cfg.num_nugget <= 0.0) {
+          dead[b] = 1;
+          out[b].status = 1;
+          out[b].message = "[ERROR] Cannot add numerical nugget which is not strictly positive: " +
+                           std::to_string(cfg.num_nugget);
+        } else {
+          diag[b] += cfg.num_nugget * std::pow(10.0, inc[b]);
+          inc[b]++;
+          retry = true;
+        }
+      }
+    }
+    if (!retry) break;
+  }
+  for (int b = 0; b < batch; ++b) {
+    out[b].nugget_increments = inc[b];
+    out[b].rcond = rc2[b];
+  }
+  tm.lap("R = _Cov(dX) & L = Chol(R)");
+
+  // ---- [F* y*] = L \ [F y], GLS, E*, SSE ----
+  for (int b = 0; b < batch; ++b) {
+    double* fy = dFY_ + (size_t)b * fystride_;
+    if (p > 0) LKG_CUDA(cudaMemcpyAsync(fy, dF_, sizeof(double) * n * p, cudaMemcpyDeviceToDevice, st_));
+    LKG_CUDA(cudaMemcpyAsync(fy + (size_t)n * p, dY_, sizeof(double) * n, cudaMemcpyDeviceToDevice, st_));
+  }
+  trsm_lower_left(dA_, lda_, mstride_, n, dDinv_, dFY_, n, fystride_, p + 1, batch, st_);
+  tm.lap("F* = L \\ F, y* = L \\ y");
+  gram_and_logdet(n, p + 1, dFY_, n, fystride_, dA_, lda_, mstride_, dgram_, gram_stride_, batch, st_);
+  if (p > 0) {
+    gls_solve(p, dgram_, gram_stride_, dbeta_, p, drstar_, p * p, dgls_info_, batch, st_);
+  } else {
+    LKG_CUDA(cudaMemsetAsync(dgls_info_, 0, sizeof(int) * batch, st_));
+  }
+  tm.lap("^b = R*^-1 R*'^-1 F*'y*");
+  residual_sse(n, p, dFY_, n, fystride_, dbeta_, std::max(p, 1), dEstar_, n, dsse_, 1, batch, st_);
+  tm.lap("z = L \\ (y - F*b), SSE = z'z");
+
+  if (with_grad) {
+    ensure_grad_buffers();
+    LKG_CUDA(cudaMemcpyAsync(dxv_, dEstar_, sizeof(double) * n * batch, cudaMemcpyDeviceToDevice, st_));
+    trsm_lower_left_t(dA_, lda_, mstride_, n, dDinv_, dxv_, n, n, 1, batch, st_);
+    tm.lap("x = tL \\ z");
+    trtri_blocked(dA_, lda_, mstride_, n, dDinv_, dW_, lda_, mstride_, batch, st_);
+    wtw_lower(dW_, lda_, mstride_, n, dRinv_, lda_, mstride_, batch, st_);
+    tm.lap("R^-1 = L^-T * L^-1");
+    adjoint_sums(kernel_, n, d, dX_, 0, dtheta_, dfactor_, dxv_, n, dRinv_, lda_, mstride_, dpart_, dadj_, batch,
+                 st_);
+    tm.lap("gradR computation [optimized]");
+  }
+
+  // ---- results to host ----
+  std::vector<double> gram((size_t)gram_stride_ * batch), sse(batch), beta((size_t)std::max(p, 1) * batch);
+  std::vector<int> gls(batch);
+  std::vector<double> adj;
+  LKG_CUDA(cudaMemcpyAsync(gram.data(), dgram_, sizeof(double) * gram.size(), cudaMemcpyDeviceToHost, st_));
+  LKG_CUDA(cudaMemcpyAsync(sse.data(), dsse_, sizeof(double) * batch, cudaMemcpyDeviceToHost, st_));
+  LKG_CUDA(cudaMemcpyAsync(beta.data(), dbeta_, sizeof(double) * beta.size(), cudaMemcpyDeviceToHost, st_));
+  LKG_CUDA(cudaMemcpyAsync(gls.data(), dgls_info_, sizeof(int) * batch, cudaMemcpyDeviceToHost, st_));
+  const int nacc = adjoint_nacc(d);
+  if (with_grad) {
+    adj.resize((size_t)nacc * batch);
+    LKG_CUDA(cudaMemcpyAsync(adj.data(), dadj_, sizeof(double) * adj.size(), cudaMemcpyDeviceToHost, st_));
+  }
+  LKG_CUDA(cudaStreamSynchronize(st_));
+  for (int b = 0; b < batch; ++b) {
+    EvalOut& o = out[b];
+    if (o.status == 0 && gls[b] != 0) {
+      o.status = 2;
+      o.message = "chol(): decomposition failed (F*'F* not positive definite)";
+    }
+    o.logdet = 2.0 * gram[(size_t)b * gram_stride_ + (p + 1) * (p + 1)];
+    o.sse = sse[b];
+    o.beta.assign(beta.begin() + (size_t)b * std::max(p, 1), beta.begin() + (size_t)b * std::max(p, 1) + p);
+    if (with_grad) o.adj.assign(adj.begin() + (size_t)b * nacc, adj.begin() + (size_t)(b + 1) * nacc);
+  }
+}
+
+void Engine::copy_model(int b, std::vector<double>* L, std::vector<double>* Fstar, std::vector<double>* ystar,
+                        std::vector<double>* Rstar, std::vector<double>* Estar) const {
+  const int n = n_, p = p_;
+  if (L) {
+    L->assign((size_t)n * n, 0.0);
+    LKG_CUDA(cudaMemcpy2DAsync(L->data(), sizeof(double) * n, dA_ + (size_t)b * mstride_, sizeof(double) * lda_,
+                               sizeof(double) * n, n, cudaMemcpyDeviceToHost, st_));
+  }
+  if (Fstar) {
+    Fstar->resize((size_t)n * p);
+    if (p > 0)
+      LKG_CUDA(cudaMemcpyAsync(Fstar->data(), dFY_ + (size_t)b * fystride_, sizeof(double) * n * p,
+                               cudaMemcpyDeviceToHost, st_));
+  }
+  if (ystar) {
+    ystar->resize(n);
+    LKG_CUDA(cudaMemcpyAsync(ystar->data(), dFY_ + (size_t)b * fystride_ + (size_t)n * p, sizeof(double) * n,
+                             cudaMemcpyDeviceToHost, st_));
+  }
+  if (Rstar) {
+    Rstar->resize((size_t)p * p);
+    if (p > 0)
+      LKG_CUDA(cudaMemcpyAsync(Rstar->data(), drstar_ + (size_t)b * p * p, sizeof(double) * p * p,
+                               cudaMemcpyDeviceToHost, st_));
+  }
+  if (Estar) {
+    Estar->resize(n);
+    LKG_CUDA(cudaMemcpyAsync(Estar->data(), dEstar_ + (size_t)b * n, sizeof(double) * n, cudaMemcpyDeviceToHost,
+                             st_));
+  }
+  LKG_CUDA(cudaStreamSynchronize(st_));
+  if (L)  // zero the (unreferenced) upper triangle so that the host copy is trimatl(L)
+    for (int j = 1; j < n; ++j)
+      for (int i = 0; i < j; ++i) (*L)[i + (size_t)j * n] = 0.0;
+}
+
+}  // namespace lkg

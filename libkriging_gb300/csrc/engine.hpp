@@ -1,0 +1,81 @@
+// engine.hpp -- device-resident evaluation engine for the exact (dense) likelihood.
+//
+// One Engine holds one design (X, y, F) in HBM and evaluates populate_Model + the log-likelihood building blocks
+// for a batch of theta values in the same launches (multistart).  It replaces, for the GPU, the seam
+// KrigingImpl::populate_Model + compute_ll_grad_theta_vecs (src/lib/KrigingImpl.cpp:73-125, :855-885).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "config.hpp"
+
+namespace lkg {
+
+struct EvalOut {
+  int status = 0;              // 0 ok; 1 Cholesky failed after max nugget increments; 2 GLS factor failed
+  std::string message;         // reference-style error text when status != 0
+  int nugget_increments = 0;   // numerical nugget increments used (safe_chol_lower_retry)
+  double logdet = 0.0;         // 2 * sum log L_ii
+  double sse = 0.0;            // Estar' Estar
+  std::vector<double> beta;    // GLS beta (p)
+  std::vector<double> adj;     // adjoint sums [T1(d), T2(d), U1, U2, D1, D2] (with_grad)
+  double rcond = -1.0;         // rcond(L)^2 of the accepted factor (when the check ran)
+};
+
+class Engine {
+ public:
+  // X: n x d column-major, y: n, F: n x p column-major (all host, copied to HBM).  batch_cap: max thetas per call.
+  Engine(int kernel, int n, int d, int p, const double* X, const double* y, const double* F, int batch_cap);
+  ~Engine();
+  Engine(const Engine&) = delete;
+  Engine& operator=(const Engine&) = delete;
+
+  // thetas: batch x d (row b = theta of entry b); factors: batch (alpha, 1 for NoiseModel None).
+  // The accepted factor L of every entry stays in HBM until the next call (see copy_model).
+  void evaluate(int batch, const double* thetas, const double* factors, bool with_grad, std::vector<EvalOut>& out,
+                std::map<std::string, double>* bench = nullptr);
+
+  // Copies of the last evaluation's state for batch entry b (host, column-major):
+  //   L (n x n lower, upper part zero), Fstar (n x p), ystar (n), Rstar (p x p upper), Estar (n)
+  void copy_model(int b, std::vector<double>* L, std::vector<double>* Fstar, std::vector<double>* ystar,
+                  std::vector<double>* Rstar, std::vector<double>* Estar) const;
+
+  int n() const { return n_; }
+  int d() const { return d_; }
+  int p() const { return p_; }
+  int kernel() const { return kernel_; }
+  int capacity() const { return cap_; }
+  cudaStream_t stream() const { return st_; }
+
+  // device pointers (batch entry 0 layout) for predict: factor, diagonal-block inverses, Fstar, Estar
+  const double* dL(int b = 0) const { return dA_ + (size_t)b * mstride_; }
+  const double* dDinv(int b = 0) const { return dDinv_ + (size_t)b * dstride_; }
+  const double* dX() const { return dX_; }
+  int64_t lda() const { return lda_; }
+  const double* dFY(int b = 0) const { return dFY_ + (size_t)b * fystride_; }
+  const double* dEstar(int b = 0) const { return dEstar_ + (size_t)b * n_; }
+  // solve L Z = B in place for entry b (B device, n x r, ldb)
+  void solve_lower_inplace(int b, double* dB, int64_t ldb, int r) const;
+
+ private:
+  void ensure_grad_buffers();
+  void rcond_batch(int batch, std::vector<double>& rc2);  // rcond(L)^2 per entry, dtrcon('1') style estimate
+
+  int kernel_, n_, d_, p_, cap_;
+  int64_t lda_, mstride_, dstride_, fystride_;
+  cudaStream_t st_ = nullptr;
+  double *dX_ = nullptr, *dY_ = nullptr, *dF_ = nullptr;
+  double *dA_ = nullptr, *dDinv_ = nullptr, *dW_ = nullptr, *dRinv_ = nullptr;
+  double *dFY_ = nullptr, *dEstar_ = nullptr, *dxv_ = nullptr;
+  double *dtheta_ = nullptr, *dfactor_ = nullptr, *ddiag_ = nullptr;
+  double *dgram_ = nullptr, *dbeta_ = nullptr, *drstar_ = nullptr, *dsse_ = nullptr;
+  double *dpart_ = nullptr, *dadj_ = nullptr, *dvec_ = nullptr, *dcol_ = nullptr;
+  int *dinfo_ = nullptr, *dgls_info_ = nullptr;
+  size_t part_size_ = 0;
+  int gram_stride_ = 0;
+};
+
+}  // namespace lkg

@@ -1,0 +1,818 @@
+// kriging.cpp -- GPU-backed Kriging facade (host C++).
+//
+// Restates the host logic of libKriging's Kriging class around the GPU engine:
+//   fit                Kriging.cpp:1591-2215 (fit_setup_impl KrigingImpl.cpp:764-841, theta_bounds Optim.cpp:179-209,
+//                      parse_method Optim.cpp:151-177, Random.cpp:13-49, make_fit_objective Kriging.cpp:1414-1470,
+//                      nugget reparametrisation Kriging.cpp:676-702)
+//   _logLikelihood     Kriging.cpp:214-341 (LL per noise model, gradient assembly, alpha-gradient)
+//   predict            Kriging.cpp:2240-2285 -> KrigingImpl.cpp:145-300 (mean, stdev, cov)
+// The multistart runs every start's L-BFGS-B in its own host thread; their objective calls are gathered by a
+// batcher into ONE batched GPU evaluation per round (the reference runs the starts one after another).
+#include "kriging.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <exception>
+#include <limits>
+#include <mutex>
+#include <random>
+#include <sstream>
+#include <stdexcept>
+#include <thread>
+
+#include "common.cuh"
+#include "dense_fp64.cuh"
+#include "lbfgsb.hpp"
+#include "lik_kernels.cuh"
+#include "predict_kernels.cuh"
+
+namespace lkg {
+
+static constexpr double kNuggetAlphaLower = 1e-3;  // Kriging.cpp:680
+
+RegressionModel regmodel_from_string(const std::string& s) {
+  if (s == "none") return RegressionModel::None;
+  if (s == "constant") return RegressionModel::Constant;
+  if (s == "linear") return RegressionModel::Linear;
+  if (s == "interactive") return RegressionModel::Interactive;
+  if (s == "quadratic") return RegressionModel::Quadratic;
+  throw std::invalid_argument("Cannot convert '" + s + "' as a regression model");
+}
+
+const char* regmodel_to_string(RegressionModel r) {
+  static const char* names[] = {"none", "constant", "linear", "interactive", "quadratic"};
+  return names[(int)r];
+}
+
+std::vector<double> regression_matrix(RegressionModel r, const std::vector<double>& X, int n, int d, int* p_out) {
+  std::vector<std::vector<double>> cols;
+  auto col = [&](int i) { return std::vector<double>(X.begin() + (size_t)i * n, X.begin() + (size_t)(i + 1) * n); };
+  auto prod = [&](int i, int j) {
+    std::vector<double> v(n);
+    for (int a = 0; a < n; ++a) v[a] = X[a + (size_t)i * n] * X[a + (size_t)j * n];
+    return v;
+  };
+  if (r != RegressionModel::None) cols.push_back(std::vector<double>(n, 1.0));
+  if (r == RegressionModel::Linear) {
+    for (int i = 0; i < d; ++i) cols.push_back(col(i));
+  } else if (r == RegressionModel::Interactive) {
+    for (int i = 0; i < d; ++i) {
+      cols.push_back(col(i));
+      for (int j = 0; j < i; ++j) cols.push_back(prod(i, j));
+    }
+  } else if (r == RegressionModel::Quadratic) {
+    for (int i = 0; i < d; ++i) {
+      cols.push_back(col(i));
+      for (int j = 0; j <= i; ++j) cols.push_back(prod(i, j));
+    }
+  }
+  *p_out = (int)cols.size();
+  std::vector<double> F((size_t)n * cols.size());
+  for (size_t q = 0; q < cols.size(); ++q) std::copy(cols[q].begin(), cols[q].end(), F.begin() + q * n);
+  return F;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// Random (Random.cpp:13-49): a process-wide mt19937 seeded with 123, re-seeded by each BFGS fit
+namespace {
+std::mt19937& rng_engine() {
+  static std::mt19937 e(123);
+  return e;
+}
+unsigned int& rng_seed() {
+  static unsigned int s = 123;
+  return s;
+}
+Mat randu_mat(int rows, int cols) {  // column-major fill (arma imbue)
+  std::uniform_real_distribution<double> dist{};
+  Mat m;
+  m.rows = rows;
+  m.cols = cols;
+  m.v.resize((size_t)rows * cols);
+  for (auto& x : m.v) x = dist(rng_engine());
+  return m;
+}
+std::vector<double> randu_vec(int n) {
+  std::uniform_real_distribution<double> dist{};
+  std::vector<double> v(n);
+  for (auto& x : v) x = dist(rng_engine());
+  return v;
+}
+
+// Optim::parse_method (Optim.cpp:151-177)
+std::pair<std::string, int> parse_method(const std::string& method, const std::string& prefix) {
+  if (method.rfind(prefix, 0) != 0) return {method, 1};
+  size_t pos = prefix.size(), e = pos;
+  while (e < method.size() && std::isdigit((unsigned char)method[e])) ++e;
+  if (e == pos) return {method, 1};
+  int ms = 1;
+  try {
+    ms = std::stoi(method.substr(pos, e - pos));
+  } catch (...) {
+    ms = 1;
+  }
+  if (ms < 1) ms = 1;
+  return {prefix + method.substr(e), ms};
+}
+
+// Evaluation batcher: worker threads submit one request each and block; when every still-active worker has a
+// request pending, the last arrival runs them as one batched GPU evaluation.
+struct EvalRequest {
+  std::vector<double> theta;
+  double factor = 1.0;
+  bool want_grad = false;
+  EvalOut out;
+  std::exception_ptr err;
+  bool done = false;
+};
+
+class Batcher {
+ public:
+  Batcher(int workers, std::function<void(std::vector<EvalRequest*>&)> run) : active_(workers), run_(std::move(run)) {}
+  void submit(EvalRequest* r) {
+    std::unique_lock<std::mutex> lk(mu_);
+    pending_.push_back(r);
+    maybe_run(lk);
+    cv_.wait(lk, [&] { return r->done; });
+  }
+  void leave() {
+    std::unique_lock<std::mutex> lk(mu_);
+    active_--;
+    maybe_run(lk);
+  }
+
+ private:
+  void maybe_run(std::unique_lock<std::mutex>& lk) {
+    if (pending_.empty() || (int)pending_.size() < active_) return;
+    std::vector<EvalRequest*> batch;
+    batch.swap(pending_);
+    lk.unlock();
+    try {
+      run_(batch);
+    } catch (...) {
+      for (auto* r : batch) r->err = std::current_exception();
+    }
+    lk.lock();
+    for (auto* r : batch) r->done = true;
+    cv_.notify_all();
+  }
+  std::mutex mu_;
+  std::condition_variable cv_;
+  int active_;
+  std::vector<EvalRequest*> pending_;
+  std::function<void(std::vector<EvalRequest*>&)> run_;
+};
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------------------------
+Kriging::Kriging(const std::string& covType, NoiseModel nm)
+    : m_covType(covType), m_kernel(kernel_from_name(covType)), m_noise_model(nm) {}
+
+Kriging::~Kriging() = default;
+
+void Kriging::ensure_engine(int batch_cap) {
+  if (m_n == 0) throw std::runtime_error("Kriging model has no data: call fit() first");
+  if (!m_eval || m_eval->capacity() < batch_cap)
+    m_eval = std::make_unique<Engine>(m_kernel, m_n, m_d, m_p, m_X.data(), m_y.data(), m_F.data(),
+                                      std::max(batch_cap, 1));
+}
+
+double Kriging::loglik_from(const EvalOut& o, double extra_param, std::vector<double>* grad, int gdim) const {
+  if (o.status != 0) throw std::runtime_error(o.message);
+  const double n = m_n;
+  const int d = m_d;
+  double sigma2_grad, ll;
+  if (m_noise_model == NoiseModel::Nugget) {
+    double a = extra_param, s2 = m_sigma2, nu = m_nugget;
+    if (m_est_sigma2) {
+      if (m_est_nugget) {
+        const double var = o.sse / n;
+        s2 = a * var;
+        nu = (1.0 - a) * var;
+      } else {
+        s2 = m_nugget * a / (1.0 - a);
+      }
+    } else {
+      if (m_est_nugget)
+        nu = m_sigma2 * (1.0 - a) / a;
+      else
+        a = m_sigma2 / (m_sigma2 + m_nugget);
+    }
+    const double tv = s2 + nu;
+    ll = -0.5 * (n * std::log(2 * M_PI * tv) + o.logdet + o.sse / tv);
+    sigma2_grad = tv;
+  } else {
+    if (m_est_sigma2) {
+      sigma2_grad = o.sse / n;
+      ll = -0.5 * (n * std::log(2 * M_PI * sigma2_grad) + o.logdet + n);
+    } else {
+      sigma2_grad = m_sigma2;
+      ll = -0.5 * (n * std::log(2 * M_PI * sigma2_grad) + o.logdet + o.sse / sigma2_grad);
+    }
+  }
+  if (grad) {
+    grad->assign(gdim, 0.0);
+    const std::vector<double>& A = o.adj;  // [T1(d), T2(d), U1, U2, D1, D2]
+    for (int k = 0; k < d; ++k) {
+      // (term1_k / sigma2 + term2_k) / 2 with term1_k = 2 T1_k, term2_k = -2 T2_k
+      (*grad)[k] = ((2.0 * A[k]) / sigma2_grad + (-2.0 * A[d + k])) / 2.0;
+    }
+    if (gdim > d && m_noise_model == NoiseModel::Nugget) {
+      const double a = extra_param;
+      const double U1 = A[2 * d], U2 = A[2 * d + 1], D1 = A[2 * d + 2], D2 = A[2 * d + 3];
+      if (m_est_sigma2 && m_est_nugget) {
+        const double var = sigma2_grad;
+        const double term1_a = -(2.0 * U1) / var;
+        const double term2_a = 2.0 * U2;
+        (*grad)[d] = -0.5 * (term1_a + term2_a);
+      } else if (m_est_sigma2 && !m_est_nugget) {
+        const double tv = sigma2_grad;
+        const double term1_a = -(2.0 * U1 + D1) / (tv * tv);
+        const double term2_a = (2.0 * U2 + D2) / tv;
+        (*grad)[d] = -0.5 * (term1_a + term2_a) * m_nugget / (1.0 - a) / (1.0 - a);
+      } else {
+        (*grad)[d] = 0.0;
+      }
+    }
+  }
+  return ll;
+}
+
+std::tuple<double, std::vector<double>> Kriging::logLikelihoodFun(const std::vector<double>& gamma, bool return_grad,
+                                                                  bool bench) {
+  const int d = m_d;
+  if (m_n == 0) throw std::runtime_error("Kriging model has no data: call fit() first");
+  if ((int)gamma.size() != d && !((int)gamma.size() == d + 1 && m_noise_model == NoiseModel::Nugget))
+    throw std::invalid_argument("logLikelihoodFun: gamma should have length " + std::to_string(d) +
+                                (m_noise_model == NoiseModel::Nugget ? " or " + std::to_string(d + 1) : ""));
+  ensure_engine(1);
+  double extra = (gamma.size() > (size_t)d) ? gamma[d] : (m_noise_model == NoiseModel::Nugget ? m_alpha : m_sigma2);
+  if (m_noise_model == NoiseModel::Nugget && !m_est_sigma2 && !m_est_nugget) extra = m_sigma2 / (m_sigma2 + m_nugget);
+  const double factor = (m_noise_model == NoiseModel::Nugget) ? extra : 1.0;
+  std::vector<EvalOut> out;
+  m_bench.clear();
+  m_eval->evaluate(1, gamma.data(), &factor, return_grad, out, bench ? &m_bench : nullptr);
+  m_evals++;
+  std::vector<double> grad;
+  const double ll = loglik_from(out[0], extra, return_grad ? &grad : nullptr, (int)gamma.size());
+  return {ll, grad};
+}
+
+void Kriging::logLikelihoodFunBatch(const Mat& gammas, bool return_grad, std::vector<double>& ll,
+                                    std::vector<double>& grad) {
+  const int k = gammas.rows, gd = gammas.cols, d = m_d;
+  if (gd != d && !(gd == d + 1 && m_noise_model == NoiseModel::Nugget))
+    throw std::invalid_argument("logLikelihoodFunBatch: gamma rows should have length " + std::to_string(d));
+  ensure_engine(k);
+  std::vector<double> th((size_t)k * d), fac(k), extra(k);
+  for (int b = 0; b < k; ++b) {
+    for (int j = 0; j < d; ++j) th[(size_t)b * d + j] = gammas(b, j);
+    double e = (gd > d) ? gammas(b, d) : (m_noise_model == NoiseModel::Nugget ? m_alpha : m_sigma2);
+    if (m_noise_model == NoiseModel::Nugget && !m_est_sigma2 && !m_est_nugget) e = m_sigma2 / (m_sigma2 + m_nugget);
+    extra[b] = e;
+    fac[b] = (m_noise_model == NoiseModel::Nugget) ? e : 1.0;
+  }
+  std::vector<EvalOut> out;
+  m_eval->evaluate(k, th.data(), fac.data(), return_grad, out, nullptr);
+  m_evals += k;
+  ll.assign(k, 0.0);
+  grad.assign(return_grad ? (size_t)k * gd : 0, 0.0);
+  for (int b = 0; b < k; ++b) {
+    std::vector<double> g;
+    ll[b] = loglik_from(out[b], extra[b], return_grad ? &g : nullptr, gd);
+    if (return_grad) std::copy(g.begin(), g.end(), grad.begin() + (size_t)b * gd);
+  }
+}
+
+double Kriging::logLikelihood() {
+  std::vector<double> g = m_theta;
+  if (m_noise_model == NoiseModel::Nugget) g.push_back(m_alpha);
+  return std::get<0>(logLikelihoodFun(g, false, false));
+}
+
+// commit the model at (theta, alpha): one exact evaluation kept in the model engine (KModel -> m_T, m_M, ...)
+void Kriging::commit(const std::vector<double>& theta, double alpha) {
+  if (!m_model)
+    m_model = std::make_unique<Engine>(m_kernel, m_n, m_d, m_p, m_X.data(), m_y.data(), m_F.data(), 1);
+  const double factor = (m_noise_model == NoiseModel::Nugget) ? alpha : 1.0;
+  std::vector<EvalOut> out;
+  m_model->evaluate(1, theta.data(), &factor, false, out, nullptr);
+  if (out[0].status != 0) throw std::runtime_error(out[0].message);
+  m_last_commit = out[0];
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+void Kriging::fit(const std::vector<double>& y, const Mat& Xin, RegressionModel regmodel, bool normalize,
+                  const std::string& optim, const std::string& objective, const Parameters& parameters) {
+  const int n = Xin.rows, d = Xin.cols;
+  if ((int)y.size() != n)
+    throw std::runtime_error("Dimension of new data should be the same:\n X: (" + std::to_string(n) + "x" +
+                             std::to_string(d) + "), y: (" + std::to_string(y.size()) + ")");
+  if (objective != "LL")
+    throw std::invalid_argument("Unsupported fit objective for the GPU build: " + objective +
+                                " (supported is: LL; LLVecchia(m) through the Vecchia entry points)");
+  if (d > MAX_D) throw std::invalid_argument("input dimension d > 32 is not supported by the GPU kernels");
+  m_optim = optim;
+  m_objective = objective;
+  m_eval.reset();
+  m_model.reset();
+  // ---- fit_setup_impl (KrigingImpl.cpp:764-841) ----
+  m_n = n;
+  m_d = d;
+  m_normalize = normalize;
+  m_centerX.assign(d, 0.0);
+  m_scaleX.assign(d, 1.0);
+  m_centerY = 0.0;
+  m_scaleY = 1.0;
+  if (normalize) {
+    for (int j = 0; j < d; ++j) {
+      double mn = Xin(0, j), mx = Xin(0, j);
+      for (int i = 1; i < n; ++i) {
+        mn = std::min(mn, Xin(i, j));
+        mx = std::max(mx, Xin(i, j));
+      }
+      m_centerX[j] = mn;
+      m_scaleX[j] = mx - mn;
+    }
+    double mn = *std::min_element(y.begin(), y.end()), mx = *std::max_element(y.begin(), y.end());
+    m_centerY = mn;
+    m_scaleY = mx - mn;
+  }
+  m_X.resize((size_t)n * d);
+  for (int j = 0; j < d; ++j)
+    for (int i = 0; i < n; ++i) m_X[i + (size_t)j * n] = (Xin(i, j) - m_centerX[j]) / m_scaleX[j];
+  m_y.resize(n);
+  for (int i = 0; i < n; ++i) m_y[i] = (y[i] - m_centerY) / m_scaleY;
+  std::vector<double> maxdX(d);
+  for (int j = 0; j < d; ++j) {
+    double mn = m_X[(size_t)j * n], mx = mn;
+    for (int i = 1; i < n; ++i) {
+      mn = std::min(mn, m_X[i + (size_t)j * n]);
+      mx = std::max(mx, m_X[i + (size_t)j * n]);
+    }
+    maxdX[j] = mx - mn;
+  }
+  m_regmodel = regmodel;
+  m_F = regression_matrix(regmodel, m_X, n, d, &m_p);
+  m_est_beta = parameters.is_beta_estim && (m_regmodel != RegressionModel::None);
+  if (!m_est_beta && parameters.beta.has_value() && !parameters.beta->empty()) {
+    m_est_beta = false;
+    m_beta = *parameters.beta;
+    if (m_normalize)
+      for (auto& b : m_beta) b /= m_scaleY;
+  } else {
+    m_est_beta = true;
+  }
+  Mat theta0;
+  if (parameters.theta.has_value()) {
+    theta0 = *parameters.theta;
+    if (theta0.cols != d && theta0.rows == d) {  // transpose
+      Mat t;
+      t.rows = theta0.cols;
+      t.cols = theta0.rows;
+      t.v.resize(theta0.v.size());
+      for (int i = 0; i < t.rows; ++i)
+        for (int j = 0; j < t.cols; ++j) t(i, j) = theta0(j, i);
+      theta0 = t;
+    }
+    if (m_normalize)
+      for (int i = 0; i < theta0.rows; ++i)
+        for (int j = 0; j < theta0.cols; ++j) theta0(i, j) /= m_scaleX[j];
+    if (theta0.cols != d)
+      throw std::runtime_error("Dimension of theta should be nx" + std::to_string(d) + " instead of " +
+                               std::to_string(theta0.rows) + "x" + std::to_string(theta0.cols));
+  }
+  const Config& cfg = config();
+
+  if (optim == "none") {  // Kriging.cpp:1633-1715
+    if (!parameters.theta.has_value())
+      throw std::runtime_error("Theta should be given (1x" + std::to_string(d) + ") matrix, when optim=none");
+    m_theta.resize(d);
+    for (int j = 0; j < d; ++j) m_theta[j] = theta0(0, j);
+    m_est_theta = false;
+    double sigma2 = -1;
+    m_est_sigma2 = parameters.is_sigma2_estim;
+    if (parameters.sigma2.has_value()) {
+      sigma2 = *parameters.sigma2;
+      if (m_normalize) sigma2 /= (m_scaleY * m_scaleY);
+    } else {
+      m_est_sigma2 = true;
+    }
+    double nugget_param = 0.0;
+    if (m_noise_model == NoiseModel::Nugget) {
+      m_est_nugget = parameters.is_nugget_estim;
+      if (parameters.nugget.has_value()) {
+        nugget_param = *parameters.nugget;
+        if (m_normalize) nugget_param /= (m_scaleY * m_scaleY);
+      }
+      if (sigma2 > 0 && (sigma2 + nugget_param) > 0)
+        m_alpha = sigma2 / (sigma2 + nugget_param);
+      else
+        m_alpha = 1.0 - kNuggetAlphaLower;
+    }
+    commit(m_theta, m_alpha);
+    const EvalOut& m = m_last_commit;
+    m_is_empty = false;
+    if (m_est_beta) m_beta = m.beta;
+    if (m_noise_model == NoiseModel::Nugget) {
+      if (m_est_sigma2) {
+        const double total_var = m.sse / n;
+        m_sigma2 = m_alpha * total_var;
+        m_nugget = m_est_nugget ? (1.0 - m_alpha) * total_var : nugget_param;
+      } else {
+        m_sigma2 = sigma2;
+        m_nugget = m_est_nugget ? 0.0 : nugget_param;
+      }
+    } else if (m_est_sigma2) {
+      m_sigma2 = m.sse / n;
+    } else {
+      m_sigma2 = sigma2;
+    }
+    return;
+  }
+
+  // ---- BFGS[N] (Kriging.cpp:1717-2209) ----
+  if (optim.rfind("BFGS", 0) != 0)
+    throw std::runtime_error("Unsupported optim: " + optim + " (supported are: none, BFGS[#])");
+  std::vector<double> theta_lower(d), theta_upper(d);
+  {
+    // Optim::theta_bounds (Optim.cpp:179-209) with dX recomputed from X
+    for (int j = 0; j < d; ++j) {
+      theta_lower[j] = cfg.theta_lower_factor * maxdX[j];
+      theta_upper[j] = cfg.theta_upper_factor * maxdX[j];
+    }
+    if (cfg.variogram_bounds_heuristic && n > 0) {
+      double wsum = 0.0;
+      std::vector<double> steep(d, 0.0);
+      std::vector<double> dx(d);
+      for (int i = 0; i < n; ++i) {
+        for (int j = 0; j < n; ++j) {
+          if (i == j) continue;
+          double dx2 = 0.0;
+          for (int k = 0; k < d; ++k) {
+            dx[k] = m_X[i + (size_t)k * n] - m_X[j + (size_t)k * n];
+            dx2 += dx[k] * dx[k];
+          }
+          const double dyv = m_y[i] - m_y[j];
+          double slope = (dyv * dyv) / dx2;
+          if (std::isnan(slope)) slope = 0.0;
+          wsum += slope;
+          for (int k = 0; k < d; ++k) steep[k] += std::fabs(dx[k]) * slope;
+        }
+      }
+      if (wsum > 0.0) {
+        for (int k = 0; k < d; ++k) {
+          const double s = steep[k] / wsum;
+          theta_lower[k] = std::max(theta_lower[k], cfg.theta_lower_factor * s);
+          theta_lower[k] = std::min(theta_lower[k], theta_upper[k]);
+          theta_upper[k] = std::max(theta_lower[k], theta_upper[k]);
+        }
+      }
+    }
+  }
+  rng_engine().seed(rng_seed());  // Random::init()
+  int multistart = parse_method(optim, "BFGS").second;
+  Mat U = randu_mat(multistart, d);
+  Mat theta0_rand;
+  theta0_rand.rows = multistart;
+  theta0_rand.cols = d;
+  theta0_rand.v.resize((size_t)multistart * d);
+  for (int i = 0; i < multistart; ++i)
+    for (int j = 0; j < d; ++j) theta0_rand(i, j) = theta_lower[j] + U(i, j) * (theta_upper[j] - theta_lower[j]);
+  Mat starts;
+  if (parameters.theta.has_value()) {
+    multistart = std::max(multistart, theta0.rows);
+    starts.rows = multistart;
+    starts.cols = d;
+    starts.v.resize((size_t)multistart * d);
+    for (int i = 0; i < multistart; ++i)
+      for (int j = 0; j < d; ++j) starts(i, j) = (i < theta0.rows) ? theta0(i, j) : theta0_rand(i - theta0.rows, j);
+  } else {
+    starts = theta0_rand;
+  }
+  std::vector<double> extra0;
+  double extra_lower = 0.0, extra_upper = 1.0;
+  if (m_noise_model == NoiseModel::Nugget) {
+    extra_lower = kNuggetAlphaLower;
+    extra_upper = 1.0;
+    if (parameters.sigma2.has_value() && parameters.nugget.has_value()) {
+      const double s = *parameters.sigma2, nu = *parameters.nugget;
+      extra0 = {(s > 0 && (s + nu) > 0) ? s / (s + nu) : extra_lower + (extra_upper - extra_lower) * 0.5};
+    } else {
+      std::vector<double> u = randu_vec(starts.rows);
+      extra0.resize(u.size());
+      for (size_t i = 0; i < u.size(); ++i)
+        extra0[i] = extra_lower + (extra_upper - extra_lower) * (1.0 - std::pow(u[i], 3.0));
+    }
+  }
+  const bool nug = (m_noise_model == NoiseModel::Nugget);
+  const int gd = d + (nug ? 1 : 0);
+  auto reparam_to = [&](const std::vector<double>& ta) {  // nugget_reparam_to / Optim::reparam_to
+    std::vector<double> g(ta.size());
+    for (int j = 0; j < d; ++j) g[j] = cfg.reparametrize ? std::log(ta[j]) : ta[j];
+    if (nug) g[d] = cfg.reparametrize ? -std::log(1.0 + kNuggetAlphaLower - ta[d]) : ta[d];
+    return g;
+  };
+  auto reparam_from = [&](const std::vector<double>& g) {
+    std::vector<double> ta(g.size());
+    for (int j = 0; j < d; ++j) ta[j] = cfg.reparametrize ? std::exp(g[j]) : g[j];
+    if (nug) ta[d] = cfg.reparametrize ? 1.0 + kNuggetAlphaLower - std::exp(-g[d]) : g[d];
+    return ta;
+  };
+  std::vector<double> bl(gd), bu(gd);
+  for (int j = 0; j < d; ++j) {
+    bl[j] = theta_lower[j];
+    bu[j] = theta_upper[j];
+  }
+  if (nug) {
+    bl[d] = extra_lower;
+    bu[d] = extra_upper;
+  }
+  const std::vector<double> gamma_lower = reparam_to(bl), gamma_upper = reparam_to(bu);
+  // estimation flags (Kriging.cpp:1841-1859)
+  m_est_sigma2 = parameters.is_sigma2_estim;
+  if (!m_est_sigma2 && parameters.sigma2.has_value()) {
+    m_sigma2 = *parameters.sigma2;
+    if (m_normalize) m_sigma2 /= (m_scaleY * m_scaleY);
+  } else {
+    m_est_sigma2 = true;
+  }
+  if (nug) {
+    m_est_nugget = parameters.is_nugget_estim;
+    if (!m_est_nugget && parameters.nugget.has_value()) {
+      m_nugget = *parameters.nugget;
+      if (m_normalize) m_nugget /= (m_scaleY * m_scaleY);
+    } else {
+      m_est_nugget = true;
+    }
+  }
+  ensure_engine(multistart);
+
+  // batched objective: -LL in gamma space (make_fit_objective, Kriging.cpp:1414-1470)
+  Batcher batcher(multistart, [&](std::vector<EvalRequest*>& reqs) {
+    const int k = (int)reqs.size();
+    std::vector<double> th((size_t)k * d), fac(k);
+    bool g = false;
+    for (int b = 0; b < k; ++b) {
+      std::copy(reqs[b]->theta.begin(), reqs[b]->theta.begin() + d, th.begin() + (size_t)b * d);
+      fac[b] = reqs[b]->factor;
+      g = g || reqs[b]->want_grad;
+    }
+    std::vector<EvalOut> out;
+    m_eval->evaluate(k, th.data(), fac.data(), g, out, nullptr);
+    m_evals += k;
+    for (int b = 0; b < k; ++b) reqs[b]->out = std::move(out[b]);
+  });
+  auto eval_ll = [&](const std::vector<double>& ta, bool want_grad, std::vector<double>* grad) {
+    EvalRequest req;
+    req.theta.assign(ta.begin(), ta.begin() + d);
+    double extra = nug ? ta[d] : m_sigma2;
+    if (nug && !m_est_sigma2 && !m_est_nugget) extra = m_sigma2 / (m_sigma2 + m_nugget);
+    req.factor = nug ? extra : 1.0;
+    req.want_grad = want_grad;
+    batcher.submit(&req);
+    if (req.err) std::rethrow_exception(req.err);
+    return loglik_from(req.out, extra, grad, gd);
+  };
+  auto fit_ofn = [&](const std::vector<double>& gamma, std::vector<double>* grad_out) {
+    const std::vector<double> ta = reparam_from(gamma);
+    std::vector<double> g;
+    const double ll = eval_ll(ta, grad_out != nullptr, grad_out ? &g : nullptr);
+    if (grad_out) {
+      grad_out->resize(gd);
+      for (int j = 0; j < d; ++j) (*grad_out)[j] = -(cfg.reparametrize ? g[j] * ta[j] : g[j]);
+      if (nug) (*grad_out)[d] = -(cfg.reparametrize ? g[d] * (1.0 + kNuggetAlphaLower - ta[d]) : g[d]);
+    }
+    return -ll;
+  };
+
+  struct Result {
+    bool success = false;
+    double objective = std::numeric_limits<double>::infinity();
+    std::vector<double> theta;
+    double extra = 0.0;
+    std::string error;
+  };
+  std::vector<Result> results(multistart);
+  auto worker = [&](int s) {
+    Result& res = results[s];
+    try {
+      std::vector<double> theta_start(d);
+      for (int j = 0; j < d; ++j) theta_start[j] = starts(s, j);
+      std::vector<double> ta(theta_start);
+      if (nug) ta.push_back(extra0[s % extra0.size()]);
+      std::vector<double> gamma_tmp = reparam_to(ta);
+      std::vector<double> lo(gd), hi(gd);
+      for (int j = 0; j < gd; ++j) {
+        lo[j] = std::min(gamma_tmp[j], gamma_lower[j]);
+        hi[j] = std::max(gamma_tmp[j], gamma_upper[j]);
+      }
+      Lbfgsb opt(gd);
+      opt.iprint = -1;
+      opt.max_iter = cfg.max_iteration;
+      opt.pgtol = cfg.gradient_tolerance;
+      opt.factr = cfg.objective_rel_tolerance / 1e-13;
+      std::vector<int> btype(gd, 2);
+      int retry = 0;
+      double best_f = std::numeric_limits<double>::infinity();
+      std::vector<double> best_gamma = gamma_tmp;
+      while (retry <= cfg.max_restart) {
+        LbfgsbResult r = opt.minimize(
+            [&](const std::vector<double>& x, std::vector<double>& g) { return fit_ofn(x, &g); }, gamma_tmp,
+            lo.data(), hi.data(), btype.data());
+        if (r.f_opt < best_f) {
+          best_f = r.f_opt;
+          best_gamma = gamma_tmp;
+        }
+        std::vector<double> tp = reparam_from(gamma_tmp);
+        double sol_to_lb = std::numeric_limits<double>::infinity();
+        for (int j = 0; j < d; ++j) sol_to_lb = std::min(sol_to_lb, std::fabs(tp[j] - theta_lower[j]));
+        if (retry < cfg.max_restart &&
+            (r.task.rfind("ABNORMAL_TERMINATION_IN_LNSRCH", 0) == 0 || r.num_iters <= 2 ||
+             sol_to_lb < std::numeric_limits<double>::epsilon() || r.f_opt > best_f)) {
+          std::vector<double> rt(d);
+          for (int j = 0; j < d; ++j) rt[j] = (theta_start[j] + theta_lower[j]) / std::pow(2.0, retry + 1);
+          std::vector<double> ta2(rt);
+          if (nug) ta2.push_back(extra0[s % extra0.size()]);
+          gamma_tmp = reparam_to(ta2);
+          for (int j = 0; j < gd; ++j) {
+            lo[j] = std::min(gamma_tmp[j], lo[j]);
+            hi[j] = std::max(gamma_tmp[j], hi[j]);
+          }
+          retry++;
+        } else {
+          break;
+        }
+      }
+      res.objective = fit_ofn(best_gamma, nullptr);  // final evaluation at the best point
+      std::vector<double> ta_best = reparam_from(best_gamma);
+      res.theta.assign(ta_best.begin(), ta_best.begin() + d);
+      res.extra = nug ? ta_best[d] : 0.0;
+      res.success = true;
+    } catch (const std::exception& e) {
+      res.success = false;
+      res.error = e.what();
+    }
+    batcher.leave();
+  };
+  {
+    std::vector<std::thread> threads;
+    threads.reserve(multistart);
+    for (int s = 0; s < multistart; ++s) threads.emplace_back(worker, s);
+    for (auto& t : threads) t.join();
+  }
+  int best = -1, ok = 0;
+  double min_ofn = std::numeric_limits<double>::infinity();
+  for (int s = 0; s < multistart; ++s) {
+    if (!results[s].success) continue;
+    ok++;
+    if (results[s].objective < min_ofn) {
+      min_ofn = results[s].objective;
+      best = s;
+    }
+  }
+  if (ok == 0) throw std::runtime_error("All " + std::to_string(multistart) + " optimization attempts failed");
+  const Result& b = results[best];
+  m_theta = b.theta;
+  m_est_theta = true;
+  m_is_empty = false;
+  if (nug) m_alpha = b.extra;
+  commit(m_theta, m_alpha);
+  const EvalOut& m = m_last_commit;
+  if (m_est_beta) m_beta = m.beta;
+  if (nug) {
+    if (m_est_sigma2) {
+      if (m_est_nugget) {
+        const double total_var = m.sse / n;
+        m_sigma2 = m_alpha * total_var;
+        m_nugget = m_sigma2 / m_alpha - m_sigma2;
+      } else {
+        m_sigma2 = m_nugget * m_alpha / (1.0 - m_alpha);
+      }
+    } else {
+      if (m_est_nugget) m_nugget = m_sigma2 * (1.0 - m_alpha) / m_alpha;
+    }
+  } else if (m_est_sigma2) {
+    m_sigma2 = m.sse / n;
+  }
+  m_last_fit_starts = multistart;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+Mat Kriging::T() const {
+  Mat m;
+  if (!m_model) return m;
+  m.rows = m.cols = m_n;
+  m_model->copy_model(0, &m.v, nullptr, nullptr, nullptr, nullptr);
+  return m;
+}
+
+Mat Kriging::M() const {
+  Mat m;
+  if (!m_model) return m;
+  m.rows = m_n;
+  m.cols = m_p;
+  m_model->copy_model(0, nullptr, &m.v, nullptr, nullptr, nullptr);
+  return m;
+}
+
+std::vector<double> Kriging::z() const {
+  std::vector<double> z;
+  if (!m_model) return z;
+  if (m_est_beta) {
+    m_model->copy_model(0, nullptr, nullptr, nullptr, nullptr, &z);
+  } else {  // m_z = ystar - M beta
+    std::vector<double> ystar, Fs;
+    m_model->copy_model(0, nullptr, &Fs, &ystar, nullptr, nullptr);
+    z = ystar;
+    for (int i = 0; i < m_n; ++i)
+      for (int q = 0; q < m_p; ++q) z[i] -= Fs[i + (size_t)q * m_n] * m_beta[q];
+  }
+  return z;
+}
+
+std::tuple<std::vector<double>, std::vector<double>, Mat, Mat, Mat> Kriging::predict(const Mat& X_n, bool return_stdev,
+                                                                                      bool return_cov,
+                                                                                      bool return_deriv) {
+  if (m_is_empty || !m_model) throw std::runtime_error("predict: model is not fitted");
+  if (X_n.cols != m_d)
+    throw std::runtime_error("Predict locations have wrong dimension: " + std::to_string(X_n.cols) + " instead of " +
+                             std::to_string(m_d));
+  if (return_deriv) throw std::invalid_argument("predict: return_deriv is not supported by the GPU build");
+  const int q = X_n.rows, d = m_d, n = m_n, p = m_p;
+  const bool nug = (m_noise_model == NoiseModel::Nugget);
+  const double R_on_factor = nug ? m_alpha : 1.0;
+  const double var_scale = nug ? m_sigma2 / m_alpha : m_sigma2;
+  Mat Xnn;
+  Xnn.rows = q;
+  Xnn.cols = d;
+  Xnn.v.resize((size_t)q * d);
+  for (int j = 0; j < d; ++j)
+    for (int i = 0; i < q; ++i) Xnn(i, j) = (X_n(i, j) - m_centerX[j]) / m_scaleX[j];
+  int pn = 0;
+  std::vector<double> Fn = regression_matrix(m_regmodel, Xnn.v, q, d, &pn);
+  std::vector<double> zz = z();
+  PredictOut po = predict_gpu(*m_model, Xnn.v.data(), q, m_theta.data(), R_on_factor, zz.data(), return_stdev || return_cov,
+                              return_cov, nug ? m_alpha : 1.0, nug);
+  // yhat = F_n beta + Rstar_on' z
+  std::vector<double> mean(q), sd;
+  for (int i = 0; i < q; ++i) {
+    double fb = 0.0;
+    for (int k = 0; k < p; ++k) fb += Fn[i + (size_t)k * q] * m_beta[k];
+    mean[i] = m_centerY + m_scaleY * (fb + po.rz[i]);
+  }
+  Mat cov, md, sdd;
+  if (return_stdev || return_cov) {
+    // Ecirc = (F_n - Rstar_on' M) * circ^-1   (rsolve_upper)
+    std::vector<double> Rstar;
+    m_model->copy_model(0, nullptr, nullptr, nullptr, &Rstar, nullptr);
+    std::vector<double> Ec((size_t)q * p);
+    for (int i = 0; i < q; ++i) {
+      for (int k = 0; k < p; ++k) {
+        double e = Fn[i + (size_t)k * q] - po.rm[(size_t)i * p + k];
+        for (int l = 0; l < k; ++l) e -= Ec[i + (size_t)l * q] * Rstar[l + (size_t)k * p];
+        Ec[i + (size_t)k * q] = e / Rstar[k + (size_t)k * p];
+      }
+    }
+    if (return_stdev) {
+      sd.resize(q);
+      for (int i = 0; i < q; ++i) {
+        double e2 = 0.0;
+        for (int k = 0; k < p; ++k) e2 += Ec[i + (size_t)k * q] * Ec[i + (size_t)k * q];
+        double v = 1.0 - po.rr[i] + e2;
+        if (std::isnan(v) || v < 0) v = 0.0;
+        v *= var_scale * m_scaleY * m_scaleY;
+        sd[i] = std::sqrt(v);
+      }
+    }
+    if (return_cov) {
+      cov.rows = cov.cols = q;
+      cov.v = po.sigma;  // R_nn - Rstar_on' Rstar_on
+      for (int i = 0; i < q; ++i)
+        for (int j = 0; j < q; ++j) {
+          double e = 0.0;
+          for (int k = 0; k < p; ++k) e += Ec[i + (size_t)k * q] * Ec[j + (size_t)k * q];
+          cov(i, j) = (cov(i, j) + e) * var_scale * m_scaleY * m_scaleY;
+        }
+    }
+  }
+  return {mean, sd, cov, md, sdd};
+}
+
+std::string Kriging::summary() const {
+  std::ostringstream o;
+  o << "* data: " << m_n << "x" << m_d << "\n";
+  o << "* trend " << regmodel_to_string(m_regmodel) << (m_est_beta ? " (est.)" : "") << ": ";
+  for (double b : m_beta) o << b << " ";
+  o << "\n* variance" << (m_est_sigma2 ? " (est.)" : "") << ": " << m_sigma2 << "\n";
+  o << "* covariance:\n  * kernel: " << m_covType << "\n  * range" << (m_est_theta ? " (est.)" : "") << ": ";
+  for (double t : m_theta) o << t << " ";
+  if (m_noise_model == NoiseModel::Nugget) o << "\n  * nugget" << (m_est_nugget ? " (est.)" : "") << ": " << m_nugget;
+  o << "\n  * fit:\n    * objective: " << m_objective << "\n    * optim: " << m_optim << "\n";
+  return o.str();
+}
+
+}  // namespace lkg

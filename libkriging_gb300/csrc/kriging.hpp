@@ -1,0 +1,131 @@
+// kriging.hpp -- GPU-backed Kriging facade with libKriging's Kriging API (src/lib/include/libKriging/Kriging.hpp).
+//
+// Same method names, argument meaning, defaults and error behaviour as the reference for the likelihood path:
+//   Kriging(covType, NoiseModel)                         Kriging.hpp:78-79
+//   fit(y, X, regmodel, normalize, optim, objective, P)  Kriging.hpp:113-119, Kriging.cpp:1591-2215
+//   logLikelihoodFun(gamma, return_grad, bench)          Kriging.hpp:131-133, Kriging.cpp:214-349
+//   predict(X_n, return_stdev, return_cov, return_deriv) Kriging.hpp:215-218, KrigingImpl.cpp:145-300
+// Matrices are column-major std::vector<double> with explicit sizes (the reference uses arma::mat).
+#pragma once
+#include <map>
+#include <memory>
+#include <optional>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "engine.hpp"
+
+namespace lkg {
+
+enum class RegressionModel { None = 0, Constant = 1, Linear = 2, Interactive = 3, Quadratic = 4 };
+RegressionModel regmodel_from_string(const std::string& s);
+const char* regmodel_to_string(RegressionModel r);
+// Trend::regressionModelMatrix (src/lib/Trend.cpp:34-91): X n x d column-major -> F n x p
+std::vector<double> regression_matrix(RegressionModel r, const std::vector<double>& X, int n, int d, int* p_out);
+
+struct Mat {  // column-major matrix
+  int rows = 0, cols = 0;
+  std::vector<double> v;
+  double& operator()(int i, int j) { return v[i + (size_t)j * rows]; }
+  double operator()(int i, int j) const { return v[i + (size_t)j * rows]; }
+};
+
+struct Parameters {  // KrigingParameters (Kriging.hpp:18-28)
+  std::optional<double> sigma2;
+  bool is_sigma2_estim = true;
+  std::optional<Mat> theta;  // rows = starting points
+  bool is_theta_estim = true;
+  std::optional<std::vector<double>> beta;
+  bool is_beta_estim = true;
+  std::optional<double> nugget;
+  bool is_nugget_estim = true;
+};
+
+class Kriging {
+ public:
+  enum class NoiseModel { None, Nugget };
+
+  explicit Kriging(const std::string& covType, NoiseModel nm = NoiseModel::None);
+  ~Kriging();
+
+  void fit(const std::vector<double>& y, const Mat& X, RegressionModel regmodel = RegressionModel::Constant,
+           bool normalize = false, const std::string& optim = "BFGS", const std::string& objective = "LL",
+           const Parameters& parameters = {});
+
+  // gamma = theta (None) or [theta, alpha] (Nugget)
+  std::tuple<double, std::vector<double>> logLikelihoodFun(const std::vector<double>& gamma, bool return_grad,
+                                                           bool bench);
+  // Batched objective: gammas rows = candidates (k x gdim).  ll[k], grad[k x gdim] (row-major per candidate).
+  void logLikelihoodFunBatch(const Mat& gammas, bool return_grad, std::vector<double>& ll,
+                             std::vector<double>& grad);
+  double logLikelihood();
+
+  // mean, stdev, cov, mean_deriv, stdev_deriv
+  std::tuple<std::vector<double>, std::vector<double>, Mat, Mat, Mat> predict(const Mat& X_n, bool return_stdev,
+                                                                                bool return_cov, bool return_deriv);
+
+  // accessors (KrigingImpl.hpp:40-60, Kriging.hpp:94-97)
+  const std::string& kernel() const { return m_covType; }
+  NoiseModel noise_model() const { return m_noise_model; }
+  const std::vector<double>& theta() const { return m_theta; }
+  double sigma2() const { return m_sigma2; }
+  const std::vector<double>& beta() const { return m_beta; }
+  double nugget() const { return m_nugget; }
+  double alpha() const { return m_alpha; }
+  bool is_sigma2_estim() const { return m_est_sigma2; }
+  bool is_theta_estim() const { return m_est_theta; }
+  bool is_beta_estim() const { return m_est_beta; }
+  bool is_nugget_estim() const { return m_est_nugget; }
+  bool is_normalize() const { return m_normalize; }
+  const std::string& optim() const { return m_optim; }
+  const std::string& objective() const { return m_objective; }
+  RegressionModel regmodel() const { return m_regmodel; }
+  int n() const { return m_n; }
+  int d() const { return m_d; }
+  int p() const { return m_p; }
+  const std::vector<double>& X() const { return m_X; }
+  const std::vector<double>& y() const { return m_y; }
+  const std::vector<double>& centerX() const { return m_centerX; }
+  const std::vector<double>& scaleX() const { return m_scaleX; }
+  double centerY() const { return m_centerY; }
+  double scaleY() const { return m_scaleY; }
+  // committed factor and whitened quantities (m_T, m_M, m_z, m_circ) copied to host on demand
+  Mat T() const;
+  Mat M() const;
+  std::vector<double> z() const;
+  std::string summary() const;
+
+  // per-stage timings of the last logLikelihoodFun(..., bench=true) call (Bench keys of the reference)
+  const std::map<std::string, double>& last_bench() const { return m_bench; }
+  // total evaluations performed by the engine since construction (objective calls, batched entries counted once each)
+  long long evaluations() const { return m_evals; }
+
+ private:
+  double loglik_from(const EvalOut& o, double extra_param, std::vector<double>* grad, int gdim) const;
+  void ensure_engine(int batch_cap);
+  void commit(const std::vector<double>& theta, double alpha);
+
+  std::string m_covType;
+  int m_kernel;
+  NoiseModel m_noise_model;
+  int m_n = 0, m_d = 0, m_p = 0;
+  std::vector<double> m_X, m_y, m_F;  // normalised
+  std::vector<double> m_centerX, m_scaleX;
+  double m_centerY = 0.0, m_scaleY = 1.0;
+  bool m_normalize = false;
+  RegressionModel m_regmodel = RegressionModel::Constant;
+  std::string m_optim = "BFGS", m_objective = "LL";
+  std::vector<double> m_theta, m_beta;
+  double m_sigma2 = 0.0, m_nugget = 0.0, m_alpha = 1.0;
+  bool m_est_theta = false, m_est_sigma2 = false, m_est_beta = true, m_est_nugget = false;
+  bool m_is_empty = true;
+  std::unique_ptr<Engine> m_eval;   // objective evaluations (batch capacity grows as needed)
+  std::unique_ptr<Engine> m_model;  // committed model (predict)
+  std::map<std::string, double> m_bench;
+  long long m_evals = 0;
+  EvalOut m_last_commit;
+  int m_last_fit_starts = 0;
+};
+
+}  // namespace lkg

@@ -1,0 +1,435 @@
+// lik_kernels.cu -- covariance build, adjoint gradient and likelihood reductions (sm_103a).
+//
+// Reference routines these kernels replace (libKriging source tree):
+//   cov_build_lower   LinearAlgebra::cholCov pair loop + "R *= factor" + diag  (src/lib/LinearAlgebra.cpp:142-181)
+//                     with dX recomputed from X instead of the n^2 x d cube of compute_dX (:440-485)
+//   adjoint_sums      KrigingImpl::compute_ll_grad_theta_vecs (src/lib/KrigingImpl.cpp:855-885) and the Nugget
+//                     alpha-gradient dot products of Kriging::_logLikelihood (src/lib/Kriging.cpp:307-326)
+//   gram/gls/residual KrigingImpl::populate_Model GLS block (src/lib/KrigingImpl.cpp:101-124)
+//   cov_cross         KrigingImpl::predict_impl R_on loop (src/lib/KrigingImpl.cpp:194-221)
+#include "lik_kernels.cuh"
+
+namespace lkg {
+
+namespace {
+
+constexpr int T = 64;  // tile edge
+
+__device__ __forceinline__ void lower_tile_of(int64_t x, int& I, int& J) {
+  I = (int)((sqrt(8.0 * (double)x + 1.0) - 1.0) * 0.5);
+  while ((int64_t)(I + 1) * (I + 2) / 2 <= x) ++I;
+  while ((int64_t)I * (I + 1) / 2 > x) --I;
+  J = (int)(x - (int64_t)I * (I + 1) / 2);
+}
+
+// deterministic block sum (fixed shuffle tree, then warps in order); every thread gets the result
+template <int NTH>
+__device__ __forceinline__ double block_sum(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  for (int i = 0; i < NTH / 32; ++i) s += red[i];
+  return s;
+}
+
+template <int K, int DM>
+__global__ void __launch_bounds__(256) k_cov_lower(int n, int d, const double* __restrict__ X, int64_t xb,
+                                                   const double* __restrict__ theta, const double* __restrict__ factor,
+                                                   const double* __restrict__ diag, double* __restrict__ A,
+                                                   int64_t lda, int64_t mstride) {
+  int I, J;
+  lower_tile_of(blockIdx.x, I, J);
+  const int64_t b = blockIdx.z;
+  __shared__ double xi[DM][T], xj[DM][T], th[DM];
+  const int r0 = I * T, c0 = J * T, t = threadIdx.x;
+  const double* Xb = X + b * xb;
+  for (int idx = t; idx < DM * T; idx += 256) {
+    const int k = idx / T, q = idx % T;
+    xi[k][q] = (k < d && r0 + q < n) ? Xb[(r0 + q) + (int64_t)k * n] : 0.0;
+    xj[k][q] = (k < d && c0 + q < n) ? Xb[(c0 + q) + (int64_t)k * n] : 0.0;
+  }
+  if (t < DM) th[t] = (t < d) ? theta[b * d + t] : 1.0;
+  __syncthreads();
+  const double f = factor[b], dv = diag[b];
+  const int ri = t & 63, i = r0 + ri;
+  if (i >= n) return;
+  double* Ab = A + b * mstride;
+  double xr[DM];
+#pragma unroll
+  for (int k = 0; k < DM; ++k) xr[k] = xi[k][ri];
+  for (int s = 0; s < 16; ++s) {
+    const int cj = (t >> 6) + 4 * s, j = c0 + cj;
+    if (j >= n || j > i) continue;
+    double v;
+    if (j == i) {
+      v = dv;
+    } else {
+      double sum = 0.0;
+#pragma unroll
+      for (int k = 0; k < DM; ++k)
+        if (k < d) sum += cov_term<K>(xj[k][cj] - xr[k], th[k]);
+      v = cov_from_sum<K>(sum) * f;
+    }
+    Ab[i + (int64_t)j * lda] = v;
+  }
+}
+
+template <int K, int DM>
+__global__ void __launch_bounds__(256) k_cov_cross(int n_o, int q, int d, const double* __restrict__ Xo,
+                                                   const double* __restrict__ Xn, const double* __restrict__ theta,
+                                                   double factor, double* __restrict__ R) {
+  __shared__ double xo[DM][T], xn[DM][T], th[DM];
+  const int r0 = blockIdx.x * T, c0 = blockIdx.y * T, t = threadIdx.x;
+  for (int idx = t; idx < DM * T; idx += 256) {
+    const int k = idx / T, qq = idx % T;
+    xo[k][qq] = (k < d && r0 + qq < n_o) ? Xo[(r0 + qq) + (int64_t)k * n_o] : 0.0;
+    xn[k][qq] = (k < d && c0 + qq < q) ? Xn[(c0 + qq) + (int64_t)k * q] : 0.0;
+  }
+  if (t < DM) th[t] = (t < d) ? theta[t] : 1.0;
+  __syncthreads();
+  const int ri = t & 63, i = r0 + ri;
+  if (i >= n_o) return;
+  for (int s = 0; s < 16; ++s) {
+    const int cj = (t >> 6) + 4 * s, j = c0 + cj;
+    if (j >= q) continue;
+    double sum = 0.0;
+    bool coincident = true;
+#pragma unroll
+    for (int k = 0; k < DM; ++k) {
+      if (k < d) {
+        const double dx = xo[k][ri] - xn[k][cj];
+        coincident = coincident && (fabs(dx) <= 2.220446049250313e-16);
+        sum += cov_term<K>(dx, th[k]);
+      }
+    }
+    R[i + (int64_t)j * n_o] = coincident ? 1.0 : cov_from_sum<K>(sum) * factor;
+  }
+}
+
+template <int K, int DM>
+__global__ void __launch_bounds__(256) k_adjoint(int n, int d, const double* __restrict__ X, int64_t xb,
+                                                 const double* __restrict__ theta, const double* __restrict__ factor,
+                                                 const double* __restrict__ xv, int64_t xvb,
+                                                 const double* __restrict__ Rinv, int64_t ldr, int64_t rstride,
+                                                 double* __restrict__ partials, int64_t ntiles) {
+  int I, J;
+  lower_tile_of(blockIdx.x, I, J);
+  const int64_t b = blockIdx.z;
+  constexpr int NA = 2 * DM + 4;
+  __shared__ double xi[DM][T], xj[DM][T], th[DM], vi[T], vj[T];
+  __shared__ double red[NA][8];
+  const int r0 = I * T, c0 = J * T, t = threadIdx.x;
+  const double* Xb = X + b * xb;
+  for (int idx = t; idx < DM * T; idx += 256) {
+    const int k = idx / T, q = idx % T;
+    xi[k][q] = (k < d && r0 + q < n) ? Xb[(r0 + q) + (int64_t)k * n] : 0.0;
+    xj[k][q] = (k < d && c0 + q < n) ? Xb[(c0 + q) + (int64_t)k * n] : 0.0;
+  }
+  if (t < T) {
+    vi[t] = (r0 + t < n) ? xv[b * xvb + r0 + t] : 0.0;
+    vj[t] = (c0 + t < n) ? xv[b * xvb + c0 + t] : 0.0;
+  }
+  if (t < DM) th[t] = (t < d) ? theta[b * d + t] : 1.0;
+  __syncthreads();
+  const double f = factor[b];
+  double t1[DM], t2[DM];
+#pragma unroll
+  for (int k = 0; k < DM; ++k) t1[k] = t2[k] = 0.0;
+  double u1 = 0.0, u2 = 0.0, d1 = 0.0, d2 = 0.0;
+  const int ri = t & 63, i = r0 + ri;
+  const double* Rb = Rinv + b * rstride;
+  if (i < n) {
+    double xr[DM];
+#pragma unroll
+    for (int k = 0; k < DM; ++k) xr[k] = xi[k][ri];
+    const double x_i = vi[ri];
+    for (int s = 0; s < 16; ++s) {
+      const int cj = (t >> 6) + 4 * s, j = c0 + cj;
+      if (j >= n || j > i) continue;
+      const double rinv = Rb[i + (int64_t)j * ldr];
+      if (j == i) {
+        d1 += x_i * x_i;
+        d2 += rinv;
+        continue;
+      }
+      double dxk[DM];
+      double sum = 0.0;
+#pragma unroll
+      for (int k = 0; k < DM; ++k) {
+        dxk[k] = xj[k][cj] - xr[k];
+        if (k < d) sum += cov_term<K>(dxk[k], th[k]);
+      }
+      const double c = cov_from_sum<K>(sum);
+      const double rij = c * f;
+      const double wx = x_i * vj[cj];
+      u1 += wx * c;
+      u2 += rinv * c;
+#pragma unroll
+      for (int k = 0; k < DM; ++k) {
+        if (k < d) {
+          const double g = rij * dlncov_term<K>(dxk[k], th[k]);
+          t1[k] += wx * g;
+          t2[k] += rinv * g;
+        }
+      }
+    }
+  }
+  // deterministic block reduction of the NA accumulators
+  const int w = t >> 5, l = t & 31;
+  auto wred = [&](double v, int a) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (l == 0) red[a][w] = v;
+  };
+#pragma unroll
+  for (int k = 0; k < DM; ++k) {
+    wred(t1[k], k);
+    wred(t2[k], DM + k);
+  }
+  wred(u1, 2 * DM);
+  wred(u2, 2 * DM + 1);
+  wred(d1, 2 * DM + 2);
+  wred(d2, 2 * DM + 3);
+  __syncthreads();
+  // compact layout: [T1(d), T2(d), U1, U2, D1, D2]
+  const int nacc = 2 * d + 4;
+  if (t < nacc) {
+    int a;
+    if (t < d) a = t;
+    else if (t < 2 * d) a = DM + (t - d);
+    else a = 2 * DM + (t - 2 * d);
+    double s = 0.0;
+    for (int q = 0; q < 8; ++q) s += red[a][q];
+    partials[(b * ntiles + blockIdx.x) * nacc + t] = s;
+  }
+}
+
+// out[b*nacc + a] = sum over tiles (fixed order)
+__global__ void k_reduce_partials(const double* __restrict__ partials, int64_t ntiles, int nacc,
+                                  double* __restrict__ out) {
+  const int64_t b = blockIdx.z;
+  const int a = blockIdx.x;
+  __shared__ double red[32];
+  double s = 0.0;
+  for (int64_t tt = threadIdx.x; tt < ntiles; tt += blockDim.x) s += partials[(b * ntiles + tt) * nacc + a];
+  s = block_sum<1024>(s, red);
+  if (threadIdx.x == 0) out[b * nacc + a] = s;
+}
+
+__global__ void k_gram_logdet(int n, int ncols, const double* __restrict__ M, int64_t ldm, int64_t mstride,
+                              const double* __restrict__ L, int64_t ldl, int64_t lstride, double* __restrict__ out,
+                              int64_t out_bstride) {
+  const int64_t b = blockIdx.z;
+  const int npairs = ncols * (ncols + 1) / 2;
+  __shared__ double red[32];
+  double s = 0.0;
+  if ((int)blockIdx.x < npairs) {
+    int q1, q2;
+    lower_tile_of(blockIdx.x, q1, q2);
+    const double* a = M + b * mstride + (int64_t)q1 * ldm;
+    const double* c = M + b * mstride + (int64_t)q2 * ldm;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s = fma(a[i], c[i], s);
+    s = block_sum<256>(s, red);
+    if (threadIdx.x == 0) out[b * out_bstride + q1 * ncols + q2] = s;
+  } else {
+    const double* Lb = L + b * lstride;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s += log(Lb[i + (int64_t)i * ldl]);
+    s = block_sum<256>(s, red);
+    if (threadIdx.x == 0) out[b * out_bstride + ncols * ncols] = s;
+  }
+}
+
+constexpr int PMAX = 64;
+
+__global__ void k_gls_solve(int p, const double* __restrict__ gram, int64_t gram_bstride, double* __restrict__ beta,
+                            int64_t beta_bstride, double* __restrict__ rstar, int64_t rstar_bstride,
+                            int* __restrict__ info) {
+  const int64_t b = blockIdx.x;
+  if (threadIdx.x != 0) return;
+  const int nc = p + 1;
+  const double* g = gram + b * gram_bstride;
+  double* U = rstar + b * rstar_bstride;  // p x p column-major, upper
+  double h[PMAX], z[PMAX];
+  for (int i = 0; i < p; ++i) h[i] = g[p * nc + i];  // row p (y*), col i (F*_i)
+  // upper Cholesky U'U = G
+  for (int j = 0; j < p; ++j) {
+    for (int i = 0; i <= j; ++i) {
+      double s = g[j * nc + i];  // G(i, j) = G(j, i), stored at row j col i (j >= i)
+      for (int k = 0; k < i; ++k) s -= U[k + i * p] * U[k + j * p];
+      if (i == j) {
+        if (!(s > 0.0)) {
+          info[b] = j + 1;
+          return;
+        }
+        U[j + j * p] = sqrt(s);
+      } else {
+        U[i + j * p] = s / U[i + i * p];
+      }
+    }
+    for (int i = j + 1; i < p; ++i) U[i + j * p] = 0.0;
+  }
+  // U' z = h ; U beta = z
+  for (int i = 0; i < p; ++i) {
+    double s = h[i];
+    for (int k = 0; k < i; ++k) s -= U[k + i * p] * z[k];
+    z[i] = s / U[i + i * p];
+  }
+  double* bt = beta + b * beta_bstride;
+  for (int i = p - 1; i >= 0; --i) {
+    double s = z[i];
+    for (int k = i + 1; k < p; ++k) s -= U[i + k * p] * bt[k];
+    bt[i] = s / U[i + i * p];
+  }
+  info[b] = 0;
+}
+
+__global__ void k_residual_sse(int n, int p, const double* __restrict__ FY, int64_t ldfy, int64_t fystride,
+                               const double* __restrict__ beta, int64_t beta_bstride, double* __restrict__ Estar,
+                               int64_t estride, double* __restrict__ sse, int64_t sse_bstride) {
+  const int64_t b = blockIdx.x;
+  __shared__ double red[32];
+  __shared__ double bt[PMAX];
+  if (threadIdx.x < p) bt[threadIdx.x] = beta[b * beta_bstride + threadIdx.x];
+  __syncthreads();
+  const double* M = FY + b * fystride;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double fb = 0.0;
+    for (int q = 0; q < p; ++q) fb = fma(M[i + (int64_t)q * ldfy], bt[q], fb);
+    const double e = M[i + (int64_t)p * ldfy] - fb;
+    Estar[b * estride + i] = e;
+    s = fma(e, e, s);
+  }
+  s = block_sum<1024>(s, red);
+  if (threadIdx.x == 0) sse[b * sse_bstride] = s;
+}
+
+__global__ void k_lower_colsum_abs(int n, const double* __restrict__ L, int64_t ldl, int64_t lstride,
+                                   double* __restrict__ colsum) {
+  const int64_t b = blockIdx.z;
+  const int lane = threadIdx.x & 31;
+  const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (j >= n) return;
+  const double* c = L + b * lstride + (int64_t)j * ldl;
+  double s = 0.0;
+  for (int i = j + lane; i < n; i += 32) s += fabs(c[i]);
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) colsum[b * n + j] = s;
+}
+
+template <template <int, int> class Launch, typename... Args>
+void dispatch_kd(int kernel, int d, Args&&... args) {
+  auto go = [&](auto kc) {
+    constexpr int KK = decltype(kc)::value;
+    if (d <= 4) Launch<KK, 4>::run(args...);
+    else if (d <= 8) Launch<KK, 8>::run(args...);
+    else if (d <= 16) Launch<KK, 16>::run(args...);
+    else if (d <= 32) Launch<KK, 32>::run(args...);
+    else throw std::invalid_argument("input dimension d > 32 is not supported by the GPU kernels");
+  };
+  switch (kernel) {
+    case KGAUSS: go(std::integral_constant<int, KGAUSS>{}); break;
+    case KEXP: go(std::integral_constant<int, KEXP>{}); break;
+    case KMATERN32: go(std::integral_constant<int, KMATERN32>{}); break;
+    case KMATERN52: go(std::integral_constant<int, KMATERN52>{}); break;
+    default: throw std::invalid_argument("Unsupported covariance kernel id");
+  }
+}
+
+template <int K, int DM>
+struct CovLowerLaunch {
+  static void run(int n, int d, const double* X, int64_t xb, const double* theta, const double* factor,
+                  const double* diag, double* A, int64_t lda, int64_t mstride, int batch, cudaStream_t st) {
+    const int nb = ceil_div(n, T);
+    const int64_t ntiles = (int64_t)nb * (nb + 1) / 2;
+    k_cov_lower<K, DM><<<dim3((unsigned)ntiles, 1, batch), 256, 0, st>>>(n, d, X, xb, theta, factor, diag, A, lda,
+                                                                          mstride);
+    LKG_LAUNCH("k_cov_lower");
+  }
+};
+
+template <int K, int DM>
+struct CovCrossLaunch {
+  static void run(int n_o, int q, int d, const double* Xo, const double* Xn, const double* theta, double factor,
+                  double* R, cudaStream_t st) {
+    k_cov_cross<K, DM><<<dim3(ceil_div(n_o, T), ceil_div(q, T), 1), 256, 0, st>>>(n_o, q, d, Xo, Xn, theta, factor,
+                                                                                   R);
+    LKG_LAUNCH("k_cov_cross");
+  }
+};
+
+template <int K, int DM>
+struct AdjointLaunch {
+  static void run(int n, int d, const double* X, int64_t xb, const double* theta, const double* factor,
+                  const double* xv, int64_t xvb, const double* Rinv, int64_t ldr, int64_t rstride, double* partials,
+                  int64_t ntiles, int batch, cudaStream_t st) {
+    k_adjoint<K, DM><<<dim3((unsigned)ntiles, 1, batch), 256, 0, st>>>(n, d, X, xb, theta, factor, xv, xvb, Rinv, ldr,
+                                                                        rstride, partials, ntiles);
+    LKG_LAUNCH("k_adjoint");
+  }
+};
+
+}  // namespace
+
+void cov_build_lower(int kernel, int n, int d, const double* X, int64_t x_bstride, const double* theta,
+                     const double* factor, const double* diag, double* A, int64_t lda, int64_t mstride, int batch,
+                     cudaStream_t st) {
+  if (n <= 0) return;
+  dispatch_kd<CovLowerLaunch>(kernel, d, n, d, X, x_bstride, theta, factor, diag, A, lda, mstride, batch, st);
+}
+
+void cov_cross(int kernel, int n_o, int q, int d, const double* Xo, const double* Xn, const double* theta,
+               double factor, double* R, cudaStream_t st) {
+  if (n_o <= 0 || q <= 0) return;
+  dispatch_kd<CovCrossLaunch>(kernel, d, n_o, q, d, Xo, Xn, theta, factor, R, st);
+}
+
+size_t adjoint_partials_size(int n, int d, int batch) {
+  const int nb = ceil_div(n, T);
+  return (size_t)nb * (nb + 1) / 2 * adjoint_nacc(d) * batch;
+}
+
+void adjoint_sums(int kernel, int n, int d, const double* X, int64_t x_bstride, const double* theta,
+                  const double* factor, const double* xv, int64_t xv_bstride, const double* Rinv, int64_t ldr,
+                  int64_t rstride, double* partials, double* out, int batch, cudaStream_t st) {
+  const int nb = ceil_div(n, T);
+  const int64_t ntiles = (int64_t)nb * (nb + 1) / 2;
+  dispatch_kd<AdjointLaunch>(kernel, d, n, d, X, x_bstride, theta, factor, xv, xv_bstride, Rinv, ldr, rstride,
+                             partials, ntiles, batch, st);
+  const int nacc = adjoint_nacc(d);
+  k_reduce_partials<<<dim3(nacc, 1, batch), 1024, 0, st>>>(partials, ntiles, nacc, out);
+  LKG_LAUNCH("k_reduce_partials");
+}
+
+void gram_and_logdet(int n, int ncols, const double* Mat, int64_t ldm, int64_t mstride, const double* L, int64_t ldl,
+                     int64_t lstride, double* out, int64_t out_bstride, int batch, cudaStream_t st) {
+  const int npairs = ncols * (ncols + 1) / 2;
+  k_gram_logdet<<<dim3(npairs + 1, 1, batch), 256, 0, st>>>(n, ncols, Mat, ldm, mstride, L, ldl, lstride, out,
+                                                             out_bstride);
+  LKG_LAUNCH("k_gram_logdet");
+}
+
+void gls_solve(int p, const double* gram, int64_t gram_bstride, double* beta, int64_t beta_bstride, double* rstar,
+               int64_t rstar_bstride, int* gls_info, int batch, cudaStream_t st) {
+  if (p > PMAX) throw std::invalid_argument("trend with more than 64 columns is not supported");
+  k_gls_solve<<<batch, 32, 0, st>>>(p, gram, gram_bstride, beta, beta_bstride, rstar, rstar_bstride, gls_info);
+  LKG_LAUNCH("k_gls_solve");
+}
+
+void residual_sse(int n, int p, const double* FY, int64_t ldfy, int64_t fystride, const double* beta,
+                  int64_t beta_bstride, double* Estar, int64_t estride, double* sse, int64_t sse_bstride, int batch,
+                  cudaStream_t st) {
+  k_residual_sse<<<batch, 1024, 0, st>>>(n, p, FY, ldfy, fystride, beta, beta_bstride, Estar, estride, sse,
+                                         sse_bstride);
+  LKG_LAUNCH("k_residual_sse");
+}
+
+void lower_colsum_abs(int n, const double* L, int64_t ldl, int64_t lstride, double* colsum, int batch,
+                      cudaStream_t st) {
+  k_lower_colsum_abs<<<dim3(ceil_div(n, 8), 1, batch), 256, 0, st>>>(n, L, ldl, lstride, colsum);
+  LKG_LAUNCH("k_lower_colsum_abs");
+}
+
+}  // namespace lkg

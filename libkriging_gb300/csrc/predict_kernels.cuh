@@ -1,0 +1,21 @@
+// predict_kernels.cuh -- GPU part of Kriging::predict (KrigingImpl::predict_impl, src/lib/KrigingImpl.cpp:145-251).
+#pragma once
+#include <vector>
+
+#include "engine.hpp"
+
+namespace lkg {
+
+struct PredictOut {
+  std::vector<double> rz;     // q:     Rstar_on' z
+  std::vector<double> rr;     // q:     colsum(Rstar_on % Rstar_on)
+  std::vector<double> rm;     // q x p (row-major per point): Rstar_on' M
+  std::vector<double> sigma;  // q x q column-major: R_nn - Rstar_on' Rstar_on (when need_cov)
+};
+
+// Xn: q x d column-major, already normalised.  R_on = factor * C(X_o - X_n) (coincident points -> 1),
+// Rstar_on = L \ R_on with the committed factor of `model`.
+PredictOut predict_gpu(const Engine& model, const double* Xn, int q, const double* theta, double factor,
+                       const double* z, bool need_rr, bool need_cov, double nn_factor, bool nugget);
+
+}  // namespace lkg

@@ -1,0 +1,279 @@
+"""Python ``Kriging`` mirroring pylibkriging's ``Kriging`` (= ``WrappedPyKriging``).
+
+Same constructor forms, method names, argument names / defaults and return tuples as the reference binding
+(bindings/Python/pylibkriging/src/_pylibkriging/pylibkriging.cpp:120-205, Kriging_binding.cpp:260-264):
+
+    Kriging(kernel) / Kriging(kernel, noise_model) / Kriging(y, X, kernel, regmodel="constant", normalize=False,
+            optim="BFGS", objective="LL", parameters={}, noise=None)
+    fit(y, X, regmodel, normalize, optim, objective, parameters)
+    logLikelihoodFun(theta, return_grad=False, want_hess=False) -> (ll, grad, hess)
+    predict(X, return_stdev=True, return_cov=False, return_deriv=False) -> (mean, stdev, cov, dmean, dstdev)
+
+Every call goes through the C ABI of include/libkriging_gb300.h into the sm_103a kernels.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, cstr, f64, ptr
+
+_PARAM_KEYS = ("sigma2", "is_sigma2_estim", "theta", "is_theta_estim", "beta", "is_beta_estim", "nugget",
+               "is_nugget_estim")
+
+
+def _as_X(X, n=None):
+    X = np.asarray(X, dtype=np.float64)
+    if X.ndim == 1:
+        X = X.reshape(-1, 1)
+    return f64(X)
+
+
+class Kriging:
+    def __init__(self, *args, **kwargs):
+        self._h = None
+        L = _lib.load()
+        if len(args) >= 3 or "y" in kwargs:
+            names = ("y", "X", "kernel", "regmodel", "normalize", "optim", "objective", "parameters", "noise")
+            a = dict(zip(names, args))
+            a.update(kwargs)
+            noise_model = a.pop("noise_model", "none")
+            if a.get("noise") is not None:
+                raise ValueError("per-observation noise is not supported by the GPU build")
+            self._h = L.lkg_kriging_new(cstr(a["kernel"]), cstr(noise_model))
+            if not self._h:
+                raise _lib.LibKrigingError(_lib.last_error())
+            self.fit(a["y"], a["X"], a.get("regmodel", "constant"), a.get("normalize", False), a.get("optim", "BFGS"),
+                     a.get("objective", "LL"), a.get("parameters") or {})
+        else:
+            kernel = args[0] if args else kwargs["kernel"]
+            noise_model = args[1] if len(args) > 1 else kwargs.get("noise_model", "none")
+            self._h = L.lkg_kriging_new(cstr(kernel), cstr(noise_model))
+            if not self._h:
+                raise _lib.LibKrigingError(_lib.last_error())
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                _lib.load().lkg_kriging_delete(h)
+            except Exception:
+                pass
+            self._h = None
+
+    # ---------------------------------------------------------------------------------------------------------
+    def fit(self, y, X, regmodel="constant", normalize=False, optim="BFGS", objective="LL", parameters=None):
+        X = _as_X(X)
+        y = np.ascontiguousarray(np.asarray(y, dtype=np.float64).reshape(-1))
+        n, d = X.shape
+        P = dict(parameters or {})
+        bad = set(P) - set(_PARAM_KEYS)
+        if bad:
+            raise ValueError("unknown parameters: %s" % sorted(bad))
+        sigma2 = P.get("sigma2")
+        nugget = P.get("nugget")
+        theta = P.get("theta")
+        beta = P.get("beta")
+        s2 = None if sigma2 is None else np.array([sigma2], dtype=np.float64)
+        nu = None if nugget is None else np.array([nugget], dtype=np.float64)
+        th = None
+        rows = 0
+        if theta is not None:
+            th = np.atleast_2d(np.asarray(theta, dtype=np.float64))
+            if th.shape[1] != d and th.shape[0] == d:
+                th = th.T
+            rows = th.shape[0]
+            th = f64(th)
+        bt = None if beta is None else np.ascontiguousarray(np.asarray(beta, dtype=np.float64).reshape(-1))
+        check(_lib.load().lkg_kriging_fit_params(
+            self._h, ptr(y), n, ptr(X), n, d, cstr(regmodel), int(bool(normalize)), cstr(optim), cstr(objective),
+            ptr(s2), int(P.get("is_sigma2_estim", True)), ptr(th), rows, int(P.get("is_theta_estim", True)),
+            ptr(bt), 0 if bt is None else bt.size, int(P.get("is_beta_estim", True)), ptr(nu),
+            int(P.get("is_nugget_estim", True))))
+        return self
+
+    def logLikelihoodFun(self, theta, return_grad=False, want_hess=False, bench=False):
+        if want_hess:
+            raise ValueError("logLikelihoodFun: the Hessian is not supported by the GPU build")
+        t = np.ascontiguousarray(np.asarray(theta, dtype=np.float64).reshape(-1))
+        ll = ctypes.c_double()
+        g = np.zeros(t.size) if return_grad else None
+        if bench:
+            buf = ctypes.create_string_buffer(4096)
+            check(_lib.load().lkg_kriging_log_likelihood_fun_bench(self._h, ptr(t), t.size, int(bool(return_grad)),
+                                                                   ctypes.byref(ll), ptr(g), buf, 4096))
+            self.last_bench = {kv.split("\t")[0]: float(kv.split("\t")[1])
+                               for kv in buf.value.decode().split("\n") if kv}
+        else:
+            check(_lib.load().lkg_kriging_log_likelihood_fun(self._h, ptr(t), t.size, int(bool(return_grad)), 0,
+                                                             ctypes.byref(ll), ptr(g), None))
+        return ll.value, (g if return_grad else np.zeros(0)), np.zeros((0, 0))
+
+    def logLikelihoodFunBatch(self, thetas, return_grad=True):
+        """k candidate gammas (rows) in one batched GPU evaluation -> (ll[k], grad[k, gdim])."""
+        T = f64(np.atleast_2d(np.asarray(thetas, dtype=np.float64)))
+        k, gd = T.shape
+        ll = np.zeros(k)
+        g = np.zeros((k, gd), order="F") if return_grad else None
+        check(_lib.load().lkg_kriging_log_likelihood_fun_batch(self._h, ptr(T), k, gd, int(bool(return_grad)),
+                                                               ptr(ll), ptr(g)))
+        return ll, (np.ascontiguousarray(g) if return_grad else None)
+
+    def logLikelihood(self):
+        v = _lib.load().lkg_kriging_log_likelihood(self._h)
+        if np.isnan(v):
+            err = _lib.last_error()
+            if err:
+                raise _lib.LibKrigingError(err)
+        return v
+
+    def predict(self, X, return_stdev=True, return_cov=False, return_deriv=False):
+        X = _as_X(X)
+        m, d = X.shape
+        mean = np.zeros(m)
+        sd = np.zeros(m) if return_stdev else None
+        cov = np.zeros((m, m), order="F") if return_cov else None
+        check(_lib.load().lkg_kriging_predict(self._h, ptr(X), m, d, int(bool(return_stdev)), int(bool(return_cov)),
+                                              int(bool(return_deriv)), ptr(mean), ptr(sd), ptr(cov), None, None))
+        return mean, sd, cov, None, None
+
+    def summary(self):
+        s = _lib.load().lkg_kriging_summary(self._h)
+        return s.decode() if s else ""
+
+    # ---- accessors (pylibkriging.cpp:196-230) ----
+    def _vec(self, fn):
+        n = ctypes.c_int()
+        check(fn(self._h, None, ctypes.byref(n)))
+        out = np.zeros(n.value)
+        check(fn(self._h, ptr(out), ctypes.byref(n)))
+        return out
+
+    def _mat(self, fn):
+        r, c = ctypes.c_int(), ctypes.c_int()
+        check(fn(self._h, None, ctypes.byref(r), ctypes.byref(c)))
+        out = np.zeros((r.value, c.value), order="F")
+        check(fn(self._h, ptr(out), ctypes.byref(r), ctypes.byref(c)))
+        return out
+
+    def kernel(self):
+        return _lib.load().lkg_kriging_kernel(self._h).decode()
+
+    def optim(self):
+        return _lib.load().lkg_kriging_optim(self._h).decode()
+
+    def objective(self):
+        return _lib.load().lkg_kriging_objective(self._h).decode()
+
+    def regmodel(self):
+        return _lib.load().lkg_kriging_regmodel(self._h).decode()
+
+    def normalize(self):
+        return bool(_lib.load().lkg_kriging_is_normalize(self._h))
+
+    def X(self):
+        return self._mat(_lib.load().lkg_kriging_get_X)
+
+    def y(self):
+        return self._vec(_lib.load().lkg_kriging_get_y)
+
+    def centerX(self):
+        return self._vec(_lib.load().lkg_kriging_get_centerX)
+
+    def scaleX(self):
+        return self._vec(_lib.load().lkg_kriging_get_scaleX)
+
+    def centerY(self):
+        return _lib.load().lkg_kriging_get_centerY(self._h)
+
+    def scaleY(self):
+        return _lib.load().lkg_kriging_get_scaleY(self._h)
+
+    def T(self):
+        return self._mat(_lib.load().lkg_kriging_get_T)
+
+    def M(self):
+        return self._mat(_lib.load().lkg_kriging_get_M)
+
+    def z(self):
+        return self._vec(_lib.load().lkg_kriging_get_z)
+
+    def beta(self):
+        return self._vec(_lib.load().lkg_kriging_get_beta)
+
+    def is_beta_estim(self):
+        return bool(_lib.load().lkg_kriging_is_beta_estim(self._h))
+
+    def theta(self):
+        return self._vec(_lib.load().lkg_kriging_get_theta)
+
+    def is_theta_estim(self):
+        return bool(_lib.load().lkg_kriging_is_theta_estim(self._h))
+
+    def sigma2(self):
+        return _lib.load().lkg_kriging_get_sigma2(self._h)
+
+    def is_sigma2_estim(self):
+        return bool(_lib.load().lkg_kriging_is_sigma2_estim(self._h))
+
+    def noise_model(self):
+        return _lib.load().lkg_kriging_noise_model(self._h).decode()
+
+    def nugget(self):
+        return _lib.load().lkg_kriging_get_nugget(self._h)
+
+    def is_nugget_estim(self):
+        return bool(_lib.load().lkg_kriging_is_nugget_estim(self._h))
+
+
+# ---- process-wide settings (LinearAlgebra / Optim statics) ----
+def set_num_nugget(v):
+    _lib.load().lkg_set_num_nugget(float(v))
+
+
+def get_num_nugget():
+    return _lib.load().lkg_get_num_nugget()
+
+
+def check_chol_rcond(b):
+    _lib.load().lkg_check_chol_rcond(int(bool(b)))
+
+
+class Optim:
+    @staticmethod
+    def use_reparametrize(b):
+        _lib.load().lkg_optim_use_reparametrize(int(bool(b)))
+
+    @staticmethod
+    def set_theta_lower_factor(f):
+        _lib.load().lkg_optim_set_theta_lower_factor(float(f))
+
+    @staticmethod
+    def set_theta_upper_factor(f):
+        _lib.load().lkg_optim_set_theta_upper_factor(float(f))
+
+    @staticmethod
+    def use_variogram_bounds_heuristic(b):
+        _lib.load().lkg_optim_use_variogram_bounds_heuristic(int(bool(b)))
+
+    @staticmethod
+    def set_log_level(level):
+        _lib.load().lkg_optim_set_log_level(int(level))
+
+    @staticmethod
+    def set_max_iteration(m):
+        _lib.load().lkg_optim_set_max_iteration(int(m))
+
+    @staticmethod
+    def set_gradient_tolerance(t):
+        _lib.load().lkg_optim_set_gradient_tolerance(float(t))
+
+    @staticmethod
+    def set_objective_rel_tolerance(t):
+        _lib.load().lkg_optim_set_objective_rel_tolerance(float(t))
+
+    @staticmethod
+    def set_max_restart(m):
+        _lib.load().lkg_optim_set_max_restart(int(m))

@@ -1,0 +1,520 @@
+"""CPU FP64 oracle for the libKriging likelihood hot path.
+
+TEST INFRASTRUCTURE ONLY: this module is the checker for the GPU implementation.  Only the tests,
+``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` import it; the product package never
+does.  It restates the reference's algorithm in the reference's operation order:
+
+* pair loops (covariance build, gradient loop, Vecchia conditionals) in C: ``oracle/lk_oracle.c``;
+* dense linear algebra through LAPACK (scipy's bundled OpenBLAS), mirroring Armadillo's calls:
+  ``arma::chol`` -> dpotrf, ``arma::rcond`` on a triangular factor -> dtrcon('1'),
+  ``arma::solve(trimatl/trimatu(..), B)`` -> dtrtrs.
+
+Reference routines restated here (paths relative to the libKriging source tree):
+
+* ``safe_chol_lower``         src/lib/LinearAlgebra.cpp:43-98, ``rcond_chol`` :106-115
+* ``populate_model``          src/lib/KrigingImpl.cpp:73-125, src/lib/LinearAlgebra.cpp:142-204, :695-714
+* ``OracleKriging.log_likelihood``  src/lib/Kriging.cpp:214-341 (all NoiseModel None / Nugget branches)
+* ``regression_matrix``       src/lib/Trend.cpp:34-91
+* ``theta_bounds``            src/lib/Optim.cpp:179-209
+* ``OracleKriging.predict``   src/lib/KrigingImpl.cpp:145-251 (mean / stdev), src/lib/Kriging.cpp:2240-2285
+* ``vecchia_*``               src/lib/Kriging.cpp:736-924 (through the C restatement)
+
+Parity pin: ``tests/golden/loglik_golden.json`` (the reference's tests/references/data2-grad-*, data1-scal
+known answers, checked at 1e-12 relative in tests/test_oracle.py).
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+import subprocess
+from dataclasses import dataclass, field
+from pathlib import Path
+
+import numpy as np
+from scipy.linalg import lapack
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+SO = BUILD / "liblk_oracle.so"
+
+KERNELS = {"gauss": 0, "exp": 1, "matern3_2": 2, "matern5_2": 3}
+
+
+def build(force: bool = False) -> Path:
+    """Compile lk_oracle.c into oracle/_build/liblk_oracle.so (gcc, no FMA contraction)."""
+    src = HERE / "lk_oracle.c"
+    if SO.exists() and not force and SO.stat().st_mtime >= src.stat().st_mtime:
+        return SO
+    BUILD.mkdir(exist_ok=True)
+    tmp = SO.with_suffix(".so.tmp%d" % os.getpid())
+    subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-o", str(tmp), str(src), "-lm"])
+    os.replace(tmp, SO)
+    return SO
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(str(SO))
+        dp = ctypes.POINTER(ctypes.c_double)
+        ip = ctypes.POINTER(ctypes.c_int32)
+        L.ora_cov.restype = ctypes.c_double
+        L.ora_cov.argtypes = [ctypes.c_int, dp, dp, ctypes.c_int]
+        L.ora_dlncov.restype = None
+        L.ora_dlncov.argtypes = [ctypes.c_int, dp, dp, ctypes.c_int, dp]
+        L.ora_build_R.restype = None
+        L.ora_build_R.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, ctypes.c_double, dp, dp]
+        L.ora_grad_terms.restype = None
+        L.ora_grad_terms.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp, dp, dp, dp, dp]
+        L.ora_alpha_terms.restype = None
+        L.ora_alpha_terms.argtypes = [ctypes.c_int, dp, dp, dp, ctypes.c_double, ctypes.c_double, dp]
+        L.ora_vecchia_sets.restype = None
+        L.ora_vecchia_sets.argtypes = [ctypes.c_int, ctypes.c_int, dp, ctypes.c_int, ip, ip]
+        L.ora_vecchia_ll.restype = ctypes.c_double
+        L.ora_vecchia_ll.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp, dp, ip, ip,
+                                     ctypes.c_int, ctypes.c_double, dp, dp, dp]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) if a is not None else None
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+
+
+def _colmajor(a):
+    return np.asfortranarray(np.asarray(a, dtype=np.float64))
+
+
+# --------------------------------------------------------------------------------------------------------------
+# configuration statics (LinearAlgebra.cpp:33-63,100; Optim.cpp:39-139)
+# --------------------------------------------------------------------------------------------------------------
+@dataclass
+class Config:
+    num_nugget: float = 1e-10
+    chol_rcond_check: bool = True
+    min_rcond: float = 1e-18
+    max_inc_choldiag: int = 10
+    theta_lower_factor: float = 0.02
+    theta_upper_factor: float = 10.0
+    variogram_bounds_heuristic: bool = True
+
+
+CONFIG = Config()
+
+
+class CholeskyError(RuntimeError):
+    pass
+
+
+# --------------------------------------------------------------------------------------------------------------
+# kernels and the covariance build
+# --------------------------------------------------------------------------------------------------------------
+def cov(kernel: str, dx, theta) -> float:
+    dx = np.ascontiguousarray(dx, dtype=np.float64)
+    theta = np.ascontiguousarray(theta, dtype=np.float64)
+    return lib().ora_cov(KERNELS[kernel], _dp(dx), _dp(theta), dx.size)
+
+
+def dlncov(kernel: str, dx, theta):
+    dx = np.ascontiguousarray(dx, dtype=np.float64)
+    theta = np.ascontiguousarray(theta, dtype=np.float64)
+    out = np.empty(dx.size)
+    lib().ora_dlncov(KERNELS[kernel], _dp(dx), _dp(theta), dx.size, _dp(out))
+    return out
+
+
+def build_R(kernel: str, X, theta, factor: float = 1.0, diag=None):
+    """cholCov's covariance build (LinearAlgebra.cpp:142-181): full symmetric n x n, column-major."""
+    X = _colmajor(X)
+    n, d = X.shape
+    theta = np.ascontiguousarray(theta, dtype=np.float64)
+    R = np.empty((n, n), order="F")
+    dg = None if diag is None else np.ascontiguousarray(diag, dtype=np.float64)
+    lib().ora_build_R(KERNELS[kernel], n, d, _dp(X), _dp(theta), float(factor), _dp(dg), _dp(R))
+    return R
+
+
+# --------------------------------------------------------------------------------------------------------------
+# dense linear algebra (Armadillo -> LAPACK)
+# --------------------------------------------------------------------------------------------------------------
+def rcond_chol(L) -> float:
+    """LinearAlgebra.cpp:106-115: arma::rcond on the (lower triangular) factor, squared."""
+    rc, info = lapack.dtrcon(L, norm="1", uplo="L", diag="N")
+    return float(rc) ** 2
+
+
+def safe_chol_lower(A, cfg: Config = CONFIG):
+    """LinearAlgebra.cpp:43-98: dpotrf; on failure or rcond^2 < min_rcond add num_nugget*10^k to the diagonal
+    of a copy (cumulatively) and retry, k = 0..max_inc_choldiag.  Returns (L, increments used)."""
+    X = np.array(A, order="F", dtype=np.float64, copy=True)
+    inc = 0
+    while True:
+        L, info = lapack.dpotrf(X, lower=1, clean=1, overwrite_a=0)
+        ok = info == 0
+        wrong_rcond = cfg.chol_rcond_check
+        if ok:
+            wrong_rcond = wrong_rcond and (rcond_chol(L) < cfg.min_rcond)
+        if not ok or wrong_rcond:
+            if inc > cfg.max_inc_choldiag:
+                raise CholeskyError("Exceed max numerical nugget (%d x 1e%g) added to force chol matrix"
+                                    % (inc, math.log10(cfg.num_nugget)))
+            if cfg.num_nugget <= 0.0:
+                raise CholeskyError("Cannot add numerical nugget which is not strictly positive")
+            X[np.diag_indices_from(X)] += cfg.num_nugget * 10.0 ** inc
+            inc += 1
+            continue
+        return np.asfortranarray(L), inc
+
+
+def solve_lower(L, B):
+    x, info = lapack.dtrtrs(L, np.asfortranarray(B, dtype=np.float64), lower=1, trans=0)
+    assert info == 0
+    return x
+
+
+def solve_upper_t(L, B):
+    """solve(trimatu(L.t()), B)."""
+    x, info = lapack.dtrtrs(L, np.asfortranarray(B, dtype=np.float64), lower=1, trans=1)
+    assert info == 0
+    return x
+
+
+def inv_sympd(L):
+    """LinearAlgebra.cpp:708-710: solve(trimatu(L'), solve(trimatl(L), I)) -- two full triangular solves."""
+    n = L.shape[0]
+    return solve_upper_t(L, solve_lower(L, np.eye(n, order="F")))
+
+
+# --------------------------------------------------------------------------------------------------------------
+# trend, bounds
+# --------------------------------------------------------------------------------------------------------------
+def regression_matrix(regmodel: str, X):
+    """Trend.cpp:34-91."""
+    X = np.asarray(X, dtype=np.float64)
+    n, d = X.shape
+    cols = []
+    if regmodel == "none":
+        return np.zeros((n, 0), order="F")
+    cols.append(np.ones(n))
+    if regmodel == "constant":
+        pass
+    elif regmodel == "linear":
+        cols += [X[:, i] for i in range(d)]
+    elif regmodel == "interactive":
+        for i in range(d):
+            cols.append(X[:, i])
+            for j in range(i):
+                cols.append(X[:, i] * X[:, j])
+    elif regmodel == "quadratic":
+        for i in range(d):
+            cols.append(X[:, i])
+            for j in range(i + 1):
+                cols.append(X[:, i] * X[:, j])
+    else:
+        raise ValueError("Cannot convert '%s' as a regression model" % regmodel)
+    return np.asfortranarray(np.stack(cols, axis=1))
+
+
+def theta_bounds(X, y, cfg: Config = CONFIG):
+    """Optim.cpp:179-209 with dX recomputed: [lower, upper] factors of maxdX, variogram heuristic."""
+    X = np.asarray(X, dtype=np.float64)
+    n, d = X.shape
+    maxdX = X.max(axis=0) - X.min(axis=0)
+    lower = cfg.theta_lower_factor * maxdX
+    upper = cfg.theta_upper_factor * maxdX
+    if cfg.variogram_bounds_heuristic and n > 0:
+        diff = X[:, None, :] - X[None, :, :]          # (i, j, k) = X_i - X_j
+        dy2 = (y[:, None] - y[None, :]) ** 2
+        dx2 = (diff ** 2).sum(axis=2)
+        with np.errstate(invalid="ignore", divide="ignore"):
+            slope = dy2 / dx2
+        slope[np.isnan(slope)] = 0.0
+        wsum = slope.sum()
+        if wsum > 0.0:
+            w = slope / wsum
+            steep = np.einsum("ijk,ij->k", np.abs(diff), w)
+            lower = np.maximum(lower, cfg.theta_lower_factor * steep)
+            lower = np.minimum(lower, upper)
+            upper = np.maximum(lower, upper)
+    return lower, upper
+
+
+# --------------------------------------------------------------------------------------------------------------
+# populate_Model and the log-likelihood
+# --------------------------------------------------------------------------------------------------------------
+@dataclass
+class KModel:
+    R: np.ndarray
+    L: np.ndarray
+    Rinv: np.ndarray | None
+    Fstar: np.ndarray
+    ystar: np.ndarray
+    Rstar: np.ndarray
+    betahat: np.ndarray
+    Estar: np.ndarray
+    SSEstar: float
+    nugget_increments: int = 0
+
+
+def populate_model(kernel, X, y, F, theta, alpha=1.0, diag=None, with_rinv=True, cfg: Config = CONFIG) -> KModel:
+    """KrigingImpl.cpp:73-125 (+ cholCov LinearAlgebra.cpp:142-204)."""
+    R = build_R(kernel, X, theta, alpha, diag)
+    L, inc = safe_chol_lower(R, cfg)
+    Rinv = inv_sympd(L) if with_rinv else None
+    Fstar = solve_lower(L, F)
+    ystar = solve_lower(L, y.reshape(-1, 1))[:, 0]
+    FtF = Fstar.T @ Fstar
+    if FtF.shape[0] > 0:
+        Rstar, info = lapack.dpotrf(FtF, lower=0, clean=1)
+        assert info == 0
+        rhs = Fstar.T @ ystar
+        beta = lapack.dtrtrs(Rstar, lapack.dtrtrs(Rstar, rhs.reshape(-1, 1), lower=0, trans=1)[0], lower=0)[0][:, 0]
+    else:
+        Rstar = np.zeros((0, 0))
+        beta = np.zeros(0)
+    residual = y - F @ beta
+    Estar = solve_lower(L, residual.reshape(-1, 1))[:, 0]
+    SSE = float(Estar @ Estar)
+    return KModel(R, L, Rinv, Fstar, ystar, Rstar, beta, Estar, SSE, inc)
+
+
+class OracleKriging:
+    """The state a fitted ``Kriging`` carries into ``logLikelihoodFun`` (Kriging.hpp, KrigingImpl.hpp)."""
+
+    def __init__(self, y, X, kernel, regmodel="constant", normalize=False, noise_model="none",
+                 est_sigma2=True, sigma2=None, est_nugget=True, nugget=None, est_beta=True, beta=None,
+                 alpha=1.0, cfg: Config = CONFIG):
+        X = np.atleast_2d(np.asarray(X, dtype=np.float64))
+        if X.shape[0] == 1 and np.size(y) != 1:
+            X = X.T
+        y = np.asarray(y, dtype=np.float64).reshape(-1)
+        if normalize:
+            cX, sX = X.min(axis=0), X.max(axis=0) - X.min(axis=0)
+            cY, sY = y.min(), y.max() - y.min()
+        else:
+            cX, sX, cY, sY = np.zeros(X.shape[1]), np.ones(X.shape[1]), 0.0, 1.0
+        self.centerX, self.scaleX, self.centerY, self.scaleY = cX, sX, cY, sY
+        self.X = np.asfortranarray((X - cX) / sX)
+        self.y = (y - cY) / sY
+        self.kernel = kernel
+        self.regmodel = regmodel
+        self.F = regression_matrix(regmodel, self.X)
+        self.noise_model = noise_model
+        self.est_sigma2, self.sigma2 = est_sigma2, sigma2
+        self.est_nugget, self.nugget = est_nugget, nugget
+        self.est_beta, self.beta = est_beta, beta
+        self.alpha = alpha
+        self.cfg = cfg
+        self.theta = None
+        self.model = None
+
+    # Kriging.cpp:214-341
+    def log_likelihood(self, gamma, return_grad=True, keep_model=False):
+        n, d = self.X.shape
+        gamma = np.asarray(gamma, dtype=np.float64).reshape(-1)
+        theta = gamma[:d]
+        if gamma.size > d:
+            extra = float(gamma[d])
+        else:
+            extra = self.alpha if self.noise_model == "nugget" else (self.sigma2 or 0.0)
+        if self.noise_model == "nugget" and not self.est_sigma2 and not self.est_nugget:
+            extra = self.sigma2 / (self.sigma2 + self.nugget)
+        alpha = extra if self.noise_model == "nugget" else 1.0
+        m = populate_model(self.kernel, self.X, self.y, self.F, theta, alpha, None, True, self.cfg)
+        if not self.est_beta:
+            m.betahat = np.zeros_like(m.betahat)
+        logdet = 2.0 * np.sum(np.log(np.diag(m.L)))
+        if self.noise_model == "nugget":
+            _alpha = extra
+            s2, nu = self.sigma2, self.nugget
+            if self.est_sigma2:
+                if self.est_nugget:
+                    var = m.SSEstar / n
+                    s2, nu = _alpha * var, (1.0 - _alpha) * var
+                else:
+                    s2 = self.nugget * _alpha / (1.0 - _alpha)
+            else:
+                if self.est_nugget:
+                    nu = self.sigma2 * (1.0 - _alpha) / _alpha
+                else:
+                    _alpha = self.sigma2 / (self.sigma2 + self.nugget)
+            total_var = s2 + nu
+            ll = -0.5 * (n * math.log(2 * math.pi * total_var) + logdet + m.SSEstar / total_var)
+            sigma2_grad = total_var
+        else:
+            if self.est_sigma2:
+                sigma2_grad = m.SSEstar / n
+                ll = -0.5 * (n * math.log(2 * math.pi * sigma2_grad) + logdet + n)
+            else:
+                sigma2_grad = self.sigma2
+                ll = -0.5 * (n * math.log(2 * math.pi * sigma2_grad) + logdet + float(m.Estar @ m.Estar) / sigma2_grad)
+        if keep_model:
+            self.model = m
+        if not return_grad:
+            return ll, None
+        x = solve_upper_t(m.L, m.Estar.reshape(-1, 1))[:, 0]
+        t1 = np.zeros(d)
+        t2 = np.zeros(d)
+        lib().ora_grad_terms(KERNELS[self.kernel], n, d, _dp(self.X), _dp(np.ascontiguousarray(theta)),
+                             _dp(m.R), _dp(m.Rinv), _dp(x), _dp(t1), _dp(t2))
+        grad = np.zeros(gamma.size)
+        grad[:d] = (t1 / sigma2_grad + t2) / 2.0
+        if gamma.size > d and self.noise_model == "nugget":
+            _alpha = extra
+            out = np.zeros(2)
+            if self.est_sigma2 and self.est_nugget:
+                lib().ora_alpha_terms(n, _dp(m.R), _dp(m.Rinv), _dp(x), _alpha, 0.0, _dp(out))
+                term1_a = -out[0] / sigma2_grad
+                term2_a = out[1]
+                grad[d] = -0.5 * (term1_a + term2_a)
+            elif self.est_sigma2 and not self.est_nugget:
+                lib().ora_alpha_terms(n, _dp(m.R), _dp(m.Rinv / sigma2_grad), _dp(x), _alpha, 1.0, _dp(out))
+                term1_a = -out[0] / (sigma2_grad * sigma2_grad)
+                term2_a = out[1]
+                grad[d] = -0.5 * (term1_a + term2_a) * self.nugget / (1.0 - _alpha) / (1.0 - _alpha)
+            else:
+                grad[d] = 0.0
+        return ll, grad
+
+    # KrigingImpl.cpp:145-251, Kriging.cpp:2240-2285 (mean and stdev)
+    def predict(self, Xn, theta, beta, sigma2, alpha=1.0, return_stdev=True):
+        Xn = np.atleast_2d(np.asarray(Xn, dtype=np.float64))
+        Xn_n = (Xn - self.centerX) / self.scaleX
+        Fn = regression_matrix(self.regmodel, Xn_n)
+        m = populate_model(self.kernel, self.X, self.y, self.F, theta, alpha, None, False, self.cfg)
+        n_o, q = self.X.shape[0], Xn_n.shape[0]
+        R_on = np.empty((n_o, q), order="F")
+        for j in range(q):
+            for i in range(n_o):
+                dij = self.X[i] - Xn_n[j]
+                if np.all(np.abs(dij) <= np.finfo(float).eps):
+                    R_on[i, j] = 1.0
+                else:
+                    R_on[i, j] = cov(self.kernel, dij, theta) * alpha
+        z = m.Estar
+        Rs = solve_lower(m.L, R_on)
+        yhat = Fn @ beta + Rs.T @ z
+        yhat = self.centerY + self.scaleY * yhat
+        if not return_stdev:
+            return yhat, None
+        E = Fn - Rs.T @ m.Fstar
+        # rsolve_upper(circ, E): X * circ = E
+        Ec = lapack.dtrtrs(m.Rstar, np.asfortranarray(E.T), lower=0, trans=1)[0].T if m.Rstar.size else E
+        sd2 = 1.0 - np.sum(Rs * Rs, axis=0) + np.sum(Ec * Ec, axis=1)
+        sd2 = np.where(np.isnan(sd2) | (sd2 < 0), 0.0, sd2)
+        var_scale = sigma2 / alpha if self.noise_model == "nugget" else sigma2
+        sd2 = sd2 * var_scale * self.scaleY * self.scaleY
+        return yhat, np.sqrt(sd2)
+
+
+    # Kriging.cpp:1717-2209 (BFGS[N], objective LL), with scipy's L-BFGS-B (Fortran/C port of Nocedal's 3.0 code)
+    # standing in for the un-vendored lbfgsb_cpp: same bounds, starts, tolerances, restart rules and commit.
+    def fit_bfgs(self, multistart=1, theta0=None, max_iter=20, pgtol=1e-3, factr=1e10, max_restart=10):
+        from scipy.optimize import fmin_l_bfgs_b
+        n, d = self.X.shape
+        lower, upper = theta_bounds(self.X, self.y, self.cfg)
+        mt = MT19937Stream(123)
+        U = mt.randu_mat(multistart, d)
+        rand = lower + U * (upper - lower)
+        if theta0 is not None:
+            t0 = np.atleast_2d(np.asarray(theta0, dtype=np.float64))
+            multistart = max(multistart, t0.shape[0])
+            starts = np.vstack([t0, rand])[:multistart]
+        else:
+            starts = rand
+        glo, ghi = np.log(lower), np.log(upper)
+
+        def ofn(g):
+            th = np.exp(g)
+            ll, gr = self.log_likelihood(th, True)
+            return -ll, -gr * th
+
+        best = (np.inf, None)
+        for s in range(multistart):
+            th_start = starts[s]
+            gamma = np.log(th_start)
+            lo, hi = np.minimum(gamma, glo), np.maximum(gamma, ghi)
+            best_f, best_g = np.inf, gamma
+            for retry in range(max_restart + 1):
+                x, f, info = fmin_l_bfgs_b(ofn, gamma, bounds=list(zip(lo, hi)), m=5, factr=factr, pgtol=pgtol,
+                                           maxiter=max_iter)
+                if f < best_f:
+                    best_f, best_g = f, x
+                tp = np.exp(x)
+                to_lb = np.min(np.abs(tp - lower))
+                task = info["task"] if isinstance(info["task"], str) else info["task"].decode()
+                if retry < max_restart and (task.startswith("ABNORMAL_TERMINATION_IN_LNSRCH") or info["nit"] <= 2
+                                            or to_lb < np.finfo(float).eps or f > best_f):
+                    rt = (th_start + lower) / 2.0 ** (retry + 1)
+                    gamma = np.log(rt)
+                    lo, hi = np.minimum(gamma, lo), np.maximum(gamma, hi)
+                else:
+                    break
+            f_final = -self.log_likelihood(np.exp(best_g), False)[0]
+            if f_final < best[0]:
+                best = (f_final, np.exp(best_g))
+        theta = best[1]
+        m = populate_model(self.kernel, self.X, self.y, self.F, theta, 1.0, None, False, self.cfg)
+        self.theta = theta
+        self.beta = m.betahat
+        self.sigma2 = m.SSEstar / n
+        return theta, -best[0]
+
+
+# --------------------------------------------------------------------------------------------------------------
+# Vecchia
+# --------------------------------------------------------------------------------------------------------------
+def vecchia_sets(X, m):
+    """Kriging.cpp:736-804 (O(n^2): small n only).  Returns (order[n], nbr[n, m]) with -1 padding."""
+    X = _colmajor(X)
+    n, d = X.shape
+    order = np.empty(n, dtype=np.int32)
+    nbr = np.empty((n, m), dtype=np.int32)
+    lib().ora_vecchia_sets(n, d, _dp(X), m, _ip(order), _ip(nbr))
+    return order, nbr
+
+
+def vecchia_ll(kernel, X, y, F, theta, order, nbr, num_nugget=None, return_grad=True):
+    """Kriging.cpp:806-924.  Returns (vll, grad or None, beta, sigma2)."""
+    X = _colmajor(X)
+    n, d = X.shape
+    F = _colmajor(F)
+    p = F.shape[1]
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    theta = np.ascontiguousarray(theta, dtype=np.float64)
+    order = np.ascontiguousarray(order, dtype=np.int32)
+    nbr = np.ascontiguousarray(nbr, dtype=np.int32)
+    m = nbr.shape[1]
+    grad = np.zeros(d) if return_grad else None
+    beta = np.zeros(max(p, 1))
+    s2 = np.zeros(1)
+    nn = CONFIG.num_nugget if num_nugget is None else num_nugget
+    v = lib().ora_vecchia_ll(KERNELS[kernel], n, d, p, _dp(X), _dp(y), _dp(F), _dp(theta), _ip(order), _ip(nbr),
+                             m, nn, _dp(grad), _dp(beta), _dp(s2))
+    return v, grad, beta[:p], float(s2[0])
+
+
+# --------------------------------------------------------------------------------------------------------------
+# mt19937 draws as the reference makes them (Random.cpp:13-49, libstdc++ uniform_real_distribution<double>)
+# --------------------------------------------------------------------------------------------------------------
+class MT19937Stream:
+    def __init__(self, seed=123):
+        self.bg = np.random.MT19937()
+        self.bg._legacy_seeding(seed)
+
+    def uniform(self, k):
+        raw = self.bg.random_raw(2 * k).astype(np.float64).reshape(k, 2)
+        u = (raw[:, 0] + raw[:, 1] * 4294967296.0) / 18446744073709551616.0
+        return np.where(u >= 1.0, np.nextafter(1.0, 0.0), u)
+
+    def randu_mat(self, rows, cols):
+        return self.uniform(rows * cols).reshape(cols, rows).T

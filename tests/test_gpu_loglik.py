@@ -1,0 +1,116 @@
+"""GPU parity of the dense likelihood path through the C ABI against the oracle and the reference's known
+answers.  Tolerances: LL 1e-10 relative, gradient 1e-7 relative (FP64 path), known answers 1e-10."""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+LL_TOL = 1e-10
+GRAD_TOL = 1e-7
+
+
+@pytest.mark.parametrize("i", range(11))
+def test_known_answers(gpu_lib, golden, i):
+    c = golden["cases"][i]
+    X, y = np.array(c["X"]), np.array(c["y"])
+    k = gpu_lib.Kriging("gauss")
+    k.fit(y, X, "constant", False, "none", "LL", {"theta": 0.3 * np.ones((1, X.shape[1]))})
+    ll, g, _ = k.logLikelihoodFun(golden["theta_value"] * np.ones(X.shape[1]), True)
+    assert rel_err(ll, c["ll"]) < 1e-10
+    assert rel_err(g, c["grad"]) < 1e-10
+
+
+def _data(n, d, seed, f="sin"):
+    rng = np.random.default_rng(seed)
+    X = rng.uniform(size=(n, d))
+    y = np.sin(2 * np.pi * X).sum(axis=1) + 0.1 * rng.standard_normal(n)
+    return X, y
+
+
+CASES = [  # (kernel, n, d, regmodel)
+    ("gauss", 70, 2, "constant"),
+    ("exp", 130, 3, "linear"),
+    ("matern3_2", 200, 4, "constant"),
+    ("matern5_2", 257, 8, "quadratic"),
+    ("matern5_2", 1, 2, "none"),
+    ("gauss", 64, 5, "interactive"),
+    ("matern5_2", 513, 6, "constant"),
+]
+
+
+@pytest.mark.parametrize("kernel,n,d,reg", CASES)
+def test_ll_grad_vs_oracle(gpu_lib, kernel, n, d, reg):
+    X, y = _data(n, d, n + d)
+    lo, hi = (0.05, 0.15) if kernel == "gauss" else (0.2, 1.5)  # keep cond(R) <= ~1e7 (no nugget retry)
+    th = np.random.default_rng(7).uniform(lo, hi, size=d)
+    ora = O.OracleKriging(y, X, kernel, regmodel=reg)
+    ll_o, g_o = ora.log_likelihood(th)
+    k = gpu_lib.Kriging(kernel)
+    k.fit(y, X, reg, False, "none", "LL", {"theta": th.reshape(1, -1)})
+    ll, g, _ = k.logLikelihoodFun(th, True)
+    assert rel_err(ll, ll_o) < LL_TOL, (ll, ll_o)
+    assert rel_err(g, g_o) < GRAD_TOL, (g, g_o)
+    ll2, _, _ = k.logLikelihoodFun(th, False)
+    assert ll2 == ll  # the LL value does not depend on whether the gradient was requested
+
+
+@pytest.mark.parametrize("est", [(True, True), (True, False), (False, False)])
+def test_nugget_ll_grad_vs_oracle(gpu_lib, est):
+    X, y = _data(90, 3, 11)
+    ora = O.OracleKriging(y, X, "matern5_2", noise_model="nugget", est_sigma2=est[0], sigma2=0.5,
+                          est_nugget=est[1], nugget=0.1)
+    ta = np.array([0.4, 0.6, 0.5, 0.9])
+    ll_o, g_o = ora.log_likelihood(ta)
+    k = gpu_lib.Kriging("matern5_2", "nugget")
+    k.fit(y, X, "constant", False, "none", "LL",
+          {"theta": ta[:3].reshape(1, -1), "sigma2": 0.5, "is_sigma2_estim": est[0], "nugget": 0.1,
+           "is_nugget_estim": est[1]})
+    ll, g, _ = k.logLikelihoodFun(ta, True)
+    assert rel_err(ll, ll_o) < LL_TOL
+    assert rel_err(g, g_o) < GRAD_TOL
+
+
+def test_batch_matches_single(gpu_lib):
+    X, y = _data(150, 3, 5)
+    k = gpu_lib.Kriging("gauss")
+    k.fit(y, X, "constant", False, "none", "LL", {"theta": np.full((1, 3), 0.5)})
+    thetas = np.random.default_rng(3).uniform(0.1, 2.0, size=(9, 3))
+    ll_b, g_b = k.logLikelihoodFunBatch(thetas, True)
+    for i in range(9):
+        ll, g, _ = k.logLikelihoodFun(thetas[i], True)
+        assert ll == ll_b[i]
+        assert np.array_equal(g, g_b[i])
+
+
+def test_gradient_vs_central_fd(gpu_lib):
+    X, y = _data(120, 2, 9)
+    k = gpu_lib.Kriging("matern3_2")
+    k.fit(y, X, "constant", False, "none", "LL", {"theta": np.full((1, 2), 0.5)})
+    th = np.array([0.3, 0.45])
+    _, g, _ = k.logLikelihoodFun(th, True)
+    for j in range(2):
+        h = 1e-6 * th[j]
+        e = np.zeros(2)
+        e[j] = h
+        fd = (k.logLikelihoodFun(th + e)[0] - k.logLikelihoodFun(th - e)[0]) / (2 * h)
+        assert abs(g[j] - fd) < 1e-5 * max(1.0, abs(fd))
+
+
+def test_retry_semantics_duplicated_point(gpu_lib):
+    # safe_chol_lower_retry (LinearAlgebra.cpp:68-98): an exactly duplicated design point makes R singular; one
+    # numerical-nugget increment (1e-10) restores rcond(L)^2 ~ 1e-12 > 1e-18, on both the oracle and the GPU.
+    x = np.linspace(0, 1, 40).reshape(-1, 1)
+    x = np.vstack([x, x[5:6]])
+    y = np.sin(3 * x[:, 0])
+    th = np.array([0.2])
+    ora = O.OracleKriging(y, x, "gauss")
+    assert O.populate_model("gauss", ora.X, ora.y, ora.F, th).nugget_increments == 1
+    ll_o, g_o = ora.log_likelihood(th)
+    k = gpu_lib.Kriging("gauss")
+    k.fit(y, x, "constant", False, "none", "LL", {"theta": th.reshape(1, -1)})
+    ll, g, _ = k.logLikelihoodFun(th, True)
+    assert rel_err(ll, ll_o) < 1e-8
+    assert rel_err(g, g_o) < 1e-5

@@ -1,0 +1,104 @@
+"""CPU tests of the oracle (the checker): pinned to the reference's known answers, plus the reference's own
+finite-difference and identity checks (tests/KrigingLogLikTest.cpp, NuggetKrigingLogLikTest.cpp,
+KrigingVecchiaTest.cpp:46-84 of libKriging)."""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from oracle import oracle as O
+
+TOL_GOLDEN = 1e-12  # bindings/Python/pylibkriging/tests/binding_consistency_test.py:11
+
+
+@pytest.mark.parametrize("i", range(11))
+def test_oracle_matches_reference_known_answers(golden, i):
+    c = golden["cases"][i]
+    X, y = np.array(c["X"]), np.array(c["y"])
+    k = O.OracleKriging(y, X, "gauss")
+    ll, g = k.log_likelihood(golden["theta_value"] * np.ones(X.shape[1]))
+    assert rel_err(ll, c["ll"]) < TOL_GOLDEN
+    assert rel_err(g, c["grad"]) < TOL_GOLDEN
+
+
+def _data(n, d, seed):
+    rng = np.random.default_rng(seed)
+    X = rng.uniform(size=(n, d))
+    y = np.sin(2 * np.pi * X).sum(axis=1) + 0.5 * X[:, 0] * X[:, -1]
+    return X, y
+
+
+@pytest.mark.parametrize("kernel", ["gauss", "exp", "matern3_2", "matern5_2"])
+def test_oracle_gradient_vs_central_fd(kernel):
+    X, y = _data(30, 2, 1)
+    k = O.OracleKriging(y, X, kernel)
+    th = np.array([0.4, 0.3])
+    _, g = k.log_likelihood(th)
+    h = 1e-6
+    fd = np.array([(k.log_likelihood(th + h * e, False)[0] - k.log_likelihood(th - h * e, False)[0]) / (2 * h)
+                   for e in np.eye(2)])
+    assert np.all(np.abs(g - fd) / (np.abs(g) + 1e-10) < 1e-3)
+
+
+@pytest.mark.parametrize("est", [(True, True), (True, False), (False, False)])
+def test_oracle_nugget_gradient_vs_fd(est):
+    # NuggetKrigingLogLikTest.cpp:11-80 pattern: [theta, alpha] gradient vs central FD
+    X = np.array([[0.0, 0.0], [1.0, 0.0], [0.0, 1.0], [1.0, 1.0], [0.5, 0.5], [0.3, 0.7]])
+    y = np.array([0.0, 1.0, 1.0, 2.0, 1.0, 0.8])
+    k = O.OracleKriging(y, X, "gauss", noise_model="nugget", est_sigma2=est[0], sigma2=0.5, est_nugget=est[1],
+                        nugget=0.1)
+    ta = np.array([0.4, 0.6, 0.45])
+    _, g = k.log_likelihood(ta)
+    h = 1e-7
+    fd = np.array([(k.log_likelihood(ta + h * e, False)[0] - k.log_likelihood(ta - h * e, False)[0]) / (2 * h)
+                   for e in np.eye(3)])
+    if est == (False, False):
+        assert g[2] == 0.0
+        fd[2] = 0.0
+    assert np.all(np.abs(g - fd) / (np.abs(g) + 1e-10) < 1e-3)
+
+
+def test_oracle_vecchia_full_conditioning_equals_exact_ll():
+    # KrigingVecchiaTest.cpp:46-61: VLL(n-1) ~= LL
+    X, y = _data(40, 2, 3)
+    k = O.OracleKriging(y, X, "matern5_2")
+    order, nbr = O.vecchia_sets(k.X, 39)
+    for th in ([0.2, 0.2], [0.4, 0.3]):
+        vll, _, _, _ = O.vecchia_ll("matern5_2", k.X, k.y, k.F, np.array(th), order, nbr, return_grad=False)
+        ll, _ = k.log_likelihood(np.array(th), False)
+        assert abs(vll - ll) < 1e-3 * abs(ll) + 1e-3
+
+
+def test_oracle_vecchia_gradient_vs_fd():
+    # KrigingVecchiaTest.cpp:63-84
+    X, y = _data(80, 2, 4)
+    k = O.OracleKriging(y, X, "matern5_2")
+    order, nbr = O.vecchia_sets(k.X, 15)
+    th = np.array([0.2, 0.3])
+    _, g, _, _ = O.vecchia_ll("matern5_2", k.X, k.y, k.F, th, order, nbr)
+    h = 1e-6
+    for j in range(2):
+        e = np.eye(2)[j] * h
+        fd = (O.vecchia_ll("matern5_2", k.X, k.y, k.F, th + e, order, nbr, return_grad=False)[0]
+              - O.vecchia_ll("matern5_2", k.X, k.y, k.F, th - e, order, nbr, return_grad=False)[0]) / (2 * h)
+        assert abs(g[j] - fd) < 1e-3 * max(1.0, abs(fd))
+
+
+def test_oracle_vecchia_sets_properties():
+    X, _ = _data(60, 3, 5)
+    order, nbr = O.vecchia_sets(X, 10)
+    assert sorted(order.tolist()) == list(range(60))
+    pos = {int(o): t for t, o in enumerate(order)}
+    for t in range(60):
+        ids = [int(v) for v in nbr[t] if v >= 0]
+        assert len(ids) == min(10, t)
+        assert all(pos[i] < t for i in ids)  # neighbours are earlier in the ordering
+
+
+def test_mt19937_stream_matches_std_uniform_real():
+    # std::mt19937(123) + uniform_real_distribution<double> (libstdc++: two 32-bit draws per double)
+    s = O.MT19937Stream(123)
+    u = s.uniform(3)
+    assert np.all((u >= 0) & (u < 1))
+    # first raw outputs of std::mt19937 seeded with 123 (published reference sequence of the generator)
+    raw = O.MT19937Stream(123).bg.random_raw(2)
+    assert raw.tolist() == [2991312382, 3062119789]
