@@ -62,6 +62,15 @@ int lkg_kriging_log_likelihood_fun_batch(void* ptr, const double* thetas, int k,
 int lkg_kriging_log_likelihood_fun_bench(void* ptr, const double* theta, int theta_n, int return_grad, double* ll_out,
                                          double* grad_out, char* bench_out, int bench_cap);
 
+/* No counterpart in the reference (it has only the FP64 LAPACK path): precision of this model's objective
+ * evaluations.  slices = 0 selects the FP64 path (default); 4..8 the mixed path, where the O(n^3) products of the
+ * Cholesky, the triangular inverse and R^-1 run on the bf16 tensor cores by error-free splitting into `slices`
+ * base-256 digits (7 ~ FP64-level products); a mixed factorisation that meets a non-positive pivot is redone on
+ * the FP64 path.  lkg_kriging_last_slices reports what the last logLikelihoodFun used (0 after such a retreat). */
+int lkg_kriging_set_precision(void* ptr, int slices);
+int lkg_kriging_get_precision(void* ptr);
+int lkg_kriging_last_slices(void* ptr);
+
 /* getters, libkriging_c.h:141-166 */
 const char* lkg_kriging_kernel(void* ptr);
 const char* lkg_kriging_optim(void* ptr);
@@ -112,6 +121,16 @@ const char* lkg_device_name(void);
 /* No counterpart in the reference: measured FP64 FMA throughput (TFLOP/s) of this GPU, the roofline denominator of
  * the FP64 kernels (the DFMA pipe; FP64 mma.sync is slower on GB300). */
 int lkg_probe_fp64_peak(double* tflops_out);
+/* No counterpart in the reference (it times stages with Bench::tic/toc, src/lib/Bench.cpp): per-kernel launch
+ * counts, and with timing enabled CUDA-event durations on each launch's own stream plus the launch's algorithmic
+ * flops and bytes.  lkg_stats_report writes "name<TAB>launches<TAB>timed<TAB>ms<TAB>flops<TAB>bytes<LF>" lines and
+ * returns the length needed (including the terminating NUL), or -1. */
+void lkg_stats_enable(int on);
+void lkg_stats_reset(void);
+int lkg_stats_report(char* out, int cap);
+/* No counterpart in the reference: C = A B^T (A M x K, B N x K, C M x N, column-major host buffers) through the
+ * split-bf16 tensor-core GEMM with `slices` digits -- the check hook of the mixed path's emulated products. */
+int lkg_ozaki_gemm_check(int M, int N, int K, const double* A, const double* B, int slices, double* C);
 
 #ifdef __cplusplus
 }

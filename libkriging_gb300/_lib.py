@@ -76,6 +76,13 @@ _SIGS = {
     "lkg_optim_set_max_restart": (None, [_i]),
     "lkg_device_name": (_cp, []),
     "lkg_probe_fp64_peak": (_i, [_dp]),
+    "lkg_stats_enable": (None, [_i]),
+    "lkg_stats_reset": (None, []),
+    "lkg_stats_report": (_i, [ctypes.c_char_p, _i]),
+    "lkg_kriging_set_precision": (_i, [_vp, _i]),
+    "lkg_kriging_get_precision": (_i, [_vp]),
+    "lkg_kriging_last_slices": (_i, [_vp]),
+    "lkg_ozaki_gemm_check": (_i, [_i, _i, _i, _dp, _dp, _i, _dp]),
 }
 
 _lib = None

@@ -401,3 +401,30 @@ void lkg_optim_set_objective_rel_tolerance(double t) { lkg::config().objective_r
 void lkg_optim_set_max_restart(int m) { lkg::config().max_restart = m; }
 
 }  // extern "C"
+
+// ---- mixed precision (no counterpart in the reference) ----
+extern "C" {
+
+int lkg_kriging_set_precision(void* ptr, int slices) {
+  try {
+    K(ptr)->set_precision(slices);
+    return 0;
+  }
+  CATCH_RETURN
+}
+
+int lkg_kriging_get_precision(void* ptr) {
+  try {
+    return K(ptr)->precision();
+  }
+  CATCH_RETURN
+}
+
+int lkg_kriging_last_slices(void* ptr) {
+  try {
+    return K(ptr)->last_slices();
+  }
+  CATCH_RETURN
+}
+
+}  // extern "C"

@@ -6,6 +6,8 @@
 //   solve(trimatl(L), B), solve(trimatu(L'), B) -> trsm_lower_left[_t] (blocked, uses the diagonal-block inverses)
 #include "dense_fp64.cuh"
 
+#include "stats.hpp"
+
 namespace lkg {
 
 namespace {
@@ -287,6 +289,9 @@ void gemm_tiles(int M, int N, int K, double alpha, MatView A, MatView B, double 
                 int64_t c_batch, int batch, bool lower_only, cudaStream_t st) {
   if (M <= 0 || N <= 0) return;
   dim3 grid(ceil_div(M, TB), ceil_div(N, TB), batch);
+  const double fl = (lower_only && M == N) ? (double)K * M * (M + 1.0) : 2.0 * M * N * K;
+  const double by = 8.0 * ((double)M * K + (double)K * N + (beta == 0.0 ? 1.0 : 2.0) * M * N);
+  LaunchTimer lt("k_gemm_tiles", st, fl * batch, by * batch);
   k_gemm_tiles<<<grid, NT, 0, st>>>(M, N, K, alpha, A, B, beta, C, ldc, c_batch, lower_only);
   LKG_LAUNCH("k_gemm_tiles");
 }
@@ -298,6 +303,7 @@ void potrf_diag(double* A, int64_t lda, int64_t mstride, int k0, int nb, double*
     LKG_CUDA(cudaFuncSetAttribute(k_potrf_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     g_diag_attr_set = true;
   }
+  LaunchTimer lt("k_potrf_diag", st, 2.0 * nb * nb * nb / 3.0 * batch, 16.0 * nb * nb * batch);
   k_potrf_diag<<<dim3(1, 1, batch), NT, smem, st>>>(A, lda, mstride, k0, nb, Dinv, dinv_bstride, blk, info);
   LKG_LAUNCH("k_potrf_diag");
 }
@@ -323,6 +329,13 @@ void potrf_blocked(double* A, int64_t lda, int64_t mstride, int n, double* Dinv,
   }
 }
 
+void copy_dinv_block(const double* Dinv, int64_t dinv_bstride, int blk, double* W, int64_t ldw, int64_t wstride,
+                     int k0, int nb, int batch, cudaStream_t st) {
+  LaunchTimer lt("k_copy_dinv_block", st, 0.0, 16.0 * nb * nb * batch);
+  k_copy_dinv_block<<<dim3(1, 1, batch), 256, 0, st>>>(Dinv, dinv_bstride, blk, W, ldw, wstride, k0, nb);
+  LKG_LAUNCH("k_copy_dinv_block");
+}
+
 void trtri_blocked(const double* L, int64_t lda, int64_t mstride, int n, const double* Dinv, double* W, int64_t ldw,
                    int64_t wstride, int batch, cudaStream_t st) {
   const int nblk = ceil_div(n, NB);
@@ -331,6 +344,7 @@ void trtri_blocked(const double* L, int64_t lda, int64_t mstride, int n, const d
     LKG_CUDA(cudaMemset2DAsync(W + b * wstride, ldw * sizeof(double), 0, n * sizeof(double), n, st));
   for (int k = 0; k < nblk; ++k) {
     const int k0 = k * NB, nb = std::min(NB, n - k0);
+    LaunchTimer lt("k_copy_dinv_block", st, 0.0, 16.0 * nb * nb * batch);
     k_copy_dinv_block<<<dim3(1, 1, batch), 256, 0, st>>>(Dinv, dstride, k, W, ldw, wstride, k0, nb);
     LKG_LAUNCH("k_copy_dinv_block");
     if (k0 > 0) {
@@ -353,6 +367,8 @@ void wtw_lower(const double* W, int64_t ldw, int64_t wstride, int n, double* C, 
                int batch, cudaStream_t st) {
   const int nblk = ceil_div(n, TB);
   const int64_t ntiles = (int64_t)nblk * (nblk + 1) / 2;
+  // sum over the lower triangle of 2 (n - i) flops per entry = n (n + 1) (n + 2) / 3
+  LaunchTimer lt("k_wtw", st, (double)n * (n + 1.0) * (n + 2.0) / 3.0 * batch, 8.0 * n * (n + 1.0) * batch);
   k_wtw<<<dim3((unsigned)ntiles, 1, batch), NT, 0, st>>>(W, ldw, wstride, n, C, ldc, cstride);
   LKG_LAUNCH("k_wtw");
 }
@@ -377,9 +393,13 @@ void trsm_lower_left(const double* L, int64_t lda, int64_t mstride, int n, const
       }
       continue;
     }
-    k_small_apply<<<dim3(1, 1, batch), 256, smem, st>>>(Dinv, dstride, k, B, ldb, bstride, k0, nb, r, false);
+    {
+      LaunchTimer lt("k_small_apply", st, (double)nb * nb * r * batch, 16.0 * nb * r * batch);
+      k_small_apply<<<dim3(1, 1, batch), 256, smem, st>>>(Dinv, dstride, k, B, ldb, bstride, k0, nb, r, false);
+    }
     LKG_LAUNCH("k_small_apply");
     if (M > 0) {
+      LaunchTimer lt("k_panel_update", st, 2.0 * M * nb * r * batch, 8.0 * ((double)M * nb + 2.0 * M * r) * batch);
       k_panel_update<<<dim3(ceil_div(M, 128), 1, batch), 128, smem, st>>>(L, lda, mstride, B, ldb, bstride, k0, nb, M,
                                                                           r);
       LKG_LAUNCH("k_panel_update");
@@ -394,9 +414,13 @@ void trsm_lower_left_t(const double* L, int64_t lda, int64_t mstride, int n, con
   const size_t smem = sizeof(double) * NB * r;
   for (int k = nblk - 1; k >= 0; --k) {
     const int k0 = k * NB, nb = std::min(NB, n - k0);
-    k_small_apply<<<dim3(1, 1, batch), 256, smem, st>>>(Dinv, dstride, k, B, ldb, bstride, k0, nb, r, true);
+    {
+      LaunchTimer lt("k_small_apply", st, (double)nb * nb * r * batch, 16.0 * nb * r * batch);
+      k_small_apply<<<dim3(1, 1, batch), 256, smem, st>>>(Dinv, dstride, k, B, ldb, bstride, k0, nb, r, true);
+    }
     LKG_LAUNCH("k_small_apply");
     if (k0 > 0) {
+      LaunchTimer lt("k_panel_update_t", st, 2.0 * k0 * nb * r * batch, 8.0 * ((double)k0 * nb + 2.0 * k0 * r) * batch);
       k_panel_update_t<<<dim3(ceil_div(k0, 8), 1, batch), 256, smem, st>>>(L, lda, mstride, B, ldb, bstride, k0, nb,
                                                                            r);
       LKG_LAUNCH("k_panel_update_t");

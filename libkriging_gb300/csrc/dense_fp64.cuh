@@ -42,6 +42,29 @@ void trtri_blocked(const double* L, int64_t lda, int64_t mstride, int n, const d
 void wtw_lower(const double* W, int64_t ldw, int64_t wstride, int n, double* C, int64_t ldc, int64_t cstride,
                int batch, cudaStream_t st);
 
+// W(k0:k0+nb, k0:k0+nb) = Dinv block blk (full NB x NB block with its zero upper part).
+void copy_dinv_block(const double* Dinv, int64_t dinv_bstride, int blk, double* W, int64_t ldw, int64_t wstride,
+                     int k0, int nb, int batch, cudaStream_t st);
+
+// Mixed-precision variants (trailing updates, trtri updates and W^T W on the bf16 tensor cores by error-free
+// splitting into `slices` digit planes, see ozaki.cuh); diagonal blocks, panels and small products stay FP64.
+struct MixedWorkspace {
+  int slices = 7;
+  void* panel = nullptr;  // bf16 planes, split_plane_elems(n, 64, slices) per batch entry
+  int* panel_exp = nullptr;
+  void* rowblk = nullptr;  // bf16 planes, same size
+  int* rowblk_exp = nullptr;
+  void* wfull = nullptr;  // bf16 planes, split_plane_elems(n, n, slices) per batch entry
+  int* wfull_exp = nullptr;
+  int n = 0;
+};
+void potrf_blocked_mixed(double* A, int64_t lda, int64_t mstride, int n, double* Dinv, int* info, int batch,
+                         const MixedWorkspace& ws, cudaStream_t st);
+void trtri_blocked_mixed(const double* L, int64_t lda, int64_t mstride, int n, const double* Dinv, double* W,
+                         int64_t ldw, int64_t wstride, int batch, const MixedWorkspace& ws, cudaStream_t st);
+void wtw_lower_mixed(const double* W, int64_t ldw, int64_t wstride, int n, double* C, int64_t ldc, int64_t cstride,
+                     int batch, const MixedWorkspace& ws, cudaStream_t st);
+
 // Solve L X = B in place (B n x r column-major, ldb, batch stride bstride).
 void trsm_lower_left(const double* L, int64_t lda, int64_t mstride, int n, const double* Dinv, double* B,
                      int64_t ldb, int64_t bstride, int r, int batch, cudaStream_t st);

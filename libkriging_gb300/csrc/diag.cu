@@ -70,3 +70,48 @@ int lkg_probe_fp64_peak(double* tflops_out) {
 }
 
 }  // extern "C"
+
+// ---- emulated-GEMM check entry point (host buffers) ----
+#include "ozaki.cuh"
+
+extern "C" int lkg_ozaki_gemm_check(int M, int N, int K, const double* A, const double* B, int slices, double* C) {
+  // C = A * B^T with A (M x K) and B (N x K) column-major, computed by the split-bf16 tensor-core path
+  double *dA = nullptr, *dB = nullptr, *dC = nullptr;
+  void *pa = nullptr, *pb = nullptr;
+  int *ea = nullptr, *eb = nullptr;
+  int rc = -1;
+  try {
+    LKG_CUDA(cudaMalloc(&dA, sizeof(double) * M * K));
+    LKG_CUDA(cudaMalloc(&dB, sizeof(double) * N * K));
+    LKG_CUDA(cudaMalloc(&dC, sizeof(double) * M * N));
+    LKG_CUDA(cudaMemcpy(dA, A, sizeof(double) * M * K, cudaMemcpyHostToDevice));
+    LKG_CUDA(cudaMemcpy(dB, B, sizeof(double) * N * K, cudaMemcpyHostToDevice));
+    LKG_CUDA(cudaMalloc(&pa, lkg::split_plane_elems(M, K, slices) * 2));
+    LKG_CUDA(cudaMalloc(&pb, lkg::split_plane_elems(N, K, slices) * 2));
+    LKG_CUDA(cudaMalloc(&ea, lkg::split_exp_elems(M, K) * sizeof(int)));
+    LKG_CUDA(cudaMalloc(&eb, lkg::split_exp_elems(N, K) * sizeof(int)));
+    lkg::SplitBuf sa, sb;
+    sa.planes = static_cast<__nv_bfloat16*>(pa);
+    sa.exps = ea;
+    sa.S = slices;
+    sb.planes = static_cast<__nv_bfloat16*>(pb);
+    sb.exps = eb;
+    sb.S = slices;
+    lkg::ozaki_split(M, K, dA, 1, M, 0, 1, sa, 0);
+    lkg::ozaki_split(N, K, dB, 1, N, 0, 1, sb, 0);
+    lkg::ozaki_gemm(M, N, 0, sa.nchunk, 1.0, sa, 0, sb, 0, 0.0, dC, M, 0, 1, false, 0);
+    LKG_CUDA(cudaDeviceSynchronize());
+    LKG_CUDA(cudaMemcpy(C, dC, sizeof(double) * M * N, cudaMemcpyDeviceToHost));
+    rc = 0;
+  } catch (const std::exception&) {
+    rc = -1;
+  }
+  cudaFree(dA);
+  cudaFree(dB);
+  cudaFree(dC);
+  cudaFree(pa);
+  cudaFree(pb);
+  cudaFree(ea);
+  cudaFree(eb);
+  return rc;
+}

@@ -17,6 +17,7 @@
 #include "common.cuh"
 #include "dense_fp64.cuh"
 #include "lik_kernels.cuh"
+#include "ozaki.cuh"
 
 namespace lkg {
 
@@ -133,7 +134,43 @@ Engine::~Engine() {
     if (p) cudaFree(p);
   if (dinfo_) cudaFree(dinfo_);
   if (dgls_info_) cudaFree(dgls_info_);
+  for (void* p : {dpanel_, drowblk_, dwfull_})
+    if (p) cudaFree(p);
+  for (int* p : {dpanel_exp_, drowblk_exp_, dwfull_exp_})
+    if (p) cudaFree(p);
   if (st_) cudaStreamDestroy(st_);
+}
+
+void Engine::set_slices(int s) {
+  if (s != 0 && (s < 4 || s > 8)) throw std::invalid_argument("mixed precision: slices must be 0 (FP64) or 4..8");
+  slices_ = s;
+}
+
+void Engine::ensure_mixed_buffers(bool with_grad) {
+  if (mixed_alloc_slices_ != slices_) {
+    for (void** p : {&dpanel_, &drowblk_, &dwfull_})
+      if (*p) {
+        cudaFree(*p);
+        *p = nullptr;
+      }
+    for (int** p : {&dpanel_exp_, &drowblk_exp_, &dwfull_exp_})
+      if (*p) {
+        cudaFree(*p);
+        *p = nullptr;
+      }
+    mixed_alloc_slices_ = slices_;
+  }
+  const size_t pe = split_plane_elems(n_, NB, slices_) * cap_, ee = split_exp_elems(n_, NB) * cap_;
+  if (!dpanel_) {
+    LKG_CUDA(cudaMalloc(&dpanel_, pe * 2));
+    LKG_CUDA(cudaMalloc(&drowblk_, pe * 2));
+    dalloc(&dpanel_exp_, ee);
+    dalloc(&drowblk_exp_, ee);
+  }
+  if (with_grad && !dwfull_) {
+    LKG_CUDA(cudaMalloc(&dwfull_, split_plane_elems(n_, n_, slices_) * cap_ * 2));
+    dalloc(&dwfull_exp_, split_exp_elems(n_, n_) * cap_);
+  }
 }
 
 void Engine::ensure_grad_buffers() {
@@ -285,13 +322,77 @@ void Engine::evaluate(int batch, const double* thetas, const double* factors, bo
   std::vector<char> dead(batch, 0);
   std::vector<int> info(batch, 0);
   std::vector<double> rc2(batch, -1.0);
+  MixedWorkspace mw;
+  if (slices_ > 0) {
+    ensure_mixed_buffers(with_grad);
+    mw.slices = slices_;
+    mw.n = n;
+    mw.panel = dpanel_;
+    mw.panel_exp = dpanel_exp_;
+    mw.rowblk = drowblk_;
+    mw.rowblk_exp = drowblk_exp_;
+    mw.wfull = dwfull_;
+    mw.wfull_exp = dwfull_exp_;
+  }
+  bool retreated = false;
+  bool w_valid = false;  // W = L^-1 of the accepted factor is already in dW_
   for (int attempt = 0;; ++attempt) {
     LKG_CUDA(cudaMemcpyAsync(ddiag_, diag.data(), sizeof(double) * batch, cudaMemcpyHostToDevice, st_));
     cov_build_lower(kernel_, n, d, dX_, 0, dtheta_, dfactor_, ddiag_, dA_, lda_, mstride_, batch, st_);
-    potrf_blocked(dA_, lda_, mstride_, n, dDinv_, dinfo_, batch, st_);
+    if (slices_ > 0 && !retreated) {
+      potrf_blocked_mixed(dA_, lda_, mstride_, n, dDinv_, dinfo_, batch, mw, st_);
+      LKG_CUDA(cudaMemcpyAsync(info.data(), dinfo_, sizeof(int) * batch, cudaMemcpyDeviceToHost, st_));
+      LKG_CUDA(cudaStreamSynchronize(st_));
+      bool any_fail = false;
+      for (int b = 0; b < batch; ++b) any_fail = any_fail || (info[b] != 0 && !dead[b]);
+      if (any_fail) {  // retreat: redo this factorisation on the FP64 path before the nugget-retry rules apply
+        retreated = true;
+        cov_build_lower(kernel_, n, d, dX_, 0, dtheta_, dfactor_, ddiag_, dA_, lda_, mstride_, batch, st_);
+        potrf_blocked(dA_, lda_, mstride_, n, dDinv_, dinfo_, batch, st_);
+      }
+    } else {
+      potrf_blocked(dA_, lda_, mstride_, n, dDinv_, dinfo_, batch, st_);
+    }
     LKG_CUDA(cudaMemcpyAsync(info.data(), dinfo_, sizeof(int) * batch, cudaMemcpyDeviceToHost, st_));
     LKG_CUDA(cudaStreamSynchronize(st_));
-    if (cfg.chol_rcond_check) rcond_batch(batch, rc2);
+    w_valid = false;
+    if (cfg.chol_rcond_check) {
+      if (with_grad) {
+        // The gradient needs W = L^-1 anyway: rcond_exact = 1 / (|L|_1 |L^-1|_1) <= the dlacn2 estimate, so
+        // rcond_exact^2 >= min_rcond already decides "no retry"; only entries below it run the estimator.
+        ensure_grad_buffers();
+        if (slices_ > 0 && !retreated)
+          trtri_blocked_mixed(dA_, lda_, mstride_, n, dDinv_, dW_, lda_, mstride_, batch, mw, st_);
+        else
+          trtri_blocked(dA_, lda_, mstride_, n, dDinv_, dW_, lda_, mstride_, batch, st_);
+        w_valid = true;
+        std::vector<double> cl((size_t)n * batch), cw((size_t)n * batch);
+        lower_colsum_abs(n, dA_, lda_, mstride_, dcol_, batch, st_);
+        LKG_CUDA(cudaMemcpyAsync(cl.data(), dcol_, sizeof(double) * n * batch, cudaMemcpyDeviceToHost, st_));
+        lower_colsum_abs(n, dW_, lda_, mstride_, dvec_, batch, st_);
+        LKG_CUDA(cudaMemcpyAsync(cw.data(), dvec_, sizeof(double) * n * batch, cudaMemcpyDeviceToHost, st_));
+        LKG_CUDA(cudaStreamSynchronize(st_));
+        bool need_est = false;
+        for (int b = 0; b < batch; ++b) {
+          double an = 0.0, wn = 0.0;
+          for (int j = 0; j < n; ++j) {
+            an = std::max(an, cl[(size_t)b * n + j]);
+            wn = std::max(wn, cw[(size_t)b * n + j]);
+          }
+          const double rc = (an > 0.0 && wn > 0.0 && std::isfinite(wn)) ? (1.0 / an) / wn : 0.0;
+          rc2[b] = rc * rc;
+          if (info[b] == 0 && !dead[b] && !(rc2[b] >= cfg.min_rcond)) need_est = true;
+        }
+        if (need_est) {
+          std::vector<double> est;
+          rcond_batch(batch, est);
+          for (int b = 0; b < batch; ++b)
+            if (!(rc2[b] >= cfg.min_rcond)) rc2[b] = est[b];
+        }
+      } else {
+        rcond_batch(batch, rc2);
+      }
+    }
     bool retry = false;
     for (int b = 0; b < batch; ++b) {
       if (dead[b]) continue;
@@ -320,6 +421,8 @@ void Engine::evaluate(int batch, const double* thetas, const double* factors, bo
   for (int b = 0; b < batch; ++b) {
     out[b].nugget_increments = inc[b];
     out[b].rcond = rc2[b];
+    out[b].slices = retreated ? 0 : slices_;
+    out[b].retreated = retreated;
   }
   tm.lap("R = _Cov(dX) & L = Chol(R)");
 
@@ -346,8 +449,13 @@ void Engine::evaluate(int batch, const double* thetas, const double* factors, bo
     LKG_CUDA(cudaMemcpyAsync(dxv_, dEstar_, sizeof(double) * n * batch, cudaMemcpyDeviceToDevice, st_));
     trsm_lower_left_t(dA_, lda_, mstride_, n, dDinv_, dxv_, n, n, 1, batch, st_);
     tm.lap("x = tL \\ z");
-    trtri_blocked(dA_, lda_, mstride_, n, dDinv_, dW_, lda_, mstride_, batch, st_);
-    wtw_lower(dW_, lda_, mstride_, n, dRinv_, lda_, mstride_, batch, st_);
+    if (slices_ > 0 && !retreated) {
+      if (!w_valid) trtri_blocked_mixed(dA_, lda_, mstride_, n, dDinv_, dW_, lda_, mstride_, batch, mw, st_);
+      wtw_lower_mixed(dW_, lda_, mstride_, n, dRinv_, lda_, mstride_, batch, mw, st_);
+    } else {
+      if (!w_valid) trtri_blocked(dA_, lda_, mstride_, n, dDinv_, dW_, lda_, mstride_, batch, st_);
+      wtw_lower(dW_, lda_, mstride_, n, dRinv_, lda_, mstride_, batch, st_);
+    }
     tm.lap("R^-1 = L^-T * L^-1");
     adjoint_sums(kernel_, n, d, dX_, 0, dtheta_, dfactor_, dxv_, n, dRinv_, lda_, mstride_, dpart_, dadj_, batch,
                  st_);

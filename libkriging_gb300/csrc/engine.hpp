@@ -23,6 +23,8 @@ struct EvalOut {
   std::vector<double> beta;    // GLS beta (p)
   std::vector<double> adj;     // adjoint sums [T1(d), T2(d), U1, U2, D1, D2] (with_grad)
   double rcond = -1.0;         // rcond(L)^2 of the accepted factor (when the check ran)
+  int slices = 0;              // 0: FP64 path; > 0: tensor-core digit slices used for the O(n^3) products
+  bool retreated = false;      // the mixed factorisation hit a non-positive pivot and was redone in FP64
 };
 
 class Engine {
@@ -48,6 +50,9 @@ class Engine {
   int p() const { return p_; }
   int kernel() const { return kernel_; }
   int capacity() const { return cap_; }
+  // 0 selects the FP64 path; 4..8 the mixed path with that many bf16 digit slices (7 ~ FP64-level products)
+  void set_slices(int s);
+  int slices() const { return slices_; }
   cudaStream_t stream() const { return st_; }
 
   // device pointers (batch entry 0 layout) for predict: factor, diagonal-block inverses, Fstar, Estar
@@ -62,9 +67,14 @@ class Engine {
 
  private:
   void ensure_grad_buffers();
+  void ensure_mixed_buffers(bool with_grad);
   void rcond_batch(int batch, std::vector<double>& rc2);  // rcond(L)^2 per entry, dtrcon('1') style estimate
 
   int kernel_, n_, d_, p_, cap_;
+  int slices_ = 0;
+  void *dpanel_ = nullptr, *drowblk_ = nullptr, *dwfull_ = nullptr;
+  int *dpanel_exp_ = nullptr, *drowblk_exp_ = nullptr, *dwfull_exp_ = nullptr;
+  int mixed_alloc_slices_ = 0;
   int64_t lda_, mstride_, dstride_, fystride_;
   cudaStream_t st_ = nullptr;
   double *dX_ = nullptr, *dY_ = nullptr, *dF_ = nullptr;

@@ -178,6 +178,14 @@ void Kriging::ensure_engine(int batch_cap) {
   if (!m_eval || m_eval->capacity() < batch_cap)
     m_eval = std::make_unique<Engine>(m_kernel, m_n, m_d, m_p, m_X.data(), m_y.data(), m_F.data(),
                                       std::max(batch_cap, 1));
+  m_eval->set_slices(m_slices);
+}
+
+void Kriging::set_precision(int slices) {
+  if (slices != 0 && (slices < 4 || slices > 8))
+    throw std::invalid_argument("set_precision: slices must be 0 (FP64) or 4..8");
+  m_slices = slices;
+  if (m_eval) m_eval->set_slices(slices);
 }
 
 double Kriging::loglik_from(const EvalOut& o, double extra_param, std::vector<double>* grad, int gdim) const {
@@ -256,6 +264,7 @@ std::tuple<double, std::vector<double>> Kriging::logLikelihoodFun(const std::vec
   m_bench.clear();
   m_eval->evaluate(1, gamma.data(), &factor, return_grad, out, bench ? &m_bench : nullptr);
   m_evals++;
+  m_last_slices = out[0].slices;
   std::vector<double> grad;
   const double ll = loglik_from(out[0], extra, return_grad ? &grad : nullptr, (int)gamma.size());
   return {ll, grad};

@@ -100,6 +100,12 @@ class Kriging {
   const std::map<std::string, double>& last_bench() const { return m_bench; }
   // total evaluations performed by the engine since construction (objective calls, batched entries counted once each)
   long long evaluations() const { return m_evals; }
+  // 0: FP64 path (default); 4..8: mixed path with that many bf16 digit slices for the O(n^3) products of the
+  // objective evaluations (logLikelihoodFun and the fit); the committed model used by predict stays FP64.
+  void set_precision(int slices);
+  int precision() const { return m_slices; }
+  // mixed-path bookkeeping of the last logLikelihoodFun: slices used (0 = FP64, also after a retreat)
+  int last_slices() const { return m_last_slices; }
 
  private:
   double loglik_from(const EvalOut& o, double extra_param, std::vector<double>* grad, int gdim) const;
@@ -126,6 +132,8 @@ class Kriging {
   long long m_evals = 0;
   EvalOut m_last_commit;
   int m_last_fit_starts = 0;
+  int m_slices = 0;
+  int m_last_slices = 0;
 };
 
 }  // namespace lkg

@@ -9,6 +9,8 @@
 //   cov_cross         KrigingImpl::predict_impl R_on loop (src/lib/KrigingImpl.cpp:194-221)
 #include "lik_kernels.cuh"
 
+#include "stats.hpp"
+
 namespace lkg {
 
 namespace {
@@ -344,6 +346,7 @@ struct CovLowerLaunch {
                   const double* diag, double* A, int64_t lda, int64_t mstride, int batch, cudaStream_t st) {
     const int nb = ceil_div(n, T);
     const int64_t ntiles = (int64_t)nb * (nb + 1) / 2;
+    LaunchTimer lt("k_cov_lower", st, 0.5 * n * (n - 1.0) * batch, 4.0 * n * (n + 1.0) * batch);
     k_cov_lower<K, DM><<<dim3((unsigned)ntiles, 1, batch), 256, 0, st>>>(n, d, X, xb, theta, factor, diag, A, lda,
                                                                           mstride);
     LKG_LAUNCH("k_cov_lower");
@@ -354,6 +357,7 @@ template <int K, int DM>
 struct CovCrossLaunch {
   static void run(int n_o, int q, int d, const double* Xo, const double* Xn, const double* theta, double factor,
                   double* R, cudaStream_t st) {
+    LaunchTimer lt("k_cov_cross", st, (double)n_o * q, 8.0 * n_o * q);
     k_cov_cross<K, DM><<<dim3(ceil_div(n_o, T), ceil_div(q, T), 1), 256, 0, st>>>(n_o, q, d, Xo, Xn, theta, factor,
                                                                                    R);
     LKG_LAUNCH("k_cov_cross");
@@ -365,6 +369,7 @@ struct AdjointLaunch {
   static void run(int n, int d, const double* X, int64_t xb, const double* theta, const double* factor,
                   const double* xv, int64_t xvb, const double* Rinv, int64_t ldr, int64_t rstride, double* partials,
                   int64_t ntiles, int batch, cudaStream_t st) {
+    LaunchTimer lt("k_adjoint", st, 0.5 * n * (n - 1.0) * batch, 4.0 * n * (n + 1.0) * batch);
     k_adjoint<K, DM><<<dim3((unsigned)ntiles, 1, batch), 256, 0, st>>>(n, d, X, xb, theta, factor, xv, xvb, Rinv, ldr,
                                                                         rstride, partials, ntiles);
     LKG_LAUNCH("k_adjoint");
@@ -399,6 +404,7 @@ void adjoint_sums(int kernel, int n, int d, const double* X, int64_t x_bstride, 
   dispatch_kd<AdjointLaunch>(kernel, d, n, d, X, x_bstride, theta, factor, xv, xv_bstride, Rinv, ldr, rstride,
                              partials, ntiles, batch, st);
   const int nacc = adjoint_nacc(d);
+  LaunchTimer lt("k_reduce_partials", st, 0.0, 8.0 * ntiles * nacc * batch);
   k_reduce_partials<<<dim3(nacc, 1, batch), 1024, 0, st>>>(partials, ntiles, nacc, out);
   LKG_LAUNCH("k_reduce_partials");
 }
@@ -406,6 +412,7 @@ void adjoint_sums(int kernel, int n, int d, const double* X, int64_t x_bstride, 
 void gram_and_logdet(int n, int ncols, const double* Mat, int64_t ldm, int64_t mstride, const double* L, int64_t ldl,
                      int64_t lstride, double* out, int64_t out_bstride, int batch, cudaStream_t st) {
   const int npairs = ncols * (ncols + 1) / 2;
+  LaunchTimer lt("k_gram_logdet", st, 2.0 * n * npairs * batch, 8.0 * n * ncols * batch);
   k_gram_logdet<<<dim3(npairs + 1, 1, batch), 256, 0, st>>>(n, ncols, Mat, ldm, mstride, L, ldl, lstride, out,
                                                              out_bstride);
   LKG_LAUNCH("k_gram_logdet");
@@ -414,6 +421,7 @@ void gram_and_logdet(int n, int ncols, const double* Mat, int64_t ldm, int64_t m
 void gls_solve(int p, const double* gram, int64_t gram_bstride, double* beta, int64_t beta_bstride, double* rstar,
                int64_t rstar_bstride, int* gls_info, int batch, cudaStream_t st) {
   if (p > PMAX) throw std::invalid_argument("trend with more than 64 columns is not supported");
+  LaunchTimer lt("k_gls_solve", st, 0.0, 0.0);
   k_gls_solve<<<batch, 32, 0, st>>>(p, gram, gram_bstride, beta, beta_bstride, rstar, rstar_bstride, gls_info);
   LKG_LAUNCH("k_gls_solve");
 }
@@ -421,6 +429,7 @@ void gls_solve(int p, const double* gram, int64_t gram_bstride, double* beta, in
 void residual_sse(int n, int p, const double* FY, int64_t ldfy, int64_t fystride, const double* beta,
                   int64_t beta_bstride, double* Estar, int64_t estride, double* sse, int64_t sse_bstride, int batch,
                   cudaStream_t st) {
+  LaunchTimer lt("k_residual_sse", st, 2.0 * n * (p + 1.0) * batch, 8.0 * n * (p + 2.0) * batch);
   k_residual_sse<<<batch, 1024, 0, st>>>(n, p, FY, ldfy, fystride, beta, beta_bstride, Estar, estride, sse,
                                          sse_bstride);
   LKG_LAUNCH("k_residual_sse");
@@ -428,6 +437,7 @@ void residual_sse(int n, int p, const double* FY, int64_t ldfy, int64_t fystride
 
 void lower_colsum_abs(int n, const double* L, int64_t ldl, int64_t lstride, double* colsum, int batch,
                       cudaStream_t st) {
+  LaunchTimer lt("k_lower_colsum_abs", st, 0.5 * n * (n + 1.0) * batch, 4.0 * n * (n + 1.0) * batch);
   k_lower_colsum_abs<<<dim3(ceil_div(n, 8), 1, batch), 256, 0, st>>>(n, L, ldl, lstride, colsum);
   LKG_LAUNCH("k_lower_colsum_abs");
 }

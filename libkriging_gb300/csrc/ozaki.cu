@@ -1,0 +1,298 @@
+// ozaki.cu -- FP64 GEMM emulated with bf16 mma.sync by error-free digit splitting (see ozaki.cuh for the method).
+#include "ozaki.cuh"
+
+#include "stats.hpp"
+
+namespace lkg {
+
+namespace {
+
+constexpr int OZ_PAD = 72;  // smem row stride (bf16): 144 B rows keep the 32-bit fragment loads conflict-free
+
+__global__ void k_oz_split(int rows, int K, const double* __restrict__ p, int64_t s_r, int64_t s_k, int64_t bstride,
+                           SplitBuf out) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r = blockIdx.x * 8 + warp, c = blockIdx.y;
+  const int64_t b = blockIdx.z;
+  if (r >= out.rows_pad) return;
+  double x0 = 0.0, x1 = 0.0;
+  const int k0 = c * OZ_CHUNK + lane, k1 = k0 + 32;
+  if (r < rows) {
+    const double* pb = p + b * bstride + (int64_t)r * s_r;
+    if (k0 < K) x0 = pb[(int64_t)k0 * s_k];
+    if (k1 < K) x1 = pb[(int64_t)k1 * s_k];
+  }
+  double m = fmax(fabs(x0), fabs(x1));
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  int e = 0;
+  if (m > 0.0) {
+    int E;
+    frexp(m, &E);
+    e = E + 1;  // |x| 2^-e < 1/2, so every balanced base-256 digit lies in [-128, 128]
+  }
+  double v0 = ldexp(x0, -e), v1 = ldexp(x1, -e);
+  __nv_bfloat16* base = out.planes + b * out.plane_bstride;
+  for (int i = 0; i < out.S; ++i) {
+    v0 *= 256.0;
+    v1 *= 256.0;
+    const double d0 = rint(v0), d1 = rint(v1);
+    v0 -= d0;
+    v1 -= d1;
+    __nv_bfloat16* row = base + (((int64_t)i * out.nchunk + c) * out.rows_pad + r) * OZ_CHUNK;
+    row[lane] = __double2bfloat16(d0);
+    row[lane + 32] = __double2bfloat16(d1);
+  }
+  if (lane == 0) out.exps[b * out.exp_bstride + (int64_t)c * out.rows_pad + r] = e;
+}
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem));
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n" ::);
+  asm volatile("cp.async.wait_group 0;\n" ::);
+}
+
+__device__ __forceinline__ void ldsm_x4(unsigned& r0, unsigned& r1, unsigned& r2, unsigned& r3, const void* p) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(s));
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// exact (v * 2^E) as a double for an integer-valued float v (|v| < 2^24), by exponent arithmetic on the bits
+__device__ __forceinline__ double scaled_to_double(float v, int E) {
+  const unsigned u = __float_as_uint(v);
+  if ((u & 0x7fffffffu) == 0u) return 0.0;
+  const int fld = (int)((u >> 23) & 0xffu) + 896 + E;  // 1023 - 127 = 896
+  if (fld <= 0 || fld >= 2047) return ldexp((double)v, E);
+  const unsigned hi = (u & 0x80000000u) | ((unsigned)fld << 20) | ((u & 0x7fffffu) >> 3);
+  const unsigned lo = (u & 0x7u) << 29;
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+struct OzArgs {
+  int M, N, c0, c1;
+  double alpha, beta;
+  SplitBuf SA, SB;
+  int a_row0, b_row0;
+  double* C;
+  int64_t ldc, c_batch;
+  bool lower_only;
+  int wtw_n;  // > 0: R^-1 = W^T W tile mode over n
+};
+
+template <int S>
+__global__ void __launch_bounds__(128) k_oz_gemm(OzArgs g) {
+  extern __shared__ __align__(16) unsigned char oz_smem[];
+  __nv_bfloat16* sA = reinterpret_cast<__nv_bfloat16*>(oz_smem);       // [S][64][OZ_PAD]
+  __nv_bfloat16* sB = sA + (size_t)S * 64 * OZ_PAD;                     // [S][64][OZ_PAD]
+  int* sea = reinterpret_cast<int*>(sB + (size_t)S * 64 * OZ_PAD);       // [64]
+  int* seb = sea + 64;                                                   // [64]
+  int m0, n0, c0 = g.c0, arow, brow;
+  bool diag_tile;
+  if (g.wtw_n > 0) {
+    const int64_t x = blockIdx.x;
+    int I = (int)((sqrt(8.0 * (double)x + 1.0) - 1.0) * 0.5);
+    while ((int64_t)(I + 1) * (I + 2) / 2 <= x) ++I;
+    while ((int64_t)I * (I + 1) / 2 > x) --I;
+    const int J = (int)(x - (int64_t)I * (I + 1) / 2);
+    m0 = I * 64;
+    n0 = J * 64;
+    c0 = I;
+    arow = m0;
+    brow = n0;
+    diag_tile = (I == J);
+  } else {
+    m0 = blockIdx.x * 64;
+    n0 = blockIdx.y * 64;
+    if (g.lower_only && m0 + 63 < n0) return;
+    arow = g.a_row0 + m0;
+    brow = g.b_row0 + n0;
+    diag_tile = g.lower_only;
+  }
+  const int64_t b = blockIdx.z;
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const int wm = w & 1, wn = w >> 1;
+  const int gq = lane >> 2, tig = lane & 3;
+  const __nv_bfloat16* pa = g.SA.planes + b * g.SA.plane_bstride;
+  const __nv_bfloat16* pb = g.SB.planes + b * g.SB.plane_bstride;
+  const int* ea = g.SA.exps + b * g.SA.exp_bstride;
+  const int* eb = g.SB.exps + b * g.SB.exp_bstride;
+
+  double acc64[2][4][4];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc64[i][j][q] = 0.0;
+
+  for (int c = c0; c < g.c1; ++c) {
+    // ---- stage the S digit planes of A rows [arow, arow+64) and B rows [brow, brow+64) for chunk c ----
+    for (int idx = t; idx < S * 64 * 8; idx += 128) {
+      const int i = idx / 512, rem = idx % 512, row = rem >> 3, seg = rem & 7;
+      const __nv_bfloat16* ga = pa + (((int64_t)i * g.SA.nchunk + c) * g.SA.rows_pad + arow + row) * OZ_CHUNK + seg * 8;
+      const __nv_bfloat16* gb = pb + (((int64_t)i * g.SB.nchunk + c) * g.SB.rows_pad + brow + row) * OZ_CHUNK + seg * 8;
+      cp_async16(sA + ((size_t)i * 64 + row) * OZ_PAD + seg * 8, ga);
+      cp_async16(sB + ((size_t)i * 64 + row) * OZ_PAD + seg * 8, gb);
+    }
+    if (t < 64) {
+      sea[t] = ea[(int64_t)c * g.SA.rows_pad + arow + t];
+      seb[t] = eb[(int64_t)c * g.SB.rows_pad + brow + t];
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    int er[2][2], ec[4][2];
+#pragma unroll
+    for (int mb = 0; mb < 2; ++mb) {
+      er[mb][0] = sea[wm * 32 + mb * 16 + gq];
+      er[mb][1] = sea[wm * 32 + mb * 16 + gq + 8];
+    }
+#pragma unroll
+    for (int nb = 0; nb < 4; ++nb) {
+      ec[nb][0] = seb[wn * 32 + nb * 8 + 2 * tig];
+      ec[nb][1] = seb[wn * 32 + nb * 8 + 2 * tig + 1];
+    }
+    // ---- diagonals t = i + j of the digit products ----
+#pragma unroll 1
+    for (int dg = 2; dg <= S + 1; ++dg) {
+      float acc[2][4][4];
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.f;
+      const int ilo = dg - S > 1 ? dg - S : 1, ihi = dg - 1 < S ? dg - 1 : S;
+#pragma unroll 1
+      for (int i = ilo; i <= ihi; ++i) {
+        const int j = dg - i;
+        const __nv_bfloat16* A = sA + (size_t)(i - 1) * 64 * OZ_PAD;
+        const __nv_bfloat16* B = sB + (size_t)(j - 1) * 64 * OZ_PAD;
+#pragma unroll
+        for (int kk = 0; kk < 64; kk += 16) {
+          unsigned af[2][4], bf[4][2];
+#pragma unroll
+          for (int mb = 0; mb < 2; ++mb) {
+            const int row = wm * 32 + mb * 16 + (lane & 7) + ((lane >> 3) & 1) * 8;
+            const int col = kk + ((lane >> 4) & 1) * 8;
+            ldsm_x4(af[mb][0], af[mb][1], af[mb][2], af[mb][3], A + (size_t)row * OZ_PAD + col);
+          }
+#pragma unroll
+          for (int nb = 0; nb < 4; nb += 2) {
+            const int row = wn * 32 + nb * 8 + (lane & 7) + ((lane >> 4) & 1) * 8;
+            const int col = kk + ((lane >> 3) & 1) * 8;
+            ldsm_x4(bf[nb][0], bf[nb][1], bf[nb + 1][0], bf[nb + 1][1], B + (size_t)row * OZ_PAD + col);
+          }
+#pragma unroll
+          for (int mb = 0; mb < 2; ++mb)
+#pragma unroll
+            for (int nb = 0; nb < 4; ++nb) mma_bf16(acc[mb][nb], af[mb], bf[nb][0], bf[nb][1]);
+        }
+      }
+      // fold this diagonal into the FP64 accumulator: value * 2^(ea + eb - 8 dg), exact conversion
+#pragma unroll
+      for (int mb = 0; mb < 2; ++mb)
+#pragma unroll
+        for (int nb = 0; nb < 4; ++nb)
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            acc64[mb][nb][q] += scaled_to_double(acc[mb][nb][q], er[mb][q >> 1] + ec[nb][q & 1] - 8 * dg);
+    }
+    __syncthreads();
+  }
+  // ---- epilogue ----
+  double* Cb = g.C + b * g.c_batch;
+  const int mrow0 = (g.wtw_n > 0) ? m0 : m0, ncol0 = n0;
+#pragma unroll
+  for (int mb = 0; mb < 2; ++mb)
+#pragma unroll
+    for (int nb = 0; nb < 4; ++nb)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int r = mrow0 + wm * 32 + mb * 16 + gq + (q >> 1) * 8;
+        const int c = ncol0 + wn * 32 + nb * 8 + 2 * tig + (q & 1);
+        if (r < g.M && c < g.N && (!diag_tile || r >= c)) {
+          double* cp = Cb + r + (int64_t)c * g.ldc;
+          const double v = acc64[mb][nb][q];
+          *cp = (g.beta == 0.0) ? g.alpha * v : fma(g.alpha, v, g.beta * *cp);
+        }
+      }
+}
+
+template <int S>
+void launch_oz(const OzArgs& a, dim3 grid, cudaStream_t st) {
+  const size_t smem = (size_t)2 * S * 64 * OZ_PAD * sizeof(__nv_bfloat16) + 128 * sizeof(int);
+  static bool attr = false;
+  if (!attr) {
+    LKG_CUDA(cudaFuncSetAttribute(k_oz_gemm<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  k_oz_gemm<S><<<grid, 128, smem, st>>>(a);
+  LKG_LAUNCH("k_oz_gemm");
+}
+
+void dispatch_oz(int S, const OzArgs& a, dim3 grid, cudaStream_t st) {
+  switch (S) {
+    case 4: launch_oz<4>(a, grid, st); break;
+    case 5: launch_oz<5>(a, grid, st); break;
+    case 6: launch_oz<6>(a, grid, st); break;
+    case 7: launch_oz<7>(a, grid, st); break;
+    case 8: launch_oz<8>(a, grid, st); break;
+    default: throw std::invalid_argument("ozaki: number of slices must be in [4, 8]");
+  }
+}
+
+}  // namespace
+
+size_t split_plane_elems(int rows, int K, int S) {
+  const int rp = ceil_div(rows, 64) * 64, nc = ceil_div(K, OZ_CHUNK);
+  return (size_t)S * nc * rp * OZ_CHUNK;
+}
+
+size_t split_exp_elems(int rows, int K) { return (size_t)ceil_div(K, OZ_CHUNK) * ceil_div(rows, 64) * 64; }
+
+void ozaki_split(int rows, int K, const double* p, int64_t s_r, int64_t s_k, int64_t bstride, int batch, SplitBuf& out,
+                 cudaStream_t st) {
+  out.rows_pad = ceil_div(rows, 64) * 64;
+  out.nchunk = ceil_div(K, OZ_CHUNK);
+  if (out.plane_bstride == 0) out.plane_bstride = (int64_t)split_plane_elems(rows, K, out.S);
+  if (out.exp_bstride == 0) out.exp_bstride = (int64_t)split_exp_elems(rows, K);
+  dim3 grid(out.rows_pad / 8, out.nchunk, batch);
+  LaunchTimer lt("k_oz_split", st, 0.0, ((double)rows * K * (8.0 + 2.0 * out.S)) * batch);
+  k_oz_split<<<grid, 256, 0, st>>>(rows, K, p, s_r, s_k, bstride, out);
+  LKG_LAUNCH("k_oz_split");
+}
+
+void ozaki_gemm(int M, int N, int c0, int c1, double alpha, const SplitBuf& SA, int a_row0, const SplitBuf& SB,
+                int b_row0, double beta, double* C, int64_t ldc, int64_t c_batch, int batch, bool lower_only,
+                cudaStream_t st) {
+  if (M <= 0 || N <= 0 || c1 <= c0) return;
+  if (SA.S != SB.S) throw std::invalid_argument("ozaki_gemm: operands split with different slice counts");
+  OzArgs a{M, N, c0, c1, alpha, beta, SA, SB, a_row0, b_row0, C, ldc, c_batch, lower_only, 0};
+  dim3 grid(ceil_div(M, 64), ceil_div(N, 64), batch);
+  const double K = (double)(c1 - c0) * OZ_CHUNK;
+  const double fl = (lower_only && M == N) ? K * M * (M + 1.0) : 2.0 * M * N * K;
+  LaunchTimer lt("k_oz_gemm", st, fl * batch, 8.0 * ((beta == 0.0) ? 1.0 : 2.0) * M * N * batch);
+  dispatch_oz(SA.S, a, grid, st);
+}
+
+void ozaki_wtw(int n, const SplitBuf& SW, double* C, int64_t ldc, int64_t cstride, int batch, cudaStream_t st) {
+  const int nblk = ceil_div(n, 64);
+  const int64_t ntiles = (int64_t)nblk * (nblk + 1) / 2;
+  OzArgs a{n, n, 0, SW.nchunk, 1.0, 0.0, SW, SW, 0, 0, C, ldc, cstride, false, n};
+  LaunchTimer lt("k_oz_wtw", st, (double)n * (n + 1.0) * (n + 2.0) / 3.0 * batch, 8.0 * n * (n + 1.0) * batch);
+  dispatch_oz(SW.S, a, dim3((unsigned)ntiles, 1, batch), st);
+}
+
+}  // namespace lkg

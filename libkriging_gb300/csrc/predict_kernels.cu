@@ -5,6 +5,8 @@
 // Sigma_n = R_nn - Rstar_on' Rstar_on + Ecirc Ecirc' (:248).  The p-column trend algebra stays on the host.
 #include "predict_kernels.cuh"
 
+#include "stats.hpp"
+
 #include "common.cuh"
 #include "dense_fp64.cuh"
 #include "lik_kernels.cuh"
@@ -73,6 +75,7 @@ PredictOut predict_gpu(const Engine& model, const double* Xn, int q, const doubl
   LKG_CUDA(cudaMemcpyAsync(dz.p, z, sizeof(double) * n, cudaMemcpyHostToDevice, st));
   cov_cross(model.kernel(), n, q, d, model.dX(), dXn.p, dth.p, factor, dRs.p, st);
   model.solve_lower_inplace(0, dRs.p, n, q);
+  LaunchTimer lt("k_predict_reduce", st, 2.0 * n * q * (p + 2.0), 8.0 * n * q);
   k_predict_reduce<<<dim3(q, 2 + p), 256, 0, st>>>(n, q, p, dRs.p, dz.p, model.dFY(0), drz.p, drr.p, drm.p);
   LKG_LAUNCH("k_predict_reduce");
   o.rz.resize(q);

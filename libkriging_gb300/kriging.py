@@ -139,6 +139,17 @@ class Kriging:
                                               int(bool(return_deriv)), ptr(mean), ptr(sd), ptr(cov), None, None))
         return mean, sd, cov, None, None
 
+    def set_precision(self, slices):
+        """0: FP64 path (default); 4..8: mixed path with that many bf16 digit slices (see the C header)."""
+        check(_lib.load().lkg_kriging_set_precision(self._h, int(slices)))
+        return self
+
+    def precision(self):
+        return _lib.load().lkg_kriging_get_precision(self._h)
+
+    def last_slices(self):
+        return _lib.load().lkg_kriging_last_slices(self._h)
+
     def summary(self):
         s = _lib.load().lkg_kriging_summary(self._h)
         return s.decode() if s else ""

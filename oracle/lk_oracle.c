@@ -104,6 +104,55 @@ void ora_build_R(int kernel, int n, int d, const double* X, const double* theta,
   for (int i = 0; i < n; i++) R[i + (size_t)i * n] = diag ? diag[i] : 1.0;
 }
 
+/* Rows [i0, i1) of the cholCov pair loop (LinearAlgebra.cpp:150-155), serial like the reference: the timed sample of
+ * the CPU baseline.  Writes both triangles of those rows. */
+void ora_build_R_rows(int kernel, int n, int d, const double* X, const double* theta, int i0, int i1, double* R) {
+  double dx[64];
+  for (int i = i0; i < i1; i++) {
+    for (int j = 0; j < i; j++) {
+      pair_dx(n, d, X, i, j, dx);
+      double c = ora_cov(kernel, dx, theta, d);
+      R[i + (size_t)j * n] = c;
+      R[j + (size_t)i * n] = c;
+    }
+  }
+}
+
+/* Full covariance build spread over OpenMP threads: set-up of the CPU baseline only (not a reference routine). */
+void ora_build_R_parallel(int kernel, int n, int d, const double* X, const double* theta, double factor, double* R) {
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int i = 0; i < n; i++) {
+    double dx[64];
+    for (int j = 0; j < i; j++) {
+      pair_dx(n, d, X, i, j, dx);
+      double c = ora_cov(kernel, dx, theta, d) * factor;
+      R[i + (size_t)j * n] = c;
+      R[j + (size_t)i * n] = c;
+    }
+    R[i + (size_t)i * n] = 1.0;
+  }
+}
+
+/* Rows [i0, i1) of the compute_ll_grad_theta_vecs loop (KrigingImpl.cpp:863-884), serial: timed sample. */
+void ora_grad_terms_rows(int kernel, int n, int d, const double* X, const double* theta, const double* R,
+                         const double* Rinv, const double* x, int i0, int i1, double* term1, double* term2) {
+  double dx[64], dln[64];
+  for (int i = i0; i < i1; i++) {
+    for (int j = 0; j < i; j++) {
+      pair_dx(n, d, X, i, j, dx);
+      ora_dlncov(kernel, dx, theta, d, dln);
+      double R_ij = R[i + (size_t)j * n];
+      double x_i = x[i], x_j = x[j];
+      double Rinv_ij = Rinv[i + (size_t)j * n];
+      for (int k = 0; k < d; k++) {
+        double g = R_ij * dln[k];
+        term1[k] += 2.0 * x_i * g * x_j;
+        term2[k] -= 2.0 * Rinv_ij * g;
+      }
+    }
+  }
+}
+
 /* KrigingImpl.cpp:855-885: serial i>j loop; term1_k += 2 x_i gradR_k x_j, term2_k -= 2 Rinv_ij gradR_k,
  * gradR_k = R_ij * dlnCov_k.  term1/term2 are accumulated into (caller zeroes them). */
 void ora_grad_terms(int kernel, int n, int d, const double* X, const double* theta, const double* R,

@@ -48,7 +48,8 @@ def build(force: bool = False) -> Path:
         return SO
     BUILD.mkdir(exist_ok=True)
     tmp = SO.with_suffix(".so.tmp%d" % os.getpid())
-    subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-o", str(tmp), str(src), "-lm"])
+    subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-o", str(tmp), str(src),
+                           "-lm"])
     os.replace(tmp, SO)
     return SO
 
@@ -71,6 +72,14 @@ def lib():
         L.ora_build_R.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, ctypes.c_double, dp, dp]
         L.ora_grad_terms.restype = None
         L.ora_grad_terms.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp, dp, dp, dp, dp]
+        L.ora_build_R_rows.restype = None
+        L.ora_build_R_rows.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, ctypes.c_int, ctypes.c_int,
+                                       dp]
+        L.ora_build_R_parallel.restype = None
+        L.ora_build_R_parallel.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, ctypes.c_double, dp]
+        L.ora_grad_terms_rows.restype = None
+        L.ora_grad_terms_rows.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp, dp, dp, ctypes.c_int,
+                                          ctypes.c_int, dp, dp]
         L.ora_alpha_terms.restype = None
         L.ora_alpha_terms.argtypes = [ctypes.c_int, dp, dp, dp, ctypes.c_double, ctypes.c_double, dp]
         L.ora_vecchia_sets.restype = None

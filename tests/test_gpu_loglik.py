@@ -92,7 +92,7 @@ def test_gradient_vs_central_fd(gpu_lib):
     th = np.array([0.3, 0.45])
     _, g, _ = k.logLikelihoodFun(th, True)
     for j in range(2):
-        h = 1e-6 * th[j]
+        h = 1e-4 * th[j]  # central FD truncation ~1e-8 relative here; roundoff dominates below h ~ 1e-5 theta
         e = np.zeros(2)
         e[j] = h
         fd = (k.logLikelihoodFun(th + e)[0] - k.logLikelihoodFun(th - e)[0]) / (2 * h)
@@ -112,5 +112,5 @@ def test_retry_semantics_duplicated_point(gpu_lib):
     k = gpu_lib.Kriging("gauss")
     k.fit(y, x, "constant", False, "none", "LL", {"theta": th.reshape(1, -1)})
     ll, g, _ = k.logLikelihoodFun(th, True)
-    assert rel_err(ll, ll_o) < 1e-8
+    assert rel_err(ll, ll_o) < 1e-7  # cond(R) ~ 1e11 after the increment
     assert rel_err(g, g_o) < 1e-5
