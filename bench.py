@@ -242,7 +242,9 @@ def run_gpu(args):
     tf = ROOT / "profiles" / "dram_traffic.json"
     if tf.exists():
         try:
-            traffic = json.loads(tf.read_text()).get(name, {}).get("bytes_per_launch_scaled")
+            ratio = json.loads(tf.read_text()).get(name, {}).get("ratio")
+            if ratio is not None and s["launches"] > 0:
+                traffic = ratio * s["bytes"] / s["launches"]  # DRAM bytes per launch, scaled from the ncu capture
         except ValueError:
             traffic = None
     roofline = dict(bound="fp64", kernel=name, achieved=achieved, peak=peak_fp64.value, unit="TFLOP/s",

@@ -71,6 +71,21 @@ int lkg_kriging_set_precision(void* ptr, int slices);
 int lkg_kriging_get_precision(void* ptr);
 int lkg_kriging_last_slices(void* ptr);
 
+/* Vecchia approximation (objective "LLVecchia" / "LLVecchia(m)" of lkg_kriging_fit[_params]).  The reference
+ * exposes these through its C++ Kriging class only (Kriging.hpp:145-173; no lk_* counterpart):
+ *   logLikelihoodVecchiaFun(theta, return_grad) -> (vll, grad)  Kriging.hpp:145-150, Kriging.cpp:926-941
+ *   set_vecchia_exact_commit, vecchia_neighbors, is_vecchia_light  Kriging.hpp:152-173
+ * lkg_kriging_get_vecchia_sets returns the maxmin order (n) and the neighbour sets (n x m row-major, -1 padded) as
+ * built by make_vecchia_sets (Kriging.cpp:736-804); lkg_vecchia_sets builds them on the GPU for a given X
+ * (n x d column-major) without a model. */
+int lkg_kriging_log_likelihood_vecchia_fun(void* ptr, const double* theta, int theta_n, int return_grad,
+                                           double* vll_out, double* grad_out);
+int lkg_kriging_set_vecchia_exact_commit(void* ptr, int b);
+int lkg_kriging_vecchia_neighbors(void* ptr);
+int lkg_kriging_is_vecchia_light(void* ptr);
+int lkg_kriging_get_vecchia_sets(void* ptr, int* order_out, int* nbr_out, int* n, int* m);
+int lkg_vecchia_sets(int n, int d, const double* X, int m, int* order_out, int* nbr_out);
+
 /* getters, libkriging_c.h:141-166 */
 const char* lkg_kriging_kernel(void* ptr);
 const char* lkg_kriging_optim(void* ptr);

@@ -6,7 +6,7 @@ triangular solves, concentrated log-likelihood with its one-pass adjoint theta-g
 ``include/libkriging_gb300.h``.
 """
 from ._lib import LibKrigingError, header_symbols, load
-from .kriging import Kriging, Optim, check_chol_rcond, get_num_nugget, set_num_nugget
+from .kriging import Kriging, Optim, check_chol_rcond, get_num_nugget, set_num_nugget, vecchia_sets
 
-__all__ = ["Kriging", "Optim", "set_num_nugget", "get_num_nugget", "check_chol_rcond", "LibKrigingError", "load",
+__all__ = ["Kriging", "Optim", "vecchia_sets", "set_num_nugget", "get_num_nugget", "check_chol_rcond", "LibKrigingError", "load",
            "header_symbols"]

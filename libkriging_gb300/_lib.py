@@ -83,6 +83,12 @@ _SIGS = {
     "lkg_kriging_get_precision": (_i, [_vp]),
     "lkg_kriging_last_slices": (_i, [_vp]),
     "lkg_ozaki_gemm_check": (_i, [_i, _i, _i, _dp, _dp, _i, _dp]),
+    "lkg_kriging_log_likelihood_vecchia_fun": (_i, [_vp, _dp, _i, _i, _dp, _dp]),
+    "lkg_kriging_set_vecchia_exact_commit": (_i, [_vp, _i]),
+    "lkg_kriging_vecchia_neighbors": (_i, [_vp]),
+    "lkg_kriging_is_vecchia_light": (_i, [_vp]),
+    "lkg_kriging_get_vecchia_sets": (_i, [_vp, _ip, _ip, _ip, _ip]),
+    "lkg_vecchia_sets": (_i, [_i, _i, _dp, _i, _ip, _ip]),
 }
 
 _lib = None

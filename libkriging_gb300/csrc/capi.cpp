@@ -428,3 +428,66 @@ int lkg_kriging_last_slices(void* ptr) {
 }
 
 }  // extern "C"
+
+// ---- Vecchia (C++ API of the reference: Kriging.hpp:145-173; its C ABI has no Vecchia entry points) ----
+extern "C" {
+
+int lkg_kriging_log_likelihood_vecchia_fun(void* ptr, const double* theta, int theta_n, int return_grad,
+                                           double* vll_out, double* grad_out) {
+  try {
+    std::vector<double> t(theta, theta + theta_n);
+    auto [vll, grad] = K(ptr)->logLikelihoodVecchiaFun(t, return_grad != 0);
+    if (vll_out) *vll_out = vll;
+    if (grad_out && return_grad) std::memcpy(grad_out, grad.data(), sizeof(double) * grad.size());
+    return 0;
+  }
+  CATCH_RETURN
+}
+
+int lkg_kriging_set_vecchia_exact_commit(void* ptr, int b) {
+  try {
+    K(ptr)->set_vecchia_exact_commit(b != 0);
+    return 0;
+  }
+  CATCH_RETURN
+}
+
+int lkg_kriging_vecchia_neighbors(void* ptr) {
+  try {
+    return K(ptr)->vecchia_neighbors();
+  }
+  CATCH_RETURN
+}
+
+int lkg_kriging_is_vecchia_light(void* ptr) {
+  try {
+    return K(ptr)->is_vecchia_light() ? 1 : 0;
+  }
+  CATCH_RETURN
+}
+
+int lkg_kriging_get_vecchia_sets(void* ptr, int* order_out, int* nbr_out, int* n, int* m) {
+  try {
+    const auto& o = K(ptr)->vecchia_order();
+    const auto& nb = K(ptr)->vecchia_nbr();
+    const int nn = (int)o.size();
+    const int mm = nn > 0 ? (int)(nb.size() / nn) : 0;
+    if (n) *n = nn;
+    if (m) *m = mm;
+    if (order_out) std::memcpy(order_out, o.data(), sizeof(int) * o.size());
+    if (nbr_out) std::memcpy(nbr_out, nb.data(), sizeof(int) * nb.size());
+    return 0;
+  }
+  CATCH_RETURN
+}
+
+int lkg_vecchia_sets(int n, int d, const double* X, int m, int* order_out, int* nbr_out) {
+  try {
+    if (n < 1 || d < 1 || m < 0) throw std::invalid_argument("lkg_vecchia_sets: bad sizes");
+    lkg::vecchia_sets_gpu(n, d, X, m, order_out, nbr_out);
+    return 0;
+  }
+  CATCH_RETURN
+}
+
+}  // extern "C"

@@ -344,9 +344,7 @@ void trtri_blocked(const double* L, int64_t lda, int64_t mstride, int n, const d
     LKG_CUDA(cudaMemset2DAsync(W + b * wstride, ldw * sizeof(double), 0, n * sizeof(double), n, st));
   for (int k = 0; k < nblk; ++k) {
     const int k0 = k * NB, nb = std::min(NB, n - k0);
-    LaunchTimer lt("k_copy_dinv_block", st, 0.0, 16.0 * nb * nb * batch);
-    k_copy_dinv_block<<<dim3(1, 1, batch), 256, 0, st>>>(Dinv, dstride, k, W, ldw, wstride, k0, nb);
-    LKG_LAUNCH("k_copy_dinv_block");
+    copy_dinv_block(Dinv, dstride, k, W, ldw, wstride, k0, nb, batch, st);
     if (k0 > 0) {
       // W(k0:k0+nb, 0:k0) = -Dinv_k * Acc(k0:k0+nb, 0:k0)   (in place per column tile)
       MatView d{Dinv + (int64_t)k * NB * NB, 1, NB, dstride};

@@ -123,7 +123,9 @@ struct EvalRequest {
   std::vector<double> theta;
   double factor = 1.0;
   bool want_grad = false;
+  bool vecchia = false;  // evaluate the Vecchia likelihood instead of the exact one
   EvalOut out;
+  VecchiaOut vout;
   std::exception_ptr err;
   bool done = false;
 };
@@ -320,13 +322,21 @@ void Kriging::fit(const std::vector<double>& y, const Mat& Xin, RegressionModel 
   if ((int)y.size() != n)
     throw std::runtime_error("Dimension of new data should be the same:\n X: (" + std::to_string(n) + "x" +
                              std::to_string(d) + "), y: (" + std::to_string(y.size()) + ")");
-  if (objective != "LL")
-    throw std::invalid_argument("Unsupported fit objective for the GPU build: " + objective +
-                                " (supported is: LL; LLVecchia(m) through the Vecchia entry points)");
+  const bool vecchia = objective.rfind("LLVecchia", 0) == 0;
+  if (!vecchia && objective != "LL")
+    throw std::invalid_argument("Unsupported fit objective: " + objective +
+                                " (supported by the GPU build are: LL, LLVecchia, LLVecchia(m))");
+  if (vecchia) {
+    parse_vll_m(objective);  // validate the spec early (throws on malformed), Kriging.cpp:1522-1524
+    if (m_noise_model != NoiseModel::None)
+      throw std::invalid_argument("LLVecchia objective not supported for Nugget/Heterogeneous noise modes");
+  }
   if (d > MAX_D) throw std::invalid_argument("input dimension d > 32 is not supported by the GPU kernels");
   m_optim = optim;
   m_objective = objective;
   m_eval.reset();
+  m_vecchia.reset();
+  m_vecchia_light = false;
   m_model.reset();
   // ---- fit_setup_impl (KrigingImpl.cpp:764-841) ----
   m_n = n;
@@ -395,6 +405,17 @@ void Kriging::fit(const std::vector<double>& y, const Mat& Xin, RegressionModel 
                                std::to_string(theta0.rows) + "x" + std::to_string(theta0.cols));
   }
   const Config& cfg = config();
+  if (vecchia) {  // Kriging.cpp:1619-1624: sets built once per fit, on the GPU
+    m_vecchia_m = parse_vll_m(objective);
+    m_vorder.assign(n, 0);
+    m_vnbr.assign((size_t)n * std::min(m_vecchia_m, VECCHIA_MAX_M), -1);
+    if (m_vecchia_m > VECCHIA_MAX_M) throw std::invalid_argument("LLVecchia on the GPU supports m <= 32");
+    vecchia_sets_gpu(n, d, m_X.data(), m_vecchia_m, m_vorder.data(), m_vnbr.data());
+  } else {
+    m_vecchia_m = 0;
+    m_vorder.clear();
+    m_vnbr.clear();
+  }
 
   if (optim == "none") {  // Kriging.cpp:1633-1715
     if (!parameters.theta.has_value())
@@ -558,38 +579,60 @@ void Kriging::fit(const std::vector<double>& y, const Mat& Xin, RegressionModel 
       m_est_nugget = true;
     }
   }
-  ensure_engine(multistart);
+  if (!vecchia) ensure_engine(multistart);
+  if (vecchia) ensure_vecchia();
 
-  // batched objective: -LL in gamma space (make_fit_objective, Kriging.cpp:1414-1470)
+  // batched objective: -LL in gamma space (make_fit_objective, Kriging.cpp:1414-1470); the exact requests of one
+  // round go to the GPU as one batched evaluation, Vecchia requests one after another
   Batcher batcher(multistart, [&](std::vector<EvalRequest*>& reqs) {
-    const int k = (int)reqs.size();
+    std::vector<EvalRequest*> dense;
+    for (auto* r : reqs) {
+      if (r->vecchia) {
+        r->vout = m_vecchia->evaluate(r->theta.data(), r->want_grad, m_est_beta || (int)m_beta.size() != m_p,
+                                      m_beta.data());
+        m_evals++;
+      } else {
+        dense.push_back(r);
+      }
+    }
+    const int k = (int)dense.size();
+    if (k == 0) return;
+    ensure_engine(std::max(k, multistart));
     std::vector<double> th((size_t)k * d), fac(k);
     bool g = false;
     for (int b = 0; b < k; ++b) {
-      std::copy(reqs[b]->theta.begin(), reqs[b]->theta.begin() + d, th.begin() + (size_t)b * d);
-      fac[b] = reqs[b]->factor;
-      g = g || reqs[b]->want_grad;
+      std::copy(dense[b]->theta.begin(), dense[b]->theta.begin() + d, th.begin() + (size_t)b * d);
+      fac[b] = dense[b]->factor;
+      g = g || dense[b]->want_grad;
     }
     std::vector<EvalOut> out;
     m_eval->evaluate(k, th.data(), fac.data(), g, out, nullptr);
     m_evals += k;
-    for (int b = 0; b < k; ++b) reqs[b]->out = std::move(out[b]);
+    for (int b = 0; b < k; ++b) dense[b]->out = std::move(out[b]);
   });
-  auto eval_ll = [&](const std::vector<double>& ta, bool want_grad, std::vector<double>* grad) {
+  // exact_ll: the exact likelihood even under LLVecchia (the final exact-commit evaluation, Kriging.cpp:1532-1551)
+  auto eval_ll = [&](const std::vector<double>& ta, bool want_grad, std::vector<double>* grad, bool exact_ll) {
     EvalRequest req;
     req.theta.assign(ta.begin(), ta.begin() + d);
     double extra = nug ? ta[d] : m_sigma2;
     if (nug && !m_est_sigma2 && !m_est_nugget) extra = m_sigma2 / (m_sigma2 + m_nugget);
     req.factor = nug ? extra : 1.0;
     req.want_grad = want_grad;
+    req.vecchia = vecchia && !exact_ll;
     batcher.submit(&req);
     if (req.err) std::rethrow_exception(req.err);
+    if (req.vecchia) {
+      if (req.vout.status != 0) throw std::runtime_error(req.vout.message);
+      if (grad) *grad = req.vout.grad;
+      return req.vout.vll;
+    }
     return loglik_from(req.out, extra, grad, gd);
   };
   auto fit_ofn = [&](const std::vector<double>& gamma, std::vector<double>* grad_out) {
     const std::vector<double> ta = reparam_from(gamma);
     std::vector<double> g;
-    const double ll = eval_ll(ta, grad_out != nullptr, grad_out ? &g : nullptr);
+    const bool exact = vecchia && grad_out == nullptr && m_vecchia_exact_commit;
+    const double ll = eval_ll(ta, grad_out != nullptr, grad_out ? &g : nullptr, exact);
     if (grad_out) {
       grad_out->resize(gd);
       for (int j = 0; j < d; ++j) (*grad_out)[j] = -(cfg.reparametrize ? g[j] * ta[j] : g[j]);
@@ -688,6 +731,17 @@ void Kriging::fit(const std::vector<double>& y, const Mat& Xin, RegressionModel 
   m_theta = b.theta;
   m_est_theta = true;
   m_is_empty = false;
+  if (vecchia && !m_vecchia_exact_commit) {  // light commit (Kriging.cpp:2117-2136)
+    VecchiaOut vo = m_vecchia->evaluate(m_theta.data(), false, m_est_beta || (int)m_beta.size() != m_p,
+                                        m_beta.data());
+    if (vo.status != 0) throw std::runtime_error(vo.message);
+    if (m_est_beta) m_beta = vo.beta;
+    if (m_est_sigma2) m_sigma2 = vo.sigma2;
+    m_vecchia_light = true;
+    m_is_empty = true;
+    m_last_fit_starts = multistart;
+    return;
+  }
   if (nug) m_alpha = b.extra;
   commit(m_theta, m_alpha);
   const EvalOut& m = m_last_commit;
@@ -711,6 +765,44 @@ void Kriging::fit(const std::vector<double>& y, const Mat& Xin, RegressionModel 
 }
 
 // ---------------------------------------------------------------------------------------------------------------
+// Vecchia (Kriging.cpp:718-734 parse, :926-941 logLikelihoodVecchiaFun)
+int Kriging::parse_vll_m(const std::string& objective) {
+  if (objective == "LLVecchia") return 30;
+  if (objective.rfind("LLVecchia(", 0) == 0 && objective.back() == ')') {
+    const std::string inside = objective.substr(10, objective.size() - 11);
+    try {
+      size_t pos = 0;
+      const long m = std::stol(inside, &pos);
+      if (m >= 1) return (int)m;
+    } catch (const std::exception&) {
+    }
+  }
+  throw std::invalid_argument("Invalid Vecchia objective '" + objective +
+                              "': expected \"LLVecchia\" or \"LLVecchia(m)\" with m >= 1 (e.g. \"LLVecchia(30)\")");
+}
+
+void Kriging::ensure_vecchia() {
+  if (!m_vecchia) {
+    const int mm = m_n > 0 ? (int)(m_vnbr.size() / m_n) : 0;
+    m_vecchia = std::make_unique<VecchiaEngine>(m_kernel, m_n, m_d, m_p, m_X.data(), m_y.data(), m_F.data(),
+                                                m_vorder.data(), m_vnbr.data(), mm);
+  }
+}
+
+std::tuple<double, std::vector<double>> Kriging::logLikelihoodVecchiaFun(const std::vector<double>& theta,
+                                                                         bool return_grad) {
+  if (m_vecchia_m == 0 || (int)m_vorder.size() != m_n)
+    throw std::runtime_error("logLikelihoodVecchiaFun: model was not fitted with objective=\"LLVecchia(m)\"");
+  if ((int)theta.size() != m_d)
+    throw std::invalid_argument("logLikelihoodVecchiaFun: theta should have length " + std::to_string(m_d));
+  ensure_vecchia();
+  VecchiaOut vo = m_vecchia->evaluate(theta.data(), return_grad, m_est_beta || (int)m_beta.size() != m_p,
+                                      m_beta.data());
+  m_evals++;
+  if (vo.status != 0) throw std::runtime_error(vo.message);
+  return {vo.vll, return_grad ? vo.grad : std::vector<double>()};
+}
+
 Mat Kriging::T() const {
   Mat m;
   if (!m_model) return m;

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "engine.hpp"
+#include "vecchia.hpp"
 
 namespace lkg {
 
@@ -60,6 +61,16 @@ class Kriging {
   void logLikelihoodFunBatch(const Mat& gammas, bool return_grad, std::vector<double>& ll,
                              std::vector<double>& grad);
   double logLikelihood();
+
+  // Vecchia (objective "LLVecchia" / "LLVecchia(m)"; Kriging.hpp:145-173, Kriging.cpp:718-924)
+  std::tuple<double, std::vector<double>> logLikelihoodVecchiaFun(const std::vector<double>& theta, bool return_grad);
+  void set_vecchia_exact_commit(bool b) { m_vecchia_exact_commit = b; }
+  bool vecchia_exact_commit() const { return m_vecchia_exact_commit; }
+  int vecchia_neighbors() const { return m_vecchia_m; }
+  bool is_vecchia_light() const { return m_vecchia_light; }
+  const std::vector<int32_t>& vecchia_order() const { return m_vorder; }
+  const std::vector<int32_t>& vecchia_nbr() const { return m_vnbr; }
+  static int parse_vll_m(const std::string& objective);
 
   // mean, stdev, cov, mean_deriv, stdev_deriv
   std::tuple<std::vector<double>, std::vector<double>, Mat, Mat, Mat> predict(const Mat& X_n, bool return_stdev,
@@ -134,6 +145,13 @@ class Kriging {
   int m_last_fit_starts = 0;
   int m_slices = 0;
   int m_last_slices = 0;
+  // Vecchia state: maxmin order and neighbour sets (global row indices, -1 padded), GPU engine
+  int m_vecchia_m = 0;
+  std::vector<int32_t> m_vorder, m_vnbr;
+  bool m_vecchia_exact_commit = true;
+  bool m_vecchia_light = false;
+  std::unique_ptr<VecchiaEngine> m_vecchia;
+  void ensure_vecchia();
 };
 
 }  // namespace lkg

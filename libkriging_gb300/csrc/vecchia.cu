@@ -1,0 +1,824 @@
+// vecchia.cu -- Vecchia log-likelihood and conditioning sets on the GPU (see vecchia.hpp).
+//
+// Per ordered point t (Kriging.cpp:829-889): RN = C(N_t, N_t) + num_nugget I, r = C(N_t, x_t), LN = chol(RN) with
+// the safe_chol_lower rules (LinearAlgebra.cpp:68-115: cumulative 1e-10 * 10^k increments, rcond(LN)^2 check),
+// a = RN^-1 r, v = max(1 - r'a, 1e-15), u = y_t - a'y_N, W = f_t - F_N' a.  The theta-derivatives use
+//   da_k = RN^-1 g_k with g_k = dr_k - dRN_k a, and RN symmetric:
+//   dv_k = -(dr_k'a + r'da_k) = -(2 a'dr_k - a'dRN_k a),  du_k = -g_k' (RN^-1 y_N),  dW_k = -(RN^-1 F_N)' g_k,
+// which is the reference's algebra rearranged so that no per-k solve is needed (2 + p solves per point in total).
+#include "vecchia.hpp"
+
+#include <algorithm>
+#include <cmath>
+
+#include "common.cuh"
+#include "config.hpp"
+#include "stats.hpp"
+
+namespace lkg {
+
+namespace {
+
+constexpr int WPB = 4;    // warps per block of the point kernel
+constexpr int LDP = 33;   // shared-memory row pitch of the m x m blocks
+constexpr int VPMAX = 16; // trend columns supported by the Vecchia kernels
+constexpr unsigned FULL = 0xffffffffu;
+
+__device__ __forceinline__ double wsum(double x) {
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
+  return x;
+}
+__device__ __forceinline__ double wmax(double x) {
+  for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_xor_sync(FULL, x, o));
+  return x;
+}
+// first index of the maximum of v over lanes < mi
+__device__ __forceinline__ int wargmax(double v, int lane, int mi) {
+  double val = (lane < mi) ? v : -1.0;
+  int idx = lane;
+  for (int o = 16; o > 0; o >>= 1) {
+    const double ov = __shfl_xor_sync(FULL, val, o);
+    const int oi = __shfl_xor_sync(FULL, idx, o);
+    if (ov > val || (ov == val && oi < idx)) {
+      val = ov;
+      idx = oi;
+    }
+  }
+  return idx;
+}
+
+// solve L z = b (lane i holds b_i); lanes >= mi return 0
+__device__ double wsolve_lower(const double* L, double b, int mi, int lane) {
+  double val = (lane < mi) ? b : 0.0;
+  for (int j = 0; j < mi; ++j) {
+    const double zj = __shfl_sync(FULL, val, j) / L[j * LDP + j];
+    if (lane == j) val = zj;
+    if (lane > j && lane < mi) val -= L[lane * LDP + j] * zj;
+  }
+  return (lane < mi) ? val : 0.0;
+}
+// solve L' x = z
+__device__ double wsolve_upper_t(const double* L, double z, int mi, int lane) {
+  double val = (lane < mi) ? z : 0.0;
+  for (int j = mi - 1; j >= 0; --j) {
+    const double xj = __shfl_sync(FULL, val, j) / L[j * LDP + j];
+    if (lane == j) val = xj;
+    if (lane < j) val -= L[j * LDP + lane] * xj;
+  }
+  return (lane < mi) ? val : 0.0;
+}
+
+// in-place lower Cholesky, lane i owns row i; returns false on a non-positive / NaN pivot (uniform over the warp)
+__device__ bool wchol(double* L, int mi, int lane) {
+  for (int j = 0; j < mi; ++j) {
+    __syncwarp();
+    const double piv = L[j * LDP + j];
+    if (!(piv > 0.0)) return false;
+    const double ljj = sqrt(piv);
+    __syncwarp();
+    if (lane == j) L[j * LDP + j] = ljj;
+    if (lane > j && lane < mi) L[lane * LDP + j] /= ljj;
+    __syncwarp();
+    if (lane > j && lane < mi) {
+      const double lij = L[lane * LDP + j];
+      for (int c = j + 1; c <= lane; ++c) L[lane * LDP + c] -= lij * L[c * LDP + j];
+    }
+  }
+  __syncwarp();
+  return true;
+}
+
+// rcond(L)^2 of dtrcon('1', 'L', 'N'): |L|_1 and the dlacn2 estimate of |L^-1|_1 with warp solves
+__device__ double wrcond2(const double* L, int mi, int lane) {
+  double cs = 0.0;
+  if (lane < mi)
+    for (int i = lane; i < mi; ++i) cs += fabs(L[i * LDP + lane]);
+  const double anorm = wmax(cs);
+  if (!(anorm > 0.0)) return 0.0;
+  double y = wsolve_lower(L, 1.0 / mi, mi, lane);
+  double est;
+  if (mi == 1) {
+    est = fabs(__shfl_sync(FULL, y, 0));
+  } else {
+    est = wsum(fabs(y));
+    double xi = (y >= 0.0) ? 1.0 : -1.0;
+    double z = wsolve_upper_t(L, xi, mi, lane);
+    int j = wargmax(fabs(z), lane, mi);
+    int iter = 2;
+    for (;;) {
+      y = wsolve_lower(L, (lane == j) ? 1.0 : 0.0, mi, lane);
+      const double estold = est;
+      est = wsum(fabs(y));
+      const double sg = (y >= 0.0) ? 1.0 : -1.0;
+      const bool same = __all_sync(FULL, lane >= mi || sg == xi);
+      if (same || est <= estold) break;
+      xi = sg;
+      z = wsolve_upper_t(L, xi, mi, lane);
+      const int jlast = j;
+      j = wargmax(fabs(z), lane, mi);
+      const double zl = __shfl_sync(FULL, z, jlast), zj = __shfl_sync(FULL, z, j);
+      if (zl != fabs(zj) && iter < 5) {
+        iter++;
+        continue;
+      }
+      break;
+    }
+    const double alt = ((lane & 1) ? -1.0 : 1.0) * (1.0 + (double)lane / (double)(mi - 1));
+    y = wsolve_lower(L, alt, mi, lane);
+    const double temp = 2.0 * wsum(fabs(y)) / (3.0 * mi);
+    if (temp > est) est = temp;
+  }
+  const double rc = (1.0 / anorm) / est;
+  return rc * rc;
+}
+
+struct VPointArgs {
+  int n, d, p, m;
+  const double *X, *y, *F, *theta;
+  const int32_t *order, *nbr;
+  double num_nugget, min_rcond;
+  int rcond_check, max_inc, with_grad;
+  double *u, *v, *W, *du, *dv, *dW;
+  int* status;
+};
+
+template <int K, int DM>
+__global__ void __launch_bounds__(WPB * 32) k_vecchia_points(VPointArgs a) {
+  extern __shared__ double vsm[];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double* RN = vsm + (size_t)w * (2 * 32 * LDP + 32 * DM + 32);
+  double* LN = RN + 32 * LDP;
+  double* xs = LN + 32 * LDP;  // [32][DM]
+  double* sa = xs + 32 * DM;   // [32]
+  const int t = blockIdx.x * WPB + w;
+  if (t >= a.n) return;
+  const int n = a.n, d = a.d, p = a.p;
+  const int oi = a.order[t];
+  const int nbv = (lane < a.m) ? a.nbr[(int64_t)t * a.m + lane] : -1;
+  const int mi = __popc(__ballot_sync(FULL, nbv >= 0));
+  if (mi == 0) {
+    if (lane == 0) {
+      a.u[t] = a.y[oi];
+      a.v[t] = 1.0;
+      for (int q = 0; q < p; ++q) a.W[(int64_t)t * p + q] = a.F[oi + (int64_t)q * n];
+      if (a.with_grad)
+        for (int k = 0; k < d; ++k) {
+          a.du[(int64_t)t * d + k] = 0.0;
+          a.dv[(int64_t)t * d + k] = 0.0;
+          for (int q = 0; q < p; ++q) a.dW[((int64_t)t * d + k) * p + q] = 0.0;
+        }
+      a.status[t] = 0;
+    }
+    return;
+  }
+  double th[DM], xo[DM];
+#pragma unroll
+  for (int k = 0; k < DM; ++k) {
+    th[k] = (k < d) ? a.theta[k] : 1.0;
+    xo[k] = (k < d) ? a.X[oi + (int64_t)k * n] : 0.0;
+  }
+  if (lane < mi)
+#pragma unroll
+    for (int k = 0; k < DM; ++k) xs[lane * DM + k] = (k < d) ? a.X[nbv + (int64_t)k * n] : 0.0;
+  __syncwarp();
+  double r = 0.0;
+  if (lane < mi) {
+    for (int b = 0; b < mi; ++b) {
+      double c;
+      if (b == lane) {
+        c = 1.0 + a.num_nugget;
+      } else {
+        double s = 0.0;
+#pragma unroll
+        for (int k = 0; k < DM; ++k)
+          if (k < d) s += cov_term<K>(xs[lane * DM + k] - xs[b * DM + k], th[k]);
+        c = cov_from_sum<K>(s);
+      }
+      RN[lane * LDP + b] = c;
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < DM; ++k)
+      if (k < d) s += cov_term<K>(xs[lane * DM + k] - xo[k], th[k]);
+    r = cov_from_sum<K>(s);
+  }
+  __syncwarp();
+  // ---- factor with the numerical-nugget retry / rcond rules ----
+  int inc = 0;
+  for (;;) {
+    if (lane < mi)
+      for (int b = 0; b < mi; ++b) LN[lane * LDP + b] = RN[lane * LDP + b];
+    __syncwarp();
+    const bool ok = wchol(LN, mi, lane);
+    bool wrong = false;
+    if (ok && a.rcond_check) wrong = wrcond2(LN, mi, lane) < a.min_rcond;
+    if (ok && !wrong) break;
+    if (inc > a.max_inc || !(a.num_nugget > 0.0)) {
+      if (lane == 0) a.status[t] = -1;
+      return;
+    }
+    __syncwarp();
+    if (lane < mi) RN[lane * LDP + lane] += a.num_nugget * pow(10.0, (double)inc);
+    inc++;
+    __syncwarp();
+  }
+  // ---- a, v, u, W ----
+  const double av = wsolve_upper_t(LN, wsolve_lower(LN, r, mi, lane), mi, lane);
+  const double yN = (lane < mi) ? a.y[nbv] : 0.0;
+  const double ra = wsum(r * av), ay = wsum(av * yN);
+  double fN[VPMAX];
+  for (int q = 0; q < p; ++q) fN[q] = (lane < mi) ? a.F[nbv + (int64_t)q * n] : 0.0;
+  if (lane == 0) {
+    a.v[t] = fmax(1.0 - ra, 1e-15);
+    a.u[t] = a.y[oi] - ay;
+    a.status[t] = inc;
+  }
+  for (int q = 0; q < p; ++q) {
+    const double s = wsum(fN[q] * av);
+    if (lane == 0) a.W[(int64_t)t * p + q] = a.F[oi + (int64_t)q * n] - s;
+  }
+  if (!a.with_grad) return;
+  // ---- theta-derivatives ----
+  const double by = wsolve_upper_t(LN, wsolve_lower(LN, yN, mi, lane), mi, lane);
+  double cq[VPMAX];
+  for (int q = 0; q < p; ++q) cq[q] = wsolve_upper_t(LN, wsolve_lower(LN, fN[q], mi, lane), mi, lane);
+  if (lane < 32) sa[lane] = av;
+  __syncwarp();
+  for (int k = 0; k < d; ++k) {
+    double drk = 0.0, s = 0.0;
+    if (lane < mi) {
+      drk = r * dlncov_term<K>(xs[lane * DM + k] - xo[k], th[k]);
+      for (int b = 0; b < mi; ++b)
+        if (b != lane)
+          s += RN[lane * LDP + b] * dlncov_term<K>(xs[lane * DM + k] - xs[b * DM + k], th[k]) * sa[b];
+    }
+    const double g = drk - s;
+    const double adr = wsum(av * drk), as = wsum(av * s), gb = wsum(g * by);
+    if (lane == 0) {
+      a.dv[(int64_t)t * d + k] = -(2.0 * adr - as);
+      a.du[(int64_t)t * d + k] = -gb;
+    }
+    for (int q = 0; q < p; ++q) {
+      const double gc = wsum(g * cq[q]);
+      if (lane == 0) a.dW[((int64_t)t * d + k) * p + q] = -gc;
+    }
+  }
+}
+
+// ---- deterministic reductions over the points ----
+constexpr int RED_BLOCKS = 304;
+
+template <int NTH>
+__device__ double bsum(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  for (int i = 0; i < NTH / 32; ++i) s += red[i];
+  return s;
+}
+
+// stage 1: [A (p x p, row a col b), b (p), sum log v] partials per block
+__global__ void k_vsum1(int n, int p, const double* __restrict__ u, const double* __restrict__ v,
+                        const double* __restrict__ W, double* __restrict__ part) {
+  __shared__ double red[8];
+  const int P = p * p + p + 1;
+  const int64_t lo = (int64_t)n * blockIdx.x / gridDim.x, hi = (int64_t)n * (blockIdx.x + 1) / gridDim.x;
+  for (int e = 0; e < P; ++e) {
+    double s = 0.0;
+    for (int64_t t = lo + threadIdx.x; t < hi; t += blockDim.x) {
+      if (e < p * p) {
+        const int qa = e / p, qb = e % p;
+        s += W[t * p + qa] * W[t * p + qb] / v[t];
+      } else if (e < p * p + p) {
+        s += W[t * p + (e - p * p)] * u[t] / v[t];
+      } else {
+        s += log(v[t]);
+      }
+    }
+    s = bsum<256>(s, red);
+    if (threadIdx.x == 0) part[(int64_t)blockIdx.x * P + e] = s;
+  }
+}
+
+// stage 2: [Q, dQ_k (d), sum dv_k / v (d)] partials per block, given beta
+__global__ void k_vsum2(int n, int p, int d, const double* __restrict__ u, const double* __restrict__ v,
+                        const double* __restrict__ W, const double* __restrict__ du, const double* __restrict__ dv,
+                        const double* __restrict__ dW, const double* __restrict__ beta, int with_grad,
+                        double* __restrict__ part) {
+  __shared__ double red[8];
+  const int P = 1 + 2 * d;
+  const int64_t lo = (int64_t)n * blockIdx.x / gridDim.x, hi = (int64_t)n * (blockIdx.x + 1) / gridDim.x;
+  for (int e = 0; e < (with_grad ? P : 1); ++e) {
+    double s = 0.0;
+    for (int64_t t = lo + threadIdx.x; t < hi; t += blockDim.x) {
+      double wb = 0.0;
+      for (int q = 0; q < p; ++q) wb += W[t * p + q] * beta[q];
+      const double et = u[t] - wb, vt = v[t];
+      if (e == 0) {
+        s += et * et / vt;
+      } else if (e <= d) {
+        const int k = e - 1;
+        double dwb = 0.0;
+        for (int q = 0; q < p; ++q) dwb += dW[(t * d + k) * p + q] * beta[q];
+        const double de = du[t * d + k] - dwb;
+        s += 2.0 * et * de / vt - (et * et / (vt * vt)) * dv[t * d + k];
+      } else {
+        s += dv[t * d + (e - d - 1)] / vt;
+      }
+    }
+    s = bsum<256>(s, red);
+    if (threadIdx.x == 0) part[(int64_t)blockIdx.x * P + e] = s;
+  }
+}
+
+__global__ void k_vsum_final(int nblocks, int P, const double* __restrict__ part, double* __restrict__ out) {
+  __shared__ double red[8];
+  for (int e = 0; e < P; ++e) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += part[(int64_t)b * P + e];
+    s = bsum<256>(s, red);
+    if (threadIdx.x == 0) out[e] = s;
+  }
+}
+
+__global__ void k_count_status(int n, const int* __restrict__ status, int* __restrict__ out) {
+  // out[0] = number of failed points, out[1] = number of points that needed nugget increments
+  int f = 0, c = 0;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    f += status[t] < 0;
+    c += status[t] > 0;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    f += __shfl_xor_sync(FULL, f, o);
+    c += __shfl_xor_sync(FULL, c, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(out, f);  // integer counts: order-independent
+    atomicAdd(out + 1, c);
+  }
+}
+
+template <int K, int DM>
+struct VPointLaunch {
+  static void run(const VPointArgs& a, cudaStream_t st) {
+    const size_t smem = (size_t)WPB * (2 * 32 * LDP + 32 * DM + 32) * sizeof(double);
+    static bool attr = false;
+    if (!attr) {
+      LKG_CUDA(cudaFuncSetAttribute(k_vecchia_points<K, DM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      attr = true;
+    }
+    k_vecchia_points<K, DM><<<ceil_div(a.n, WPB), WPB * 32, smem, st>>>(a);
+    LKG_LAUNCH("k_vecchia_points");
+  }
+};
+
+void launch_points(int kernel, const VPointArgs& a, cudaStream_t st) {
+  auto go = [&](auto kc) {
+    constexpr int KK = decltype(kc)::value;
+    if (a.d <= 4) VPointLaunch<KK, 4>::run(a, st);
+    else if (a.d <= 8) VPointLaunch<KK, 8>::run(a, st);
+    else throw std::invalid_argument("LLVecchia on the GPU supports d <= 8");
+  };
+  switch (kernel) {
+    case KGAUSS: go(std::integral_constant<int, KGAUSS>{}); break;
+    case KEXP: go(std::integral_constant<int, KEXP>{}); break;
+    case KMATERN32: go(std::integral_constant<int, KMATERN32>{}); break;
+    case KMATERN52: go(std::integral_constant<int, KMATERN52>{}); break;
+    default: throw std::invalid_argument("Unsupported covariance kernel id");
+  }
+}
+
+template <typename P>
+void valloc(P** p, size_t count) {
+  LKG_CUDA(cudaMalloc((void**)p, sizeof(P) * std::max<size_t>(count, 1)));
+}
+
+// host Cholesky solve of the small GLS system (arma::solve with likely_sympd)
+bool small_spd_solve(int p, std::vector<double> A, std::vector<double> b, std::vector<double>& x) {
+  for (int j = 0; j < p; ++j) {
+    double s = A[j * p + j];
+    for (int k = 0; k < j; ++k) s -= A[j * p + k] * A[j * p + k];
+    if (!(s > 0.0)) return false;
+    A[j * p + j] = std::sqrt(s);
+    for (int i = j + 1; i < p; ++i) {
+      double t = A[i * p + j];
+      for (int k = 0; k < j; ++k) t -= A[i * p + k] * A[j * p + k];
+      A[i * p + j] = t / A[j * p + j];
+    }
+  }
+  for (int i = 0; i < p; ++i) {
+    for (int k = 0; k < i; ++k) b[i] -= A[i * p + k] * b[k];
+    b[i] /= A[i * p + i];
+  }
+  for (int i = p - 1; i >= 0; --i) {
+    for (int k = i + 1; k < p; ++k) b[i] -= A[k * p + i] * b[k];
+    b[i] /= A[i * p + i];
+  }
+  x = b;
+  return true;
+}
+
+}  // namespace
+
+VecchiaEngine::VecchiaEngine(int kernel, int n, int d, int p, const double* X, const double* y, const double* F,
+                             const int32_t* order, const int32_t* nbr, int m)
+    : kernel_(kernel), n_(n), d_(d), p_(p), m_(m) {
+  if (m < 0 || m > VECCHIA_MAX_M) throw std::invalid_argument("LLVecchia on the GPU supports m <= 32");
+  if (p > VPMAX) throw std::invalid_argument("LLVecchia on the GPU supports at most 16 trend columns");
+  if (d < 1 || d > 8) throw std::invalid_argument("LLVecchia on the GPU supports d <= 8");
+  LKG_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+  valloc(&dX_, (size_t)n * d);
+  valloc(&dY_, n);
+  valloc(&dF_, (size_t)n * std::max(p, 1));
+  valloc(&dth_, d);
+  valloc(&dorder_, n);
+  valloc(&dnbr_, (size_t)n * std::max(m, 1));
+  LKG_CUDA(cudaMemcpyAsync(dX_, X, sizeof(double) * n * d, cudaMemcpyHostToDevice, st_));
+  LKG_CUDA(cudaMemcpyAsync(dY_, y, sizeof(double) * n, cudaMemcpyHostToDevice, st_));
+  if (p > 0) LKG_CUDA(cudaMemcpyAsync(dF_, F, sizeof(double) * n * p, cudaMemcpyHostToDevice, st_));
+  LKG_CUDA(cudaMemcpyAsync(dorder_, order, sizeof(int32_t) * n, cudaMemcpyHostToDevice, st_));
+  if (m > 0) LKG_CUDA(cudaMemcpyAsync(dnbr_, nbr, sizeof(int32_t) * n * m, cudaMemcpyHostToDevice, st_));
+  valloc(&du_, n);
+  valloc(&dv_, n);
+  valloc(&dW_, (size_t)n * std::max(p, 1));
+  valloc(&ddu_, (size_t)n * d);
+  valloc(&ddv_, (size_t)n * d);
+  valloc(&ddW_, (size_t)n * d * std::max(p, 1));
+  valloc(&dstatus_, n + 2);
+  nblk_red_ = RED_BLOCKS;
+  valloc(&dpart_, (size_t)nblk_red_ * (VPMAX * VPMAX + VPMAX + 1 + 2 * 8 + 1) + 512);
+  valloc(&dbeta_, VPMAX);
+  LKG_CUDA(cudaStreamSynchronize(st_));
+}
+
+VecchiaEngine::~VecchiaEngine() {
+  for (double* p : {dX_, dY_, dF_, dth_, du_, dv_, dW_, ddu_, ddv_, ddW_, dpart_, dbeta_})
+    if (p) cudaFree(p);
+  if (dorder_) cudaFree(dorder_);
+  if (dnbr_) cudaFree(dnbr_);
+  if (dstatus_) cudaFree(dstatus_);
+  if (st_) cudaStreamDestroy(st_);
+}
+
+VecchiaOut VecchiaEngine::evaluate(const double* theta, bool with_grad, bool est_beta, const double* beta_fixed) {
+  const Config& cfg = config();
+  const int n = n_, d = d_, p = p_;
+  VecchiaOut out;
+  LKG_CUDA(cudaMemcpyAsync(dth_, theta, sizeof(double) * d, cudaMemcpyHostToDevice, st_));
+  VPointArgs a{n, d, p, m_, dX_, dY_, dF_, dth_, dorder_, dnbr_, cfg.num_nugget, cfg.min_rcond,
+               cfg.chol_rcond_check ? 1 : 0, cfg.max_inc_choldiag, with_grad ? 1 : 0, du_, dv_, dW_, ddu_, ddv_,
+               ddW_, dstatus_};
+  {
+    LaunchTimer lt("k_vecchia_points", st_, (double)n * m_ * (m_ + 1) / 2.0, 8.0 * n * (1.0 + d) * m_);
+    launch_points(kernel_, a, st_);
+  }
+  int* dcount = dstatus_ + n;
+  LKG_CUDA(cudaMemsetAsync(dcount, 0, 2 * sizeof(int), st_));
+  {
+    LaunchTimer lt("k_count_status", st_, 0.0, 4.0 * n);
+    k_count_status<<<152, 256, 0, st_>>>(n, dstatus_, dcount);
+    LKG_LAUNCH("k_count_status");
+  }
+  const int P1 = p * p + p + 1;
+  double* fin = dpart_ + (size_t)nblk_red_ * (VPMAX * VPMAX + VPMAX + 1 + 2 * 8 + 1);
+  {
+    LaunchTimer lt("k_vsum1", st_, 0.0, 8.0 * n * (2.0 + p));
+    k_vsum1<<<nblk_red_, 256, 0, st_>>>(n, p, du_, dv_, dW_, dpart_);
+    LKG_LAUNCH("k_vsum1");
+    k_vsum_final<<<1, 256, 0, st_>>>(nblk_red_, P1, dpart_, fin);
+    LKG_LAUNCH("k_vsum_final");
+  }
+  std::vector<double> s1(P1);
+  int counts[2];
+  LKG_CUDA(cudaMemcpyAsync(s1.data(), fin, sizeof(double) * P1, cudaMemcpyDeviceToHost, st_));
+  LKG_CUDA(cudaMemcpyAsync(counts, dcount, 2 * sizeof(int), cudaMemcpyDeviceToHost, st_));
+  LKG_CUDA(cudaStreamSynchronize(st_));
+  if (counts[0] > 0) {
+    out.status = 1;
+    out.message = "[ERROR] Exceed max numerical nugget (" + std::to_string(cfg.max_inc_choldiag + 1) + " x 1e" +
+                  std::to_string(std::log10(cfg.num_nugget)) + ") added to force chol matrix";
+    return out;
+  }
+  out.nugget_points = counts[1];
+  std::vector<double> beta(p, 0.0);
+  if (est_beta || beta_fixed == nullptr) {
+    std::vector<double> A(s1.begin(), s1.begin() + p * p), b(s1.begin() + p * p, s1.begin() + p * p + p);
+    for (int q = 0; q < p; ++q) A[q * p + q] += cfg.num_nugget;
+    if (p > 0 && !small_spd_solve(p, A, b, beta)) {
+      out.status = 2;
+      out.message = "solve(): GLS system of the Vecchia likelihood is not positive definite";
+      return out;
+    }
+  } else {
+    beta.assign(beta_fixed, beta_fixed + p);
+  }
+  const double slogv = s1[p * p + p];
+  if (p > 0) LKG_CUDA(cudaMemcpyAsync(dbeta_, beta.data(), sizeof(double) * p, cudaMemcpyHostToDevice, st_));
+  const int P2 = 1 + 2 * d;
+  {
+    LaunchTimer lt("k_vsum2", st_, 0.0, 8.0 * n * (2.0 + p) * (with_grad ? 1.0 + d : 1.0));
+    k_vsum2<<<nblk_red_, 256, 0, st_>>>(n, p, d, du_, dv_, dW_, ddu_, ddv_, ddW_, dbeta_, with_grad ? 1 : 0, dpart_);
+    LKG_LAUNCH("k_vsum2");
+    k_vsum_final<<<1, 256, 0, st_>>>(nblk_red_, with_grad ? P2 : 1, dpart_, fin);
+    LKG_LAUNCH("k_vsum_final");
+  }
+  std::vector<double> s2(P2, 0.0);
+  LKG_CUDA(cudaMemcpyAsync(s2.data(), fin, sizeof(double) * (with_grad ? P2 : 1), cudaMemcpyDeviceToHost, st_));
+  LKG_CUDA(cudaStreamSynchronize(st_));
+  const double Q = s2[0];
+  const double sigma2 = Q / n;
+  out.sigma2 = sigma2;
+  out.beta = beta;
+  out.vll = -0.5 * n * std::log(2 * M_PI * sigma2) - 0.5 * slogv - 0.5 * n;
+  if (with_grad) {
+    out.grad.resize(d);
+    for (int k = 0; k < d; ++k) out.grad[k] = -0.5 * n * s2[1 + k] / Q - 0.5 * s2[1 + d + k];
+  }
+  return out;
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// conditioning sets
+namespace {
+
+// one launch per ordering step t: every block reduces the previous step's block maxima (identically), block 0
+// records order[t], then each block updates its range of min squared distances and writes its new (max, index)
+__global__ void k_maxmin_step(int n, int d, const double* __restrict__ Xp, double* __restrict__ mind2,
+                              const double* __restrict__ pin_v, const int* __restrict__ pin_i, double* __restrict__ pout_v,
+                              int* __restrict__ pout_i, int* __restrict__ order, int t) {
+  __shared__ double sv[256];
+  __shared__ int si[256];
+  __shared__ int next_s;
+  const int nb = gridDim.x;
+  // reduce the previous partials (nb <= 256 entries)
+  double bv = -INFINITY;
+  int bi = 0x7fffffff;
+  for (int q = threadIdx.x; q < nb; q += blockDim.x) {
+    const double v = pin_v[q];
+    const int i = pin_i[q];
+    if (v > bv || (v == bv && i < bi)) {
+      bv = v;
+      bi = i;
+    }
+  }
+  sv[threadIdx.x] = bv;
+  si[threadIdx.x] = bi;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      const double ov = sv[threadIdx.x + s];
+      const int oi = si[threadIdx.x + s];
+      if (ov > sv[threadIdx.x] || (ov == sv[threadIdx.x] && oi < si[threadIdx.x])) {
+        sv[threadIdx.x] = ov;
+        si[threadIdx.x] = oi;
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) next_s = si[0];
+  __syncthreads();
+  const int next = next_s;
+  if (blockIdx.x == 0 && threadIdx.x == 0) order[t] = next;
+  double nx[8];
+  for (int k = 0; k < d; ++k) nx[k] = Xp[(int64_t)next * d + k];
+  const int64_t lo = (int64_t)n * blockIdx.x / nb, hi = (int64_t)n * (blockIdx.x + 1) / nb;
+  bv = -INFINITY;
+  bi = 0x7fffffff;
+  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    double m = mind2[i];
+    if (m != -INFINITY) {
+      if (i == next) {
+        m = -INFINITY;
+      } else {
+        double s = 0.0;
+        for (int k = 0; k < d; ++k) {
+          const double dk = Xp[i * d + k] - nx[k];
+          s += dk * dk;
+        }
+        if (s < m) m = s;
+      }
+      mind2[i] = m;
+    }
+    if (m > bv || (m == bv && (int)i < bi)) {
+      bv = m;
+      bi = (int)i;
+    }
+  }
+  sv[threadIdx.x] = bv;
+  si[threadIdx.x] = bi;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      const double ov = sv[threadIdx.x + s];
+      const int oi = si[threadIdx.x + s];
+      if (ov > sv[threadIdx.x] || (ov == sv[threadIdx.x] && oi < si[threadIdx.x])) {
+        sv[threadIdx.x] = ov;
+        si[threadIdx.x] = oi;
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    pout_v[blockIdx.x] = sv[0];
+    pout_i[blockIdx.x] = si[0];
+  }
+}
+
+// mind2[i] = |x_i - x_first|^2, then the first step's block maxima
+__global__ void k_maxmin_init(int n, int d, const double* __restrict__ Xp, int first, double* __restrict__ mind2,
+                              double* __restrict__ pv, int* __restrict__ pi) {
+  __shared__ double sv[256];
+  __shared__ int si[256];
+  const int nb = gridDim.x;
+  const int64_t lo = (int64_t)n * blockIdx.x / nb, hi = (int64_t)n * (blockIdx.x + 1) / nb;
+  double bv = -INFINITY;
+  int bi = 0x7fffffff;
+  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    double m;
+    if (i == first) {
+      m = -INFINITY;
+    } else {
+      double s = 0.0;
+      for (int k = 0; k < d; ++k) {
+        const double dk = Xp[i * d + k] - Xp[(int64_t)first * d + k];
+        s += dk * dk;
+      }
+      m = s;
+    }
+    mind2[i] = m;
+    if (m > bv || (m == bv && (int)i < bi)) {
+      bv = m;
+      bi = (int)i;
+    }
+  }
+  sv[threadIdx.x] = bv;
+  si[threadIdx.x] = bi;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      const double ov = sv[threadIdx.x + s];
+      const int oi = si[threadIdx.x + s];
+      if (ov > sv[threadIdx.x] || (ov == sv[threadIdx.x] && oi < si[threadIdx.x])) {
+        sv[threadIdx.x] = ov;
+        si[threadIdx.x] = oi;
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    pv[blockIdx.x] = sv[0];
+    pi[blockIdx.x] = si[0];
+  }
+}
+
+// m nearest earlier-ordered points of ordered point t, one warp per t: brute force over positions [0, t) with a
+// sorted per-warp list of the m best (squared distance, global index) keys
+__global__ void __launch_bounds__(256) k_knn_earlier(int n, int d, int m, const double* __restrict__ Xo,
+                                                     const int32_t* __restrict__ order, int32_t* __restrict__ nbr) {
+  __shared__ double kd[8][VECCHIA_MAX_M];
+  __shared__ int ki[8][VECCHIA_MAX_M];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int t = blockIdx.x * 8 + w;
+  if (t >= n) return;
+  const int k = t < m ? t : m;
+  double xt[8];
+  for (int q = 0; q < d; ++q) xt[q] = Xo[(int64_t)t * d + q];
+  int cnt = 0;  // entries in the list (uniform over the warp)
+  double thr = INFINITY;
+  int thri = 0x7fffffff;
+  for (int j0 = 0; j0 < t; j0 += 32) {
+    const int j = j0 + lane;
+    double dj = INFINITY;
+    int ij = 0x7fffffff;
+    if (j < t) {
+      double s = 0.0;
+      for (int q = 0; q < d; ++q) {
+        const double dq = xt[q] - Xo[(int64_t)j * d + q];
+        s += dq * dq;
+      }
+      dj = s;
+      ij = order[j];
+    }
+    bool qual = (j < t) && (cnt < k || dj < thr || (dj == thr && ij < thri));
+    unsigned mask = __ballot_sync(FULL, qual);
+    while (mask) {
+      const int src = __ffs(mask) - 1;
+      mask &= mask - 1;
+      const double cd = __shfl_sync(FULL, dj, src);
+      const int ci = __shfl_sync(FULL, ij, src);
+      if (lane == 0) {
+        const bool full = cnt >= k;
+        if (!full || cd < kd[w][k - 1] || (cd == kd[w][k - 1] && ci < ki[w][k - 1])) {
+          int pos = full ? k - 1 : cnt;
+          while (pos > 0 && (kd[w][pos - 1] > cd || (kd[w][pos - 1] == cd && ki[w][pos - 1] > ci))) {
+            kd[w][pos] = kd[w][pos - 1];
+            ki[w][pos] = ki[w][pos - 1];
+            --pos;
+          }
+          kd[w][pos] = cd;
+          ki[w][pos] = ci;
+        }
+      }
+      cnt = cnt < k ? cnt + 1 : k;
+      __syncwarp();
+    }
+    __syncwarp();
+    if (cnt >= k && k > 0) {
+      thr = kd[w][k - 1];
+      thri = ki[w][k - 1];
+    }
+  }
+  __syncwarp();
+  for (int a = lane; a < m; a += 32) nbr[(int64_t)t * m + a] = (a < k) ? ki[w][a] : -1;
+}
+
+__global__ void k_gather_points(int n, int d, const double* __restrict__ X, const int32_t* __restrict__ order,
+                                double* __restrict__ Xo, double* __restrict__ Xp) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int q = 0; q < d; ++q) {
+    Xp[i * d + q] = X[i + (int64_t)q * n];  // point-major copy of X
+    if (order) Xo[i * d + q] = X[order[i] + (int64_t)q * n];
+  }
+}
+
+}  // namespace
+
+void vecchia_sets_gpu(int n, int d, const double* X, int m, int32_t* order, int32_t* nbr) {
+  if (d > 8) throw std::invalid_argument("Vecchia sets on the GPU support d <= 8");
+  if (m > VECCHIA_MAX_M) throw std::invalid_argument("Vecchia sets on the GPU support m <= 32");
+  const int mm = std::min(m, n - 1);
+  cudaStream_t st;
+  LKG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  double *dX, *dXp, *dXo, *dmind, *pv;
+  int *pi;
+  int32_t *dorder, *dnbr;
+  valloc(&dX, (size_t)n * d);
+  valloc(&dXp, (size_t)n * d);
+  valloc(&dXo, (size_t)n * d);
+  valloc(&dmind, n);
+  const int nb = std::min(256, std::max(1, ceil_div(n, 1024)));
+  valloc(&pv, 2 * nb);
+  valloc(&pi, 2 * nb);
+  valloc(&dorder, n);
+  valloc(&dnbr, (size_t)n * std::max(m, 1));
+  LKG_CUDA(cudaMemcpyAsync(dX, X, sizeof(double) * n * d, cudaMemcpyHostToDevice, st));
+  k_gather_points<<<ceil_div(n, 256), 256, 0, st>>>(n, d, dX, nullptr, nullptr, dXp);
+  LKG_LAUNCH("k_gather_points");
+  // first point: closest to the centroid (index_min: first minimum), computed on the host in FP64
+  std::vector<double> cen(d, 0.0);
+  for (int q = 0; q < d; ++q) {
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s += X[i + (size_t)q * n];
+    cen[q] = s / n;
+  }
+  int first = 0;
+  double best = INFINITY;
+  for (int i = 0; i < n; ++i) {
+    double s = 0.0;
+    for (int q = 0; q < d; ++q) {
+      const double dk = X[i + (size_t)q * n] - cen[q];
+      s += dk * dk;
+    }
+    if (s < best) {
+      best = s;
+      first = i;
+    }
+  }
+  LKG_CUDA(cudaMemcpyAsync(dorder, &first, sizeof(int), cudaMemcpyHostToDevice, st));
+  {
+    LaunchTimer lt("k_maxmin_init", st, 3.0 * n * d, 8.0 * n * d);
+    k_maxmin_init<<<nb, 256, 0, st>>>(n, d, dXp, first, dmind, pv, pi);
+    LKG_LAUNCH("k_maxmin_init");
+  }
+  for (int t = 1; t < n; ++t) {
+    const int in = (t - 1) & 1, outb = t & 1;
+    k_maxmin_step<<<nb, 256, 0, st>>>(n, d, dXp, dmind, pv + in * nb, pi + in * nb, pv + outb * nb, pi + outb * nb,
+                                      dorder, t);
+  }
+  LKG_LAUNCH("k_maxmin_step");
+  k_gather_points<<<ceil_div(n, 256), 256, 0, st>>>(n, d, dX, dorder, dXo, dXp);
+  LKG_LAUNCH("k_gather_points");
+  if (m > 0) {
+    LaunchTimer lt("k_knn_earlier", st, 1.5 * n * (double)n * d, 4.0 * n * (double)n * d);
+    k_knn_earlier<<<ceil_div(n, 8), 256, 0, st>>>(n, d, mm, dXo, dorder, dnbr);
+    LKG_LAUNCH("k_knn_earlier");
+  }
+  LKG_CUDA(cudaMemcpyAsync(order, dorder, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
+  std::vector<int32_t> tmp((size_t)n * std::max(mm, 1));
+  if (mm > 0)
+    LKG_CUDA(cudaMemcpyAsync(tmp.data(), dnbr, sizeof(int32_t) * n * mm, cudaMemcpyDeviceToHost, st));
+  LKG_CUDA(cudaStreamSynchronize(st));
+  for (int t = 0; t < n; ++t)
+    for (int a = 0; a < m; ++a) nbr[(size_t)t * m + a] = (a < mm) ? tmp[(size_t)t * mm + a] : -1;
+  for (double* p : {dX, dXp, dXo, dmind, pv}) cudaFree(p);
+  cudaFree(pi);
+  cudaFree(dorder);
+  cudaFree(dnbr);
+  cudaStreamDestroy(st);
+}
+
+}  // namespace lkg

@@ -1,0 +1,57 @@
+// vecchia.hpp -- Vecchia approximated log-likelihood (objective "LLVecchia(m)") on the GPU.
+//
+// Reference: Kriging::make_vecchia_sets (src/lib/Kriging.cpp:736-804) and Kriging::_logLikelihoodVecchia
+// (src/lib/Kriging.cpp:806-924).  One warp per ordered point builds its (m x m) conditional block, factors it with
+// the numerical-nugget retry and rcond rules of safe_chol_lower, and produces u, v, W and their theta-derivatives;
+// deterministic block reductions then give the GLS beta, sigma2, VLL and the envelope-theorem gradient.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace lkg {
+
+constexpr int VECCHIA_MAX_M = 32;
+
+struct VecchiaOut {
+  double vll = 0.0, sigma2 = 0.0;
+  std::vector<double> beta, grad;
+  int status = 0;  // 0 ok, 1 a conditional block stayed non-SPD after the nugget increments
+  std::string message;
+  long long nugget_points = 0;  // conditionals that needed numerical-nugget increments
+};
+
+class VecchiaEngine {
+ public:
+  // X n x d column-major (normalised), y n, F n x p column-major; order[n], nbr[n * m] (-1 padded), host arrays.
+  VecchiaEngine(int kernel, int n, int d, int p, const double* X, const double* y, const double* F,
+                const int32_t* order, const int32_t* nbr, int m);
+  ~VecchiaEngine();
+  VecchiaEngine(const VecchiaEngine&) = delete;
+  VecchiaEngine& operator=(const VecchiaEngine&) = delete;
+
+  // est_beta = false uses beta_fixed (p values), as the reference when m_est_beta is false and m_beta has p entries
+  VecchiaOut evaluate(const double* theta, bool with_grad, bool est_beta, const double* beta_fixed);
+  int n() const { return n_; }
+  int m() const { return m_; }
+  cudaStream_t stream() const { return st_; }
+
+ private:
+  int kernel_, n_, d_, p_, m_;
+  cudaStream_t st_ = nullptr;
+  double *dX_ = nullptr, *dY_ = nullptr, *dF_ = nullptr, *dth_ = nullptr;
+  int32_t *dorder_ = nullptr, *dnbr_ = nullptr;
+  double *du_ = nullptr, *dv_ = nullptr, *dW_ = nullptr, *ddu_ = nullptr, *ddv_ = nullptr, *ddW_ = nullptr;
+  int* dstatus_ = nullptr;
+  double *dpart_ = nullptr, *dbeta_ = nullptr;
+  int nblk_red_ = 0;
+};
+
+// GPU construction of the Vecchia sets, same definition as make_vecchia_sets: maxmin ordering from the point closest
+// to the centroid (argmin / argmax ties -> lowest index), then the min(m, t) nearest earlier-ordered points by
+// (squared distance, index).  X n x d column-major on the host; outputs host arrays order[n], nbr[n * m].
+void vecchia_sets_gpu(int n, int d, const double* X, int m, int32_t* order, int32_t* nbr);
+
+}  // namespace lkg

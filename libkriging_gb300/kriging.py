@@ -139,6 +139,35 @@ class Kriging:
                                               int(bool(return_deriv)), ptr(mean), ptr(sd), ptr(cov), None, None))
         return mean, sd, cov, None, None
 
+    # ---- Vecchia (Kriging.hpp:145-173) ----
+    def logLikelihoodVecchiaFun(self, theta, return_grad=False):
+        t = np.ascontiguousarray(np.asarray(theta, dtype=np.float64).reshape(-1))
+        v = ctypes.c_double()
+        g = np.zeros(t.size) if return_grad else None
+        check(_lib.load().lkg_kriging_log_likelihood_vecchia_fun(self._h, ptr(t), t.size, int(bool(return_grad)),
+                                                                 ctypes.byref(v), ptr(g)))
+        return v.value, (g if return_grad else np.zeros(0))
+
+    def set_vecchia_exact_commit(self, b):
+        check(_lib.load().lkg_kriging_set_vecchia_exact_commit(self._h, int(bool(b))))
+
+    def vecchia_neighbors(self):
+        return _lib.load().lkg_kriging_vecchia_neighbors(self._h)
+
+    def is_vecchia_light(self):
+        return bool(_lib.load().lkg_kriging_is_vecchia_light(self._h))
+
+    def vecchia_sets(self):
+        """(order[n], neighbours[n, m]) of the fitted Vecchia model (global row indices, -1 padded)."""
+        n, m = ctypes.c_int(), ctypes.c_int()
+        check(_lib.load().lkg_kriging_get_vecchia_sets(self._h, None, None, ctypes.byref(n), ctypes.byref(m)))
+        order = np.zeros(n.value, dtype=np.int32)
+        nbr = np.zeros((n.value, m.value), dtype=np.int32)
+        ip = ctypes.POINTER(ctypes.c_int)
+        check(_lib.load().lkg_kriging_get_vecchia_sets(self._h, order.ctypes.data_as(ip), nbr.ctypes.data_as(ip),
+                                                       ctypes.byref(n), ctypes.byref(m)))
+        return order, nbr
+
     def set_precision(self, slices):
         """0: FP64 path (default); 4..8: mixed path with that many bf16 digit slices (see the C header)."""
         check(_lib.load().lkg_kriging_set_precision(self._h, int(slices)))
@@ -288,3 +317,14 @@ class Optim:
     @staticmethod
     def set_max_restart(m):
         _lib.load().lkg_optim_set_max_restart(int(m))
+
+
+def vecchia_sets(X, m):
+    """GPU construction of the Vecchia sets of make_vecchia_sets: (order[n], neighbours[n, m], -1 padded)."""
+    X = _as_X(X)
+    n, d = X.shape
+    order = np.zeros(n, dtype=np.int32)
+    nbr = np.zeros((n, m), dtype=np.int32)
+    ip = ctypes.POINTER(ctypes.c_int)
+    check(_lib.load().lkg_vecchia_sets(n, d, ptr(X), m, order.ctypes.data_as(ip), nbr.ctypes.data_as(ip)))
+    return order, nbr

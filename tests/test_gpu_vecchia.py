@@ -1,0 +1,95 @@
+"""GPU Vecchia path (objective LLVecchia(m)) against the oracle's restatement of make_vecchia_sets and
+_logLikelihoodVecchia (src/lib/Kriging.cpp:736-924), plus the reference's own identity / FD checks
+(tests/KrigingVecchiaTest.cpp:46-84)."""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _data(n, d, seed):
+    rng = np.random.default_rng(seed)
+    X = rng.uniform(size=(n, d))
+    y = np.sin(2 * np.pi * X).sum(axis=1) + 0.01 * rng.standard_normal(n)
+    return X, y
+
+
+@pytest.mark.parametrize("n,d,m", [(300, 3, 10), (517, 2, 30), (64, 4, 5)])
+def test_sets_match_oracle(gpu_lib, n, d, m):
+    X, _ = _data(n, d, n)
+    order, nbr = gpu_lib.vecchia_sets(X, m)
+    o_order, o_nbr = O.vecchia_sets(X, m)
+    assert np.array_equal(order, o_order)
+    for t in range(n):
+        assert set(nbr[t][nbr[t] >= 0].tolist()) == set(o_nbr[t][o_nbr[t] >= 0].tolist()), t
+        assert np.sum(nbr[t] >= 0) == min(m, t)
+
+
+@pytest.mark.parametrize("kernel", ["gauss", "matern5_2", "matern3_2", "exp"])
+def test_vll_and_gradient_vs_oracle(gpu_lib, kernel):
+    X, y = _data(400, 3, 7)
+    k = gpu_lib.Kriging("matern5_2" if kernel == "matern5_2" else kernel)
+    k.fit(y, X, "constant", False, "none", "LLVecchia(15)", {"theta": np.full((1, 3), 0.3)})
+    order, nbr = k.vecchia_sets()
+    ora = O.OracleKriging(y, X, kernel)
+    for th in ([0.2, 0.3, 0.25], [0.5, 0.15, 0.4]):
+        th = np.array(th)
+        v, g = k.logLikelihoodVecchiaFun(th, True)
+        vo, go, _, _ = O.vecchia_ll(kernel, ora.X, ora.y, ora.F, th, order, nbr)
+        assert rel_err(v, vo) < 1e-10, (v, vo)
+        assert rel_err(g, go) < 1e-8, (g, go)
+        v2, _ = k.logLikelihoodVecchiaFun(th, False)
+        assert v2 == v
+
+
+def test_vll_full_conditioning_equals_exact_ll(gpu_lib):
+    # KrigingVecchiaTest.cpp:46-61 with m = n - 1 (the GPU kernels take m <= 32)
+    X, y = _data(33, 2, 3)
+    k = gpu_lib.Kriging("matern5_2")
+    k.fit(y, X, "constant", False, "none", "LLVecchia(32)", {"theta": np.array([[0.2, 0.2]])})
+    for th in ([0.2, 0.2], [0.4, 0.3]):
+        vll, _ = k.logLikelihoodVecchiaFun(np.array(th), False)
+        ll, _, _ = k.logLikelihoodFun(np.array(th), False)
+        assert abs(vll - ll) < 1e-3 * abs(ll) + 1e-3
+
+
+def test_vll_gradient_vs_fd(gpu_lib):
+    # KrigingVecchiaTest.cpp:63-84
+    X, y = _data(200, 2, 4)
+    k = gpu_lib.Kriging("matern5_2")
+    k.fit(y, X, "constant", False, "none", "LLVecchia(15)", {"theta": np.array([[0.2, 0.3]])})
+    th = np.array([0.2, 0.3])
+    _, g = k.logLikelihoodVecchiaFun(th, True)
+    h = 1e-6
+    for j in range(2):
+        e = np.zeros(2)
+        e[j] = h
+        fd = (k.logLikelihoodVecchiaFun(th + e)[0] - k.logLikelihoodVecchiaFun(th - e)[0]) / (2 * h)
+        assert abs(g[j] - fd) < 1e-3 * max(1.0, abs(fd))
+
+
+@pytest.mark.parametrize("exact", [True, False])
+def test_vecchia_fit(gpu_lib, exact):
+    X, y = _data(300, 2, 5)
+    k = gpu_lib.Kriging("matern5_2")
+    k.set_vecchia_exact_commit(exact)
+    k.fit(y, X, "constant", False, "BFGS", "LLVecchia(20)", {"theta": np.array([[0.3, 0.3]])})
+    assert k.vecchia_neighbors() == 20
+    assert k.is_vecchia_light() == (not exact)
+    th = k.theta()
+    v_hat, g_hat = k.logLikelihoodVecchiaFun(th, True)
+    v0, _ = k.logLikelihoodVecchiaFun(np.array([0.3, 0.3]), False)
+    assert v_hat >= v0
+    if exact:
+        mean, _, _, _, _ = k.predict(X[:10], True, False, False)
+        assert np.allclose(mean, y[:10], atol=1e-3)
+
+
+def test_vecchia_rejects_nugget(gpu_lib):
+    X, y = _data(50, 2, 6)
+    k = gpu_lib.Kriging("matern5_2", "nugget")
+    with pytest.raises(gpu_lib.LibKrigingError, match="LLVecchia objective not supported"):
+        k.fit(y, X, "constant", False, "BFGS", "LLVecchia(10)", {})
