@@ -3,13 +3,17 @@
 Workload (the single-GPU configuration of the headline metric): n = 16384 points X ~ U[0,1]^8,
 y = sum_j sin(2 pi x_j) + 0.1 N(0,1), matern5_2 kernel, NuggetKriging with alpha = 1 / (1 + 1e-6)
 (nugget = 1e-6 sigma2), theta ~ U[0.2, 1.5]^8, all drawn from numpy's PCG64 with seed 123.  One step = one
-logLikelihoodFun(gamma = [theta, alpha], return_grad = true) -- covariance build, blocked FP64 Cholesky, solves,
-GLS, R^-1 and the adjoint gradient -- on the FP64 path.
+logLikelihoodFun(gamma = [theta, alpha], return_grad = true) -- covariance build, blocked Cholesky, solves, GLS,
+R^-1 and the adjoint gradient.  The headline line is the mixed-precision path (O(n^3) products as error-free bf16
+digit products on the tensor cores, 7 digits for the Cholesky, 6 for the inverse); the same line carries the FP64
+path's figures ("fp64"), the speed-up and the relative LL / gradient difference between the two.
 
   value  device throughput: evaluations / s from the CUDA-event stage timings of each step (design resident)
   e2e    wall clock through the C ABI (lkg_kriging_log_likelihood_fun): gamma copied host -> device and
          (LL, gradient) device -> host every step
-Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--n 16384]
+Other workloads (--workload): "multistart" (BFGS64 fits of an n=2048 d=6 design, fits/s) and "vecchia"
+(Vecchia LL + gradient at n = 2^20, m = 30, evals/s).
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--n 16384] [--workload W]
 """
 from __future__ import annotations
 
@@ -174,6 +178,37 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def _timed_steps(k, lib, gamma, steps, local):
+    """K LL+grad steps; returns (mean device ms per step from the CUDA-event stage timings, last (ll, grad),
+    per-kernel stats, clock record)."""
+    lib.lkg_stats_reset()
+    lib.lkg_stats_enable(1)
+    clocks = ClockSampler(local)
+    clocks.start()
+    dev_ms = []
+    ll = g = None
+    for _ in range(steps):
+        ll, g, _ = k.logLikelihoodFun(gamma, True, False, bench=True)
+        dev_ms.append(sum(k.last_bench.values()))
+    clk = clocks.stop()
+    lib.lkg_stats_enable(0)
+    return float(np.mean(dev_ms)), (ll, np.asarray(g)), kernel_stats(lib), clk, dict(k.last_bench)
+
+
+def _e2e(lk, lib, k, gamma, steps, barrier):
+    import torch
+    gam_h = torch.tensor(gamma, dtype=torch.float64).pin_memory().numpy()
+    grad_h = torch.zeros(gamma.size, dtype=torch.float64).pin_memory().numpy()
+    llv = ctypes.c_double()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        lk._lib.check(lib.lkg_kriging_log_likelihood_fun(k._h, lk._lib.ptr(gam_h), gam_h.size, 1, 0,
+                                                          ctypes.byref(llv), lk._lib.ptr(grad_h), None))
+    barrier()
+    return (time.perf_counter() - t0) / steps
+
+
 def run_gpu(args):
     rank, world, local = dist_env()
     import torch
@@ -196,83 +231,200 @@ def run_gpu(args):
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
+    # ---- FP64 path ----
+    k.set_precision(0)
     for _ in range(args.warmup):
         k.logLikelihoodFun(gamma, True, False, bench=True)
-    # device-resident throughput (CUDA events on the library stream, per stage, summed per step)
     barrier()
-    lib.lkg_stats_reset()
-    lib.lkg_stats_enable(1)
-    clocks = ClockSampler(local)
-    clocks.start()
-    dev_ms = []
+    fp64_ms, (ll64, g64), st64, clk64, stage64 = _timed_steps(k, lib, gamma, args.steps, local)
+    barrier()
+    # ---- mixed path (headline) ----
+    k.set_precision(args.slices)
+    for _ in range(args.warmup):
+        k.logLikelihoodFun(gamma, True, False, bench=True)
+    barrier()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        ll, g, _ = k.logLikelihoodFun(gamma, True, False, bench=True)
-        dev_ms.append(sum(k.last_bench.values()))
+    mix_ms, (llm, gm), stats, clk, stage = _timed_steps(k, lib, gamma, args.steps, local)
     barrier()
     wall_value = time.perf_counter() - t0
-    clk = clocks.stop()
-    lib.lkg_stats_enable(0)
-    stats = kernel_stats(lib)
+    used = k.last_slices()
+    e2e_s = _e2e(lk, lib, k, gamma, args.steps, barrier)
     launches = sum(v["launches"] for v in stats.values())
-    # end to end through the C ABI: gamma from pinned host memory in, (LL, grad) out, wall clock
-    gam_h = torch.tensor(gamma, dtype=torch.float64).pin_memory().numpy()
-    grad_h = torch.zeros(gamma.size, dtype=torch.float64).pin_memory().numpy()
-    llv = ctypes.c_double()
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        lk._lib.check(lib.lkg_kriging_log_likelihood_fun(k._h, lk._lib.ptr(gam_h), gam_h.size, 1, 0,
-                                                          ctypes.byref(llv), lk._lib.ptr(grad_h), None))
-    barrier()
-    e2e_wall = time.perf_counter() - t0
-    max_dev = float(np.mean(dev_ms))
-    e2e_s = e2e_wall / args.steps
     if world > 1:
-        t = torch.tensor([max_dev, e2e_s], dtype=torch.float64, device="cuda")
+        t = torch.tensor([mix_ms, e2e_s, fp64_ms], dtype=torch.float64, device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        max_dev, e2e_s = float(t[0]), float(t[1])
-    value = world * 1000.0 / max_dev
-    e2e = world / e2e_s
-    # roofline of the dominant kernel (largest total CUDA-event time in the timed region)
-    dom = max(stats.items(), key=lambda kv: kv[1]["ms"])
-    name, s = dom
-    achieved = s["flops"] / (s["ms"] * 1e-3) / 1e12
-    traffic = None
-    tf = ROOT / "profiles" / "dram_traffic.json"
-    if tf.exists():
-        try:
-            ratio = json.loads(tf.read_text()).get(name, {}).get("ratio")
-            if ratio is not None and s["launches"] > 0:
-                traffic = ratio * s["bytes"] / s["launches"]  # DRAM bytes per launch, scaled from the ncu capture
-        except ValueError:
-            traffic = None
-    roofline = dict(bound="fp64", kernel=name, achieved=achieved, peak=peak_fp64.value, unit="TFLOP/s",
-                    frac=achieved / peak_fp64.value, traffic=traffic,
-                    peak_source="lkg_probe_fp64_peak measured on this GPU (DFMA pipe; MEASURED_PEAKS.json has no "
-                                "FP64 entry); per-launch algorithmic flops / mean CUDA-event launch time",
-                    launches=s["launches"], share=s["ms"] / sum(v["ms"] for v in stats.values()))
+        mix_ms, e2e_s, fp64_ms = float(t[0]), float(t[1]), float(t[2])
+    value = world * 1000.0 / mix_ms
+    rel_ll = abs(llm - ll64) / abs(ll64)
+    rel_g = float(np.linalg.norm(gm - g64) / np.linalg.norm(g64))
+    peaks = measured_peaks()
+    tensor_peak = peaks.get("bf16_tflops")
+
+    def roof(stats_, bound):
+        name, s = max(stats_.items(), key=lambda kv: kv[1]["ms"])
+        achieved = s["flops"] / (s["ms"] * 1e-3) / 1e12
+        if name.startswith("k_oz"):
+            pk, unit, src = tensor_peak, "TFLOP/s", ("MEASURED_PEAKS.json bf16_tflops (burst, cuBLAS tcgen05); this "
+                                                    "kernel issues mma.sync, measured at 605 TFLOP/s on this part")
+        else:
+            pk, unit, src = peak_fp64.value, "TFLOP/s", "lkg_probe_fp64_peak measured in this run (DFMA pipe)"
+        traffic = None
+        tf = ROOT / "profiles" / "dram_traffic.json"
+        if tf.exists():
+            try:
+                ratio = json.loads(tf.read_text()).get(name, {}).get("ratio")
+                if ratio is not None and s["launches"] > 0:
+                    traffic = ratio * s["bytes"] / s["launches"]
+            except ValueError:
+                traffic = None
+        return dict(bound=bound if name.startswith("k_oz") else "fp64", kernel=name, achieved=achieved, peak=pk,
+                    unit=unit, frac=(achieved / pk) if pk else None, traffic=traffic, peak_source=src,
+                    launches=s["launches"], share=s["ms"] / sum(v["ms"] for v in stats_.values()))
+
+    def kern(stats_):
+        return {kk: dict(launches=v["launches"], ms=round(v["ms"], 3),
+                         tflops=(v["flops"] / (v["ms"] * 1e-3) / 1e12) if v["ms"] > 0 else None)
+                for kk, v in sorted(stats_.items(), key=lambda kv: -kv[1]["ms"])}
+
     line = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=world, steps=args.steps, warmup=args.warmup,
-                ms_per_step=max_dev, higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f64",
+                ms_per_step=mix_ms, higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f64",
                 data="synthetic (seeded PCG64, seed 123)",
-                config=dict(workload="dense LL+grad, n=%d, d=8, matern5_2, nugget 1e-6, FP64 path" % args.n,
+                config=dict(workload="dense LL+grad, n=%d, d=8, matern5_2, nugget 1e-6" % args.n,
+                            precision="mixed: O(n^3) products on bf16 tensor cores by error-free digit splitting "
+                                      "(Cholesky %d digits, inverse %d), FP64 panels and reductions"
+                                      % (used, max(4, used - 1)),
                             parallelism="replicas" if world > 1 else "single GPU",
                             l2="inputs larger than L2 (R, L^-1, R^-1: 3 x %.2f GB)" % (8.0 * args.n * args.n / 1e9)),
-                e2e=dict(value=e2e, unit=UNIT, h2d_bytes_per_step=8 * gamma.size,
+                e2e=dict(value=world / e2e_s, unit=UNIT, h2d_bytes_per_step=8 * gamma.size,
                          d2h_bytes_per_step=8 * (1 + gamma.size)),
-                gpu_launches=int(launches), roofline=roofline, clocks=clk, ll=float(ll),
+                fp64=dict(value=world * 1000.0 / fp64_ms, ms_per_step=fp64_ms, roofline=roof(st64, "fp64"),
+                          stage_ms={kk: round(v, 3) for kk, v in stage64.items()}, kernels=kern(st64), clocks=clk64),
+                speedup_mixed_vs_fp64=fp64_ms / mix_ms,
+                rel_err_vs_fp64=dict(ll=rel_ll, grad=rel_g, ll_fp64=float(ll64), ll_mixed=float(llm)),
+                gpu_launches=int(launches), roofline=roof(stats, "tensor"), clocks=clk,
                 wall_s_timed_region=wall_value,
-                measured_peaks={k2: v for k2, v in measured_peaks().items() if k2 in ("hbm_gbs", "bf16_tflops")},
-                stage_ms={kk: round(v, 3) for kk, v in k.last_bench.items()},
-                kernels={kk: dict(launches=v["launches"], ms=round(v["ms"], 3),
-                                  tflops=(v["flops"] / (v["ms"] * 1e-3) / 1e12) if v["ms"] > 0 else None)
-                         for kk, v in sorted(stats.items(), key=lambda kv: -kv[1]["ms"])})
+                measured_peaks={k2: v for k2, v in peaks.items() if k2 in ("hbm_gbs", "bf16_tflops")},
+                fp64_peak_tflops=peak_fp64.value,
+                stage_ms={kk: round(v, 3) for kk, v in stage.items()}, kernels=kern(stats))
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(X, y, theta, alpha)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def make_multistart_inputs(n=2048, d=6, starts=64, seed=123):
+    """Batched multistart workload: X ~ U[0,1]^6, y = sum_j cos(3 x_j) x_j + N(0, 0.01) (variance 0.01), gauss,
+    64 starting points theta ~ U[0.1, 2]^6; the nugget 1e-8 is Nugget mode with sigma2 and nugget fixed."""
+    rng = np.random.default_rng(seed)
+    X = rng.uniform(size=(n, d))
+    y = (np.cos(3 * X) * X).sum(axis=1) + 0.1 * rng.standard_normal(n)
+    thetas = rng.uniform(0.1, 2.0, size=(starts, d))
+    s2 = float(np.var(y))
+    return X, y, thetas, dict(sigma2=s2, is_sigma2_estim=False, nugget=1e-8 * s2, is_nugget_estim=False)
+
+
+def run_gpu_multistart(args):
+    import libkriging_gb300 as lk
+    lib = lk.load()
+    X, y, thetas, params = make_multistart_inputs()
+    P = dict(params, theta=thetas)
+    k = lk.Kriging("gauss", "nugget")
+    k.set_precision(args.slices if args.mixed else 0)
+    for _ in range(args.warmup):
+        k.fit(y, X, "constant", False, "BFGS%d" % thetas.shape[0], "LL", P)
+    lib.lkg_stats_reset()
+    lib.lkg_stats_enable(1)
+    clocks = ClockSampler(0)
+    clocks.start()
+    t0 = time.perf_counter()
+    evals0 = 0
+    for _ in range(args.steps):
+        k.fit(y, X, "constant", False, "BFGS%d" % thetas.shape[0], "LL", P)
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    lib.lkg_stats_enable(0)
+    stats = kernel_stats(lib)
+    potrf = stats.get("k_potrf_diag", {"launches": 0})
+    # every evaluation runs one diagonal-block step per 64 rows for each batch entry in one launch
+    nblk = -(-X.shape[0] // 64)
+    rounds = potrf["launches"] / nblk
+    dom = max(stats.items(), key=lambda kv: kv[1]["ms"])
+    line = dict(metric="batched multistart fits/s (64 starts, n=2048, d=6, gauss, nugget 1e-8)",
+                value=args.steps / wall, unit="fits/s", n_gpus=1, steps=args.steps, warmup=args.warmup,
+                ms_per_step=1000.0 * wall / args.steps, higher_is_better=True, scaling="weak", vs_baseline=None,
+                dtype="f64", data="synthetic (seeded PCG64, seed 123)",
+                config=dict(workload="multistart BFGS64, n=2048, d=6, gauss, Nugget mode sigma2/nugget fixed",
+                            precision="mixed %d digits" % args.slices if args.mixed else "FP64"),
+                batched_rounds_per_fit=rounds / args.steps, theta=k.theta().tolist(), ll=k.logLikelihood(),
+                gpu_launches=int(sum(v["launches"] for v in stats.values())), clocks=clk,
+                roofline=dict(kernel=dom[0], achieved=dom[1]["flops"] / (dom[1]["ms"] * 1e-3) / 1e12,
+                              unit="TFLOP/s", share=dom[1]["ms"] / sum(v["ms"] for v in stats.values())))
+    print(json.dumps(line), flush=True)
+
+
+def make_vecchia_inputs(n=1 << 20, d=3, seed=123):
+    """Vecchia workload: X ~ U[0,1]^3, y = sum_j sin(2 pi x_j) + N(0, 1e-4) (variance 1e-4), gauss, m = 30; the
+    nugget 1e-6 is LinearAlgebra::set_num_nugget(1e-6) (the jitter of every conditional block)."""
+    rng = np.random.default_rng(seed)
+    X = rng.uniform(size=(n, d))
+    y = np.sin(2 * np.pi * X).sum(axis=1) + 0.01 * rng.standard_normal(n)
+    return X, y
+
+
+def run_gpu_vecchia(args):
+    import libkriging_gb300 as lk
+    lib = lk.load()
+    n = args.n if args.n != 16384 else (1 << 20)
+    X, y = make_vecchia_inputs(n)
+    lk.set_num_nugget(1e-6)
+    k = lk.Kriging("gauss")
+    k.set_vecchia_exact_commit(False)
+    t0 = time.perf_counter()
+    k.fit(y, X, "constant", False, "BFGS", "LLVecchia(30)", {"theta": np.full((1, 3), 0.1)})
+    fit_s = time.perf_counter() - t0
+    th = k.theta()
+    for _ in range(args.warmup):
+        k.logLikelihoodVecchiaFun(th, True)
+    lib.lkg_stats_reset()
+    lib.lkg_stats_enable(1)
+    clocks = ClockSampler(0)
+    clocks.start()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        vll, g = k.logLikelihoodVecchiaFun(th, True)
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    lib.lkg_stats_enable(0)
+    stats = kernel_stats(lib)
+    pts = stats.get("k_vecchia_points", {"ms": wall * 1e3})
+    line = dict(metric="VLL(30)+grad evals/s at n=2^20, d=3 (gauss, num_nugget 1e-6)", value=args.steps / wall,
+                unit="evals/s", n_gpus=1, steps=args.steps, warmup=args.warmup, ms_per_step=1000 * wall / args.steps,
+                higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f64",
+                data="synthetic (seeded PCG64, seed 123)",
+                config=dict(workload="Vecchia LLVecchia(30), n=%d, d=3, gauss, light commit" % n),
+                fit_s_including_sets=fit_s, theta=th.tolist(), vll=vll, clocks=clk,
+                gpu_launches=int(sum(v["launches"] for v in stats.values())),
+                point_kernel_ms=pts["ms"] / max(1, args.steps),
+                kernels={kk: dict(launches=v["launches"], ms=round(v["ms"], 3)) for kk, v in stats.items()})
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        O.build()
+        order, nbr = k.vecchia_sets()
+        F = np.ones((n, 1), order="F")
+        Xf = np.asfortranarray(X)
+        th_c = np.ascontiguousarray(th)
+        cnt = 4096
+        t1 = time.perf_counter()
+        O.lib().ora_vecchia_points_sample(O.KERNELS["gauss"], n, 3, 1, O._dp(Xf), O._dp(np.ascontiguousarray(y)),
+                                          O._dp(F), O._dp(th_c), O._ip(order), O._ip(np.ascontiguousarray(nbr)),
+                                          nbr.shape[1], 1e-6, 0, cnt)
+        s = (time.perf_counter() - t1) * n / cnt
+        line["cpu_baseline"] = dict(value=1.0 / s, unit="evals/s", cores=1, kind="port",
+                                    sample="serial per-point loop of _logLikelihoodVecchia with gradient on the "
+                                           "first %d of %d ordered points, scaled by n" % (cnt, n))
+    print(json.dumps(line), flush=True)
 
 
 def main():
@@ -283,9 +435,16 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=16384)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--slices", type=int, default=7, help="digit slices of the mixed path (4..8)")
+    ap.add_argument("--workload", default="dense", choices=["dense", "multistart", "vecchia"])
+    ap.add_argument("--mixed", action="store_true", help="multistart workload on the mixed path")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "multistart":
+        run_gpu_multistart(args)
+    elif args.workload == "vecchia":
+        run_gpu_vecchia(args)
     else:
         run_gpu(args)
 

@@ -75,6 +75,60 @@ __device__ __forceinline__ double dlncov_term(double dx, double th) {
   }
 }
 
+// Fast forms (no per-dimension division or log1p): with c_k = s / theta_k (s = 1, sqrt(3), sqrt(5)) and
+// t_k = c_k |dx_k|,
+//   gauss     exp(-0.5 sum (dx_k / theta_k)^2)
+//   exp       exp(-sum t_k)
+//   matern3_2 prod (1 + t_k) exp(-sum t_k)              = exp(-sum (t_k - log1p t_k))
+//   matern5_2 prod (1 + t_k + t_k^2 / 3) exp(-sum t_k)  = exp(-sum (t_k - log1p(t_k + t_k^2 / 3)))
+// Equal to the reference forms up to a few ulps; used where the reference's rounding is not the contract (the
+// gradient sums and the mixed-precision covariance build).
+template <int K>
+__device__ __forceinline__ double cov_scale() {
+  if constexpr (K == KMATERN32) return sqrt(3.0);
+  else if constexpr (K == KMATERN52) return sqrt(5.0);
+  else return 1.0;
+}
+
+// accumulate one dimension: sum_state (the exponent argument) and prod_state (the polynomial product)
+template <int K>
+__device__ __forceinline__ void cov_fast_term(double dx, double ck, double& sum_state, double& prod_state) {
+  if constexpr (K == KGAUSS) {
+    const double v = dx * ck;
+    sum_state = fma(v, v, sum_state);
+  } else {
+    const double t = fabs(dx) * ck;
+    sum_state += t;
+    if constexpr (K == KMATERN32) prod_state *= (1.0 + t);
+    if constexpr (K == KMATERN52) prod_state *= fma(t, t * (1.0 / 3.0), 1.0 + t);
+  }
+}
+
+template <int K>
+__device__ __forceinline__ double cov_fast_finish(double sum_state, double prod_state) {
+  if constexpr (K == KGAUSS) return exp(-0.5 * sum_state);
+  else if constexpr (K == KEXP) return exp(-sum_state);
+  else return prod_state * exp(-sum_state);
+}
+
+// dlnC/dtheta_k with inv = 1 / theta_k and ck = s / theta_k
+template <int K>
+__device__ __forceinline__ double dlncov_fast(double dx, double inv, double ck) {
+  if constexpr (K == KGAUSS) {
+    const double v = dx * inv;
+    return v * v * inv;
+  } else if constexpr (K == KEXP) {
+    return fabs(dx) * inv * inv;
+  } else if constexpr (K == KMATERN32) {
+    const double t = fabs(dx) * ck;
+    return (t * t) / (1.0 + t) * inv;
+  } else {
+    const double t = fabs(dx) * ck;
+    const double a = 1.0 + t, b = t * t * (1.0 / 3.0);
+    return (a * b) / (a + b) * inv;
+  }
+}
+
 // dispatch a runtime kernel id to a template functor call
 template <typename F>
 inline void dispatch_kernel(int k, F&& f) {

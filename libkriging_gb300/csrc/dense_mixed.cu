@@ -47,8 +47,8 @@ void trtri_blocked_mixed(const double* L, int64_t lda, int64_t mstride, int n, c
   const int64_t dstride = (int64_t)nblk * NB * NB;
   for (int b = 0; b < batch; ++b)
     LKG_CUDA(cudaMemset2DAsync(W + b * wstride, ldw * sizeof(double), 0, n * sizeof(double), n, st));
-  SplitBuf SL = make_split(ws.panel, ws.panel_exp, ws.slices, ws.n, NB);
-  SplitBuf SR = make_split(ws.rowblk, ws.rowblk_exp, ws.slices, ws.n, NB);
+  SplitBuf SL = make_split(ws.panel, ws.panel_exp, ws.slices_inv, ws.n, NB);
+  SplitBuf SR = make_split(ws.rowblk, ws.rowblk_exp, ws.slices_inv, ws.n, NB);
   for (int k = 0; k < nblk; ++k) {
     const int k0 = k * NB, nb = std::min(NB, n - k0);
     copy_dinv_block(Dinv, dstride, k, W, ldw, wstride, k0, nb, batch, st);
@@ -70,7 +70,7 @@ void trtri_blocked_mixed(const double* L, int64_t lda, int64_t mstride, int n, c
 
 void wtw_lower_mixed(const double* W, int64_t ldw, int64_t wstride, int n, double* C, int64_t ldc, int64_t cstride,
                      int batch, const MixedWorkspace& ws, cudaStream_t st) {
-  SplitBuf SW = make_split(ws.wfull, ws.wfull_exp, ws.slices, ws.n, ws.n);
+  SplitBuf SW = make_split(ws.wfull, ws.wfull_exp, ws.slices_inv, ws.n, ws.n);
   // rows of the split = columns of W, k = rows of W
   ozaki_split(n, n, W, ldw, 1, wstride, batch, SW, st);
   ozaki_wtw(n, SW, C, ldc, cstride, batch, st);

@@ -1,5 +1,5 @@
 // diag.cu -- device diagnostics exported through the C ABI: device name and the FP64 FMA throughput probe that
-// serves as the roofline denominator of the FP64 kernels (MEASURED peaks of this machine cover HBM and bf16 only).
+// serves as the roofline denominator of the FP64 kernels (the published HBM and bf16 peaks do not cover the FP64 pipe).
 #include <string>
 
 #include "../../include/libkriging_gb300.h"

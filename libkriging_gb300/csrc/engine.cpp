@@ -326,6 +326,7 @@ void Engine::evaluate(int batch, const double* thetas, const double* factors, bo
   if (slices_ > 0) {
     ensure_mixed_buffers(with_grad);
     mw.slices = slices_;
+    mw.slices_inv = std::max(4, slices_ - 1);  // L^-1 and R^-1 feed only the gradient (tolerance 1e-6)
     mw.n = n;
     mw.panel = dpanel_;
     mw.panel_exp = dpanel_exp_;
@@ -338,7 +339,8 @@ void Engine::evaluate(int batch, const double* thetas, const double* factors, bo
   bool w_valid = false;  // W = L^-1 of the accepted factor is already in dW_
   for (int attempt = 0;; ++attempt) {
     LKG_CUDA(cudaMemcpyAsync(ddiag_, diag.data(), sizeof(double) * batch, cudaMemcpyHostToDevice, st_));
-    cov_build_lower(kernel_, n, d, dX_, 0, dtheta_, dfactor_, ddiag_, dA_, lda_, mstride_, batch, st_);
+    cov_build_lower(kernel_, n, d, dX_, 0, dtheta_, dfactor_, ddiag_, dA_, lda_, mstride_, batch, st_,
+                    slices_ > 0 && !retreated);
     if (slices_ > 0 && !retreated) {
       potrf_blocked_mixed(dA_, lda_, mstride_, n, dDinv_, dinfo_, batch, mw, st_);
       LKG_CUDA(cudaMemcpyAsync(info.data(), dinfo_, sizeof(int) * batch, cudaMemcpyDeviceToHost, st_));

@@ -37,7 +37,7 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
   return s;
 }
 
-template <int K, int DM>
+template <int K, int DM, bool FAST>
 __global__ void __launch_bounds__(256) k_cov_lower(int n, int d, const double* __restrict__ X, int64_t xb,
                                                    const double* __restrict__ theta, const double* __restrict__ factor,
                                                    const double* __restrict__ diag, double* __restrict__ A,
@@ -59,15 +59,24 @@ __global__ void __launch_bounds__(256) k_cov_lower(int n, int d, const double* _
   const int ri = t & 63, i = r0 + ri;
   if (i >= n) return;
   double* Ab = A + b * mstride;
-  double xr[DM];
+  double xr[DM], ck[DM];
 #pragma unroll
-  for (int k = 0; k < DM; ++k) xr[k] = xi[k][ri];
+  for (int k = 0; k < DM; ++k) {
+    xr[k] = xi[k][ri];
+    ck[k] = FAST ? cov_scale<K>() / th[k] : 0.0;
+  }
   for (int s = 0; s < 16; ++s) {
     const int cj = (t >> 6) + 4 * s, j = c0 + cj;
     if (j >= n || j > i) continue;
     double v;
     if (j == i) {
       v = dv;
+    } else if (FAST) {
+      double sum = 0.0, prod = 1.0;
+#pragma unroll
+      for (int k = 0; k < DM; ++k)
+        if (k < d) cov_fast_term<K>(xj[k][cj] - xr[k], ck[k], sum, prod);
+      v = cov_fast_finish<K>(sum, prod) * f;
     } else {
       double sum = 0.0;
 #pragma unroll
@@ -144,9 +153,14 @@ __global__ void __launch_bounds__(256) k_adjoint(int n, int d, const double* __r
   const int ri = t & 63, i = r0 + ri;
   const double* Rb = Rinv + b * rstride;
   if (i < n) {
-    double xr[DM];
+    // the gradient sums use the division- and log1p-free forms of the kernel and of dlnC/dtheta (common.cuh)
+    double xr[DM], inv[DM], ck[DM];
 #pragma unroll
-    for (int k = 0; k < DM; ++k) xr[k] = xi[k][ri];
+    for (int k = 0; k < DM; ++k) {
+      xr[k] = xi[k][ri];
+      inv[k] = 1.0 / th[k];
+      ck[k] = cov_scale<K>() * inv[k];
+    }
     const double x_i = vi[ri];
     for (int s = 0; s < 16; ++s) {
       const int cj = (t >> 6) + 4 * s, j = c0 + cj;
@@ -158,13 +172,13 @@ __global__ void __launch_bounds__(256) k_adjoint(int n, int d, const double* __r
         continue;
       }
       double dxk[DM];
-      double sum = 0.0;
+      double sum = 0.0, prod = 1.0;
 #pragma unroll
       for (int k = 0; k < DM; ++k) {
         dxk[k] = xj[k][cj] - xr[k];
-        if (k < d) sum += cov_term<K>(dxk[k], th[k]);
+        if (k < d) cov_fast_term<K>(dxk[k], ck[k], sum, prod);
       }
-      const double c = cov_from_sum<K>(sum);
+      const double c = cov_fast_finish<K>(sum, prod);
       const double rij = c * f;
       const double wx = x_i * vj[cj];
       u1 += wx * c;
@@ -172,7 +186,7 @@ __global__ void __launch_bounds__(256) k_adjoint(int n, int d, const double* __r
 #pragma unroll
       for (int k = 0; k < DM; ++k) {
         if (k < d) {
-          const double g = rij * dlncov_term<K>(dxk[k], th[k]);
+          const double g = rij * dlncov_fast<K>(dxk[k], inv[k], ck[k]);
           t1[k] += wx * g;
           t2[k] += rinv * g;
         }
@@ -343,12 +357,16 @@ void dispatch_kd(int kernel, int d, Args&&... args) {
 template <int K, int DM>
 struct CovLowerLaunch {
   static void run(int n, int d, const double* X, int64_t xb, const double* theta, const double* factor,
-                  const double* diag, double* A, int64_t lda, int64_t mstride, int batch, cudaStream_t st) {
+                  const double* diag, double* A, int64_t lda, int64_t mstride, int batch, bool fast, cudaStream_t st) {
     const int nb = ceil_div(n, T);
     const int64_t ntiles = (int64_t)nb * (nb + 1) / 2;
     LaunchTimer lt("k_cov_lower", st, 0.5 * n * (n - 1.0) * batch, 4.0 * n * (n + 1.0) * batch);
-    k_cov_lower<K, DM><<<dim3((unsigned)ntiles, 1, batch), 256, 0, st>>>(n, d, X, xb, theta, factor, diag, A, lda,
-                                                                          mstride);
+    if (fast)
+      k_cov_lower<K, DM, true><<<dim3((unsigned)ntiles, 1, batch), 256, 0, st>>>(n, d, X, xb, theta, factor, diag, A,
+                                                                                  lda, mstride);
+    else
+      k_cov_lower<K, DM, false><<<dim3((unsigned)ntiles, 1, batch), 256, 0, st>>>(n, d, X, xb, theta, factor, diag,
+                                                                                   A, lda, mstride);
     LKG_LAUNCH("k_cov_lower");
   }
 };
@@ -380,9 +398,9 @@ struct AdjointLaunch {
 
 void cov_build_lower(int kernel, int n, int d, const double* X, int64_t x_bstride, const double* theta,
                      const double* factor, const double* diag, double* A, int64_t lda, int64_t mstride, int batch,
-                     cudaStream_t st) {
+                     cudaStream_t st, bool fast) {
   if (n <= 0) return;
-  dispatch_kd<CovLowerLaunch>(kernel, d, n, d, X, x_bstride, theta, factor, diag, A, lda, mstride, batch, st);
+  dispatch_kd<CovLowerLaunch>(kernel, d, n, d, X, x_bstride, theta, factor, diag, A, lda, mstride, batch, fast, st);
 }
 
 void cov_cross(int kernel, int n_o, int q, int d, const double* Xo, const double* Xn, const double* theta,

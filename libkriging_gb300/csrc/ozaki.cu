@@ -7,7 +7,6 @@ namespace lkg {
 
 namespace {
 
-constexpr int OZ_PAD = 72;  // smem row stride (bf16): 144 B rows keep the 32-bit fragment loads conflict-free
 
 __global__ void k_oz_split(int rows, int K, const double* __restrict__ p, int64_t s_r, int64_t s_k, int64_t bstride,
                            SplitBuf out) {
@@ -69,15 +68,16 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4], 
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-// exact (v * 2^E) as a double for an integer-valued float v (|v| < 2^24), by exponent arithmetic on the bits
-__device__ __forceinline__ double scaled_to_double(float v, int E) {
-  const unsigned u = __float_as_uint(v);
-  if ((u & 0x7fffffffu) == 0u) return 0.0;
-  const int fld = (int)((u >> 23) & 0xffu) + 896 + E;  // 1023 - 127 = 896
-  if (fld <= 0 || fld >= 2047) return ldexp((double)v, E);
-  const unsigned hi = (u & 0x80000000u) | ((unsigned)fld << 20) | ((u & 0x7fffffu) >> 3);
-  const unsigned lo = (u & 0x7u) << 29;
-  return __hiloint2double((int)hi, (int)lo);
+// exact (h * 2^E) as a double for |h| < 2^53, by building the IEEE bits
+__device__ __forceinline__ double ll_scaled_to_double(long long h, int E) {
+  if (h == 0) return 0.0;
+  const unsigned long long sgn = (h < 0) ? 0x8000000000000000ull : 0ull;
+  const unsigned long long a = (unsigned long long)(h < 0 ? -h : h);
+  const int lz = __clzll((long long)a);
+  const int fld = (63 - lz) + 1023 + E;
+  if (fld <= 0 || fld >= 2047) return ldexp((double)h, E);
+  const unsigned long long mant = ((a << lz) << 1) >> 12;  // drop the leading one, keep 52 fraction bits
+  return __longlong_as_double((long long)(sgn | ((unsigned long long)fld << 52) | mant));
 }
 
 struct OzArgs {
@@ -93,11 +93,13 @@ struct OzArgs {
 
 template <int S>
 __global__ void __launch_bounds__(128) k_oz_gemm(OzArgs g) {
+  // [S][64 rows][64 k] bf16 per operand; the 16-byte chunk c of row r is stored at chunk c ^ (r & 7), so the
+  // eight row addresses of every ldmatrix phase and of the cp.async stores hit distinct bank groups
   extern __shared__ __align__(16) unsigned char oz_smem[];
-  __nv_bfloat16* sA = reinterpret_cast<__nv_bfloat16*>(oz_smem);       // [S][64][OZ_PAD]
-  __nv_bfloat16* sB = sA + (size_t)S * 64 * OZ_PAD;                     // [S][64][OZ_PAD]
-  int* sea = reinterpret_cast<int*>(sB + (size_t)S * 64 * OZ_PAD);       // [64]
-  int* seb = sea + 64;                                                   // [64]
+  __nv_bfloat16* sA = reinterpret_cast<__nv_bfloat16*>(oz_smem);
+  __nv_bfloat16* sB = sA + (size_t)S * 64 * 64;
+  int* sea = reinterpret_cast<int*>(sB + (size_t)S * 64 * 64);  // [64]
+  int* seb = sea + 64;                                          // [64]
   int m0, n0, c0 = g.c0, arow, brow;
   bool diag_tile;
   if (g.wtw_n > 0) {
@@ -143,8 +145,8 @@ __global__ void __launch_bounds__(128) k_oz_gemm(OzArgs g) {
       const int i = idx / 512, rem = idx % 512, row = rem >> 3, seg = rem & 7;
       const __nv_bfloat16* ga = pa + (((int64_t)i * g.SA.nchunk + c) * g.SA.rows_pad + arow + row) * OZ_CHUNK + seg * 8;
       const __nv_bfloat16* gb = pb + (((int64_t)i * g.SB.nchunk + c) * g.SB.rows_pad + brow + row) * OZ_CHUNK + seg * 8;
-      cp_async16(sA + ((size_t)i * 64 + row) * OZ_PAD + seg * 8, ga);
-      cp_async16(sB + ((size_t)i * 64 + row) * OZ_PAD + seg * 8, gb);
+      cp_async16(sA + ((size_t)i * 64 + row) * 64 + ((seg ^ (row & 7)) * 8), ga);
+      cp_async16(sB + ((size_t)i * 64 + row) * 64 + ((seg ^ (row & 7)) * 8), gb);
     }
     if (t < 64) {
       sea[t] = ea[(int64_t)c * g.SA.rows_pad + arow + t];
@@ -163,7 +165,11 @@ __global__ void __launch_bounds__(128) k_oz_gemm(OzArgs g) {
       ec[nb][0] = seb[wn * 32 + nb * 8 + 2 * tig];
       ec[nb][1] = seb[wn * 32 + nb * 8 + 2 * tig + 1];
     }
-    // ---- diagonals t = i + j of the digit products ----
+    // ---- diagonals dg = i + j of the digit products ----
+    // Each diagonal's FP32 sum is an exact integer below 2^23; diagonals are chained in int64 by Horner in base
+    // 256 over groups [2..5] and [6..S+1] (below 2^48, exact as a double) and each group is folded into the FP64
+    // accumulator with one add: 2 FP64 operations per element per chunk instead of S.
+    long long hacc[2][4][4];
 #pragma unroll 1
     for (int dg = 2; dg <= S + 1; ++dg) {
       float acc[2][4][4];
@@ -177,22 +183,23 @@ __global__ void __launch_bounds__(128) k_oz_gemm(OzArgs g) {
 #pragma unroll 1
       for (int i = ilo; i <= ihi; ++i) {
         const int j = dg - i;
-        const __nv_bfloat16* A = sA + (size_t)(i - 1) * 64 * OZ_PAD;
-        const __nv_bfloat16* B = sB + (size_t)(j - 1) * 64 * OZ_PAD;
+        const __nv_bfloat16* A = sA + (size_t)(i - 1) * 64 * 64;
+        const __nv_bfloat16* B = sB + (size_t)(j - 1) * 64 * 64;
 #pragma unroll
         for (int kk = 0; kk < 64; kk += 16) {
           unsigned af[2][4], bf[4][2];
 #pragma unroll
           for (int mb = 0; mb < 2; ++mb) {
             const int row = wm * 32 + mb * 16 + (lane & 7) + ((lane >> 3) & 1) * 8;
-            const int col = kk + ((lane >> 4) & 1) * 8;
-            ldsm_x4(af[mb][0], af[mb][1], af[mb][2], af[mb][3], A + (size_t)row * OZ_PAD + col);
+            const int chunk = (kk >> 3) + ((lane >> 4) & 1);
+            ldsm_x4(af[mb][0], af[mb][1], af[mb][2], af[mb][3], A + (size_t)row * 64 + ((chunk ^ (row & 7)) * 8));
           }
 #pragma unroll
           for (int nb = 0; nb < 4; nb += 2) {
             const int row = wn * 32 + nb * 8 + (lane & 7) + ((lane >> 4) & 1) * 8;
-            const int col = kk + ((lane >> 3) & 1) * 8;
-            ldsm_x4(bf[nb][0], bf[nb][1], bf[nb + 1][0], bf[nb + 1][1], B + (size_t)row * OZ_PAD + col);
+            const int chunk = (kk >> 3) + ((lane >> 3) & 1);
+            ldsm_x4(bf[nb][0], bf[nb][1], bf[nb + 1][0], bf[nb + 1][1],
+                    B + (size_t)row * 64 + ((chunk ^ (row & 7)) * 8));
           }
 #pragma unroll
           for (int mb = 0; mb < 2; ++mb)
@@ -200,14 +207,19 @@ __global__ void __launch_bounds__(128) k_oz_gemm(OzArgs g) {
             for (int nb = 0; nb < 4; ++nb) mma_bf16(acc[mb][nb], af[mb], bf[nb][0], bf[nb][1]);
         }
       }
-      // fold this diagonal into the FP64 accumulator: value * 2^(ea + eb - 8 dg), exact conversion
+      const bool gstart = (dg == 2) || (dg == 6);
+      const bool gend = (dg == 5) || (dg == S + 1);
 #pragma unroll
       for (int mb = 0; mb < 2; ++mb)
 #pragma unroll
         for (int nb = 0; nb < 4; ++nb)
 #pragma unroll
-          for (int q = 0; q < 4; ++q)
-            acc64[mb][nb][q] += scaled_to_double(acc[mb][nb][q], er[mb][q >> 1] + ec[nb][q & 1] - 8 * dg);
+          for (int q = 0; q < 4; ++q) {
+            const long long v = (long long)__float2int_rn(acc[mb][nb][q]);
+            hacc[mb][nb][q] = gstart ? v : hacc[mb][nb][q] * 256 + v;
+            if (gend)
+              acc64[mb][nb][q] += ll_scaled_to_double(hacc[mb][nb][q], er[mb][q >> 1] + ec[nb][q & 1] - 8 * dg);
+          }
     }
     __syncthreads();
   }
@@ -232,7 +244,7 @@ __global__ void __launch_bounds__(128) k_oz_gemm(OzArgs g) {
 
 template <int S>
 void launch_oz(const OzArgs& a, dim3 grid, cudaStream_t st) {
-  const size_t smem = (size_t)2 * S * 64 * OZ_PAD * sizeof(__nv_bfloat16) + 128 * sizeof(int);
+  const size_t smem = (size_t)2 * S * 64 * 64 * sizeof(__nv_bfloat16) + 128 * sizeof(int);
   static bool attr = false;
   if (!attr) {
     LKG_CUDA(cudaFuncSetAttribute(k_oz_gemm<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -283,7 +295,9 @@ void ozaki_gemm(int M, int N, int c0, int c1, double alpha, const SplitBuf& SA, 
   dim3 grid(ceil_div(M, 64), ceil_div(N, 64), batch);
   const double K = (double)(c1 - c0) * OZ_CHUNK;
   const double fl = (lower_only && M == N) ? K * M * (M + 1.0) : 2.0 * M * N * K;
-  LaunchTimer lt("k_oz_gemm", st, fl * batch, 8.0 * ((beta == 0.0) ? 1.0 : 2.0) * M * N * batch);
+  // flops recorded = the bf16 tensor work executed: S (S + 1) / 2 digit GEMMs of the FP64-equivalent product
+  LaunchTimer lt("k_oz_gemm", st, fl * batch * SA.S * (SA.S + 1) / 2.0,
+                 8.0 * ((beta == 0.0) ? 1.0 : 2.0) * M * N * batch);
   dispatch_oz(SA.S, a, grid, st);
 }
 
@@ -291,7 +305,8 @@ void ozaki_wtw(int n, const SplitBuf& SW, double* C, int64_t ldc, int64_t cstrid
   const int nblk = ceil_div(n, 64);
   const int64_t ntiles = (int64_t)nblk * (nblk + 1) / 2;
   OzArgs a{n, n, 0, SW.nchunk, 1.0, 0.0, SW, SW, 0, 0, C, ldc, cstride, false, n};
-  LaunchTimer lt("k_oz_wtw", st, (double)n * (n + 1.0) * (n + 2.0) / 3.0 * batch, 8.0 * n * (n + 1.0) * batch);
+  LaunchTimer lt("k_oz_wtw", st, (double)n * (n + 1.0) * (n + 2.0) / 3.0 * batch * SW.S * (SW.S + 1) / 2.0,
+                 8.0 * n * (n + 1.0) * batch);
   dispatch_oz(SW.S, a, dim3((unsigned)ntiles, 1, batch), st);
 }
 

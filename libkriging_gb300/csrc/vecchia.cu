@@ -334,11 +334,13 @@ __global__ void k_vsum2(int n, int p, int d, const double* __restrict__ u, const
   }
 }
 
-__global__ void k_vsum_final(int nblocks, int P, const double* __restrict__ part, double* __restrict__ out) {
+// out[e] = sum over blocks of part[b * stride + e], e < count (fixed order)
+__global__ void k_vsum_final(int nblocks, int stride, int count, const double* __restrict__ part,
+                             double* __restrict__ out) {
   __shared__ double red[8];
-  for (int e = 0; e < P; ++e) {
+  for (int e = 0; e < count; ++e) {
     double s = 0.0;
-    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += part[(int64_t)b * P + e];
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += part[(int64_t)b * stride + e];
     s = bsum<256>(s, red);
     if (threadIdx.x == 0) out[e] = s;
   }
@@ -488,7 +490,7 @@ VecchiaOut VecchiaEngine::evaluate(const double* theta, bool with_grad, bool est
     LaunchTimer lt("k_vsum1", st_, 0.0, 8.0 * n * (2.0 + p));
     k_vsum1<<<nblk_red_, 256, 0, st_>>>(n, p, du_, dv_, dW_, dpart_);
     LKG_LAUNCH("k_vsum1");
-    k_vsum_final<<<1, 256, 0, st_>>>(nblk_red_, P1, dpart_, fin);
+    k_vsum_final<<<1, 256, 0, st_>>>(nblk_red_, P1, P1, dpart_, fin);
     LKG_LAUNCH("k_vsum_final");
   }
   std::vector<double> s1(P1);
@@ -522,7 +524,7 @@ VecchiaOut VecchiaEngine::evaluate(const double* theta, bool with_grad, bool est
     LaunchTimer lt("k_vsum2", st_, 0.0, 8.0 * n * (2.0 + p) * (with_grad ? 1.0 + d : 1.0));
     k_vsum2<<<nblk_red_, 256, 0, st_>>>(n, p, d, du_, dv_, dW_, ddu_, ddv_, ddW_, dbeta_, with_grad ? 1 : 0, dpart_);
     LKG_LAUNCH("k_vsum2");
-    k_vsum_final<<<1, 256, 0, st_>>>(nblk_red_, with_grad ? P2 : 1, dpart_, fin);
+    k_vsum_final<<<1, 256, 0, st_>>>(nblk_red_, P2, with_grad ? P2 : 1, dpart_, fin);
     LKG_LAUNCH("k_vsum_final");
   }
   std::vector<double> s2(P2, 0.0);

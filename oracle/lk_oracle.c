@@ -1,7 +1,7 @@
 /*
  * lk_oracle.c -- CPU FP64 restatement of libKriging's likelihood hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker: the GPU product never links, loads or calls it.
+ * TEST INFRASTRUCTURE ONLY.  The GPU results are compared with it; the GPU product never links, loads or calls it.
  * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it.
  *
  * Each function restates one reference routine (paths relative to the libKriging source tree) in the same
@@ -232,8 +232,95 @@ static void chol_solve(int m, const double* L, const double* r, double* a) {
   }
 }
 
-/* safe_chol_lower_retry (LinearAlgebra.cpp:68-98) restricted to the plain failure test: on failure add
- * num_nugget*10^k to the diagonal of a copy, k = 0..max_inc.  Returns number of increments or -1. */
+/* x <- L^-1 x (kind 1) or L^-T x (kind 2) for lower-triangular L (m x m column-major) */
+static void tri_apply_inv(int m, const double* L, double* x, int kind) {
+  if (kind == 1) {
+    for (int i = 0; i < m; i++) {
+      double s = x[i];
+      for (int k = 0; k < i; k++) s -= L[i + k * m] * x[k];
+      x[i] = s / L[i + i * m];
+    }
+  } else {
+    for (int i = m - 1; i >= 0; i--) {
+      double s = x[i];
+      for (int k = i + 1; k < m; k++) s -= L[k + i * m] * x[k];
+      x[i] = s / L[i + i * m];
+    }
+  }
+}
+
+/* rcond(L)^2 as LinearAlgebra::rcond_chol computes it (LinearAlgebra.cpp:106-115): LAPACK dtrcon('1', 'L', 'N'),
+ * i.e. 1 / (|L|_1 * est(|L^-1|_1)) with the dlacn2 estimator (Hager / Higham). */
+static double rcond2_small(int m, const double* L) {
+  double anorm = 0.0;
+  for (int j = 0; j < m; j++) {
+    double s = 0.0;
+    for (int i = j; i < m; i++) s += fabs(L[i + j * m]);
+    if (s > anorm) anorm = s;
+  }
+  if (!(anorm > 0.0)) return 0.0;
+  double x[128], xi[128], est;
+  for (int i = 0; i < m; i++) x[i] = 1.0 / m;
+  tri_apply_inv(m, L, x, 1);
+  if (m == 1) {
+    est = fabs(x[0]);
+  } else {
+    est = 0.0;
+    for (int i = 0; i < m; i++) est += fabs(x[i]);
+    for (int i = 0; i < m; i++) xi[i] = (x[i] >= 0.0) ? 1.0 : -1.0;
+    for (int i = 0; i < m; i++) x[i] = xi[i];
+    tri_apply_inv(m, L, x, 2);
+    int j = 0;
+    for (int i = 1; i < m; i++)
+      if (fabs(x[i]) > fabs(x[j])) j = i;
+    int iter = 2;
+    for (;;) {
+      for (int i = 0; i < m; i++) x[i] = (i == j) ? 1.0 : 0.0;
+      tri_apply_inv(m, L, x, 1);
+      double estold = est;
+      est = 0.0;
+      for (int i = 0; i < m; i++) est += fabs(x[i]);
+      int same = 1;
+      for (int i = 0; i < m; i++)
+        if (((x[i] >= 0.0) ? 1.0 : -1.0) != xi[i]) same = 0;
+      if (same || est <= estold) break;
+      for (int i = 0; i < m; i++) xi[i] = (x[i] >= 0.0) ? 1.0 : -1.0;
+      for (int i = 0; i < m; i++) x[i] = xi[i];
+      tri_apply_inv(m, L, x, 2);
+      int jlast = j;
+      j = 0;
+      for (int i = 1; i < m; i++)
+        if (fabs(x[i]) > fabs(x[j])) j = i;
+      if (x[jlast] != fabs(x[j]) && iter < 5) {
+        iter++;
+        continue;
+      }
+      break;
+    }
+    double altsgn = 1.0;
+    for (int i = 0; i < m; i++) {
+      x[i] = altsgn * (1.0 + (double)i / (double)(m - 1));
+      altsgn = -altsgn;
+    }
+    tri_apply_inv(m, L, x, 1);
+    double temp = 0.0;
+    for (int i = 0; i < m; i++) temp += fabs(x[i]);
+    temp = 2.0 * temp / (3.0 * m);
+    if (temp > est) est = temp;
+  }
+  double rc = (1.0 / anorm) / est;
+  return rc * rc;
+}
+
+static int g_rcond_check = 1;
+static double g_min_rcond = 1e-18;
+void ora_set_rcond_check(int check, double min_rcond) {
+  g_rcond_check = check;
+  g_min_rcond = min_rcond;
+}
+
+/* safe_chol_lower_retry (LinearAlgebra.cpp:68-98): on failure, or rcond(L)^2 < min_rcond when the check is on,
+ * add num_nugget*10^k to the diagonal of a copy (cumulatively), k = 0..max_inc.  Returns increments or -1. */
 static int safe_chol_small(int m, const double* A, double* L, double num_nugget, int max_inc) {
   double* W = L;
   memcpy(W, A, sizeof(double) * m * m);
@@ -241,7 +328,7 @@ static int safe_chol_small(int m, const double* A, double* L, double num_nugget,
   memcpy(base, A, sizeof(double) * m * m);
   for (int inc = 0;; inc++) {
     memcpy(W, base, sizeof(double) * m * m);
-    if (chol_lower(m, W) == 0) {
+    if (chol_lower(m, W) == 0 && !(g_rcond_check && rcond2_small(m, W) < g_min_rcond)) {
       free(base);
       return inc;
     }
@@ -343,6 +430,72 @@ void ora_vecchia_sets(int n, int d, const double* X, int m_max, int32_t* order, 
   free(Xt);
   free(mind2);
   free(centroid);
+}
+
+/*
+ * Timed sample of the per-point loop of _logLikelihoodVecchia (Kriging.cpp:829-889) with gradient: ordered points
+ * [t0, t1) only, results discarded (the CPU baseline scales the time by n / (t1 - t0)).  Returns the number of
+ * points whose conditional block needed numerical-nugget increments.
+ */
+int ora_vecchia_points_sample(int kernel, int n, int d, int p, const double* X, const double* y, const double* F,
+                              const double* theta, const int32_t* order, const int32_t* nbr, int m_max,
+                              double num_nugget, int t0, int t1) {
+  int M = m_max, bumped = 0;
+  double* RN = (double*)malloc(sizeof(double) * M * M);
+  double* LN = (double*)malloc(sizeof(double) * M * M);
+  double* dRN = (double*)malloc(sizeof(double) * (size_t)M * M * d);
+  double* dr = (double*)malloc(sizeof(double) * M * d);
+  double r[128], a_vec[128], rhs[128], da[128], dx[64], dln[64];
+  volatile double sink = 0.0;
+  for (int t = t0; t < t1; t++) {
+    int oi = order[t];
+    int mi = 0;
+    while (mi < M && nbr[(size_t)t * M + mi] >= 0) mi++;
+    const int32_t* Ni = nbr + (size_t)t * M;
+    if (mi == 0) continue;
+    for (int q = 0; q < mi * mi; q++) RN[q] = 1.0;
+    memset(dRN, 0, sizeof(double) * mi * mi * d);
+    for (int a = 0; a < mi; a++) {
+      for (int b = a + 1; b < mi; b++) {
+        for (int k = 0; k < d; k++) dx[k] = X[Ni[a] + (size_t)k * n] - X[Ni[b] + (size_t)k * n];
+        double c = ora_cov(kernel, dx, theta, d);
+        RN[a + b * mi] = RN[b + a * mi] = c;
+        ora_dlncov(kernel, dx, theta, d, dln);
+        for (int k = 0; k < d; k++) dRN[a + b * mi + k * mi * mi] = dRN[b + a * mi + k * mi * mi] = c * dln[k];
+      }
+      for (int k = 0; k < d; k++) dx[k] = X[Ni[a] + (size_t)k * n] - X[oi + (size_t)k * n];
+      double c = ora_cov(kernel, dx, theta, d);
+      r[a] = c;
+      ora_dlncov(kernel, dx, theta, d, dln);
+      for (int k = 0; k < d; k++) dr[a + k * mi] = c * dln[k];
+    }
+    for (int a = 0; a < mi; a++) RN[a + a * mi] += num_nugget;
+    int inc = safe_chol_small(mi, RN, LN, num_nugget, 10);
+    if (inc < 0) continue;
+    bumped += inc > 0;
+    chol_solve(mi, LN, r, a_vec);
+    double ra = 0.0;
+    for (int a = 0; a < mi; a++) ra += r[a] * a_vec[a];
+    for (int k = 0; k < d; k++) {
+      for (int a = 0; a < mi; a++) {
+        double s = 0.0;
+        for (int b = 0; b < mi; b++) s += dRN[a + b * mi + k * mi * mi] * a_vec[b];
+        rhs[a] = dr[a + k * mi] - s;
+      }
+      chol_solve(mi, LN, rhs, da);
+      double s2 = 0.0;
+      for (int a = 0; a < mi; a++) s2 += r[a] * da[a] + da[a] * y[Ni[a]];
+      sink += s2;
+    }
+    sink += ra;
+    (void)F;
+    (void)p;
+  }
+  free(RN);
+  free(LN);
+  free(dRN);
+  free(dr);
+  return bumped;
 }
 
 /*

@@ -1,6 +1,6 @@
 """CPU FP64 oracle for the libKriging likelihood hot path.
 
-TEST INFRASTRUCTURE ONLY: this module is the checker for the GPU implementation.  Only the tests,
+TEST INFRASTRUCTURE ONLY: this module is the reference restatement the GPU results are compared with.  Only the tests,
 ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` import it; the product package never
 does.  It restates the reference's algorithm in the reference's operation order:
 
@@ -84,6 +84,12 @@ def lib():
         L.ora_alpha_terms.argtypes = [ctypes.c_int, dp, dp, dp, ctypes.c_double, ctypes.c_double, dp]
         L.ora_vecchia_sets.restype = None
         L.ora_vecchia_sets.argtypes = [ctypes.c_int, ctypes.c_int, dp, ctypes.c_int, ip, ip]
+        L.ora_set_rcond_check.restype = None
+        L.ora_set_rcond_check.argtypes = [ctypes.c_int, ctypes.c_double]
+        L.ora_vecchia_points_sample.restype = ctypes.c_int
+        L.ora_vecchia_points_sample.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp,
+                                                dp, ip, ip, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                                                ctypes.c_int]
         L.ora_vecchia_ll.restype = ctypes.c_double
         L.ora_vecchia_ll.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp, dp, ip, ip,
                                      ctypes.c_int, ctypes.c_double, dp, dp, dp]

@@ -1,4 +1,4 @@
-"""CPU tests of the oracle (the checker): pinned to the reference's known answers, plus the reference's own
+"""CPU tests of the oracle (the CPU restatement the GPU results are compared with): pinned to the reference's known answers, plus the reference's own
 finite-difference and identity checks (tests/KrigingLogLikTest.cpp, NuggetKrigingLogLikTest.cpp,
 KrigingVecchiaTest.cpp:46-84 of libKriging)."""
 import numpy as np
