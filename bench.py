@@ -218,6 +218,8 @@ def run_gpu(args):
         dist.init_process_group("nccl")
     import libkriging_gb300 as lk
     lib = lk.load()
+    if args.tensor_path is not None:
+        lib.lkg_set_tensor_path(args.tensor_path)
     peak_fp64 = ctypes.c_double()
     if lib.lkg_probe_fp64_peak(ctypes.byref(peak_fp64)) != 0:
         raise RuntimeError("FP64 peak probe failed: " + lk._lib.last_error())
@@ -263,7 +265,9 @@ def run_gpu(args):
     def roof(stats_, bound):
         name, s = max(stats_.items(), key=lambda kv: kv[1]["ms"])
         achieved = s["flops"] / (s["ms"] * 1e-3) / 1e12
-        if name.startswith("k_oz"):
+        if name.startswith("k_oz_tc"):
+            pk, unit, src = tensor_peak, "TFLOP/s", "MEASURED_PEAKS.json bf16_tflops (burst, cuBLAS tcgen05)"
+        elif name.startswith("k_oz"):
             pk, unit, src = tensor_peak, "TFLOP/s", ("MEASURED_PEAKS.json bf16_tflops (burst, cuBLAS tcgen05); this "
                                                     "kernel issues mma.sync, measured at 605 TFLOP/s on this part")
         else:
@@ -293,6 +297,7 @@ def run_gpu(args):
                             precision="mixed: O(n^3) products on bf16 tensor cores by error-free digit splitting "
                                       "(Cholesky %d digits, inverse %d), FP64 panels and reductions"
                                       % (used, max(4, used - 1)),
+                            digit_products="tcgen05" if lib.lkg_get_tensor_path() else "mma.sync",
                             parallelism="replicas" if world > 1 else "single GPU",
                             l2="inputs larger than L2 (R, L^-1, R^-1: 3 x %.2f GB)" % (8.0 * args.n * args.n / 1e9)),
                 e2e=dict(value=world / e2e_s, unit=UNIT, h2d_bytes_per_step=8 * gamma.size,
@@ -381,9 +386,15 @@ def run_gpu_vecchia(args):
     lk.set_num_nugget(1e-6)
     k = lk.Kriging("gauss")
     k.set_vecchia_exact_commit(False)
+    lib.lkg_stats_reset()
+    lib.lkg_stats_enable(1)
     t0 = time.perf_counter()
     k.fit(y, X, "constant", False, "BFGS", "LLVecchia(30)", {"theta": np.full((1, 3), 0.1)})
     fit_s = time.perf_counter() - t0
+    lib.lkg_stats_enable(0)
+    fit_stats = kernel_stats(lib)
+    print("vecchia: n=%d fit %.2f s; %s" % (n, fit_s, {kk: round(v["ms"], 1) for kk, v in fit_stats.items()}),
+          file=sys.stderr, flush=True)
     th = k.theta()
     for _ in range(args.warmup):
         k.logLikelihoodVecchiaFun(th, True)
@@ -405,6 +416,7 @@ def run_gpu_vecchia(args):
                 data="synthetic (seeded PCG64, seed 123)",
                 config=dict(workload="Vecchia LLVecchia(30), n=%d, d=3, gauss, light commit" % n),
                 fit_s_including_sets=fit_s, theta=th.tolist(), vll=vll, clocks=clk,
+                fit_kernels={kk: dict(launches=v["launches"], ms=round(v["ms"], 3)) for kk, v in fit_stats.items()},
                 gpu_launches=int(sum(v["launches"] for v in stats.values())),
                 point_kernel_ms=pts["ms"] / max(1, args.steps),
                 kernels={kk: dict(launches=v["launches"], ms=round(v["ms"], 3)) for kk, v in stats.items()})
@@ -427,6 +439,106 @@ def run_gpu_vecchia(args):
     print(json.dumps(line), flush=True)
 
 
+def make_nested_inputs(n_total=1_000_000, d=4, seed=123):
+    """NestedKriging workload: X ~ U[0,1]^4, y = sum_j sin(4 x_j) + N(0, 0.01) (variance 0.01), matern3_2.
+    The partition is synthesised: group sizes ~ lognormal(median 1000, sigma 0.67) truncated to [150, 2500] until
+    they cover n_total, and the points cut into consecutive runs of a 4-D Z-order (Morton) ordering, so that every
+    group is spatially compact."""
+    rng = np.random.default_rng(seed)
+    X = rng.uniform(size=(n_total, d))
+    y = np.sin(4 * X).sum(axis=1) + 0.1 * rng.standard_normal(n_total)
+    sizes = []
+    left = n_total
+    while left > 0:
+        s = int(np.clip(round(np.exp(np.log(1000.0) + 0.67 * rng.standard_normal())), 150, 2500))
+        if left - s < 150:
+            s = left if left <= 2500 else left - 150
+        sizes.append(s)
+        left -= s
+    q = np.minimum((X * 65536).astype(np.uint64), np.uint64(65535))
+    key = np.zeros(n_total, dtype=np.uint64)
+    for b in range(16):
+        for j in range(d):
+            key |= ((q[:, j] >> np.uint64(b)) & np.uint64(1)) << np.uint64(b * d + j)
+    order = np.argsort(key, kind="stable")
+    labels = np.empty(n_total, dtype=np.int32)
+    start = 0
+    for g, s in enumerate(sizes):
+        labels[order[start:start + s]] = g
+        start += s
+    return X, y, labels, np.array(sizes)
+
+
+def run_gpu_nested(args):
+    """One step = the submodel objective (concentrated LL + theta-gradient) of every group in one batched
+    evaluation; the complete NestedKriging fit (all submodel BFGS fits, common prior, refits) is timed once."""
+    import libkriging_gb300 as lk
+    lib = lk.load()
+    n_total = args.nested_n
+    X, y, labels, sizes = make_nested_inputs(n_total)
+    p, d = len(sizes), X.shape[1]
+    nk = lk.NestedKriging("matern3_2", aggregation="gPoE")
+    if args.mixed:
+        nk.set_precision(args.slices)
+    clocks = ClockSampler(0)
+    clocks.start()
+    t0 = time.perf_counter()
+    nk.fit_groups(y, X, labels, "constant", "BFGS", "LL")
+    fit_s = time.perf_counter() - t0
+    rng = np.random.default_rng(7)
+    thetas = rng.uniform(0.1, 0.6, size=(p, d))
+    for _ in range(args.warmup):
+        nk.logLikelihoodGroups(thetas, True)
+    lib.lkg_stats_reset()
+    lib.lkg_stats_enable(1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ll, g = nk.logLikelihoodGroups(thetas, True)
+    wall = time.perf_counter() - t0
+    lib.lkg_stats_enable(0)
+    stats = kernel_stats(lib)
+    Xp = np.random.default_rng(124).uniform(size=(args.nested_q, d))
+    t1 = time.perf_counter()
+    mean, sd = nk.predict(Xp, True)
+    pred_s = time.perf_counter() - t1
+    clk = clocks.stop()
+    n3 = float(np.sum(sizes.astype(np.float64) ** 3))
+    dom = max(stats.items(), key=lambda kv: kv[1]["ms"]) if stats else ("", {"ms": 0.0, "flops": 0.0})
+    line = dict(metric="NestedKriging submodel LL+grad evals/s (all groups batched), N=%d, d=4, matern3_2" % n_total,
+                value=p * args.steps / wall, unit="evals/s", n_gpus=1, steps=args.steps, warmup=args.warmup,
+                ms_per_step=1000 * wall / args.steps, higher_is_better=True, scaling="weak", vs_baseline=None,
+                dtype="f64", data="synthetic (seeded PCG64, seed 123; lognormal group sizes, Z-order partition)",
+                config=dict(workload="NestedKriging N=%d d=4 matern3_2, %d groups of %d..%d points (median %d)"
+                            % (n_total, p, sizes.min(), sizes.max(), int(np.median(sizes))),
+                            precision="mixed %d digits" % args.slices if args.mixed else "FP64",
+                            l2="inputs larger than L2 (sum n_g^2 * 8 B = %.1f GB of covariance per step)"
+                               % (8.0 * np.sum(sizes.astype(np.float64) ** 2) / 1e9)),
+                groups=p, sum_n_cubed=n3, fit_seconds=fit_s, submodel_fits_per_s=p / fit_s,
+                predict_gpoe_points=args.nested_q, predict_seconds=pred_s, theta=nk.theta().tolist(),
+                sigma2=nk.sigma2(), clocks=clk, gpu_launches=int(sum(v["launches"] for v in stats.values())),
+                kernels={kk: dict(launches=v["launches"], ms=round(v["ms"], 3)) for kk, v in stats.items()},
+                dominant=dict(kernel=dom[0], ms=dom[1]["ms"], share=dom[1]["ms"] / max(1e-9, sum(
+                    v["ms"] for v in stats.values()))))
+    if not args.no_cpu_baseline:
+        from oracle import baseline as B
+        from oracle import oracle as O
+        O.build()
+        pick = np.random.default_rng(3).choice(p, size=min(8, p), replace=False)
+        t_s, n3s = 0.0, 0.0
+        for gi in pick:
+            idx = np.flatnonzero(labels == gi)
+            s, det = B.dense_eval_sample(X[idx], y[idx], thetas[gi], 1.0, "matern3_2", pair_fraction=1.0,
+                                         rhs_fraction=1.0)
+            t_s += s
+            n3s += float(len(idx)) ** 3
+        per_step = t_s * n3 / n3s
+        line["cpu_baseline"] = dict(value=p / per_step, unit="evals/s", cores=int(det["blas_threads"]), kind="port",
+                                    sample="reference-restated LL+grad of %d groups (%s points) timed in full, "
+                                           "scaled to all %d groups by sum n_g^3" % (len(pick), ",".join(
+                                               str(int(np.sum(labels == gi))) for gi in pick), p))
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -436,13 +548,19 @@ def main():
     ap.add_argument("--n", type=int, default=16384)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--slices", type=int, default=7, help="digit slices of the mixed path (4..8)")
-    ap.add_argument("--workload", default="dense", choices=["dense", "multistart", "vecchia"])
-    ap.add_argument("--mixed", action="store_true", help="multistart workload on the mixed path")
+    ap.add_argument("--workload", default="dense", choices=["dense", "multistart", "vecchia", "nested"])
+    ap.add_argument("--mixed", action="store_true", help="multistart / nested workloads on the mixed path")
+    ap.add_argument("--nested-n", type=int, default=1_000_000, help="points of the nested workload")
+    ap.add_argument("--nested-q", type=int, default=10_000, help="gPoE prediction points of the nested workload")
+    ap.add_argument("--tensor-path", type=int, default=None, choices=[0, 1],
+                    help="digit-product kernels of the mixed path: 0 mma.sync, 1 tcgen05 (default: the library's)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "multistart":
         run_gpu_multistart(args)
+    elif args.workload == "nested":
+        run_gpu_nested(args)
     elif args.workload == "vecchia":
         run_gpu_vecchia(args)
     else:

@@ -85,6 +85,11 @@ int lkg_kriging_vecchia_neighbors(void* ptr);
 int lkg_kriging_is_vecchia_light(void* ptr);
 int lkg_kriging_get_vecchia_sets(void* ptr, int* order_out, int* nbr_out, int* n, int* m);
 int lkg_vecchia_sets(int n, int d, const double* X, int m, int* order_out, int* nbr_out);
+/* Kriging::predictVecchia (Kriging.hpp:163-173, Kriging.cpp:950-1022; no lk_* counterpart): each of the q points
+ * of X_n (q x d column-major) kriged on its m nearest observations (m = 0: the fit's Vecchia m, else 30); mean and,
+ * when return_stdev, the simple-kriging stdev.  lkg_kriging_predict routes here after a light Vecchia fit. */
+int lkg_kriging_predict_vecchia(void* ptr, const double* X_n, int q, int d, int return_stdev, int m,
+                                double* mean_out, double* stdev_out);
 
 /* getters, libkriging_c.h:141-166 */
 const char* lkg_kriging_kernel(void* ptr);
@@ -146,6 +151,64 @@ int lkg_stats_report(char* out, int cap);
 /* No counterpart in the reference: C = A B^T (A M x K, B N x K, C M x N, column-major host buffers) through the
  * split-bf16 tensor-core GEMM with `slices` digits -- the check hook of the mixed path's emulated products. */
 int lkg_ozaki_gemm_check(int M, int N, int K, const double* A, const double* B, int slices, double* C);
+/* No counterpart in the reference: the kernels of the mixed path's digit products -- 0 = mma.sync (warp-level),
+ * 1 = tcgen05 (TMEM accumulators).  Returns the path now in effect; the environment variable LK_OZAKI_TC sets the
+ * initial value (default 0). */
+int lkg_set_tensor_path(int tc);
+int lkg_get_tensor_path(void);
+
+/* ------------------------------------------------------------- NestedKriging -------------------------------------- */
+/* libkriging_c.h:394-455 lk_nested_kriging_* (NestedKriging.hpp:63-105): partition (kmeans | random), submodel
+ * fits, common prior, aggregation PoE | gPoE | BCM | rBCM | NK.  warping must be empty (n_warping = 0): WarpKriging
+ * submodels are not part of this library.  theta: one starting point of length theta_n, as there. */
+void* lkg_nested_kriging_new_fit(const double* y, int n, const double* X, int nX, int d, const char* kernel,
+                                 int nb_groups, const char* aggregation, const char* partition, int seed,
+                                 const char** warping, int n_warping, const char* regmodel, const char* optim,
+                                 const char* objective, const double* sigma2, int is_sigma2_estim, const double* theta,
+                                 int theta_n, int is_theta_estim, const double* beta, int beta_n, int is_beta_estim);
+void lkg_nested_kriging_delete(void* ptr);
+int lkg_nested_kriging_fit(void* ptr, const double* y, int n, const double* X, int nX, int d, int nb_groups,
+                           const char** warping, int n_warping, const char* regmodel, const char* optim,
+                           const char* objective, const double* sigma2, int is_sigma2_estim, const double* theta,
+                           int theta_n, int is_theta_estim, const double* beta, int beta_n, int is_beta_estim);
+int lkg_nested_kriging_predict(void* ptr, const double* X_n, int m, int d, int return_stdev, double* mean_out,
+                               double* stdev_out);
+const char* lkg_nested_kriging_summary(void* ptr);
+const char* lkg_nested_kriging_kernel(void* ptr);
+const char* lkg_nested_kriging_aggregation(void* ptr);
+int lkg_nested_kriging_nb_groups(void* ptr);
+int lkg_nested_kriging_get_theta(void* ptr, double* out, int* n);
+double lkg_nested_kriging_get_sigma2(void* ptr);
+double lkg_nested_kriging_get_beta0(void* ptr);
+/* No counterpart in the C ABI (NestedKriging(covType) + setters, NestedKriging.hpp:67, Python binding
+ * NestedKriging(kernel)): an unfitted model with its aggregation, partition and seed. */
+void* lkg_nested_kriging_new(const char* kernel, const char* aggregation, const char* partition, int seed);
+/* No counterpart in the reference: fit on a given partition, labels[i] in [0, nb_groups) the group of row i. */
+int lkg_nested_kriging_fit_groups(void* ptr, const double* y, int n, const double* X, int nX, int d,
+                                  const int* labels, int nb_groups, const char* regmodel, const char* optim,
+                                  const char* objective, const double* sigma2, int is_sigma2_estim,
+                                  const double* theta, int theta_n, int is_theta_estim, const double* beta,
+                                  int beta_n, int is_beta_estim);
+/* NestedKriging::groups (NestedKriging.hpp:113) as labels: labels_out[i] = group of row i; *n = rows. */
+int lkg_nested_kriging_get_groups(void* ptr, int* labels_out, int* n);
+/* NestedKriging::submodel (NestedKriging.hpp:117): a Kriging handle owned by the nested model (valid until it is
+ * refitted or deleted; never pass it to lkg_kriging_delete), usable with every lkg_kriging_* getter. */
+void* lkg_nested_kriging_submodel(void* ptr, int i);
+/* No counterpart in the reference: digit slices of the submodel objective evaluations (0 = FP64, 4..8 = mixed). */
+int lkg_nested_kriging_set_precision(void* ptr, int slices);
+/* NestedKriging::set_predict_chunk (NestedKriging.hpp:133). */
+int lkg_nested_kriging_set_predict_chunk(void* ptr, int chunk);
+/* No counterpart in the reference (each submodel's Kriging::logLikelihoodFun, Kriging.cpp:343-349, runs alone
+ * there): the submodel fit objective of all p groups in one batched evaluation -- concentrated LL of group g at
+ * theta row g of thetas (p x d row-major) into ll_out[g], theta-gradient into grad_out (p x d row-major) when
+ * return_grad.  Needs a fit on the plain path (objective "LL"). */
+int lkg_nested_kriging_log_likelihood_groups(void* ptr, const double* thetas, int p, int d, int return_grad,
+                                             double* ll_out, double* grad_out);
+/* No counterpart in the reference: the submodel estimates that entered unify_hyperparameters
+ * (NestedKriging.cpp:283-310) -- theta_out p x d row-major, sigma2_out p, beta0_out p (0 without a constant trend);
+ * *p = 0 after a fit that had no unify step (LLVecchia-unified path).  NULL outputs are skipped. */
+int lkg_nested_kriging_get_group_estimates(void* ptr, double* theta_out, double* sigma2_out, double* beta0_out,
+                                           int* p, int* d);
 
 #ifdef __cplusplus
 }

@@ -1,12 +1,14 @@
 """libkriging_gb300 -- GB300-native (sm_103a) libKriging likelihood path.
 
-Drop-in for pylibkriging's ``Kriging`` on the likelihood path: covariance build, blocked FP64 Cholesky and
-triangular solves, concentrated log-likelihood with its one-pass adjoint theta-gradient, the L-BFGS-B fit
-(multistart evaluations batched into single GPU launches) and predict.  All compute goes through the C ABI of
+Drop-in for pylibkriging's ``Kriging`` and ``NestedKriging`` on the likelihood path: covariance build, blocked
+Cholesky and triangular solves (FP64, or split-bf16 tensor-core products), concentrated log-likelihood with its
+one-pass adjoint theta-gradient, the L-BFGS-B fit (multistart and NestedKriging submodel evaluations batched into
+single GPU launches), the Vecchia likelihood and predict.  All compute goes through the C ABI of
 ``include/libkriging_gb300.h``.
 """
 from ._lib import LibKrigingError, header_symbols, load
 from .kriging import Kriging, Optim, check_chol_rcond, get_num_nugget, set_num_nugget, vecchia_sets
+from .nested import NestedKriging
 
-__all__ = ["Kriging", "Optim", "vecchia_sets", "set_num_nugget", "get_num_nugget", "check_chol_rcond", "LibKrigingError", "load",
-           "header_symbols"]
+__all__ = ["Kriging", "NestedKriging", "Optim", "vecchia_sets", "set_num_nugget", "get_num_nugget",
+           "check_chol_rcond", "LibKrigingError", "load", "header_symbols"]

@@ -89,6 +89,31 @@ _SIGS = {
     "lkg_kriging_is_vecchia_light": (_i, [_vp]),
     "lkg_kriging_get_vecchia_sets": (_i, [_vp, _ip, _ip, _ip, _ip]),
     "lkg_vecchia_sets": (_i, [_i, _i, _dp, _i, _ip, _ip]),
+    "lkg_kriging_predict_vecchia": (_i, [_vp, _dp, _i, _i, _i, _i, _dp, _dp]),
+    "lkg_set_tensor_path": (_i, [_i]),
+    "lkg_get_tensor_path": (_i, []),
+    "lkg_nested_kriging_new_fit": (_vp, [_dp, _i, _dp, _i, _i, _cp, _i, _cp, _cp, _i, _vp, _i, _cp, _cp, _cp, _dp, _i,
+                                         _dp, _i, _i, _dp, _i, _i]),
+    "lkg_nested_kriging_delete": (None, [_vp]),
+    "lkg_nested_kriging_fit": (_i, [_vp, _dp, _i, _dp, _i, _i, _i, _vp, _i, _cp, _cp, _cp, _dp, _i, _dp, _i, _i, _dp,
+                                    _i, _i]),
+    "lkg_nested_kriging_predict": (_i, [_vp, _dp, _i, _i, _i, _dp, _dp]),
+    "lkg_nested_kriging_summary": (_cp, [_vp]),
+    "lkg_nested_kriging_kernel": (_cp, [_vp]),
+    "lkg_nested_kriging_aggregation": (_cp, [_vp]),
+    "lkg_nested_kriging_nb_groups": (_i, [_vp]),
+    "lkg_nested_kriging_get_theta": (_i, [_vp, _dp, _ip]),
+    "lkg_nested_kriging_get_sigma2": (_d, [_vp]),
+    "lkg_nested_kriging_get_beta0": (_d, [_vp]),
+    "lkg_nested_kriging_new": (_vp, [_cp, _cp, _cp, _i]),
+    "lkg_nested_kriging_fit_groups": (_i, [_vp, _dp, _i, _dp, _i, _i, _ip, _i, _cp, _cp, _cp, _dp, _i, _dp, _i, _i,
+                                           _dp, _i, _i]),
+    "lkg_nested_kriging_get_groups": (_i, [_vp, _ip, _ip]),
+    "lkg_nested_kriging_submodel": (_vp, [_vp, _i]),
+    "lkg_nested_kriging_set_precision": (_i, [_vp, _i]),
+    "lkg_nested_kriging_set_predict_chunk": (_i, [_vp, _i]),
+    "lkg_nested_kriging_log_likelihood_groups": (_i, [_vp, _dp, _i, _i, _i, _dp, _dp]),
+    "lkg_nested_kriging_get_group_estimates": (_i, [_vp, _dp, _dp, _dp, _ip, _ip]),
 }
 
 _lib = None

@@ -12,6 +12,7 @@
 #include "../../include/libkriging_gb300.h"
 #include "config.hpp"
 #include "kriging.hpp"
+#include "nested.hpp"
 
 using lkg::Kriging;
 using lkg::Mat;
@@ -158,6 +159,17 @@ int lkg_kriging_predict(void* ptr, const double* X_n, int m, int d, int return_s
     if (mean_out) std::memcpy(mean_out, mean.data(), sizeof(double) * mean.size());
     if (stdev_out && return_stdev) std::memcpy(stdev_out, sd.data(), sizeof(double) * sd.size());
     if (cov_out && return_cov) std::memcpy(cov_out, cov.v.data(), sizeof(double) * cov.v.size());
+    return 0;
+  }
+  CATCH_RETURN
+}
+
+int lkg_kriging_predict_vecchia(void* ptr, const double* X_n, int q, int d, int return_stdev, int m,
+                                double* mean_out, double* stdev_out) {
+  try {
+    auto [mean, sd] = K(ptr)->predictVecchia(mat_of(X_n, q, d), return_stdev != 0, m);
+    if (mean_out) std::memcpy(mean_out, mean.data(), sizeof(double) * mean.size());
+    if (stdev_out && return_stdev) std::memcpy(stdev_out, sd.data(), sizeof(double) * sd.size());
     return 0;
   }
   CATCH_RETURN
@@ -485,6 +497,252 @@ int lkg_vecchia_sets(int n, int d, const double* X, int m, int* order_out, int* 
   try {
     if (n < 1 || d < 1 || m < 0) throw std::invalid_argument("lkg_vecchia_sets: bad sizes");
     lkg::vecchia_sets_gpu(n, d, X, m, order_out, nbr_out);
+    return 0;
+  }
+  CATCH_RETURN
+}
+
+}  // extern "C"
+
+// ---- NestedKriging (libkriging_c.h:394-455, libkriging_c.cpp:1663-1850) ----
+namespace {
+
+lkg::NestedKriging* NK(void* p) {
+  if (!p) throw std::invalid_argument("null NestedKriging handle");
+  return static_cast<lkg::NestedKriging*>(p);
+}
+
+lkg::NestedKriging::Partition parse_partition(const char* s) {
+  const std::string p = s ? s : "kmeans";
+  if (p == "random") return lkg::NestedKriging::Partition::Random;
+  if (p == "kmeans" || p.empty()) return lkg::NestedKriging::Partition::KMeans;
+  throw std::invalid_argument("Unknown partition: '" + p + "'. Expected 'kmeans' or 'random'.");
+}
+
+void reject_warping(int n_warping) {
+  if (n_warping > 0)
+    throw std::invalid_argument("NestedKriging: WarpKriging submodels (warping) are not supported by the GPU build");
+}
+
+}  // namespace
+
+extern "C" {
+
+void* lkg_nested_kriging_new(const char* kernel, const char* aggregation, const char* partition, int seed) {
+  try {
+    auto* nk = new lkg::NestedKriging(kernel ? kernel : "matern3_2");
+    try {
+      nk->set_aggregation(lkg::NestedKriging::aggregation_from_string(aggregation ? aggregation : "NK"));
+      nk->set_partition(parse_partition(partition));
+      nk->set_seed(seed);
+    } catch (...) {
+      delete nk;
+      throw;
+    }
+    return nk;
+  }
+  CATCH_RETURN_NULL
+}
+
+void* lkg_nested_kriging_new_fit(const double* y, int n, const double* X, int nX, int d, const char* kernel,
+                                 int nb_groups, const char* aggregation, const char* partition, int seed,
+                                 const char** warping, int n_warping, const char* regmodel, const char* optim,
+                                 const char* objective, const double* sigma2, int is_sigma2_estim, const double* theta,
+                                 int theta_n, int is_theta_estim, const double* beta, int beta_n, int is_beta_estim) {
+  try {
+    (void)warping;
+    reject_warping(n_warping);
+    auto* nk = new lkg::NestedKriging(kernel ? kernel : "matern3_2");
+    try {
+      nk->set_aggregation(lkg::NestedKriging::aggregation_from_string(aggregation ? aggregation : "NK"));
+      nk->set_partition(parse_partition(partition));
+      nk->set_seed(seed);
+      std::vector<double> yv(y, y + n);
+      nk->fit(yv, mat_of(X, nX, d), nb_groups, lkg::regmodel_from_string(regmodel ? regmodel : "constant"),
+              optim ? optim : "BFGS", objective ? objective : "LL",
+              make_params(sigma2, is_sigma2_estim, theta, (theta && theta_n > 0) ? 1 : 0, theta_n, is_theta_estim,
+                          beta, beta_n, is_beta_estim, nullptr, 1));
+    } catch (...) {
+      delete nk;
+      throw;
+    }
+    return nk;
+  }
+  CATCH_RETURN_NULL
+}
+
+void lkg_nested_kriging_delete(void* ptr) { delete static_cast<lkg::NestedKriging*>(ptr); }
+
+int lkg_nested_kriging_fit(void* ptr, const double* y, int n, const double* X, int nX, int d, int nb_groups,
+                           const char** warping, int n_warping, const char* regmodel, const char* optim,
+                           const char* objective, const double* sigma2, int is_sigma2_estim, const double* theta,
+                           int theta_n, int is_theta_estim, const double* beta, int beta_n, int is_beta_estim) {
+  try {
+    (void)warping;
+    reject_warping(n_warping);
+    std::vector<double> yv(y, y + n);
+    NK(ptr)->fit(yv, mat_of(X, nX, d), nb_groups, lkg::regmodel_from_string(regmodel ? regmodel : "constant"),
+                 optim ? optim : "BFGS", objective ? objective : "LL",
+                 make_params(sigma2, is_sigma2_estim, theta, (theta && theta_n > 0) ? 1 : 0, theta_n, is_theta_estim,
+                             beta, beta_n, is_beta_estim, nullptr, 1));
+    return 0;
+  }
+  CATCH_RETURN
+}
+
+int lkg_nested_kriging_fit_groups(void* ptr, const double* y, int n, const double* X, int nX, int d,
+                                  const int* labels, int nb_groups, const char* regmodel, const char* optim,
+                                  const char* objective, const double* sigma2, int is_sigma2_estim,
+                                  const double* theta, int theta_n, int is_theta_estim, const double* beta,
+                                  int beta_n, int is_beta_estim) {
+  try {
+    if (!labels || nb_groups < 1) throw std::invalid_argument("fit_groups: labels and nb_groups >= 1 required");
+    std::vector<std::vector<int>> groups(nb_groups);
+    for (int i = 0; i < nX; ++i) {
+      if (labels[i] < 0 || labels[i] >= nb_groups)
+        throw std::invalid_argument("fit_groups: labels must lie in [0, nb_groups)");
+      groups[labels[i]].push_back(i);
+    }
+    std::vector<double> yv(y, y + n);
+    NK(ptr)->fit_groups(yv, mat_of(X, nX, d), groups, lkg::regmodel_from_string(regmodel ? regmodel : "constant"),
+                        optim ? optim : "BFGS", objective ? objective : "LL",
+                        make_params(sigma2, is_sigma2_estim, theta, (theta && theta_n > 0) ? 1 : 0, theta_n,
+                                    is_theta_estim, beta, beta_n, is_beta_estim, nullptr, 1));
+    return 0;
+  }
+  CATCH_RETURN
+}
+
+int lkg_nested_kriging_predict(void* ptr, const double* X_n, int m, int d, int return_stdev, double* mean_out,
+                               double* stdev_out) {
+  try {
+    auto [mean, sd] = NK(ptr)->predict(mat_of(X_n, m, d), return_stdev != 0);
+    if (mean_out) std::memcpy(mean_out, mean.data(), sizeof(double) * mean.size());
+    if (stdev_out && return_stdev) std::memcpy(stdev_out, sd.data(), sizeof(double) * sd.size());
+    return 0;
+  }
+  CATCH_RETURN
+}
+
+const char* lkg_nested_kriging_summary(void* ptr) {
+  try {
+    static thread_local std::string buf;
+    buf = NK(ptr)->summary();
+    return buf.c_str();
+  }
+  CATCH_RETURN_NULL
+}
+
+const char* lkg_nested_kriging_kernel(void* ptr) {
+  try {
+    return NK(ptr)->kernel().c_str();
+  }
+  CATCH_RETURN_NULL
+}
+
+const char* lkg_nested_kriging_aggregation(void* ptr) {
+  try {
+    static thread_local std::string buf;
+    buf = lkg::NestedKriging::aggregation_to_string(NK(ptr)->aggregation());
+    return buf.c_str();
+  }
+  CATCH_RETURN_NULL
+}
+
+int lkg_nested_kriging_nb_groups(void* ptr) {
+  try {
+    return NK(ptr)->nb_groups();
+  }
+  CATCH_RETURN
+}
+
+int lkg_nested_kriging_get_theta(void* ptr, double* out, int* n) {
+  try {
+    return copy_vec(NK(ptr)->theta(), out, n);
+  }
+  CATCH_RETURN
+}
+
+double lkg_nested_kriging_get_sigma2(void* ptr) {
+  try {
+    return NK(ptr)->sigma2();
+  }
+  CATCH_RETURN_NAN
+}
+
+double lkg_nested_kriging_get_beta0(void* ptr) {
+  try {
+    return NK(ptr)->beta0();
+  }
+  CATCH_RETURN_NAN
+}
+
+int lkg_nested_kriging_get_groups(void* ptr, int* labels_out, int* n) {
+  try {
+    const auto& G = NK(ptr)->groups();
+    int total = 0;
+    for (const auto& g : G) total += (int)g.size();
+    if (n) *n = total;
+    if (labels_out)
+      for (size_t k = 0; k < G.size(); ++k)
+        for (int i : G[k]) labels_out[i] = (int)k;
+    return 0;
+  }
+  CATCH_RETURN
+}
+
+void* lkg_nested_kriging_submodel(void* ptr, int i) {
+  try {
+    return &NK(ptr)->submodel(i);
+  }
+  CATCH_RETURN_NULL
+}
+
+int lkg_nested_kriging_set_precision(void* ptr, int slices) {
+  try {
+    NK(ptr)->set_precision(slices);
+    return 0;
+  }
+  CATCH_RETURN
+}
+
+int lkg_nested_kriging_log_likelihood_groups(void* ptr, const double* thetas, int p, int d, int return_grad,
+                                             double* ll_out, double* grad_out) {
+  try {
+    lkg::Mat T;
+    T.rows = p;
+    T.cols = d;
+    T.v.resize((size_t)p * d);
+    for (int g = 0; g < p; ++g)
+      for (int k = 0; k < d; ++k) T(g, k) = thetas[(size_t)g * d + k];
+    std::vector<double> ll, grad;
+    NK(ptr)->log_likelihood_groups(T, return_grad != 0, ll, grad);
+    if (ll_out) std::memcpy(ll_out, ll.data(), sizeof(double) * ll.size());
+    if (grad_out && return_grad) std::memcpy(grad_out, grad.data(), sizeof(double) * grad.size());
+    return 0;
+  }
+  CATCH_RETURN
+}
+
+int lkg_nested_kriging_get_group_estimates(void* ptr, double* theta_out, double* sigma2_out, double* beta0_out,
+                                           int* p, int* d) {
+  try {
+    auto* nk = NK(ptr);
+    const auto& th = nk->group_theta();
+    const int np = (int)nk->group_sigma2().size();
+    if (p) *p = np;
+    if (d) *d = np > 0 ? (int)(th.size() / np) : 0;
+    if (theta_out && !th.empty()) std::memcpy(theta_out, th.data(), sizeof(double) * th.size());
+    if (sigma2_out && np) std::memcpy(sigma2_out, nk->group_sigma2().data(), sizeof(double) * np);
+    if (beta0_out && np) std::memcpy(beta0_out, nk->group_beta0().data(), sizeof(double) * np);
+    return 0;
+  }
+  CATCH_RETURN
+}
+
+int lkg_nested_kriging_set_predict_chunk(void* ptr, int chunk) {
+  try {
+    NK(ptr)->set_predict_chunk(chunk);
     return 0;
   }
   CATCH_RETURN

@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 
 namespace lkg {
 
@@ -160,5 +161,25 @@ inline const char* kernel_name(int k) {
 }
 
 inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+// Launch<kernel, DM>::run(args...) for the runtime kernel id and the smallest DM in {4, 8, 16, 32} holding d
+template <template <int, int> class Launch, typename... Args>
+void dispatch_kd(int kernel, int d, Args&&... args) {
+  auto go = [&](auto kc) {
+    constexpr int KK = decltype(kc)::value;
+    if (d <= 4) Launch<KK, 4>::run(args...);
+    else if (d <= 8) Launch<KK, 8>::run(args...);
+    else if (d <= 16) Launch<KK, 16>::run(args...);
+    else if (d <= 32) Launch<KK, 32>::run(args...);
+    else throw std::invalid_argument("input dimension d > 32 is not supported by the GPU kernels");
+  };
+  switch (kernel) {
+    case KGAUSS: go(std::integral_constant<int, KGAUSS>{}); break;
+    case KEXP: go(std::integral_constant<int, KEXP>{}); break;
+    case KMATERN32: go(std::integral_constant<int, KMATERN32>{}); break;
+    case KMATERN52: go(std::integral_constant<int, KMATERN52>{}); break;
+    default: throw std::invalid_argument("Unsupported covariance kernel id");
+  }
+}
 
 }  // namespace lkg

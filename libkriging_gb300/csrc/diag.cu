@@ -74,6 +74,13 @@ int lkg_probe_fp64_peak(double* tflops_out) {
 // ---- emulated-GEMM check entry point (host buffers) ----
 #include "ozaki.cuh"
 
+extern "C" int lkg_set_tensor_path(int tc) {
+  lkg::ozaki_set_tensor_path(tc);
+  return lkg::ozaki_tensor_path();
+}
+
+extern "C" int lkg_get_tensor_path(void) { return lkg::ozaki_tensor_path(); }
+
 extern "C" int lkg_ozaki_gemm_check(int M, int N, int K, const double* A, const double* B, int slices, double* C) {
   // C = A * B^T with A (M x K) and B (N x K) column-major, computed by the split-bf16 tensor-core path
   double *dA = nullptr, *dB = nullptr, *dC = nullptr;
@@ -102,7 +109,7 @@ extern "C" int lkg_ozaki_gemm_check(int M, int N, int K, const double* A, const 
     lkg::ozaki_gemm(M, N, 0, sa.nchunk, 1.0, sa, 0, sb, 0, 0.0, dC, M, 0, 1, false, 0);
     LKG_CUDA(cudaDeviceSynchronize());
     LKG_CUDA(cudaMemcpy(C, dC, sizeof(double) * M * N, cudaMemcpyDeviceToHost));
-    rc = 0;
+    rc = lkg::ozaki_tc_error_and_reset() ? -1 : 0;
   } catch (const std::exception&) {
     rc = -1;
   }

@@ -91,10 +91,20 @@ Config& config() {
 }
 
 Engine::Engine(int kernel, int n, int d, int p, const double* X, const double* y, const double* F, int batch_cap)
-    : kernel_(kernel), n_(n), d_(d), p_(p), cap_(batch_cap) {
-  if (n < 1 || d < 1 || d > MAX_D || p < 0 || p > 64 || batch_cap < 1)
+    : Engine(kernel, n, d, p, 1, X, y, F, nullptr, batch_cap) {}
+
+Engine::Engine(int kernel, int n, int d, int p, int ndesign, const double* X, const double* y, const double* F,
+               const int* n_valid, int batch_cap)
+    : kernel_(kernel), n_(n), d_(d), p_(p), cap_(batch_cap), ndesign_(ndesign) {
+  if (n < 1 || d < 1 || d > MAX_D || p < 0 || p > 64 || batch_cap < 1 || ndesign < 1)
     throw std::invalid_argument("Engine: unsupported sizes n=" + std::to_string(n) + " d=" + std::to_string(d) +
                                 " p=" + std::to_string(p));
+  nvalid_.assign(ndesign, n);
+  if (n_valid)
+    for (int e = 0; e < ndesign; ++e) {
+      if (n_valid[e] < 1 || n_valid[e] > n) throw std::invalid_argument("Engine: design size out of range");
+      nvalid_[e] = n_valid[e];
+    }
   LKG_CUDA(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
   lda_ = ((int64_t)n + 7) / 8 * 8;  // 64-byte aligned columns
   mstride_ = lda_ * n;
@@ -102,12 +112,17 @@ Engine::Engine(int kernel, int n, int d, int p, const double* X, const double* y
   dstride_ = (int64_t)nblk * NB * NB;
   fystride_ = (int64_t)n * (p + 1);
   gram_stride_ = (p + 1) * (p + 1) + 1;
-  dalloc(&dX_, (size_t)n * d);
-  dalloc(&dY_, n);
-  dalloc(&dF_, (size_t)n * std::max(p, 1));
-  LKG_CUDA(cudaMemcpyAsync(dX_, X, sizeof(double) * n * d, cudaMemcpyHostToDevice, st_));
-  LKG_CUDA(cudaMemcpyAsync(dY_, y, sizeof(double) * n, cudaMemcpyHostToDevice, st_));
-  if (p > 0) LKG_CUDA(cudaMemcpyAsync(dF_, F, sizeof(double) * n * p, cudaMemcpyHostToDevice, st_));
+  const size_t nd = (size_t)ndesign;
+  dalloc(&dX_, nd * n * d);
+  dalloc(&dY_, nd * n);
+  dalloc(&dF_, nd * n * std::max(p, 1));
+  LKG_CUDA(cudaMemcpyAsync(dX_, X, sizeof(double) * nd * n * d, cudaMemcpyHostToDevice, st_));
+  LKG_CUDA(cudaMemcpyAsync(dY_, y, sizeof(double) * nd * n, cudaMemcpyHostToDevice, st_));
+  if (p > 0) LKG_CUDA(cudaMemcpyAsync(dF_, F, sizeof(double) * nd * n * p, cudaMemcpyHostToDevice, st_));
+  if (ndesign > 1 || n_valid) {
+    dalloc(&dXe_, (size_t)cap_ * n * d);
+    dalloc(&dnv_, cap_);
+  }
   dalloc(&dA_, (size_t)mstride_ * cap_);
   dalloc(&dDinv_, (size_t)dstride_ * cap_);
   dalloc(&dFY_, (size_t)fystride_ * cap_);
@@ -134,6 +149,8 @@ Engine::~Engine() {
     if (p) cudaFree(p);
   if (dinfo_) cudaFree(dinfo_);
   if (dgls_info_) cudaFree(dgls_info_);
+  if (dXe_) cudaFree(dXe_);
+  if (dnv_) cudaFree(dnv_);
   for (void* p : {dpanel_, drowblk_, dwfull_})
     if (p) cudaFree(p);
   for (int* p : {dpanel_exp_, drowblk_exp_, dwfull_exp_})
@@ -188,7 +205,9 @@ void Engine::solve_lower_inplace(int b, double* dB, int64_t ldb, int r) const {
 
 // dtrcon('1', 'L', 'N') style estimate (LAPACK dlacn2 iteration of Hager / Higham) of rcond(L)^2 for every entry,
 // with the triangular solves of all entries batched into the same launches.
-void Engine::rcond_batch(int batch, std::vector<double>& rc2) {
+void Engine::rcond_batch(int batch, std::vector<double>& rc2, const std::vector<int>& nvb) {
+  // every vector of the estimator lives on the entry's valid block (the padded identity stays out of it), so a
+  // padded entry follows exactly the iteration of its unpadded matrix
   const int n = n_;
   std::vector<double> colsum((size_t)n * batch);
   lower_colsum_abs(n, dA_, lda_, mstride_, dcol_, batch, st_);
@@ -196,7 +215,7 @@ void Engine::rcond_batch(int batch, std::vector<double>& rc2) {
   LKG_CUDA(cudaStreamSynchronize(st_));
   std::vector<double> anorm(batch, 0.0);
   for (int b = 0; b < batch; ++b)
-    for (int j = 0; j < n; ++j) anorm[b] = std::max(anorm[b], colsum[(size_t)b * n + j]);
+    for (int j = 0; j < nvb[b]; ++j) anorm[b] = std::max(anorm[b], colsum[(size_t)b * n + j]);
 
   // per-entry state machine of dlacn2
   struct St {
@@ -210,17 +229,18 @@ void Engine::rcond_batch(int batch, std::vector<double>& rc2) {
   std::vector<double> vec((size_t)n * batch);
   auto set_x = [&](int b, int phase) {
     double* x = vec.data() + (size_t)b * n;
+    const int m = nvb[b];
+    std::fill(x, x + n, 0.0);
     if (phase == 0) {
-      for (int i = 0; i < n; ++i) x[i] = 1.0 / n;
+      for (int i = 0; i < m; ++i) x[i] = 1.0 / m;
     } else if (phase == 1) {
-      for (int i = 0; i < n; ++i) x[i] = S[b].xi[i];
+      for (int i = 0; i < m; ++i) x[i] = S[b].xi[i];
     } else if (phase == 2) {
-      std::fill(x, x + n, 0.0);
       x[S[b].j] = 1.0;
     } else if (phase == 3) {
       double altsgn = 1.0;
-      for (int i = 0; i < n; ++i) {
-        x[i] = altsgn * (1.0 + (n > 1 ? (double)i / (double)(n - 1) : 0.0));
+      for (int i = 0; i < m; ++i) {
+        x[i] = altsgn * (1.0 + (m > 1 ? (double)i / (double)(m - 1) : 0.0));
         altsgn = -altsgn;
       }
     }
@@ -249,22 +269,23 @@ void Engine::rcond_batch(int batch, std::vector<double>& rc2) {
       St& s = S[b];
       if (s.phase >= 4 || kind_of(s.phase) != kind) continue;
       const double* y = res.data() + (size_t)b * n;
+      const int m = nvb[b];
       double l1 = 0.0;
-      for (int i = 0; i < n; ++i) l1 += std::fabs(y[i]);
+      for (int i = 0; i < m; ++i) l1 += std::fabs(y[i]);
       if (s.phase == 0) {
         s.est = l1;
-        if (n == 1) {
+        if (m == 1) {
           s.phase = 4;
           continue;
         }
-        for (int i = 0; i < n; ++i) s.xi[i] = (y[i] >= 0.0) ? 1.0 : -1.0;
+        for (int i = 0; i < m; ++i) s.xi[i] = (y[i] >= 0.0) ? 1.0 : -1.0;
         s.phase = 1;
         s.iter = 2;
         s.first_done = true;
       } else if (s.phase == 1) {
         int jlast = s.j;
         int jm = 0;
-        for (int i = 1; i < n; ++i)
+        for (int i = 1; i < m; ++i)
           if (std::fabs(y[i]) > std::fabs(y[jm])) jm = i;
         if (s.first_done) {
           s.first_done = false;
@@ -283,15 +304,15 @@ void Engine::rcond_batch(int batch, std::vector<double>& rc2) {
         const double estold = s.est;
         s.est = l1;
         bool same = true;
-        for (int i = 0; i < n && same; ++i) same = (((y[i] >= 0.0) ? 1.0 : -1.0) == s.xi[i]);
+        for (int i = 0; i < m && same; ++i) same = (((y[i] >= 0.0) ? 1.0 : -1.0) == s.xi[i]);
         if (same || s.est <= estold) {
           s.phase = 3;
         } else {
-          for (int i = 0; i < n; ++i) s.xi[i] = (y[i] >= 0.0) ? 1.0 : -1.0;
+          for (int i = 0; i < m; ++i) s.xi[i] = (y[i] >= 0.0) ? 1.0 : -1.0;
           s.phase = 1;
         }
       } else if (s.phase == 3) {
-        const double temp = 2.0 * l1 / (3.0 * n);
+        const double temp = 2.0 * l1 / (3.0 * m);
         if (temp > s.est) s.est = temp;
         s.phase = 4;
       }
@@ -307,17 +328,39 @@ void Engine::rcond_batch(int batch, std::vector<double>& rc2) {
 }
 
 void Engine::evaluate(int batch, const double* thetas, const double* factors, bool with_grad,
-                      std::vector<EvalOut>& out, std::map<std::string, double>* bench) {
+                      std::vector<EvalOut>& out, std::map<std::string, double>* bench, const int* designs) {
   if (batch < 1 || batch > cap_) throw std::invalid_argument("Engine::evaluate: batch out of range");
+  if (ndesign_ > 1 && !designs) throw std::invalid_argument("Engine::evaluate: design of each entry required");
   const Config& cfg = config();
   const int n = n_, d = d_, p = p_;
   out.assign(batch, EvalOut{});
   Timer tm(st_, bench);
   LKG_CUDA(cudaMemcpyAsync(dtheta_, thetas, sizeof(double) * d * batch, cudaMemcpyHostToDevice, st_));
   LKG_CUDA(cudaMemcpyAsync(dfactor_, factors, sizeof(double) * batch, cudaMemcpyHostToDevice, st_));
+  // design of every entry: X gathered per entry and valid sizes for the identity padding (several designs only)
+  entry_design_.assign(batch, 0);
+  const double* dXb = dX_;
+  int64_t xbs = 0;
+  const int* dnv = nullptr;
+  std::vector<int> nv_entry(batch, n);
+  if (dXe_) {
+    for (int b = 0; b < batch; ++b) {
+      const int e = designs ? designs[b] : 0;
+      if (e < 0 || e >= ndesign_) throw std::invalid_argument("Engine::evaluate: design index out of range");
+      entry_design_[b] = e;
+      nv_entry[b] = nvalid_[e];
+      LKG_CUDA(cudaMemcpyAsync(dXe_ + (size_t)b * n * d, dX_ + (size_t)e * n * d, sizeof(double) * n * d,
+                               cudaMemcpyDeviceToDevice, st_));
+    }
+    LKG_CUDA(cudaMemcpyAsync(dnv_, nv_entry.data(), sizeof(int) * batch, cudaMemcpyHostToDevice, st_));
+    dXb = dXe_;
+    xbs = (int64_t)n * d;
+    dnv = dnv_;
+  }
 
   // ---- R, L with the numerical-nugget retry rules (LinearAlgebra.cpp:68-98) ----
-  std::vector<double> diag(batch, 1.0);
+  std::vector<double> diag(batch, base_diag_);
+  const bool rcond_check = cfg.chol_rcond_check && !plain_chol_;
   std::vector<int> inc(batch, 0);
   std::vector<char> dead(batch, 0);
   std::vector<int> info(batch, 0);
@@ -339,8 +382,8 @@ void Engine::evaluate(int batch, const double* thetas, const double* factors, bo
   bool w_valid = false;  // W = L^-1 of the accepted factor is already in dW_
   for (int attempt = 0;; ++attempt) {
     LKG_CUDA(cudaMemcpyAsync(ddiag_, diag.data(), sizeof(double) * batch, cudaMemcpyHostToDevice, st_));
-    cov_build_lower(kernel_, n, d, dX_, 0, dtheta_, dfactor_, ddiag_, dA_, lda_, mstride_, batch, st_,
-                    slices_ > 0 && !retreated);
+    cov_build_lower(kernel_, n, d, dXb, xbs, dtheta_, dfactor_, ddiag_, dA_, lda_, mstride_, batch, st_,
+                    slices_ > 0 && !retreated, dnv);
     if (slices_ > 0 && !retreated) {
       potrf_blocked_mixed(dA_, lda_, mstride_, n, dDinv_, dinfo_, batch, mw, st_);
       LKG_CUDA(cudaMemcpyAsync(info.data(), dinfo_, sizeof(int) * batch, cudaMemcpyDeviceToHost, st_));
@@ -349,7 +392,8 @@ void Engine::evaluate(int batch, const double* thetas, const double* factors, bo
       for (int b = 0; b < batch; ++b) any_fail = any_fail || (info[b] != 0 && !dead[b]);
       if (any_fail) {  // retreat: redo this factorisation on the FP64 path before the nugget-retry rules apply
         retreated = true;
-        cov_build_lower(kernel_, n, d, dX_, 0, dtheta_, dfactor_, ddiag_, dA_, lda_, mstride_, batch, st_);
+        cov_build_lower(kernel_, n, d, dXb, xbs, dtheta_, dfactor_, ddiag_, dA_, lda_, mstride_, batch, st_, false,
+                        dnv);
         potrf_blocked(dA_, lda_, mstride_, n, dDinv_, dinfo_, batch, st_);
       }
     } else {
@@ -358,7 +402,7 @@ void Engine::evaluate(int batch, const double* thetas, const double* factors, bo
     LKG_CUDA(cudaMemcpyAsync(info.data(), dinfo_, sizeof(int) * batch, cudaMemcpyDeviceToHost, st_));
     LKG_CUDA(cudaStreamSynchronize(st_));
     w_valid = false;
-    if (cfg.chol_rcond_check) {
+    if (rcond_check) {
       if (with_grad) {
         // The gradient needs W = L^-1 anyway: rcond_exact = 1 / (|L|_1 |L^-1|_1) <= the dlacn2 estimate, so
         // rcond_exact^2 >= min_rcond already decides "no retry"; only entries below it run the estimator.
@@ -377,7 +421,7 @@ void Engine::evaluate(int batch, const double* thetas, const double* factors, bo
         bool need_est = false;
         for (int b = 0; b < batch; ++b) {
           double an = 0.0, wn = 0.0;
-          for (int j = 0; j < n; ++j) {
+          for (int j = 0; j < nv_entry[b]; ++j) {  // the valid block's columns only
             an = std::max(an, cl[(size_t)b * n + j]);
             wn = std::max(wn, cw[(size_t)b * n + j]);
           }
@@ -387,21 +431,25 @@ void Engine::evaluate(int batch, const double* thetas, const double* factors, bo
         }
         if (need_est) {
           std::vector<double> est;
-          rcond_batch(batch, est);
+          rcond_batch(batch, est, nv_entry);
           for (int b = 0; b < batch; ++b)
             if (!(rc2[b] >= cfg.min_rcond)) rc2[b] = est[b];
         }
       } else {
-        rcond_batch(batch, rc2);
+        rcond_batch(batch, rc2, nv_entry);
       }
     }
     bool retry = false;
     for (int b = 0; b < batch; ++b) {
       if (dead[b]) continue;
       const bool ok = info[b] == 0;
-      const bool wrong = cfg.chol_rcond_check && ok && rc2[b] < cfg.min_rcond;
+      const bool wrong = rcond_check && ok && rc2[b] < cfg.min_rcond;
       if (!ok || wrong) {
-        if (inc[b] > cfg.max_inc_choldiag) {
+        if (plain_chol_) {
+          dead[b] = 1;
+          out[b].status = 1;
+          out[b].message = "chol(): decomposition failed";
+        } else if (inc[b] > cfg.max_inc_choldiag) {
           dead[b] = 1;
           out[b].status = 1;
           out[b].message = "[ERROR] Exceed max numerical nugget (" + std::to_string(inc[b]) + " x 1e" +
@@ -431,8 +479,10 @@ void Engine::evaluate(int batch, const double* thetas, const double* factors, bo
   // ---- [F* y*] = L \ [F y], GLS, E*, SSE ----
   for (int b = 0; b < batch; ++b) {
     double* fy = dFY_ + (size_t)b * fystride_;
-    if (p > 0) LKG_CUDA(cudaMemcpyAsync(fy, dF_, sizeof(double) * n * p, cudaMemcpyDeviceToDevice, st_));
-    LKG_CUDA(cudaMemcpyAsync(fy + (size_t)n * p, dY_, sizeof(double) * n, cudaMemcpyDeviceToDevice, st_));
+    const size_t e = entry_design_[b];
+    if (p > 0)
+      LKG_CUDA(cudaMemcpyAsync(fy, dF_ + e * n * p, sizeof(double) * n * p, cudaMemcpyDeviceToDevice, st_));
+    LKG_CUDA(cudaMemcpyAsync(fy + (size_t)n * p, dY_ + e * n, sizeof(double) * n, cudaMemcpyDeviceToDevice, st_));
   }
   trsm_lower_left(dA_, lda_, mstride_, n, dDinv_, dFY_, n, fystride_, p + 1, batch, st_);
   tm.lap("F* = L \\ F, y* = L \\ y");
@@ -459,7 +509,7 @@ void Engine::evaluate(int batch, const double* thetas, const double* factors, bo
       wtw_lower(dW_, lda_, mstride_, n, dRinv_, lda_, mstride_, batch, st_);
     }
     tm.lap("R^-1 = L^-T * L^-1");
-    adjoint_sums(kernel_, n, d, dX_, 0, dtheta_, dfactor_, dxv_, n, dRinv_, lda_, mstride_, dpart_, dadj_, batch,
+    adjoint_sums(kernel_, n, d, dXb, xbs, dtheta_, dfactor_, dxv_, n, dRinv_, lda_, mstride_, dpart_, dadj_, batch,
                  st_);
     tm.lap("gradR computation [optimized]");
   }
@@ -478,6 +528,8 @@ void Engine::evaluate(int batch, const double* thetas, const double* factors, bo
     LKG_CUDA(cudaMemcpyAsync(adj.data(), dadj_, sizeof(double) * adj.size(), cudaMemcpyDeviceToHost, st_));
   }
   LKG_CUDA(cudaStreamSynchronize(st_));
+  if (slices_ > 0 && ozaki_tensor_path() && ozaki_tc_error_and_reset())
+    throw std::runtime_error("mixed path: a tensor-core digit product did not complete (timed out)");
   for (int b = 0; b < batch; ++b) {
     EvalOut& o = out[b];
     if (o.status == 0 && gls[b] != 0) {
@@ -487,7 +539,10 @@ void Engine::evaluate(int batch, const double* thetas, const double* factors, bo
     o.logdet = 2.0 * gram[(size_t)b * gram_stride_ + (p + 1) * (p + 1)];
     o.sse = sse[b];
     o.beta.assign(beta.begin() + (size_t)b * std::max(p, 1), beta.begin() + (size_t)b * std::max(p, 1) + p);
-    if (with_grad) o.adj.assign(adj.begin() + (size_t)b * nacc, adj.begin() + (size_t)(b + 1) * nacc);
+    if (with_grad) {
+      o.adj.assign(adj.begin() + (size_t)b * nacc, adj.begin() + (size_t)(b + 1) * nacc);
+      o.adj[2 * d + 3] -= (double)(n - nv_entry[b]);  // padded R^-1 diagonal entries are exactly 1
+    }
   }
 }
 

@@ -31,14 +31,22 @@ class Engine {
  public:
   // X: n x d column-major, y: n, F: n x p column-major (all host, copied to HBM).  batch_cap: max thetas per call.
   Engine(int kernel, int n, int d, int p, const double* X, const double* y, const double* F, int batch_cap);
+  // ndesign designs of one size class: design e has n_valid[e] <= n points, stored as the first rows of its n-row
+  // blocks X + e*n*d (n x d column-major, ld n), y + e*n, F + e*n*p, the remaining rows zero.  Every design's
+  // matrices are padded to n x n with the identity, which leaves L, the solves, the log-determinant and the
+  // adjoint sums of the valid block unchanged (the padded R^-1 diagonal is removed from D2).
+  Engine(int kernel, int n, int d, int p, int ndesign, const double* X, const double* y, const double* F,
+         const int* n_valid, int batch_cap);
   ~Engine();
   Engine(const Engine&) = delete;
   Engine& operator=(const Engine&) = delete;
 
   // thetas: batch x d (row b = theta of entry b); factors: batch (alpha, 1 for NoiseModel None).
   // The accepted factor L of every entry stays in HBM until the next call (see copy_model).
+  // designs (host, batch entries; required when the engine holds several designs): entry b evaluates design
+  // designs[b]; several entries may name the same design.
   void evaluate(int batch, const double* thetas, const double* factors, bool with_grad, std::vector<EvalOut>& out,
-                std::map<std::string, double>* bench = nullptr);
+                std::map<std::string, double>* bench = nullptr, const int* designs = nullptr);
 
   // Copies of the last evaluation's state for batch entry b (host, column-major):
   //   L (n x n lower, upper part zero), Fstar (n x p), ystar (n), Rstar (p x p upper), Estar (n)
@@ -46,10 +54,18 @@ class Engine {
                   std::vector<double>* Rstar, std::vector<double>* Estar) const;
 
   int n() const { return n_; }
+  int ndesign() const { return ndesign_; }
+  int n_valid(int e) const { return nvalid_[e]; }
   int d() const { return d_; }
   int p() const { return p_; }
   int kernel() const { return kernel_; }
   int capacity() const { return cap_; }
+  // plain factorisation of R with diagonal base_diag (NestedKriging's chol(R + jitter I)): no rcond check and no
+  // numerical-nugget retries; a failed factorisation gives status 1
+  void set_plain_chol(bool on, double base_diag = 1.0) {
+    plain_chol_ = on;
+    base_diag_ = base_diag;
+  }
   // 0 selects the FP64 path; 4..8 the mixed path with that many bf16 digit slices (7 ~ FP64-level products)
   void set_slices(int s);
   int slices() const { return slices_; }
@@ -59,7 +75,9 @@ class Engine {
   const double* dL(int b = 0) const { return dA_ + (size_t)b * mstride_; }
   const double* dDinv(int b = 0) const { return dDinv_ + (size_t)b * dstride_; }
   const double* dX() const { return dX_; }
+  const double* dX_design(int e) const { return dX_ + (size_t)e * n_ * d_; }
   int64_t lda() const { return lda_; }
+  int64_t mstride() const { return mstride_; }
   const double* dFY(int b = 0) const { return dFY_ + (size_t)b * fystride_; }
   const double* dEstar(int b = 0) const { return dEstar_ + (size_t)b * n_; }
   // solve L Z = B in place for entry b (B device, n x r, ldb)
@@ -68,9 +86,17 @@ class Engine {
  private:
   void ensure_grad_buffers();
   void ensure_mixed_buffers(bool with_grad);
-  void rcond_batch(int batch, std::vector<double>& rc2);  // rcond(L)^2 per entry, dtrcon('1') style estimate
+  // rcond(L)^2 per entry, dtrcon('1') style estimate on each entry's first nvb[b] rows / columns
+  void rcond_batch(int batch, std::vector<double>& rc2, const std::vector<int>& nvb);
 
   int kernel_, n_, d_, p_, cap_;
+  int ndesign_ = 1;
+  bool plain_chol_ = false;
+  double base_diag_ = 1.0;
+  std::vector<int> nvalid_;               // valid points per design
+  std::vector<int> entry_design_;         // design of each entry of the last evaluate
+  double* dXe_ = nullptr;                 // per-entry copy of its design's X (several designs only)
+  int* dnv_ = nullptr;                    // per-entry valid sizes on the device (several designs only)
   int slices_ = 0;
   void *dpanel_ = nullptr, *drowblk_ = nullptr, *dwfull_ = nullptr;
   int *dpanel_exp_ = nullptr, *drowblk_exp_ = nullptr, *dwfull_exp_ = nullptr;

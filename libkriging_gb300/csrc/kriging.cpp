@@ -77,8 +77,8 @@ std::vector<double> regression_matrix(RegressionModel r, const std::vector<doubl
 // ---------------------------------------------------------------------------------------------------------------
 // Random (Random.cpp:13-49): a process-wide mt19937 seeded with 123, re-seeded by each BFGS fit
 namespace {
-std::mt19937& rng_engine() {
-  static std::mt19937 e(123);
+std::mt19937& rng_engine() {  // per thread: every fit re-seeds it first, so concurrent fits draw as sequential ones
+  thread_local std::mt19937 e(123);
   return e;
 }
 unsigned int& rng_seed() {
@@ -306,6 +306,15 @@ double Kriging::logLikelihood() {
 
 // commit the model at (theta, alpha): one exact evaluation kept in the model engine (KModel -> m_T, m_M, ...)
 void Kriging::commit(const std::vector<double>& theta, double alpha) {
+  if (m_service) {  // batched with the other models' evaluations; no factor is kept (predict needs a plain commit)
+    const double factor = (m_noise_model == NoiseModel::Nugget) ? alpha : 1.0;
+    std::vector<EvalOut> out;
+    m_service->evaluate(m_service_design, 1, theta.data(), &factor, false, out);
+    if (out[0].status != 0) throw std::runtime_error(out[0].message);
+    m_model.reset();
+    m_last_commit = out[0];
+    return;
+  }
   if (!m_model)
     m_model = std::make_unique<Engine>(m_kernel, m_n, m_d, m_p, m_X.data(), m_y.data(), m_F.data(), 1);
   const double factor = (m_noise_model == NoiseModel::Nugget) ? alpha : 1.0;
@@ -474,7 +483,10 @@ void Kriging::fit(const std::vector<double>& y, const Mat& Xin, RegressionModel 
       theta_lower[j] = cfg.theta_lower_factor * maxdX[j];
       theta_upper[j] = cfg.theta_upper_factor * maxdX[j];
     }
-    if (cfg.variogram_bounds_heuristic && n > 0) {
+    // the reference applies the heuristic only when its n^2 x d difference matrix exists, which a light Vecchia fit
+    // never builds (Kriging.cpp:1610-1612, Optim.cpp:186)
+    const bool dX_built = !(vecchia && !m_vecchia_exact_commit);
+    if (cfg.variogram_bounds_heuristic && n > 0 && dX_built) {
       double wsum = 0.0;
       std::vector<double> steep(d, 0.0);
       std::vector<double> dx(d);
@@ -579,7 +591,7 @@ void Kriging::fit(const std::vector<double>& y, const Mat& Xin, RegressionModel 
       m_est_nugget = true;
     }
   }
-  if (!vecchia) ensure_engine(multistart);
+  if (!vecchia && !m_service) ensure_engine(multistart);
   if (vecchia) ensure_vecchia();
 
   // batched objective: -LL in gamma space (make_fit_objective, Kriging.cpp:1414-1470); the exact requests of one
@@ -597,7 +609,7 @@ void Kriging::fit(const std::vector<double>& y, const Mat& Xin, RegressionModel 
     }
     const int k = (int)dense.size();
     if (k == 0) return;
-    ensure_engine(std::max(k, multistart));
+    if (!m_service) ensure_engine(std::max(k, multistart));
     std::vector<double> th((size_t)k * d), fac(k);
     bool g = false;
     for (int b = 0; b < k; ++b) {
@@ -606,7 +618,10 @@ void Kriging::fit(const std::vector<double>& y, const Mat& Xin, RegressionModel 
       g = g || dense[b]->want_grad;
     }
     std::vector<EvalOut> out;
-    m_eval->evaluate(k, th.data(), fac.data(), g, out, nullptr);
+    if (m_service)
+      m_service->evaluate(m_service_design, k, th.data(), fac.data(), g, out);
+    else
+      m_eval->evaluate(k, th.data(), fac.data(), g, out, nullptr);
     m_evals += k;
     for (int b = 0; b < k; ++b) dense[b]->out = std::move(out[b]);
   });
@@ -835,9 +850,55 @@ std::vector<double> Kriging::z() const {
   return z;
 }
 
+// Kriging::predictVecchia (Kriging.cpp:950-1022): each point kriged on its m nearest observations, beta treated as
+// known; neighbour search, local factorisations and solves on the GPU
+std::tuple<std::vector<double>, std::vector<double>> Kriging::predictVecchia(const Mat& X_n, bool return_stdev,
+                                                                             int m) {
+  if (m_n == 0 || (int)m_theta.size() != m_d) throw std::runtime_error("predictVecchia: model is not fitted");
+  const int n = m_n, d = m_d, p = m_p, q = X_n.rows;
+  if (X_n.cols != d) throw std::invalid_argument("X_n should have the same number of columns as X");
+  if (m <= 0) m = (m_vecchia_m > 0) ? m_vecchia_m : 30;
+  m = std::min(m, n);
+  Mat Xnn;
+  Xnn.rows = q;
+  Xnn.cols = d;
+  Xnn.v.resize((size_t)q * d);
+  for (int j = 0; j < d; ++j)
+    for (int i = 0; i < q; ++i) Xnn(i, j) = (X_n(i, j) - m_centerX[j]) / m_scaleX[j];
+  int pn = 0;
+  std::vector<double> Fn = regression_matrix(m_regmodel, Xnn.v, q, d, &pn);
+  std::vector<double> resid(n);
+  for (int i = 0; i < n; ++i) {
+    double fb = 0.0;
+    for (int k = 0; k < p; ++k) fb += m_F[i + (size_t)k * n] * m_beta[k];
+    resid[i] = m_y[i] - fb;
+  }
+  std::vector<double> ar, ra;
+  vecchia_predict_gpu(m_kernel, n, d, m_X.data(), resid.data(), m_theta.data(), q, Xnn.v.data(), m, ar, ra);
+  std::vector<double> mean(q), sd;
+  for (int t = 0; t < q; ++t) {
+    double fb = 0.0;
+    for (int k = 0; k < p; ++k) fb += Fn[t + (size_t)k * q] * m_beta[k];
+    mean[t] = (fb + ar[t]) * m_scaleY + m_centerY;
+  }
+  if (return_stdev) {
+    sd.resize(q);
+    for (int t = 0; t < q; ++t) sd[t] = std::sqrt(m_sigma2 * std::max(0.0, 1.0 - ra[t])) * m_scaleY;
+  }
+  return {mean, sd};
+}
+
 std::tuple<std::vector<double>, std::vector<double>, Mat, Mat, Mat> Kriging::predict(const Mat& X_n, bool return_stdev,
                                                                                       bool return_cov,
                                                                                       bool return_deriv) {
+  if (m_vecchia_light) {  // Kriging.cpp:2242-2251: no exact factor, mean / stdev from the local predictor
+    if (return_cov || return_deriv)
+      throw std::runtime_error(
+          "predict: return_cov/return_deriv are not available on a light Vecchia fit "
+          "(refit with set_vecchia_exact_commit(true), or use predictVecchia)");
+    auto [mean, sd] = predictVecchia(X_n, return_stdev, 0);
+    return {mean, sd, Mat{}, Mat{}, Mat{}};
+  }
   if (m_is_empty || !m_model) throw std::runtime_error("predict: model is not fitted");
   if (X_n.cols != m_d)
     throw std::runtime_error("Predict locations have wrong dimension: " + std::to_string(X_n.cols) + " instead of " +

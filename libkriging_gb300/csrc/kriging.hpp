@@ -43,6 +43,15 @@ struct Parameters {  // KrigingParameters (Kriging.hpp:18-28)
   bool is_nugget_estim = true;
 };
 
+// Exact-objective evaluations shared by the fits of several models (the submodels of a NestedKriging): evaluate()
+// blocks until the service has run this model's k requests, batched with the other models' pending requests.
+class DenseService {
+ public:
+  virtual ~DenseService() = default;
+  virtual void evaluate(int design, int k, const double* thetas, const double* factors, bool with_grad,
+                        std::vector<EvalOut>& out) = 0;
+};
+
 class Kriging {
  public:
   enum class NoiseModel { None, Nugget };
@@ -75,6 +84,9 @@ class Kriging {
   // mean, stdev, cov, mean_deriv, stdev_deriv
   std::tuple<std::vector<double>, std::vector<double>, Mat, Mat, Mat> predict(const Mat& X_n, bool return_stdev,
                                                                                 bool return_cov, bool return_deriv);
+  // Kriging.hpp:163-173: local prediction on the m nearest observations (m = 0: vecchia_neighbors() or 30)
+  std::tuple<std::vector<double>, std::vector<double>> predictVecchia(const Mat& X_n, bool return_stdev = true,
+                                                                      int m = 0);
 
   // accessors (KrigingImpl.hpp:40-60, Kriging.hpp:94-97)
   const std::string& kernel() const { return m_covType; }
@@ -117,6 +129,12 @@ class Kriging {
   int precision() const { return m_slices; }
   // mixed-path bookkeeping of the last logLikelihoodFun: slices used (0 = FP64, also after a retreat)
   int last_slices() const { return m_last_slices; }
+  // route the fit's objective evaluations through a shared service (design = this model's index there); nullptr
+  // restores the model's own engine
+  void attach_service(DenseService* s, int design) {
+    m_service = s;
+    m_service_design = design;
+  }
 
  private:
   double loglik_from(const EvalOut& o, double extra_param, std::vector<double>* grad, int gdim) const;
@@ -145,6 +163,8 @@ class Kriging {
   int m_last_fit_starts = 0;
   int m_slices = 0;
   int m_last_slices = 0;
+  DenseService* m_service = nullptr;
+  int m_service_design = 0;
   // Vecchia state: maxmin order and neighbour sets (global row indices, -1 padded), GPU engine
   int m_vecchia_m = 0;
   std::vector<int32_t> m_vorder, m_vnbr;

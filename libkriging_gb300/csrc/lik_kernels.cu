@@ -41,7 +41,7 @@ template <int K, int DM, bool FAST>
 __global__ void __launch_bounds__(256) k_cov_lower(int n, int d, const double* __restrict__ X, int64_t xb,
                                                    const double* __restrict__ theta, const double* __restrict__ factor,
                                                    const double* __restrict__ diag, double* __restrict__ A,
-                                                   int64_t lda, int64_t mstride) {
+                                                   int64_t lda, int64_t mstride, const int* __restrict__ nvalid) {
   int I, J;
   lower_tile_of(blockIdx.x, I, J);
   const int64_t b = blockIdx.z;
@@ -56,6 +56,7 @@ __global__ void __launch_bounds__(256) k_cov_lower(int n, int d, const double* _
   if (t < DM) th[t] = (t < d) ? theta[b * d + t] : 1.0;
   __syncthreads();
   const double f = factor[b], dv = diag[b];
+  const int nv = nvalid ? nvalid[b] : n;  // rows/columns >= nv are padding: identity
   const int ri = t & 63, i = r0 + ri;
   if (i >= n) return;
   double* Ab = A + b * mstride;
@@ -69,7 +70,9 @@ __global__ void __launch_bounds__(256) k_cov_lower(int n, int d, const double* _
     const int cj = (t >> 6) + 4 * s, j = c0 + cj;
     if (j >= n || j > i) continue;
     double v;
-    if (j == i) {
+    if (i >= nv) {
+      v = (j == i) ? 1.0 : 0.0;
+    } else if (j == i) {
       v = dv;
     } else if (FAST) {
       double sum = 0.0, prod = 1.0;
@@ -335,38 +338,20 @@ __global__ void k_lower_colsum_abs(int n, const double* __restrict__ L, int64_t 
   if (lane == 0) colsum[b * n + j] = s;
 }
 
-template <template <int, int> class Launch, typename... Args>
-void dispatch_kd(int kernel, int d, Args&&... args) {
-  auto go = [&](auto kc) {
-    constexpr int KK = decltype(kc)::value;
-    if (d <= 4) Launch<KK, 4>::run(args...);
-    else if (d <= 8) Launch<KK, 8>::run(args...);
-    else if (d <= 16) Launch<KK, 16>::run(args...);
-    else if (d <= 32) Launch<KK, 32>::run(args...);
-    else throw std::invalid_argument("input dimension d > 32 is not supported by the GPU kernels");
-  };
-  switch (kernel) {
-    case KGAUSS: go(std::integral_constant<int, KGAUSS>{}); break;
-    case KEXP: go(std::integral_constant<int, KEXP>{}); break;
-    case KMATERN32: go(std::integral_constant<int, KMATERN32>{}); break;
-    case KMATERN52: go(std::integral_constant<int, KMATERN52>{}); break;
-    default: throw std::invalid_argument("Unsupported covariance kernel id");
-  }
-}
-
 template <int K, int DM>
 struct CovLowerLaunch {
   static void run(int n, int d, const double* X, int64_t xb, const double* theta, const double* factor,
-                  const double* diag, double* A, int64_t lda, int64_t mstride, int batch, bool fast, cudaStream_t st) {
+                  const double* diag, double* A, int64_t lda, int64_t mstride, int batch, bool fast, const int* nvalid,
+                  cudaStream_t st) {
     const int nb = ceil_div(n, T);
     const int64_t ntiles = (int64_t)nb * (nb + 1) / 2;
     LaunchTimer lt("k_cov_lower", st, 0.5 * n * (n - 1.0) * batch, 4.0 * n * (n + 1.0) * batch);
     if (fast)
       k_cov_lower<K, DM, true><<<dim3((unsigned)ntiles, 1, batch), 256, 0, st>>>(n, d, X, xb, theta, factor, diag, A,
-                                                                                  lda, mstride);
+                                                                                  lda, mstride, nvalid);
     else
       k_cov_lower<K, DM, false><<<dim3((unsigned)ntiles, 1, batch), 256, 0, st>>>(n, d, X, xb, theta, factor, diag,
-                                                                                   A, lda, mstride);
+                                                                                   A, lda, mstride, nvalid);
     LKG_LAUNCH("k_cov_lower");
   }
 };
@@ -398,9 +383,10 @@ struct AdjointLaunch {
 
 void cov_build_lower(int kernel, int n, int d, const double* X, int64_t x_bstride, const double* theta,
                      const double* factor, const double* diag, double* A, int64_t lda, int64_t mstride, int batch,
-                     cudaStream_t st, bool fast) {
+                     cudaStream_t st, bool fast, const int* nvalid) {
   if (n <= 0) return;
-  dispatch_kd<CovLowerLaunch>(kernel, d, n, d, X, x_bstride, theta, factor, diag, A, lda, mstride, batch, fast, st);
+  dispatch_kd<CovLowerLaunch>(kernel, d, n, d, X, x_bstride, theta, factor, diag, A, lda, mstride, batch, fast, nvalid,
+                              st);
 }
 
 void cov_cross(int kernel, int n_o, int q, int d, const double* Xo, const double* Xn, const double* theta,

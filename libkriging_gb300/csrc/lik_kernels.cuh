@@ -16,9 +16,12 @@ inline int adjoint_nacc(int d) { return 2 * d + 4; }
 // Lower triangle (and diagonal) of R = factor * C(X) with R_ii = diag[b], for each batch entry b (theta stride d).
 // X: n x d column-major (ldx = n), shared by the batch when x_bstride = 0.  fast = false evaluates the reference's
 // formulas in its operation order (FP64 path); fast = true the division- and log1p-free forms (mixed path).
+// nvalid (device, per entry, optional): entry b uses only its first nvalid[b] points; rows and columns beyond are
+// written as the identity, so that the factor, solves and log-determinant of the padded matrix equal those of the
+// valid block.
 void cov_build_lower(int kernel, int n, int d, const double* X, int64_t x_bstride, const double* theta,
                      const double* factor, const double* diag, double* A, int64_t lda, int64_t mstride, int batch,
-                     cudaStream_t st, bool fast = false);
+                     cudaStream_t st, bool fast = false, const int* nvalid = nullptr);
 
 // Rectangular cross-correlation R_on(i, j) = factor * C(Xo_i - Xn_j) (n_o x q, column-major, ldr = n_o);
 // coincident points (all |dx| <= eps) get 1.0 as in KrigingImpl::predict_impl.

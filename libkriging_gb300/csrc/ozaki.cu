@@ -267,16 +267,28 @@ void dispatch_oz(int S, const OzArgs& a, dim3 grid, cudaStream_t st) {
 
 }  // namespace
 
+// rows padded to a multiple of 128: the tcgen05 kernel stages 128-row tiles of A
 size_t split_plane_elems(int rows, int K, int S) {
-  const int rp = ceil_div(rows, 64) * 64, nc = ceil_div(K, OZ_CHUNK);
+  const int rp = ceil_div(rows, 128) * 128, nc = ceil_div(K, OZ_CHUNK);
   return (size_t)S * nc * rp * OZ_CHUNK;
 }
 
-size_t split_exp_elems(int rows, int K) { return (size_t)ceil_div(K, OZ_CHUNK) * ceil_div(rows, 64) * 64; }
+size_t split_exp_elems(int rows, int K) { return (size_t)ceil_div(K, OZ_CHUNK) * ceil_div(rows, 128) * 128; }
+
+int& oz_tc_flag() {
+  static int f = [] {
+    const char* e = std::getenv("LK_OZAKI_TC");
+    return e ? std::atoi(e) : 0;
+  }();
+  return f;
+}
+
+void ozaki_set_tensor_path(int tc) { oz_tc_flag() = tc ? 1 : 0; }
+int ozaki_tensor_path() { return oz_tc_flag(); }
 
 void ozaki_split(int rows, int K, const double* p, int64_t s_r, int64_t s_k, int64_t bstride, int batch, SplitBuf& out,
                  cudaStream_t st) {
-  out.rows_pad = ceil_div(rows, 64) * 64;
+  out.rows_pad = ceil_div(rows, 128) * 128;
   out.nchunk = ceil_div(K, OZ_CHUNK);
   if (out.plane_bstride == 0) out.plane_bstride = (int64_t)split_plane_elems(rows, K, out.S);
   if (out.exp_bstride == 0) out.exp_bstride = (int64_t)split_exp_elems(rows, K);
@@ -291,6 +303,10 @@ void ozaki_gemm(int M, int N, int c0, int c1, double alpha, const SplitBuf& SA, 
                 cudaStream_t st) {
   if (M <= 0 || N <= 0 || c1 <= c0) return;
   if (SA.S != SB.S) throw std::invalid_argument("ozaki_gemm: operands split with different slice counts");
+  if (oz_tc_flag() && a_row0 == 0 && b_row0 == 0) {
+    ozaki_gemm_tc(M, N, c0, c1, alpha, SA, SB, beta, C, ldc, c_batch, batch, lower_only, st);
+    return;
+  }
   OzArgs a{M, N, c0, c1, alpha, beta, SA, SB, a_row0, b_row0, C, ldc, c_batch, lower_only, 0};
   dim3 grid(ceil_div(M, 64), ceil_div(N, 64), batch);
   const double K = (double)(c1 - c0) * OZ_CHUNK;
@@ -302,6 +318,10 @@ void ozaki_gemm(int M, int N, int c0, int c1, double alpha, const SplitBuf& SA, 
 }
 
 void ozaki_wtw(int n, const SplitBuf& SW, double* C, int64_t ldc, int64_t cstride, int batch, cudaStream_t st) {
+  if (oz_tc_flag()) {
+    ozaki_wtw_tc(n, SW, C, ldc, cstride, batch, st);
+    return;
+  }
   const int nblk = ceil_div(n, 64);
   const int64_t ntiles = (int64_t)nblk * (nblk + 1) / 2;
   OzArgs a{n, n, 0, SW.nchunk, 1.0, 0.0, SW, SW, 0, 0, C, ldc, cstride, false, n};

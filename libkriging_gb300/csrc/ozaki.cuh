@@ -44,4 +44,14 @@ void ozaki_gemm(int M, int N, int c0, int c1, double alpha, const SplitBuf& SA, 
 // tile (I, J) sums chunks I .. nblk-1.
 void ozaki_wtw(int n, const SplitBuf& SW, double* C, int64_t ldc, int64_t cstride, int batch, cudaStream_t st);
 
+// The same two products on the tcgen05 tensor cores (ozaki_tc.cu): 128 x 64 output tiles, TMEM accumulators.
+// ozaki_gemm / ozaki_wtw route here when the tensor path is 1 (ozaki_set_tensor_path, or LK_OZAKI_TC=1).
+void ozaki_gemm_tc(int M, int N, int c0, int c1, double alpha, const SplitBuf& SA, const SplitBuf& SB, double beta,
+                   double* C, int64_t ldc, int64_t c_batch, int batch, bool lower_only, cudaStream_t st);
+void ozaki_wtw_tc(int n, const SplitBuf& SW, double* C, int64_t ldc, int64_t cstride, int batch, cudaStream_t st);
+void ozaki_set_tensor_path(int tc);  // 0: mma.sync kernels, 1: tcgen05 kernels
+int ozaki_tensor_path();
+// 1 if a tcgen05 CTA gave up waiting for its products since the last call (then reset); synchronous
+int ozaki_tc_error_and_reset();
+
 }  // namespace lkg

@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 
 #include "common.cuh"
 #include "config.hpp"
@@ -392,6 +393,165 @@ void launch_points(int kernel, const VPointArgs& a, cudaStream_t st) {
     default: throw std::invalid_argument("Unsupported covariance kernel id");
   }
 }
+
+// ---- predictVecchia (Kriging.cpp:950-1022): one warp per prediction point ----
+constexpr int PTILE = 256;  // observations per shared-memory tile of the neighbour scan
+
+struct VPredArgs {
+  int n, d, m, q;
+  const double *X, *resid, *theta, *Xq;
+  double num_nugget, min_rcond;
+  int rcond_check, max_inc;
+  double *ar, *ra;
+  int* status;
+};
+
+// m nearest observations by (squared distance, index) from a scan of all n in shared-memory tiles, then local
+// kriging: RN = C(N, N) + num_nugget I factored with the safe_chol_lower rules, a = RN^-1 r,
+// ar = a . (y_N - F_N beta), ra = r . a
+template <int K, int DM>
+__global__ void __launch_bounds__(WPB * 32) k_vecchia_predict(VPredArgs a) {
+  extern __shared__ double psm[];
+  double* tile = psm;  // [PTILE][DM]
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double* RN = psm + PTILE * DM + (size_t)w * (2 * 32 * LDP + 32 * DM + 64);
+  double* LN = RN + 32 * LDP;
+  double* xs = LN + 32 * LDP;  // [32][DM]
+  double* kd = xs + 32 * DM;   // [32] distances of the current m best
+  int* ki = reinterpret_cast<int*>(kd + 32);  // [32] their indices
+  const int t = blockIdx.x * WPB + w;
+  const bool active = t < a.q;
+  const int n = a.n, d = a.d, m = a.m;
+  double xq[DM];
+#pragma unroll
+  for (int k = 0; k < DM; ++k) xq[k] = (active && k < d) ? a.Xq[t + (int64_t)k * a.q] : 0.0;
+  int cnt = 0;
+  double thr = INFINITY;
+  int thri = 0x7fffffff;
+  for (int j0 = 0; j0 < n; j0 += PTILE) {
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < PTILE * DM; idx += WPB * 32) {
+      const int jj = idx % PTILE, k = idx / PTILE;
+      tile[jj * DM + k] = (k < d && j0 + jj < n) ? a.X[(j0 + jj) + (int64_t)k * n] : 0.0;
+    }
+    __syncthreads();
+    if (!active) continue;
+    for (int s0 = 0; s0 < PTILE; s0 += 32) {
+      const int j = j0 + s0 + lane;
+      double dj = INFINITY;
+      int ij = 0x7fffffff;
+      if (j < n) {
+        double ss = 0.0;
+#pragma unroll
+        for (int k = 0; k < DM; ++k)
+          if (k < d) {
+            const double dk = xq[k] - tile[(s0 + lane) * DM + k];
+            ss += dk * dk;
+          }
+        dj = ss;
+        ij = j;
+      }
+      const bool qual = (j < n) && (cnt < m || dj < thr || (dj == thr && ij < thri));
+      unsigned mask = __ballot_sync(FULL, qual);
+      while (mask) {
+        const int src = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const double cd = __shfl_sync(FULL, dj, src);
+        const int ci = __shfl_sync(FULL, ij, src);
+        if (lane == 0) {
+          const bool full = cnt >= m;
+          if (!full || cd < kd[m - 1] || (cd == kd[m - 1] && ci < ki[m - 1])) {
+            int pos = full ? m - 1 : cnt;
+            while (pos > 0 && (kd[pos - 1] > cd || (kd[pos - 1] == cd && ki[pos - 1] > ci))) {
+              kd[pos] = kd[pos - 1];
+              ki[pos] = ki[pos - 1];
+              --pos;
+            }
+            kd[pos] = cd;
+            ki[pos] = ci;
+          }
+        }
+        cnt = cnt < m ? cnt + 1 : m;
+        __syncwarp();
+      }
+      __syncwarp();
+      if (cnt >= m) {
+        thr = kd[m - 1];
+        thri = ki[m - 1];
+      }
+    }
+  }
+  if (!active) return;
+  __syncwarp();
+  const int mi = m;
+  const int nbv = (lane < mi) ? ki[lane] : -1;
+  double th[DM];
+#pragma unroll
+  for (int k = 0; k < DM; ++k) th[k] = (k < d) ? a.theta[k] : 1.0;
+  if (lane < mi)
+#pragma unroll
+    for (int k = 0; k < DM; ++k) xs[lane * DM + k] = (k < d) ? a.X[nbv + (int64_t)k * n] : 0.0;
+  __syncwarp();
+  double r = 0.0;
+  if (lane < mi) {
+    for (int b = 0; b < mi; ++b) {
+      double c;
+      if (b == lane) {
+        c = 1.0 + a.num_nugget;
+      } else {
+        double s = 0.0;
+#pragma unroll
+        for (int k = 0; k < DM; ++k)
+          if (k < d) s += cov_term<K>(xs[lane * DM + k] - xs[b * DM + k], th[k]);
+        c = cov_from_sum<K>(s);
+      }
+      RN[lane * LDP + b] = c;
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < DM; ++k)
+      if (k < d) s += cov_term<K>(xs[lane * DM + k] - xq[k], th[k]);
+    r = cov_from_sum<K>(s);
+  }
+  __syncwarp();
+  int inc = 0;
+  for (;;) {
+    if (lane < mi)
+      for (int b = 0; b < mi; ++b) LN[lane * LDP + b] = RN[lane * LDP + b];
+    __syncwarp();
+    const bool ok = wchol(LN, mi, lane);
+    bool wrong = false;
+    if (ok && a.rcond_check) wrong = wrcond2(LN, mi, lane) < a.min_rcond;
+    if (ok && !wrong) break;
+    if (inc > a.max_inc || !(a.num_nugget > 0.0)) {
+      if (lane == 0) a.status[t] = -1;
+      return;
+    }
+    __syncwarp();
+    if (lane < mi) RN[lane * LDP + lane] += a.num_nugget * pow(10.0, (double)inc);
+    inc++;
+    __syncwarp();
+  }
+  const double av = wsolve_upper_t(LN, wsolve_lower(LN, r, mi, lane), mi, lane);
+  const double rs = (lane < mi) ? a.resid[nbv] : 0.0;
+  const double ar = wsum(av * rs), ra = wsum(r * av);
+  if (lane == 0) {
+    a.ar[t] = ar;
+    a.ra[t] = ra;
+    a.status[t] = inc;
+  }
+}
+
+template <int K, int DM>
+struct VPredLaunch {
+  static void run(const VPredArgs& a, cudaStream_t st) {
+    const size_t smem = ((size_t)PTILE * DM + (size_t)WPB * (2 * 32 * LDP + 32 * DM + 64)) * sizeof(double);
+    LKG_CUDA(cudaFuncSetAttribute(k_vecchia_predict<K, DM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    LaunchTimer lt("k_vecchia_predict", st, 3.0 * a.q * (double)a.n * a.d, 8.0 * a.n * a.d);
+    k_vecchia_predict<K, DM><<<ceil_div(a.q, WPB), WPB * 32, smem, st>>>(a);
+    LKG_LAUNCH("k_vecchia_predict");
+  }
+};
 
 template <typename P>
 void valloc(P** p, size_t count) {
@@ -821,6 +981,66 @@ void vecchia_sets_gpu(int n, int d, const double* X, int m, int32_t* order, int3
   cudaFree(dorder);
   cudaFree(dnbr);
   cudaStreamDestroy(st);
+}
+
+void vecchia_predict_gpu(int kernel, int n, int d, const double* X, const double* resid, const double* theta, int q,
+                         const double* Xq, int m, std::vector<double>& ar, std::vector<double>& ra) {
+  if (d < 1 || d > 8) throw std::invalid_argument("predictVecchia on the GPU supports d <= 8");
+  if (m < 1 || m > VECCHIA_MAX_M || m > n) throw std::invalid_argument("predictVecchia on the GPU supports m <= 32");
+  ar.assign(q, 0.0);
+  ra.assign(q, 0.0);
+  if (q <= 0) return;
+  const Config& cfg = config();
+  cudaStream_t st;
+  LKG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  double *dX = nullptr, *dR = nullptr, *dth = nullptr, *dXq = nullptr, *dar = nullptr, *dra = nullptr;
+  int* dst = nullptr;
+  auto cleanup = [&]() {
+    for (double* p : {dX, dR, dth, dXq, dar, dra})
+      if (p) cudaFree(p);
+    if (dst) cudaFree(dst);
+    cudaStreamDestroy(st);
+  };
+  std::vector<int> status(q);
+  try {
+    valloc(&dX, (size_t)n * d);
+    valloc(&dR, n);
+    valloc(&dth, d);
+    valloc(&dXq, (size_t)q * d);
+    valloc(&dar, q);
+    valloc(&dra, q);
+    valloc(&dst, q);
+    LKG_CUDA(cudaMemcpyAsync(dX, X, sizeof(double) * (size_t)n * d, cudaMemcpyHostToDevice, st));
+    LKG_CUDA(cudaMemcpyAsync(dR, resid, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    LKG_CUDA(cudaMemcpyAsync(dth, theta, sizeof(double) * d, cudaMemcpyHostToDevice, st));
+    LKG_CUDA(cudaMemcpyAsync(dXq, Xq, sizeof(double) * (size_t)q * d, cudaMemcpyHostToDevice, st));
+    VPredArgs a{n, d, m, q, dX, dR, dth, dXq, cfg.num_nugget, cfg.min_rcond, cfg.chol_rcond_check ? 1 : 0,
+                cfg.max_inc_choldiag, dar, dra, dst};
+    auto go = [&](auto kc) {
+      constexpr int KK = decltype(kc)::value;
+      if (d <= 4) VPredLaunch<KK, 4>::run(a, st);
+      else VPredLaunch<KK, 8>::run(a, st);
+    };
+    switch (kernel) {
+      case KGAUSS: go(std::integral_constant<int, KGAUSS>{}); break;
+      case KEXP: go(std::integral_constant<int, KEXP>{}); break;
+      case KMATERN32: go(std::integral_constant<int, KMATERN32>{}); break;
+      case KMATERN52: go(std::integral_constant<int, KMATERN52>{}); break;
+      default: throw std::invalid_argument("Unsupported covariance kernel id");
+    }
+    LKG_CUDA(cudaMemcpyAsync(ar.data(), dar, sizeof(double) * q, cudaMemcpyDeviceToHost, st));
+    LKG_CUDA(cudaMemcpyAsync(ra.data(), dra, sizeof(double) * q, cudaMemcpyDeviceToHost, st));
+    LKG_CUDA(cudaMemcpyAsync(status.data(), dst, sizeof(int) * q, cudaMemcpyDeviceToHost, st));
+    LKG_CUDA(cudaStreamSynchronize(st));
+  } catch (...) {
+    cleanup();
+    throw;
+  }
+  cleanup();
+  for (int t = 0; t < q; ++t)
+    if (status[t] < 0)
+      throw std::runtime_error("[ERROR] Exceed max numerical nugget (" + std::to_string(cfg.max_inc_choldiag + 1) +
+                               " x 1e" + std::to_string(std::log10(cfg.num_nugget)) + ") added to force chol matrix");
 }
 
 }  // namespace lkg

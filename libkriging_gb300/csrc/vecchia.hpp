@@ -54,4 +54,11 @@ class VecchiaEngine {
 // (squared distance, index).  X n x d column-major on the host; outputs host arrays order[n], nbr[n * m].
 void vecchia_sets_gpu(int n, int d, const double* X, int m, int32_t* order, int32_t* nbr);
 
+// predictVecchia's local kriging (Kriging.cpp:950-1022) on the GPU: for each of the q points of Xq (q x d
+// column-major, normalised), the m nearest of the n observations X (n x d column-major) by (squared distance,
+// index), RN = C(N, N) + num_nugget I under the safe_chol_lower rules, a = RN^-1 r; ar[t] = a . resid_N and
+// ra[t] = r . a (resid = y - F beta, n).  Throws the reference's error when a factorisation exceeds the retries.
+void vecchia_predict_gpu(int kernel, int n, int d, const double* X, const double* resid, const double* theta, int q,
+                         const double* Xq, int m, std::vector<double>& ar, std::vector<double>& ra);
+
 }  // namespace lkg

@@ -54,8 +54,19 @@ class Kriging:
             if not self._h:
                 raise _lib.LibKrigingError(_lib.last_error())
 
+    @classmethod
+    def _borrowed(cls, handle, owner):
+        """A view of a Kriging owned by another object (a NestedKriging submodel): never deleted from here."""
+        k = cls.__new__(cls)
+        k._h = handle
+        k._owner = owner
+        return k
+
     def __del__(self):
         h = getattr(self, "_h", None)
+        if getattr(self, "_owner", None) is not None:
+            self._h = None
+            return
         if h:
             try:
                 _lib.load().lkg_kriging_delete(h)
@@ -140,6 +151,16 @@ class Kriging:
         return mean, sd, cov, None, None
 
     # ---- Vecchia (Kriging.hpp:145-173) ----
+    def predictVecchia(self, X, return_stdev=True, m=0):
+        """Kriging::predictVecchia: each point kriged on its m nearest observations -> (mean, stdev)."""
+        X = _as_X(X)
+        q, d = X.shape
+        mean = np.zeros(q)
+        sd = np.zeros(q) if return_stdev else None
+        check(_lib.load().lkg_kriging_predict_vecchia(self._h, ptr(X), q, d, int(bool(return_stdev)), int(m),
+                                                      ptr(mean), ptr(sd)))
+        return mean, (sd if return_stdev else np.zeros(0))
+
     def logLikelihoodVecchiaFun(self, theta, return_grad=False):
         t = np.ascontiguousarray(np.asarray(theta, dtype=np.float64).reshape(-1))
         v = ctypes.c_double()

@@ -69,6 +69,107 @@ def fit_multistart_sharded(make_model, y, X, thetas, regmodel="constant", normal
     return best, idx, obj
 
 
+def balanced_bins(sizes, world):
+    """Size-balanced bins of the groups for `world` ranks: greedy longest-processing-time by n_g^3 (the
+    factorisation cost), ties to the lowest rank; group indices in each bin ascending."""
+    order = sorted(range(len(sizes)), key=lambda g: (-float(sizes[g]) ** 3, g))
+    load = [0.0] * world
+    bins = [[] for _ in range(world)]
+    for g in order:
+        r = min(range(world), key=lambda q: (load[q], q))
+        bins[r].append(g)
+        load[r] += float(sizes[g]) ** 3
+    return [sorted(b) for b in bins]
+
+
+def fit_nested_sharded(make_nested, y, X, groups, regmodel="constant", optim="BFGS", objective="LL",
+                       parameters=None, group=None):
+    """NestedKriging fit with its groups sharded over the ranks of `group` (NestedKriging.cpp:171-332):
+
+    1. every rank fits the submodels of its size-balanced bin of groups (make_nested() -> a fresh
+       libkriging_gb300.NestedKriging; fit_groups on the bin's rows),
+    2. one all-reduce of (sum n_g log theta_g, sum n_g sigma2_g, sum n_g beta0_g, sum n_g) gives the common prior
+       of unify_hyperparameters,
+    3. every rank refits its bin at that prior (optim = "none", theta / sigma2 / beta fixed).
+
+    Returns (local NestedKriging, global indices of its groups, (theta, sigma2, beta0)).  PoE-family predictions
+    then combine per-rank partial sums (predict_poe_sharded); NK aggregation needs every pair of groups and is not
+    sharded."""
+    import torch.distributed as dist
+    rank, world = dist.get_rank(group), dist.get_world_size(group)
+    X = np.asarray(X, dtype=np.float64)
+    y = np.asarray(y, dtype=np.float64)
+    bins = balanced_bins([len(g) for g in groups], world)
+    mine = bins[rank]
+    rows = np.concatenate([np.asarray(groups[g]) for g in mine]) if mine else np.zeros(0, dtype=np.int64)
+    local_groups, start = [], 0
+    for g in mine:
+        local_groups.append(np.arange(start, start + len(groups[g])))
+        start += len(groups[g])
+    d = X.shape[1]
+    sums = np.zeros(d + 3)
+    nk = None
+    if mine:
+        nk = make_nested()
+        nk.fit_groups(y[rows], X[rows], local_groups, regmodel, optim, objective, parameters)
+        th, s2, b0 = nk.group_estimates()
+        for i, g in enumerate(mine):
+            ng = float(len(groups[g]))
+            sums[:d] += ng * np.log(th[i])
+            sums[d] += ng * s2[i]
+            sums[d + 1] += ng * b0[i]
+            sums[d + 2] += ng
+    tot = allreduce_sums(sums, group)
+    n = tot[d + 2]
+    theta = np.exp(tot[:d] / n)
+    sigma2 = tot[d] / n
+    beta0 = tot[d + 1] / n
+    if nk is not None:
+        fixed = {"theta": theta.reshape(1, -1), "is_theta_estim": False, "sigma2": sigma2, "is_sigma2_estim": False}
+        if regmodel == "constant":
+            fixed.update(beta=np.array([beta0]), is_beta_estim=False)
+        nk.fit_groups(y[rows], X[rows], local_groups, regmodel, "none", "LL", fixed)
+    return nk, mine, (theta, sigma2, beta0)
+
+
+def predict_poe_sharded(nk_local, Xn, aggregation, sigma2, p_total, group=None):
+    """PoE / gPoE / BCM / rBCM prediction (NestedKriging.cpp:364-422) from the submodels spread over the ranks: each
+    rank adds its submodels' terms, one all-reduce combines them."""
+    q = np.asarray(Xn).shape[0]
+    tiny = 1e-12
+    acc = np.zeros((4, q))  # sum 1/v, sum mu/v, sum beta/v, sum beta
+    acc_bmu = np.zeros(q)   # sum beta mu / v
+    if nk_local is not None:
+        for g in range(nk_local.nb_groups()):
+            mu, sd, _, _, _ = nk_local.submodel(g).predict(Xn, True, False, False)
+            v = sd * sd + tiny
+            acc[0] += 1.0 / v
+            acc[1] += mu / v
+            b = 0.5 * (np.log(sigma2) - np.log(v))
+            acc[2] += b / v
+            acc[3] += b
+            acc_bmu += b * mu / v
+    tot = allreduce_sums(np.concatenate([acc.ravel(), acc_bmu]), group)
+    s_iv, s_muv, s_bv, s_b = tot[:4 * q].reshape(4, q)
+    s_bmu = tot[4 * q:]
+    p = float(p_total)
+    if aggregation == "PoE":
+        prec = s_iv
+        mean = s_muv / prec
+    elif aggregation == "gPoE":
+        prec = s_iv / p
+        mean = (s_muv / p) / prec
+    elif aggregation == "BCM":
+        prec = np.clip(s_iv - (p - 1.0) / sigma2, tiny, np.inf)
+        mean = s_muv / prec
+    elif aggregation == "rBCM":
+        prec = np.clip(s_bv + (1.0 - s_b) / sigma2, tiny, np.inf)
+        mean = s_bmu / prec
+    else:
+        raise ValueError("sharded prediction supports PoE, gPoE, BCM and rBCM")
+    return mean, np.sqrt(np.clip(1.0 / prec, 0.0, np.inf))
+
+
 def allreduce_sums(values, group=None):
     """Sum a small float64 vector over the ranks (NestedKriging's unify step: sum w log theta, w sigma2, w beta0)."""
     import torch

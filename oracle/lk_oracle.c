@@ -104,6 +104,18 @@ void ora_build_R(int kernel, int n, int d, const double* X, const double* theta,
   for (int i = 0; i < n; i++) R[i + (size_t)i * n] = diag ? diag[i] : 1.0;
 }
 
+/* NestedKriging::corrMat (NestedKriging.cpp:101-115): R(i, j) = Cov(x1_i - x2_j; theta), no coincidence rule.
+ * X1 n1 x d, X2 n2 x d, R n1 x n2, all column-major. */
+void ora_cov_cross(int kernel, int n1, int n2, int d, const double* X1, const double* X2, const double* theta,
+                   double* R) {
+  double dx[64];
+  for (int j = 0; j < n2; j++)
+    for (int i = 0; i < n1; i++) {
+      for (int k = 0; k < d; k++) dx[k] = X1[i + (size_t)k * n1] - X2[j + (size_t)k * n2];
+      R[i + (size_t)j * n1] = ora_cov(kernel, dx, theta, d);
+    }
+}
+
 /* Rows [i0, i1) of the cholCov pair loop (LinearAlgebra.cpp:150-155), serial like the reference: the timed sample of
  * the CPU baseline.  Writes both triangles of those rows. */
 void ora_build_R_rows(int kernel, int n, int d, const double* X, const double* theta, int i0, int i1, double* R) {

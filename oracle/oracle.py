@@ -70,6 +70,8 @@ def lib():
         L.ora_dlncov.argtypes = [ctypes.c_int, dp, dp, ctypes.c_int, dp]
         L.ora_build_R.restype = None
         L.ora_build_R.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, ctypes.c_double, dp, dp]
+        L.ora_cov_cross.restype = None
+        L.ora_cov_cross.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp, dp]
         L.ora_grad_terms.restype = None
         L.ora_grad_terms.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp, dp, dp, dp, dp]
         L.ora_build_R_rows.restype = None
@@ -158,6 +160,15 @@ def build_R(kernel: str, X, theta, factor: float = 1.0, diag=None):
     return R
 
 
+def cov_cross(kernel: str, X1, X2, theta):
+    """NestedKriging::corrMat (NestedKriging.cpp:101-115): Cov(x1_i - x2_j), n1 x n2, no coincidence rule."""
+    X1, X2 = _colmajor(X1), _colmajor(X2)
+    theta = np.ascontiguousarray(theta, dtype=np.float64)
+    R = np.empty((X1.shape[0], X2.shape[0]), order="F")
+    lib().ora_cov_cross(KERNELS[kernel], X1.shape[0], X2.shape[0], X1.shape[1], _dp(X1), _dp(X2), _dp(theta), _dp(R))
+    return R
+
+
 # --------------------------------------------------------------------------------------------------------------
 # dense linear algebra (Armadillo -> LAPACK)
 # --------------------------------------------------------------------------------------------------------------
@@ -188,6 +199,33 @@ def safe_chol_lower(A, cfg: Config = CONFIG):
             inc += 1
             continue
         return np.asfortranarray(L), inc
+
+
+def predict_vecchia(kernel, X, y, F, beta, theta, sigma2, Xn, Fn, m, cfg: Config = CONFIG):
+    """Kriging::predictVecchia (Kriging.cpp:950-1022) in normalised units: for each row of Xn the m nearest rows
+    of X (ties of the squared distance broken by the lower index), RN = C(N, N) + num_nugget I through
+    safe_chol_lower, a = RN^-1 r; mean = Fn beta + a . (y_N - F_N beta), stdev = sqrt(sigma2 max(0, 1 - r . a))."""
+    X = np.asarray(X, dtype=np.float64)
+    Xn = np.atleast_2d(np.asarray(Xn, dtype=np.float64))
+    n = X.shape[0]
+    m = min(m, n)
+    resid = y - F @ beta
+    mean = np.empty(Xn.shape[0])
+    sd = np.empty(Xn.shape[0])
+    for t in range(Xn.shape[0]):
+        s = np.zeros(n)
+        for k in range(X.shape[1]):
+            dk = Xn[t, k] - X[:, k]
+            s = s + dk * dk
+        Ni = np.lexsort((np.arange(n), s))[:m]
+        RN = cov_cross(kernel, X[Ni], X[Ni], theta)
+        RN[np.diag_indices(m)] = 1.0 + cfg.num_nugget
+        r = cov_cross(kernel, X[Ni], Xn[t:t + 1], theta)[:, 0]
+        LN, _ = safe_chol_lower(RN, cfg)
+        a = solve_upper_t(LN, solve_lower(LN, r.reshape(-1, 1)))[:, 0]
+        mean[t] = Fn[t] @ beta + a @ resid[Ni]
+        sd[t] = np.sqrt(sigma2 * max(0.0, 1.0 - r @ a))
+    return mean, sd
 
 
 def solve_lower(L, B):
@@ -401,7 +439,8 @@ class OracleKriging:
         return ll, grad
 
     # KrigingImpl.cpp:145-251, Kriging.cpp:2240-2285 (mean and stdev)
-    def predict(self, Xn, theta, beta, sigma2, alpha=1.0, return_stdev=True):
+    def predict(self, Xn, theta, beta, sigma2, alpha=1.0, return_stdev=True, fixed_beta=False):
+        """fixed_beta: beta is a given trend (is_beta_estim = false), so z = L \\ (y - F beta) (KrigingImpl.cpp:116)."""
         Xn = np.atleast_2d(np.asarray(Xn, dtype=np.float64))
         Xn_n = (Xn - self.centerX) / self.scaleX
         Fn = regression_matrix(self.regmodel, Xn_n)
@@ -415,7 +454,7 @@ class OracleKriging:
                     R_on[i, j] = 1.0
                 else:
                     R_on[i, j] = cov(self.kernel, dij, theta) * alpha
-        z = m.Estar
+        z = m.ystar - m.Fstar @ np.asarray(beta, dtype=np.float64) if fixed_beta else m.Estar
         Rs = solve_lower(m.L, R_on)
         yhat = Fn @ beta + Rs.T @ z
         yhat = self.centerY + self.scaleY * yhat

@@ -40,7 +40,7 @@ def test_fit_bfgs10_beats_grid(gpu_lib):
     for t1 in grid:
         for t2 in grid:
             try:
-                ll, _ = kg.logLikelihoodFun(np.array([t1, t2]), False)
+                ll, _, _ = kg.logLikelihoodFun(np.array([t1, t2]), False)
             except RuntimeError:
                 continue  # no factorisation within the nugget retries: the point has no LL
             best = max(best, ll)
@@ -58,13 +58,16 @@ def test_fit_config1(gpu_lib):
     k = gpu_lib.Kriging(y, X, "matern5_2", "constant", False, "BFGS", "LL", {"theta": np.full((1, 3), 0.5)})
     th = k.theta()
     ora = O.OracleKriging(y, X, "matern5_2")
-    ll_g = ora.log_likelihood(th, False)[0]
-    ll_0 = ora.log_likelihood(np.full(3, 0.5), False)[0]
+    # at theta_hat rcond(L)^2 sits at min_rcond, where the GPU's dlacn2 estimate and LAPACK's dtrcon can take the
+    # nugget-retry branch differently: LL values are compared within the GPU implementation only
+    ll_g, _, _ = k.logLikelihoodFun(th, False)
+    ll_0, _, _ = k.logLikelihoodFun(np.full(3, 0.5), False)
+    assert ll_0 == pytest.approx(ora.log_likelihood(np.full(3, 0.5), False)[0], rel=1e-10)
     assert ll_g > ll_0 + 1e-3 * abs(ll_0), (th, ll_g, ll_0)
     lo, hi = O.theta_bounds(ora.X, ora.y)
     assert np.all(th >= lo * (1 - 1e-12)) and np.all(th <= hi * (1 + 1e-12))
     # the committed model is self-consistent (its LL is the objective's value at theta_hat) and interpolates
-    assert abs(k.logLikelihood() - ll_g) < 1e-3 * abs(ll_g)
+    assert abs(k.logLikelihood() - ll_g) < 1e-10 * abs(ll_g)
     mean, sd, _, _, _ = k.predict(X[:25], True, False, False)
     assert np.max(np.abs(mean - y[:25])) < 1e-4
     mean, sd, _, _, _ = k.predict(Xn[:100], True, False, False)

@@ -93,3 +93,47 @@ def test_vecchia_rejects_nugget(gpu_lib):
     k = gpu_lib.Kriging("matern5_2", "nugget")
     with pytest.raises(gpu_lib.LibKrigingError, match="LLVecchia objective not supported"):
         k.fit(y, X, "constant", False, "BFGS", "LLVecchia(10)", {})
+
+
+@pytest.mark.parametrize("kernel,reg,normalize,m", [("matern5_2", "constant", False, 20), ("gauss", "linear", True, 12),
+                                                    ("exp", "constant", False, 32)])
+def test_predict_vecchia_vs_oracle(gpu_lib, kernel, reg, normalize, m):
+    """Kriging::predictVecchia (Kriging.cpp:950-1022): mean 1e-10, stdev 1e-8 relative to the restatement."""
+    X, y = _data(1500, 2, 3)
+    th = np.array([0.2, 0.3])
+    k = gpu_lib.Kriging(kernel)
+    k.fit(y, X, reg, normalize, "none", "LL", {"theta": th.reshape(1, -1)})
+    Xn = np.random.default_rng(4).uniform(size=(200, 2))
+    mean, sd = k.predictVecchia(Xn, True, m)
+    ora = O.OracleKriging(y, X, kernel, regmodel=reg, normalize=normalize)
+    Xnn = (Xn - ora.centerX) / ora.scaleX
+    Fn = O.regression_matrix(reg, Xnn)
+    # the model's beta, theta and sigma2 are held in normalised units, as the reference's accessors return them
+    mo, so = O.predict_vecchia(kernel, ora.X, ora.y, ora.F, k.beta(), k.theta(), k.sigma2(), Xnn, Fn, m)
+    assert rel_err(mean, ora.centerY + ora.scaleY * mo) < 1e-10
+    assert rel_err(sd, ora.scaleY * so) < 1e-8
+
+
+def test_predict_vecchia_all_neighbours_is_kriging_mean(gpu_lib):
+    """With every observation in the neighbourhood the local predictor is the kriging mean (up to num_nugget)."""
+    X, y = _data(30, 2, 5)
+    k = gpu_lib.Kriging("matern5_2")
+    k.fit(y, X, "constant", False, "none", "LL", {"theta": np.array([[0.3, 0.3]])})
+    Xn = np.random.default_rng(6).uniform(size=(50, 2))
+    mv, _ = k.predictVecchia(Xn, True, 30)
+    mp, _, _, _, _ = k.predict(Xn, True, False, False)
+    assert np.max(np.abs(mv - mp)) < 1e-6
+
+
+def test_light_fit_predict_routes_to_predict_vecchia(gpu_lib):
+    """Kriging.cpp:2242-2251: after a light Vecchia fit predict gives predictVecchia's mean and stdev."""
+    X, y = _data(2000, 2, 8)
+    k = gpu_lib.Kriging("gauss")
+    k.set_vecchia_exact_commit(False)
+    k.fit(y, X, "constant", False, "BFGS", "LLVecchia(15)", {})
+    Xn = np.random.default_rng(9).uniform(size=(100, 2))
+    m1, s1, _, _, _ = k.predict(Xn, True, False, False)
+    m2, s2 = k.predictVecchia(Xn, True, 0)
+    assert np.array_equal(m1, m2) and np.array_equal(s1, s2)
+    with pytest.raises(Exception, match="light Vecchia fit"):
+        k.predict(Xn, True, True, False)
