@@ -91,6 +91,23 @@ int lkg_vecchia_sets(int n, int d, const double* X, int m, int* order_out, int* 
 int lkg_kriging_predict_vecchia(void* ptr, const double* X_n, int q, int d, int return_stdev, int m,
                                 double* mean_out, double* stdev_out);
 
+/* lkg_vecchia_sets_noalloc: no counterpart in the reference (make_vecchia_sets is internal to Kriging.cpp there).
+ * The same order and neighbour sets as lkg_vecchia_sets, bit for bit, for callers that may not allocate memory:
+ * code that runs inside another allocator's budget (a caching allocator, a fixed memory pool), a serving loop that
+ * cannot take the device-wide synchronisation a cudaFree implies, or code that queues work on a stream it does not
+ * own.  X (n x d column-major), order (n) and nbr (n x m row-major, -1 padded) are caller-owned device (or managed)
+ * buffers of the current device; stream is a cudaStream_t (NULL: the legacy default stream).  Every kernel is
+ * queued on that stream and nothing is synchronised: the outputs are ready when the stream reaches that point.
+ * The intermediates live in one fixed device array of this library, 2^20 doubles (8 MiB) per device, so calls are
+ * limited to n * (2 d + 1) + 768 <= 1048576 (d = 3: n <= 149686; d = 8: n <= 61635), with 1 <= d <= 8 and
+ * 0 <= m <= 32; larger or malformed calls fail with -1 and a message before any work is queued.  Nothing in that
+ * array has to start at zero: every word is written before it is read within a call.  The first call on each device
+ * resolves the array's address (cudaGetSymbolAddress, which may load the module) and should come before any
+ * stream capture begins.  Calls that overlap on one device -- from two threads, or on two streams that are not
+ * ordered with each other -- share the array and race: order them.  On success no memory is allocated, host or
+ * device; on failure the message is stored like every other entry point's. */
+int lkg_vecchia_sets_noalloc(int n, int d, const double* X, int m, int* order, int* nbr, void* stream);
+
 /* getters, libkriging_c.h:141-166 */
 const char* lkg_kriging_kernel(void* ptr);
 const char* lkg_kriging_optim(void* ptr);

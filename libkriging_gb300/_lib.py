@@ -92,6 +92,7 @@ _SIGS = {
     "lkg_kriging_predict_vecchia": (_i, [_vp, _dp, _i, _i, _i, _i, _dp, _dp]),
     "lkg_set_tensor_path": (_i, [_i]),
     "lkg_get_tensor_path": (_i, []),
+    "lkg_vecchia_sets_noalloc": (_i, [_i, _i, _vp, _i, _vp, _vp, _vp]),
     "lkg_nested_kriging_new_fit": (_vp, [_dp, _i, _dp, _i, _i, _cp, _i, _cp, _cp, _i, _vp, _i, _cp, _cp, _cp, _dp, _i,
                                          _dp, _i, _i, _dp, _i, _i]),
     "lkg_nested_kriging_delete": (None, [_vp]),

@@ -502,6 +502,15 @@ int lkg_vecchia_sets(int n, int d, const double* X, int m, int* order_out, int* 
   CATCH_RETURN
 }
 
+int lkg_vecchia_sets_noalloc(int n, int d, const double* X, int m, int* order, int* nbr, void* stream) {
+  const char* err = lkg::vecchia_sets_noalloc(n, d, X, m, order, nbr, static_cast<cudaStream_t>(stream));
+  if (err) {
+    g_last_error = err;  // the only allocation, and only on failure
+    return -1;
+  }
+  return 0;
+}
+
 }  // extern "C"
 
 // ---- NestedKriging (libkriging_c.h:394-455, libkriging_c.cpp:1663-1850) ----

@@ -11,6 +11,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
+#include <mutex>
 
 #include "common.cuh"
 #include "config.hpp"
@@ -1041,6 +1043,148 @@ void vecchia_predict_gpu(int kernel, int n, int d, const double* X, const double
     if (status[t] < 0)
       throw std::runtime_error("[ERROR] Exceed max numerical nugget (" + std::to_string(cfg.max_inc_choldiag + 1) +
                                " x 1e" + std::to_string(std::log10(cfg.num_nugget)) + ") added to force chol matrix");
+}
+
+// ---------------------------------------------------------------------------------------------------------------
+// conditioning sets with no allocation: the intermediates of vecchia_sets_gpu (point-major X, ordered X, running
+// minimum distances, block maxima) live in one fixed device array.  Layout in doubles, for n points in d dims:
+//   [0, nd) point-major X | [nd, 2nd) X in maxmin order | [2nd, 2nd + n) min squared distances |
+//   512 doubles of block maxima (two buffers of <= 256) | 256 doubles holding their 2 x 256 int indices
+// Every word is written before it is read within one call, so nothing has to start at zero and nothing is carried
+// from one call to the next.
+static __device__ __align__(256) double g_sets_scratch[SETS_SCRATCH_DOUBLES];
+
+namespace {
+
+constexpr int SETS_MAX_DEVICES = 64;
+constexpr long long SETS_FIXED_DOUBLES = 768;  // block maxima and their indices
+std::mutex g_sets_mu;
+double* g_sets_addr[SETS_MAX_DEVICES];  // g_sets_scratch's address on each device, resolved on first use
+thread_local char g_sets_msg[320];
+
+const char* sets_msg_cuda(const char* what, cudaError_t e) {
+  std::snprintf(g_sets_msg, sizeof g_sets_msg, "lkg_vecchia_sets_noalloc: %s failed: %s", what,
+                cudaGetErrorString(e));
+  return g_sets_msg;
+}
+
+// device (or managed) memory usable from device `dev`
+bool on_device(const void* p, int dev) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeManaged || (a.type == cudaMemoryTypeDevice && a.device == dev);
+}
+
+// first point of the maxmin order (closest to the centroid, lowest index on ties -- the host computation of
+// vecchia_sets_gpu moved to one block), min squared distances set to +inf, and step-0 block maxima that all name
+// that point, so that k_maxmin_step at t = 0 records it and computes the distances k_maxmin_init would
+__global__ void __launch_bounds__(1024) k_sets_prepare(int n, int d, const double* __restrict__ X, int nb,
+                                                       double* __restrict__ mind2, double* __restrict__ pv,
+                                                       int* __restrict__ pi) {
+  __shared__ double cen[8];
+  __shared__ double sv[1024];
+  __shared__ int si[1024];
+  if (threadIdx.x < d) {
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s += X[i + (int64_t)threadIdx.x * n];  // same order as the host sum
+    cen[threadIdx.x] = s / n;
+  }
+  __syncthreads();
+  double bv = INFINITY;
+  int bi = 0x7fffffff;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    double s = 0.0;
+    for (int q = 0; q < d; ++q) {
+      const double dk = X[i + (int64_t)q * n] - cen[q];
+      s = __dadd_rn(s, __dmul_rn(dk, dk));  // no fused multiply-add, as in the host loop
+    }
+    if (s < bv) {
+      bv = s;
+      bi = i;
+    }
+    mind2[i] = INFINITY;
+  }
+  sv[threadIdx.x] = bv;
+  si[threadIdx.x] = bi;
+  __syncthreads();
+  for (int s = 512; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      const double ov = sv[threadIdx.x + s];
+      const int oi = si[threadIdx.x + s];
+      if (ov < sv[threadIdx.x] || (ov == sv[threadIdx.x] && oi < si[threadIdx.x])) {
+        sv[threadIdx.x] = ov;
+        si[threadIdx.x] = oi;
+      }
+    }
+    __syncthreads();
+  }
+  const int first = si[0] == 0x7fffffff ? 0 : si[0];
+  for (int q = threadIdx.x; q < nb; q += blockDim.x) {
+    pv[q] = 0.0;
+    pi[q] = first;
+  }
+}
+
+}  // namespace
+
+const char* vecchia_sets_noalloc(int n, int d, const double* X, int m, int32_t* order, int32_t* nbr,
+                                 cudaStream_t st) {
+  if (n < 1 || d < 1 || d > 8 || m < 0 || m > VECCHIA_MAX_M)
+    return "lkg_vecchia_sets_noalloc: needs n >= 1, 1 <= d <= 8 and 0 <= m <= 32";
+  const long long need = (long long)n * (2 * d + 1) + SETS_FIXED_DOUBLES;
+  if (need > SETS_SCRATCH_DOUBLES) {
+    std::snprintf(g_sets_msg, sizeof g_sets_msg,
+                  "lkg_vecchia_sets_noalloc: n = %d points in d = %d dims need %lld doubles of scratch, more than the "
+                  "fixed %lld (n * (2 d + 1) + %lld <= %lld; at d = %d, n <= %lld); use lkg_vecchia_sets",
+                  n, d, need, SETS_SCRATCH_DOUBLES, SETS_FIXED_DOUBLES, SETS_SCRATCH_DOUBLES, d,
+                  (SETS_SCRATCH_DOUBLES - SETS_FIXED_DOUBLES) / (2 * d + 1));
+    return g_sets_msg;
+  }
+  if (!X || !order || (m > 0 && !nbr)) return "lkg_vecchia_sets_noalloc: null buffer";
+  if ((uintptr_t)X % alignof(double) || (uintptr_t)order % alignof(int32_t) ||
+      (m > 0 && (uintptr_t)nbr % alignof(int32_t)))
+    return "lkg_vecchia_sets_noalloc: misaligned buffer";
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return sets_msg_cuda("cudaGetDevice", e);
+  if (dev < 0 || dev >= SETS_MAX_DEVICES) return "lkg_vecchia_sets_noalloc: device ordinal >= 64";
+  if (!on_device(X, dev) || !on_device(order, dev) || (m > 0 && !on_device(nbr, dev)))
+    return "lkg_vecchia_sets_noalloc: X, order and nbr must be device (or managed) memory of the current device";
+  double* base;
+  {
+    std::lock_guard<std::mutex> lock(g_sets_mu);
+    if (!g_sets_addr[dev]) {
+      void* p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_sets_scratch);
+      if (e != cudaSuccess) return sets_msg_cuda("cudaGetSymbolAddress", e);
+      g_sets_addr[dev] = static_cast<double*>(p);
+    }
+    base = g_sets_addr[dev];
+  }
+  double* Xp = base;
+  double* Xo = Xp + (int64_t)n * d;
+  double* mind2 = Xo + (int64_t)n * d;
+  double* pv = mind2 + n;
+  int* pi = reinterpret_cast<int*>(pv + 512);
+  const int nb = std::min(256, std::max(1, ceil_div(n, 1024)));
+  k_gather_points<<<ceil_div(n, 256), 256, 0, st>>>(n, d, X, nullptr, nullptr, Xp);
+  // step t reads the maxima buffer (t + 1) & 1 and writes t & 1; step 0 reads the prepared buffer 1
+  k_sets_prepare<<<1, 1024, 0, st>>>(n, d, X, nb, mind2, pv + nb, pi + nb);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return sets_msg_cuda("kernel launch", e);
+  for (int t = 0; t < n; ++t) {
+    const int in = (t + 1) & 1, outb = t & 1;
+    k_maxmin_step<<<nb, 256, 0, st>>>(n, d, Xp, mind2, pv + in * nb, pi + in * nb, pv + outb * nb, pi + outb * nb,
+                                      order, t);
+  }
+  k_gather_points<<<ceil_div(n, 256), 256, 0, st>>>(n, d, X, order, Xo, Xp);
+  if (m > 0) k_knn_earlier<<<ceil_div(n, 8), 256, 0, st>>>(n, d, m, Xo, order, nbr);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return sets_msg_cuda("kernel launch", e);
+  return nullptr;
 }
 
 }  // namespace lkg

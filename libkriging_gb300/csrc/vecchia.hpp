@@ -61,4 +61,11 @@ void vecchia_sets_gpu(int n, int d, const double* X, int m, int32_t* order, int3
 void vecchia_predict_gpu(int kernel, int n, int d, const double* X, const double* resid, const double* theta, int q,
                          const double* Xq, int m, std::vector<double>& ar, std::vector<double>& ra);
 
+// The same sets from device buffers, with every intermediate in one fixed device array of this library
+// (SETS_SCRATCH_DOUBLES doubles) instead of allocated memory; all work is queued on `stream`, nothing is
+// synchronised.  Returns nullptr on success, else a message that stays valid until the calling thread's next call.
+constexpr long long SETS_SCRATCH_DOUBLES = 1LL << 20;  // 8 MiB
+const char* vecchia_sets_noalloc(int n, int d, const double* X, int m, int32_t* order, int32_t* nbr,
+                                 cudaStream_t stream);
+
 }  // namespace lkg
