@@ -409,9 +409,21 @@ void trsm_lower_left_t(const double* L, int64_t lda, int64_t mstride, int n, con
                        int64_t ldb, int64_t bstride, int r, int batch, cudaStream_t st) {
   const int nblk = ceil_div(n, NB);
   const int64_t dstride = (int64_t)nblk * NB * NB;
+  if (r > 16 && batch != 1 && mstride == 0)
+    throw std::invalid_argument("trsm_lower_left_t: shared factor with many right-hand sides is not supported");
   const size_t smem = sizeof(double) * NB * r;
   for (int k = nblk - 1; k >= 0; --k) {
     const int k0 = k * NB, nb = std::min(NB, n - k0);
+    if (r > 16) {  // many right-hand sides: X_k = Dinv_k^T B_k in place, then B_0:k0 -= L(k0:k0+nb, 0:k0)^T X_k
+      MatView dt{Dinv + (int64_t)k * NB * NB, NB, 1, dstride};  // (i, kk) = Dinv_k(kk, i)
+      MatView bk{B + k0, 1, ldb, bstride};
+      gemm_tiles(nb, r, nb, 1.0, dt, bk, 0.0, B + k0, ldb, bstride, batch, false, st);
+      if (k0 > 0) {
+        MatView lt{L + k0, lda, 1, mstride};  // (i, kk) = L(k0 + kk, i)
+        gemm_tiles(k0, r, nb, -1.0, lt, bk, 1.0, B, ldb, bstride, batch, false, st);
+      }
+      continue;
+    }
     {
       LaunchTimer lt("k_small_apply", st, (double)nb * nb * r * batch, 16.0 * nb * r * batch);
       k_small_apply<<<dim3(1, 1, batch), 256, smem, st>>>(Dinv, dstride, k, B, ldb, bstride, k0, nb, r, true);

@@ -257,6 +257,303 @@ __global__ void __launch_bounds__(128, 1) k_oz_tc(TcArgs g) {
   if (w == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(NCOLS));
 }
 
+// ---------------------------------------------------------------------------------------------------------------
+// Pipelined form (S <= 7): a persistent CTA runs a sequence of jobs = (128 x 64 tile, 64-chunk) with three roles
+//   warps 0-7   epilogue: warp e reads TMEM lanes 32 (e % 4) .. +31 (rows), columns 32 (e / 4) .. +31
+//   warps 8-10  producers: cp.async of the digit planes; B (S x 64 rows) double-buffered per job, A in S one-digit
+//               slots refilled as soon as the products of that digit retire
+//   warp 11     TMEM allocation; its lane 0 issues the products, A-digit major: digit i meets B digits
+//               1 .. S+1-i, then a commit to adone[i].  Diagonal i + 1 is complete once adone[i] fires, so the
+//               epilogue folds it while the products of later digits run.
+// Each mbarrier is at most one phase ahead of any waiter (every producer / consumer pair is ordered through the
+// previous job), so parity waits are unambiguous.  All waits are bounded.
+
+struct PipeBars {
+  uint64_t full_a[8], adone[8], full_b[2], jobdone[2], tmemfree;
+};
+
+__device__ __forceinline__ void mbar_arrive(uint32_t m) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(m) : "memory");
+}
+
+__device__ __forceinline__ bool warp_wait(uint32_t m, uint32_t parity) {
+  const bool ok = mbar_wait(m, parity);
+  return __all_sync(0xffffffffu, ok);
+}
+
+// exact value of the signed 128-bit integer H times 2^E, rounded to nearest (ties to even)
+__device__ __forceinline__ double i128_scaled_to_double(__int128 H, int E) {
+  if (H == 0) return 0.0;
+  const bool neg = H < 0;
+  unsigned __int128 u = neg ? (unsigned __int128)(-H) : (unsigned __int128)H;
+  const unsigned long long hi = (unsigned long long)(u >> 64), lo = (unsigned long long)u;
+  const int p = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)lo);  // position of the top bit
+  unsigned long long mant;
+  int e = p;
+  if (p <= 52) {
+    mant = lo << (52 - p);
+  } else {
+    const int sh = p - 52;
+    mant = (unsigned long long)(u >> sh);
+    const unsigned __int128 rem = u & (((unsigned __int128)1 << sh) - 1);
+    const unsigned __int128 half = (unsigned __int128)1 << (sh - 1);
+    if (rem > half || (rem == half && (mant & 1ull))) {
+      ++mant;
+      if (mant >> 53) {
+        mant >>= 1;
+        ++e;
+      }
+    }
+  }
+  const int fld = e + E + 1023;
+  if (fld <= 0 || fld >= 2047) return ldexp(neg ? -(double)u : (double)u, E);
+  return __longlong_as_double(
+      (long long)((neg ? 0x8000000000000000ull : 0ull) | ((unsigned long long)fld << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+}
+
+struct TileJob {
+  int m0, n0, c0, c1;
+};
+
+__device__ __forceinline__ bool tile_at(const TcArgs& g, long long t, TileJob& T) {
+  if (g.wtw_n > 0) {
+    int I = (int)((sqrt(4.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while ((long long)(I + 1) * (I + 2) <= t) ++I;
+    while ((long long)I * (I + 1) > t) --I;
+    T.m0 = I * TC_M;
+    T.n0 = (int)(t - (long long)I * (I + 1)) * TC_N;
+    T.c0 = 2 * I;
+    T.c1 = g.SA.nchunk;
+  } else {
+    const int tx = (g.M + TC_M - 1) / TC_M;
+    T.m0 = (int)(t % tx) * TC_M;
+    T.n0 = (int)(t / tx) * TC_N;
+    T.c0 = g.c0;
+    T.c1 = g.c1;
+  }
+  if (T.m0 >= g.M || T.n0 >= g.N || T.c1 <= T.c0) return false;
+  if ((g.lower_only || g.wtw_n > 0) && T.m0 + TC_M - 1 < T.n0) return false;
+  return true;
+}
+
+template <int S>
+__global__ void __launch_bounds__(384, 1) k_oz_tcp(TcArgs g, long long ntiles) {
+  constexpr int NCOLS = (S * TC_N <= 256) ? 256 : 512;
+  constexpr uint32_t A_SLOT = TC_M * 128, B_DIGIT = TC_N * 128, B_BUF = S * B_DIGIT;
+  extern __shared__ unsigned char tcp_raw[];
+  __shared__ PipeBars bars;
+  __shared__ uint32_t tslot;
+  const uint32_t raw = su32(tcp_raw);
+  const uint32_t sA = (raw + 1023u) & ~1023u;  // S slots of one A digit (128 rows)
+  const uint32_t sB = sA + S * A_SLOT;          // 2 buffers of S B digits (64 rows)
+  const int t = threadIdx.x, w = t >> 5, lane = t & 31;
+  const int64_t b = blockIdx.z;
+  const __nv_bfloat16* pa = g.SA.planes + b * g.SA.plane_bstride;
+  const __nv_bfloat16* pb = g.SB.planes + b * g.SB.plane_bstride;
+  const int* ea = g.SA.exps + b * g.SA.exp_bstride;
+  const int* eb = g.SB.exps + b * g.SB.exp_bstride;
+  auto bar = [&](const uint64_t& x) { return su32(&x); };
+
+  if (t == 0) {
+    for (int i = 0; i < S; ++i) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 96;\n" ::"r"(bar(bars.full_a[i])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar(bars.adone[i])));
+    }
+    for (int q = 0; q < 2; ++q) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 96;\n" ::"r"(bar(bars.full_b[q])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar(bars.jobdone[q])));
+    }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 256;\n" ::"r"(bar(bars.tmemfree)));
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (w == 11) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(su32(&tslot)),
+                 "r"(NCOLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = tslot;
+  bool ok = true;
+
+  if (w >= 8 && w <= 10) {
+    // ---------------- producers ----------------
+    const int pt = t - 256;  // 0 .. 95
+    int job = 0;
+    for (long long ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
+      TileJob T;
+      if (!tile_at(g, ti, T)) continue;
+      for (int c = T.c0; c < T.c1 && ok; ++c, ++job) {
+        const int bb = job & 1;
+        if (job >= 2 && !warp_wait(bar(bars.jobdone[bb]), ((job - 2) >> 1) & 1)) {
+          ok = false;
+          break;
+        }
+        const uint32_t bdst = sB + bb * B_BUF;
+        for (int idx = pt; idx < S * TC_N * 8; idx += 96) {
+          const int seg = idx & 7, rr = idx >> 3, i = rr / TC_N, r = rr % TC_N;
+          cp16(bdst + (uint32_t)(i * TC_N + r) * 128u + (uint32_t)((seg ^ (r & 7)) * 16),
+               pb + (((int64_t)i * g.SB.nchunk + c) * g.SB.rows_pad + T.n0 + r) * OZ_CHUNK + seg * 8);
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        for (int i = 0; i < S; ++i) {
+          if (job >= 1 && !warp_wait(bar(bars.adone[i]), (job - 1) & 1)) {
+            ok = false;
+            break;
+          }
+          const uint32_t adst = sA + i * A_SLOT;
+          for (int idx = pt; idx < TC_M * 8; idx += 96) {
+            const int seg = idx & 7, r = idx >> 3;
+            cp16(adst + (uint32_t)r * 128u + (uint32_t)((seg ^ (r & 7)) * 16),
+                 pa + (((int64_t)i * g.SA.nchunk + c) * g.SA.rows_pad + T.m0 + r) * OZ_CHUNK + seg * 8);
+          }
+          asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+          asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+          if (i == 0) mbar_arrive(bar(bars.full_b[bb]));
+          mbar_arrive(bar(bars.full_a[i]));
+        }
+      }
+    }
+    if (!ok) atomicExch(&g_oz_tc_error, 1);
+  } else if (w == 11) {
+    // ---------------- MMA issue ----------------
+    if (lane == 0) {
+      int job = 0;
+      for (long long ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
+        TileJob T;
+        if (!tile_at(g, ti, T)) continue;
+        for (int c = T.c0; c < T.c1 && ok; ++c, ++job) {
+          const int bb = job & 1;
+          if (!mbar_wait(bar(bars.full_b[bb]), (job >> 1) & 1) ||
+              (job >= 1 && !mbar_wait(bar(bars.tmemfree), (job - 1) & 1))) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+          const uint32_t bbase = sB + bb * B_BUF;
+          for (int i = 1; i <= S; ++i) {
+            if (!mbar_wait(bar(bars.full_a[i - 1]), job & 1)) {
+              ok = false;
+              break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t a0 = sA + (i - 1) * A_SLOT;
+            for (int j = 1; j <= S + 1 - i; ++j) {
+              const uint32_t d = tmem + (uint32_t)((i + j - 2) * TC_N);
+              const uint32_t b0 = bbase + (j - 1) * B_DIGIT;
+#pragma unroll
+              for (int kk = 0; kk < 4; ++kk) mma_issue(d, sdesc(a0 + kk * 32u), sdesc(b0 + kk * 32u),
+                                                       (i > 1 || kk > 0) ? 1u : 0u);
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             bar(bars.adone[i - 1]))
+                         : "memory");
+          }
+          if (!ok) break;
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                           bar(bars.jobdone[bb]))
+                       : "memory");
+        }
+      }
+      if (!ok) atomicExch(&g_oz_tc_error, 1);
+    }
+  } else {
+    // ---------------- epilogue (warps 0-7) ----------------
+    const int quarter = w & 3, half = w >> 2;
+    const uint32_t tl = tmem + ((uint32_t)(32 * quarter) << 16);
+    double* Cb = g.C + b * g.c_batch;
+    const bool lower = g.lower_only || g.wtw_n > 0;
+    int job = 0;
+    for (long long ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
+      TileJob T;
+      if (!tile_at(g, ti, T)) continue;
+      const int row = T.m0 + 32 * quarter + lane;
+      for (int c = T.c0; c < T.c1 && ok; ++c, ++job) {
+        const int er = ea[(int64_t)c * g.SA.rows_pad + T.m0 + 32 * quarter + lane];
+#pragma unroll 1
+        for (int cg = 0; cg < 2 && ok; ++cg) {
+          const int col0 = 32 * half + 16 * cg;
+          long long h1[16], h2[16];
+#pragma unroll
+          for (int q = 0; q < 16; ++q) h2[q] = 0;
+#pragma unroll 1
+          for (int i = 1; i <= S; ++i) {  // diagonal dg = i + 1 is complete after adone[i]
+            if (cg == 0 && !warp_wait(bar(bars.adone[i - 1]), job & 1)) {
+              ok = false;
+              break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const int dg = i + 1;
+            float v[16];
+            tmem_ld16(tl + (uint32_t)((dg - 2) * TC_N + col0), v);
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+              const long long iv = (long long)__float2int_rn(v[q]);
+              if (dg <= 5)
+                h1[q] = (dg == 2) ? iv : h1[q] * 256 + iv;
+              else
+                h2[q] = (dg == 6) ? iv : h2[q] * 256 + iv;
+            }
+          }
+          if (!ok) break;
+          // H = h1 256^(S-4) + h2 holds the chunk's exact product in units of 2^(er + ec - 8 (S + 1))
+#pragma unroll
+          for (int q = 0; q < 16; ++q) {
+            const int col = T.n0 + col0 + q;
+            const int ec = eb[(int64_t)c * g.SB.rows_pad + col];
+            const __int128 H = ((__int128)h1[q] << (8 * (S - 4))) + (__int128)h2[q];
+            const double val = i128_scaled_to_double(H, er + ec - 8 * (S + 1));
+            if (row < g.M && col < g.N && (!lower || row >= col)) {
+              double* cp = Cb + row + (int64_t)col * g.ldc;
+              if (c == T.c0)
+                *cp = (g.beta == 0.0) ? g.alpha * val : fma(g.alpha, val, g.beta * *cp);
+              else
+                *cp = fma(g.alpha, val, *cp);
+            }
+          }
+        }
+        if (!ok) break;
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        mbar_arrive(bar(bars.tmemfree));
+      }
+    }
+    if (!ok && lane == 0) atomicExch(&g_oz_tc_error, 1);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (w == 11) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(NCOLS));
+}
+
+template <int S>
+void launch_tcp(const TcArgs& a, long long ntiles, int batch, cudaStream_t st) {
+  const size_t smem = (size_t)S * (TC_M + 2 * TC_N) * 128 + 1024;
+  static bool attr = false;
+  if (!attr) {
+    LKG_CUDA(cudaFuncSetAttribute(k_oz_tcp<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    LKG_CUDA(cudaGetDevice(&dev));
+    LKG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  }
+  const long long gx = std::min<long long>(ntiles, std::max(1, nsm / std::max(1, batch)));
+  k_oz_tcp<S><<<dim3((unsigned)gx, 1, batch), 384, smem, st>>>(a, ntiles);
+  LKG_LAUNCH("k_oz_tcp");
+}
+
+bool dispatch_tcp(int S, const TcArgs& a, long long ntiles, int batch, cudaStream_t st) {
+  switch (S) {
+    case 4: launch_tcp<4>(a, ntiles, batch, st); return true;
+    case 5: launch_tcp<5>(a, ntiles, batch, st); return true;
+    case 6: launch_tcp<6>(a, ntiles, batch, st); return true;
+    case 7: launch_tcp<7>(a, ntiles, batch, st); return true;
+    default: return false;  // S = 8 does not fit a double-buffered B: the single-stage kernel
+  }
+}
+
 template <int S>
 void launch_tc(const TcArgs& a, dim3 grid, cudaStream_t st) {
   // operands + exponents + 1024 B for the alignment; at least 120 KB so that one CTA (one TMEM allocation) is
@@ -296,7 +593,7 @@ void ozaki_gemm_tc(int M, int N, int c0, int c1, double alpha, const SplitBuf& S
   const double fl = (lower_only && M == N) ? K * M * (M + 1.0) : 2.0 * M * N * K;
   LaunchTimer lt("k_oz_tc", st, fl * batch * SA.S * (SA.S + 1) / 2.0,
                  8.0 * ((beta == 0.0) ? 1.0 : 2.0) * M * N * batch);
-  dispatch_tc(SA.S, a, grid, st);
+  if (!dispatch_tcp(SA.S, a, (long long)grid.x * grid.y, batch, st)) dispatch_tc(SA.S, a, grid, st);
 }
 
 void ozaki_wtw_tc(int n, const SplitBuf& SW, double* C, int64_t ldc, int64_t cstride, int batch, cudaStream_t st) {
@@ -306,7 +603,7 @@ void ozaki_wtw_tc(int n, const SplitBuf& SW, double* C, int64_t ldc, int64_t cst
   TcArgs a{n, n, 0, SW.nchunk, 1.0, 0.0, SW, SW, C, ldc, cstride, false, n};
   LaunchTimer lt("k_oz_tc_wtw", st, (double)n * (n + 1.0) * (n + 2.0) / 3.0 * batch * SW.S * (SW.S + 1) / 2.0,
                  8.0 * n * (n + 1.0) * batch);
-  dispatch_tc(SW.S, a, dim3((unsigned)ntiles, 1, batch), st);
+  if (!dispatch_tcp(SW.S, a, ntiles, batch, st)) dispatch_tc(SW.S, a, dim3((unsigned)ntiles, 1, batch), st);
 }
 
 int ozaki_tc_error_and_reset() {

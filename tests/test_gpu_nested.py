@@ -41,7 +41,9 @@ def test_partition_matches_oracle(gpu_lib, partition):
 @pytest.mark.parametrize("kernel", ["gauss", "matern5_2"])
 def test_common_prior_at_fixed_theta(gpu_lib, kernel):
     X, y = _data(240)
-    th = np.array([0.15, 0.25])
+    # gauss at longer ranges is so ill-conditioned on these groups that a 1e-10 diagonal change moves sigma2 by
+    # percents (two LAPACK builds disagree at 1e-6): both kernels are compared where cond(R) stays moderate
+    th = np.array([0.08, 0.1]) if kernel == "gauss" else np.array([0.15, 0.25])
     nk = gpu_lib.NestedKriging(y, X, kernel, 4, aggregation="NK", optim="none", parameters=_none_params(th))
     groups = nk.groups()
     pr = N.fit_none(y, X, kernel, groups, th)
@@ -70,7 +72,7 @@ def test_poe_family_matches_oracle(gpu_lib, agg):
 @pytest.mark.parametrize("kernel,chunk", [("matern5_2", 128), ("gauss", 37), ("exp", 64)])
 def test_nk_matches_oracle(gpu_lib, kernel, chunk):
     X, y = _data(260)
-    th = np.array([0.15, 0.2])
+    th = np.array([0.08, 0.1]) if kernel == "gauss" else np.array([0.15, 0.2])
     nk = gpu_lib.NestedKriging(y, X, kernel, 5, aggregation="NK", optim="none", parameters=_none_params(th))
     nk.set_predict_chunk(chunk)
     Xt = np.random.default_rng(456).uniform(size=(150, 2))

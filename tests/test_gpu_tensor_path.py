@@ -1,6 +1,6 @@
 """The tcgen05 kernels of the mixed path's digit products (ozaki_tc.cu) against FP64 and against the mma.sync
-kernels: the same exact digit arithmetic, so single-chunk products agree bit for bit and multi-chunk products to
-the last rounding of the per-chunk FP64 adds."""
+kernels: the same exact digit arithmetic, so the results agree to the last rounding of the per-chunk folds (bit for
+bit where both fold alike)."""
 import ctypes
 
 import numpy as np
@@ -43,9 +43,9 @@ def test_tc_gemm_matches_fp64_and_mma_sync(gpu_lib, tensor_path, S, shape):
     assert tensor_path.lkg_set_tensor_path(1) == 1
     C_tc = _emulated(gpu_lib, A, B, S)
     scale = np.abs(A) @ np.abs(B).T
-    if K <= 64:
+    if K <= 64 and S == 8:  # the single-stage kernel folds exactly as the mma.sync kernel does
         assert np.array_equal(C_tc, C_sync)
-    else:
+    else:  # the pipelined kernel rounds the chunk's exact value once instead of twice
         assert np.max(np.abs(C_tc - C_sync) / scale) < 1e-15
     if S >= 7:
         err = np.max(np.abs(C_tc - A @ B.T) / scale)
