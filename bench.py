@@ -552,8 +552,8 @@ def main():
     ap.add_argument("--mixed", action="store_true", help="multistart / nested workloads on the mixed path")
     ap.add_argument("--nested-n", type=int, default=1_000_000, help="points of the nested workload")
     ap.add_argument("--nested-q", type=int, default=10_000, help="gPoE prediction points of the nested workload")
-    ap.add_argument("--tensor-path", type=int, default=None, choices=[0, 1],
-                    help="digit-product kernels of the mixed path: 0 mma.sync, 1 tcgen05 (default: the library's)")
+    ap.add_argument("--tensor-path", type=int, default=None, choices=[0, 1, 2],
+                    help="digit-product kernels of the mixed path: 0 mma.sync, 1 tcgen05 (W^T W on mma.sync), 2 tcgen05 (default: the library's)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

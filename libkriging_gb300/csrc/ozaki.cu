@@ -283,7 +283,7 @@ int& oz_tc_flag() {
   return f;
 }
 
-void ozaki_set_tensor_path(int tc) { oz_tc_flag() = tc ? 1 : 0; }
+void ozaki_set_tensor_path(int tc) { oz_tc_flag() = (tc < 0 || tc > 2) ? 1 : tc; }
 int ozaki_tensor_path() { return oz_tc_flag(); }
 
 void ozaki_split(int rows, int K, const double* p, int64_t s_r, int64_t s_k, int64_t bstride, int batch, SplitBuf& out,
@@ -318,7 +318,9 @@ void ozaki_gemm(int M, int N, int c0, int c1, double alpha, const SplitBuf& SA, 
 }
 
 void ozaki_wtw(int n, const SplitBuf& SW, double* C, int64_t ldc, int64_t cstride, int batch, cudaStream_t st) {
-  if (oz_tc_flag()) {
+  // W^T W sums many chunks per tile, which the mma.sync kernel folds in registers; the tcgen05 form adds every
+  // chunk into C and measured slower (209 vs 150 ms at n = 16384), so it is used only on request (tensor path 2)
+  if (oz_tc_flag() == 2) {
     ozaki_wtw_tc(n, SW, C, ldc, cstride, batch, st);
     return;
   }

@@ -397,6 +397,7 @@ __global__ void __launch_bounds__(384, 1) k_oz_tcp(TcArgs g, long long ntiles) {
                pb + (((int64_t)i * g.SB.nchunk + c) * g.SB.rows_pad + T.n0 + r) * OZ_CHUNK + seg * 8);
         }
         asm volatile("cp.async.commit_group;\n" ::: "memory");
+        // digit i's copies are issued before digit i-1's are awaited: two digits in flight
         for (int i = 0; i < S; ++i) {
           if (job >= 1 && !warp_wait(bar(bars.adone[i]), (job - 1) & 1)) {
             ok = false;
@@ -408,11 +409,19 @@ __global__ void __launch_bounds__(384, 1) k_oz_tcp(TcArgs g, long long ntiles) {
             cp16(adst + (uint32_t)r * 128u + (uint32_t)((seg ^ (r & 7)) * 16),
                  pa + (((int64_t)i * g.SA.nchunk + c) * g.SA.rows_pad + T.m0 + r) * OZ_CHUNK + seg * 8);
           }
-          asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
-          asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-          if (i == 0) mbar_arrive(bar(bars.full_b[bb]));
-          mbar_arrive(bar(bars.full_a[i]));
+          asm volatile("cp.async.commit_group;\n" ::: "memory");
+          if (i > 0) {
+            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            if (i == 1) mbar_arrive(bar(bars.full_b[bb]));
+            mbar_arrive(bar(bars.full_a[i - 1]));
+          }
         }
+        if (!ok) break;
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        if (S == 1) mbar_arrive(bar(bars.full_b[bb]));
+        mbar_arrive(bar(bars.full_a[S - 1]));
       }
     }
     if (!ok) atomicExch(&g_oz_tc_error, 1);
@@ -471,9 +480,22 @@ __global__ void __launch_bounds__(384, 1) k_oz_tcp(TcArgs g, long long ntiles) {
       const int row = T.m0 + 32 * quarter + lane;
       for (int c = T.c0; c < T.c1 && ok; ++c, ++job) {
         const int er = ea[(int64_t)c * g.SA.rows_pad + T.m0 + 32 * quarter + lane];
+        const bool first = (c == T.c0);
+        const bool need_c = !(first && g.beta == 0.0);
+        const double cscale = first ? g.beta : 1.0;
 #pragma unroll 1
         for (int cg = 0; cg < 2 && ok; ++cg) {
           const int col0 = 32 * half + 16 * cg;
+          // operands of this column group's update, loaded together (before the products retire for cg 0)
+          int ec[16];
+          double cold[16];
+#pragma unroll
+          for (int q = 0; q < 16; ++q) {
+            const int col = T.n0 + col0 + q;
+            ec[q] = eb[(int64_t)c * g.SB.rows_pad + col];
+            const bool inside = row < g.M && col < g.N && (!lower || row >= col);
+            cold[q] = (inside && need_c) ? Cb[row + (int64_t)col * g.ldc] : 0.0;
+          }
           long long h1[16], h2[16];
 #pragma unroll
           for (int q = 0; q < 16; ++q) h2[q] = 0;
@@ -497,25 +519,32 @@ __global__ void __launch_bounds__(384, 1) k_oz_tcp(TcArgs g, long long ntiles) {
             }
           }
           if (!ok) break;
+          if (cg == 1) {  // the job's last TMEM read: the next job's products may start now
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            mbar_arrive(bar(bars.tmemfree));
+          }
           // H = h1 256^(S-4) + h2 holds the chunk's exact product in units of 2^(er + ec - 8 (S + 1))
 #pragma unroll
           for (int q = 0; q < 16; ++q) {
             const int col = T.n0 + col0 + q;
-            const int ec = eb[(int64_t)c * g.SB.rows_pad + col];
             const __int128 H = ((__int128)h1[q] << (8 * (S - 4))) + (__int128)h2[q];
-            const double val = i128_scaled_to_double(H, er + ec - 8 * (S + 1));
+            const double val = i128_scaled_to_double(H, er + ec[q] - 8 * (S + 1));
             if (row < g.M && col < g.N && (!lower || row >= col)) {
-              double* cp = Cb + row + (int64_t)col * g.ldc;
-              if (c == T.c0)
-                *cp = (g.beta == 0.0) ? g.alpha * val : fma(g.alpha, val, g.beta * *cp);
+              // one FP64 operation per element where the update allows it (the FP64 pipe is the scarce one here)
+              double outv;
+              if (!need_c)
+                outv = g.alpha * val;
+              else if (cscale == 1.0 && g.alpha == -1.0)
+                outv = cold[q] - val;
+              else if (cscale == 1.0 && g.alpha == 1.0)
+                outv = cold[q] + val;
               else
-                *cp = fma(g.alpha, val, *cp);
+                outv = fma(g.alpha, val, cscale * cold[q]);
+              Cb[row + (int64_t)col * g.ldc] = outv;
             }
           }
         }
         if (!ok) break;
-        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-        mbar_arrive(bar(bars.tmemfree));
       }
     }
     if (!ok && lane == 0) atomicExch(&g_oz_tc_error, 1);

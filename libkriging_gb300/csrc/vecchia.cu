@@ -50,11 +50,16 @@ __device__ __forceinline__ int wargmax(double v, int lane, int mi) {
   return idx;
 }
 
+// The factor keeps 1 / L_jj in the spare last column of row j (index RCP = LDP - 1 = 32, never a matrix column since
+// m <= 32 fills 0 .. 31): the solves and the factorisation multiply instead of dividing (an FP64 division is a long
+// instruction sequence on this part).
+constexpr int RCP = LDP - 1;
+
 // solve L z = b (lane i holds b_i); lanes >= mi return 0
 __device__ double wsolve_lower(const double* L, double b, int mi, int lane) {
   double val = (lane < mi) ? b : 0.0;
   for (int j = 0; j < mi; ++j) {
-    const double zj = __shfl_sync(FULL, val, j) / L[j * LDP + j];
+    const double zj = __shfl_sync(FULL, val, j) * L[j * LDP + RCP];
     if (lane == j) val = zj;
     if (lane > j && lane < mi) val -= L[lane * LDP + j] * zj;
   }
@@ -64,7 +69,7 @@ __device__ double wsolve_lower(const double* L, double b, int mi, int lane) {
 __device__ double wsolve_upper_t(const double* L, double z, int mi, int lane) {
   double val = (lane < mi) ? z : 0.0;
   for (int j = mi - 1; j >= 0; --j) {
-    const double xj = __shfl_sync(FULL, val, j) / L[j * LDP + j];
+    const double xj = __shfl_sync(FULL, val, j) * L[j * LDP + RCP];
     if (lane == j) val = xj;
     if (lane < j) val -= L[j * LDP + lane] * xj;
   }
@@ -78,9 +83,13 @@ __device__ bool wchol(double* L, int mi, int lane) {
     const double piv = L[j * LDP + j];
     if (!(piv > 0.0)) return false;
     const double ljj = sqrt(piv);
+    const double rj = 1.0 / ljj;
     __syncwarp();
-    if (lane == j) L[j * LDP + j] = ljj;
-    if (lane > j && lane < mi) L[lane * LDP + j] /= ljj;
+    if (lane == j) {
+      L[j * LDP + j] = ljj;
+      L[j * LDP + RCP] = rj;
+    }
+    if (lane > j && lane < mi) L[lane * LDP + j] *= rj;
     __syncwarp();
     if (lane > j && lane < mi) {
       const double lij = L[lane * LDP + j];
@@ -174,10 +183,13 @@ __global__ void __launch_bounds__(WPB * 32) k_vecchia_points(VPointArgs a) {
     }
     return;
   }
-  double th[DM], xo[DM];
+  // division- and log1p-free covariance forms (common.cuh), equal to the reference's to a few ulps
+  double inv[DM], ck[DM], xo[DM];
 #pragma unroll
   for (int k = 0; k < DM; ++k) {
-    th[k] = (k < d) ? a.theta[k] : 1.0;
+    const double th = (k < d) ? a.theta[k] : 1.0;
+    inv[k] = 1.0 / th;
+    ck[k] = cov_scale<K>() * inv[k];
     xo[k] = (k < d) ? a.X[oi + (int64_t)k * n] : 0.0;
   }
   if (lane < mi)
@@ -191,19 +203,19 @@ __global__ void __launch_bounds__(WPB * 32) k_vecchia_points(VPointArgs a) {
       if (b == lane) {
         c = 1.0 + a.num_nugget;
       } else {
-        double s = 0.0;
+        double s = 0.0, pr = 1.0;
 #pragma unroll
         for (int k = 0; k < DM; ++k)
-          if (k < d) s += cov_term<K>(xs[lane * DM + k] - xs[b * DM + k], th[k]);
-        c = cov_from_sum<K>(s);
+          if (k < d) cov_fast_term<K>(xs[lane * DM + k] - xs[b * DM + k], ck[k], s, pr);
+        c = cov_fast_finish<K>(s, pr);
       }
       RN[lane * LDP + b] = c;
     }
-    double s = 0.0;
+    double s = 0.0, pr = 1.0;
 #pragma unroll
     for (int k = 0; k < DM; ++k)
-      if (k < d) s += cov_term<K>(xs[lane * DM + k] - xo[k], th[k]);
-    r = cov_from_sum<K>(s);
+      if (k < d) cov_fast_term<K>(xs[lane * DM + k] - xo[k], ck[k], s, pr);
+    r = cov_fast_finish<K>(s, pr);
   }
   __syncwarp();
   // ---- factor with the numerical-nugget retry / rcond rules ----
@@ -250,10 +262,10 @@ __global__ void __launch_bounds__(WPB * 32) k_vecchia_points(VPointArgs a) {
   for (int k = 0; k < d; ++k) {
     double drk = 0.0, s = 0.0;
     if (lane < mi) {
-      drk = r * dlncov_term<K>(xs[lane * DM + k] - xo[k], th[k]);
+      drk = r * dlncov_fast<K>(xs[lane * DM + k] - xo[k], inv[k], ck[k]);
       for (int b = 0; b < mi; ++b)
         if (b != lane)
-          s += RN[lane * LDP + b] * dlncov_term<K>(xs[lane * DM + k] - xs[b * DM + k], th[k]) * sa[b];
+          s += RN[lane * LDP + b] * dlncov_fast<K>(xs[lane * DM + k] - xs[b * DM + k], inv[k], ck[k]) * sa[b];
     }
     const double g = drk - s;
     const double adr = wsum(av * drk), as = wsum(av * s), gb = wsum(g * by);
@@ -487,33 +499,33 @@ __global__ void __launch_bounds__(WPB * 32) k_vecchia_predict(VPredArgs a) {
   __syncwarp();
   const int mi = m;
   const int nbv = (lane < mi) ? ki[lane] : -1;
-  double th[DM];
+  double ck[DM];
 #pragma unroll
-  for (int k = 0; k < DM; ++k) th[k] = (k < d) ? a.theta[k] : 1.0;
+  for (int k = 0; k < DM; ++k) ck[k] = cov_scale<K>() / ((k < d) ? a.theta[k] : 1.0);
   if (lane < mi)
 #pragma unroll
     for (int k = 0; k < DM; ++k) xs[lane * DM + k] = (k < d) ? a.X[nbv + (int64_t)k * n] : 0.0;
   __syncwarp();
   double r = 0.0;
-  if (lane < mi) {
+  if (lane < mi) {  // division- and log1p-free covariance forms (common.cuh)
     for (int b = 0; b < mi; ++b) {
       double c;
       if (b == lane) {
         c = 1.0 + a.num_nugget;
       } else {
-        double s = 0.0;
+        double s = 0.0, pr = 1.0;
 #pragma unroll
         for (int k = 0; k < DM; ++k)
-          if (k < d) s += cov_term<K>(xs[lane * DM + k] - xs[b * DM + k], th[k]);
-        c = cov_from_sum<K>(s);
+          if (k < d) cov_fast_term<K>(xs[lane * DM + k] - xs[b * DM + k], ck[k], s, pr);
+        c = cov_fast_finish<K>(s, pr);
       }
       RN[lane * LDP + b] = c;
     }
-    double s = 0.0;
+    double s = 0.0, pr = 1.0;
 #pragma unroll
     for (int k = 0; k < DM; ++k)
-      if (k < d) s += cov_term<K>(xs[lane * DM + k] - xq[k], th[k]);
-    r = cov_from_sum<K>(s);
+      if (k < d) cov_fast_term<K>(xs[lane * DM + k] - xq[k], ck[k], s, pr);
+    r = cov_fast_finish<K>(s, pr);
   }
   __syncwarp();
   int inc = 0;

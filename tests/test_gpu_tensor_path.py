@@ -60,8 +60,9 @@ def _config2_like(n, d=8, seed=123):
     return X, y, theta
 
 
+@pytest.mark.parametrize("path", [1, 2])
 @pytest.mark.parametrize("n", [640, 2048])
-def test_tc_mixed_loglik(gpu_lib, tensor_path, n):
+def test_tc_mixed_loglik(gpu_lib, tensor_path, n, path):
     X, y, theta = _config2_like(n)
     alpha = 1.0 / (1.0 + 1e-6)
     k = gpu_lib.Kriging("matern5_2", "nugget")
@@ -72,7 +73,7 @@ def test_tc_mixed_loglik(gpu_lib, tensor_path, n):
     k.set_precision(7)
     tensor_path.lkg_set_tensor_path(0)
     ll_s, g_s, _ = k.logLikelihoodFun(g, True)
-    tensor_path.lkg_set_tensor_path(1)
+    tensor_path.lkg_set_tensor_path(path)
     ll_t, g_t, _ = k.logLikelihoodFun(g, True)
     assert abs(ll_t - ll64) / abs(ll64) < 1e-8
     assert rel_err(g_t, g64) < 1e-6

@@ -57,18 +57,19 @@ def test_vll_full_conditioning_equals_exact_ll(gpu_lib):
 
 
 def test_vll_gradient_vs_fd(gpu_lib):
-    # KrigingVecchiaTest.cpp:63-84
-    X, y = _data(200, 2, 4)
+    # KrigingVecchiaTest.cpp:63-84: n = 100, y = sin(3 x1) + cos(5 x2) + x1 x2, two theta, h = 1e-6, 1e-3
+    X = np.random.default_rng(123).uniform(size=(100, 2))
+    y = np.sin(3.0 * X[:, 0]) + np.cos(5.0 * X[:, 1]) + X[:, 0] * X[:, 1]
     k = gpu_lib.Kriging("matern5_2")
     k.fit(y, X, "constant", False, "none", "LLVecchia(15)", {"theta": np.array([[0.2, 0.3]])})
-    th = np.array([0.2, 0.3])
-    _, g = k.logLikelihoodVecchiaFun(th, True)
     h = 1e-6
-    for j in range(2):
-        e = np.zeros(2)
-        e[j] = h
-        fd = (k.logLikelihoodVecchiaFun(th + e)[0] - k.logLikelihoodVecchiaFun(th - e)[0]) / (2 * h)
-        assert abs(g[j] - fd) < 1e-3 * max(1.0, abs(fd))
+    for th in (np.array([0.2, 0.3]), np.array([0.5, 0.15])):
+        _, g = k.logLikelihoodVecchiaFun(th, True)
+        for j in range(2):
+            e = np.zeros(2)
+            e[j] = h
+            fd = (k.logLikelihoodVecchiaFun(th + e)[0] - k.logLikelihoodVecchiaFun(th - e)[0]) / (2 * h)
+            assert abs(g[j] - fd) < 1e-3 * max(1.0, abs(fd)), (th, j, g[j], fd)
 
 
 @pytest.mark.parametrize("exact", [True, False])
