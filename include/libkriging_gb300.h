@@ -170,8 +170,8 @@ int lkg_stats_report(char* out, int cap);
 int lkg_ozaki_gemm_check(int M, int N, int K, const double* A, const double* B, int slices, double* C);
 /* No counterpart in the reference: the kernels of the mixed path's digit products -- 0 = mma.sync (warp-level),
  * 1 = tcgen05 (TMEM accumulators) for the Cholesky and triangular-inverse updates with W^T W on mma.sync (the
- * faster pair on this part), 2 = tcgen05 for all three.  Returns the path now in effect; the environment variable
- * LK_OZAKI_TC sets the initial value. */
+ * faster pair on this part; the default), 2 = tcgen05 for all three.  Returns the path now in effect; the
+ * environment variable LK_OZAKI_TC sets the initial value. */
 int lkg_set_tensor_path(int tc);
 int lkg_get_tensor_path(void);
 

@@ -21,25 +21,51 @@ __global__ void k_oz_split(int rows, int K, const double* __restrict__ p, int64_
     if (k0 < K) x0 = pb[(int64_t)k0 * s_k];
     if (k1 < K) x1 = pb[(int64_t)k1 * s_k];
   }
-  double m = fmax(fabs(x0), fabs(x1));
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-  int e = 0;
-  if (m > 0.0) {
-    int E;
-    frexp(m, &E);
-    e = E + 1;  // |x| 2^-e < 1/2, so every balanced base-256 digit lies in [-128, 128]
+  // Integer arithmetic on the IEEE-754 bits throughout (FP64 instructions are scarce on this part).  The chunk
+  // exponent e = E + 1 with max|x| = f 2^E, f in [1/2, 1), so |x| 2^-e < 1/2; every x becomes the integer
+  // V = round(x 2^(8S - e)), |V| < 2^(8S - 1), cut into S balanced base-256 digits, each in [-128, 128].
+  const unsigned long long b0 = (unsigned long long)__double_as_longlong(x0) & 0x7FFFFFFFFFFFFFFFull;
+  const unsigned long long b1 = (unsigned long long)__double_as_longlong(x1) & 0x7FFFFFFFFFFFFFFFull;
+  unsigned long long bm = b0 > b1 ? b0 : b1;  // |x| orders as its bit pattern
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long ob = __shfl_xor_sync(0xffffffffu, bm, o);
+    bm = ob > bm ? ob : bm;
   }
-  double v0 = ldexp(x0, -e), v1 = ldexp(x1, -e);
+  int e = 0;
+  if (bm != 0) {
+    const int bx = (int)(bm >> 52);
+    // E of max|x| = f 2^E: biased exponent - 1022 for a normal number; subnormals from their leading bit
+    const int E = bx ? bx - 1022 : (64 - __clzll((long long)(bm & 0xFFFFFFFFFFFFFull))) - 1074;
+    e = E + 1;
+  }
+  const int S = out.S;
+  auto to_fixed = [&](double x) -> long long {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const unsigned long long ab = bits & 0x7FFFFFFFFFFFFFFFull;
+    if (ab == 0) return 0;
+    const int bx = (int)(ab >> 52);
+    const unsigned long long mant = bx ? ((ab & 0xFFFFFFFFFFFFFull) | (1ull << 52)) : (ab & 0xFFFFFFFFFFFFFull);
+    const int ex = bx ? bx - 1075 : -1074;  // x = mant 2^ex
+    const int sh = ex + 8 * S - e;          // V = mant 2^sh
+    long long V;
+    if (sh >= 0)
+      V = (long long)(mant << sh);  // |V| < 2^(8S - 1) <= 2^63
+    else if (sh > -64)
+      V = (long long)((mant + (1ull << (-sh - 1))) >> (-sh));
+    else
+      V = 0;
+    return (bits >> 63) ? -V : V;
+  };
+  long long V0 = to_fixed(x0), V1 = to_fixed(x1);
   __nv_bfloat16* base = out.planes + b * out.plane_bstride;
-  for (int i = 0; i < out.S; ++i) {
-    v0 *= 256.0;
-    v1 *= 256.0;
-    const double d0 = rint(v0), d1 = rint(v1);
-    v0 -= d0;
-    v1 -= d1;
+  for (int i = S - 1; i >= 0; --i) {  // least significant digit first
+    const long long d0 = (i == 0) ? V0 : ((V0 + 128) & 255) - 128;
+    const long long d1 = (i == 0) ? V1 : ((V1 + 128) & 255) - 128;
+    V0 = (V0 - d0) >> 8;
+    V1 = (V1 - d1) >> 8;
     __nv_bfloat16* row = base + (((int64_t)i * out.nchunk + c) * out.rows_pad + r) * OZ_CHUNK;
-    row[lane] = __double2bfloat16(d0);
-    row[lane + 32] = __double2bfloat16(d1);
+    row[lane] = __float2bfloat16_rn((float)d0);
+    row[lane + 32] = __float2bfloat16_rn((float)d1);
   }
   if (lane == 0) out.exps[b * out.exp_bstride + (int64_t)c * out.rows_pad + r] = e;
 }
@@ -275,10 +301,12 @@ size_t split_plane_elems(int rows, int K, int S) {
 
 size_t split_exp_elems(int rows, int K) { return (size_t)ceil_div(K, OZ_CHUNK) * ceil_div(rows, 128) * 128; }
 
+// default 1: tcgen05 for the Cholesky and triangular-inverse updates, mma.sync for W^T W (the fastest measured pair:
+// 865 ms against 1040 ms per n = 16384 evaluation on the mma.sync kernels alone)
 int& oz_tc_flag() {
   static int f = [] {
     const char* e = std::getenv("LK_OZAKI_TC");
-    return e ? std::atoi(e) : 0;
+    return e ? std::atoi(e) : 1;
   }();
   return f;
 }

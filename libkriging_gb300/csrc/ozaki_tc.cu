@@ -356,7 +356,7 @@ __global__ void __launch_bounds__(384, 1) k_oz_tcp(TcArgs g, long long ntiles) {
 
   if (t == 0) {
     for (int i = 0; i < S; ++i) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 96;\n" ::"r"(bar(bars.full_a[i])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 32;\n" ::"r"(bar(bars.full_a[i])));  // its owner warp
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar(bars.adone[i])));
     }
     for (int q = 0; q < 2; ++q) {
@@ -378,8 +378,10 @@ __global__ void __launch_bounds__(384, 1) k_oz_tcp(TcArgs g, long long ntiles) {
   bool ok = true;
 
   if (w >= 8 && w <= 10) {
-    // ---------------- producers ----------------
-    const int pt = t - 256;  // 0 .. 95
+    // ---------------- producers: warp pw owns the digits i = pw (mod 3), of A and of B ----------------
+    // the three warps stream different digits at the same time, so a job's staging latency is that of about
+    // S / 3 dependent copies instead of S
+    const int pw = w - 8;
     int job = 0;
     for (long long ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
       TileJob T;
@@ -391,37 +393,38 @@ __global__ void __launch_bounds__(384, 1) k_oz_tcp(TcArgs g, long long ntiles) {
           break;
         }
         const uint32_t bdst = sB + bb * B_BUF;
-        for (int idx = pt; idx < S * TC_N * 8; idx += 96) {
-          const int seg = idx & 7, rr = idx >> 3, i = rr / TC_N, r = rr % TC_N;
-          cp16(bdst + (uint32_t)(i * TC_N + r) * 128u + (uint32_t)((seg ^ (r & 7)) * 16),
-               pb + (((int64_t)i * g.SB.nchunk + c) * g.SB.rows_pad + T.n0 + r) * OZ_CHUNK + seg * 8);
-        }
+        for (int i = pw; i < S; i += 3)
+          for (int idx = lane; idx < TC_N * 8; idx += 32) {
+            const int seg = idx & 7, r = idx >> 3;
+            cp16(bdst + (uint32_t)(i * TC_N + r) * 128u + (uint32_t)((seg ^ (r & 7)) * 16),
+                 pb + (((int64_t)i * g.SB.nchunk + c) * g.SB.rows_pad + T.n0 + r) * OZ_CHUNK + seg * 8);
+          }
         asm volatile("cp.async.commit_group;\n" ::: "memory");
-        // digit i's copies are issued before digit i-1's are awaited: two digits in flight
-        for (int i = 0; i < S; ++i) {
+        bool b_announced = false;
+        for (int i = pw; i < S; i += 3) {
           if (job >= 1 && !warp_wait(bar(bars.adone[i]), (job - 1) & 1)) {
             ok = false;
             break;
           }
           const uint32_t adst = sA + i * A_SLOT;
-          for (int idx = pt; idx < TC_M * 8; idx += 96) {
+          for (int idx = lane; idx < TC_M * 8; idx += 32) {
             const int seg = idx & 7, r = idx >> 3;
             cp16(adst + (uint32_t)r * 128u + (uint32_t)((seg ^ (r & 7)) * 16),
                  pa + (((int64_t)i * g.SA.nchunk + c) * g.SA.rows_pad + T.m0 + r) * OZ_CHUNK + seg * 8);
           }
-          asm volatile("cp.async.commit_group;\n" ::: "memory");
-          if (i > 0) {
-            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
-            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-            if (i == 1) mbar_arrive(bar(bars.full_b[bb]));
-            mbar_arrive(bar(bars.full_a[i - 1]));
+          asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+          asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+          if (!b_announced) {
+            mbar_arrive(bar(bars.full_b[bb]));
+            b_announced = true;
           }
+          mbar_arrive(bar(bars.full_a[i]));
         }
-        if (!ok) break;
-        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-        if (S == 1) mbar_arrive(bar(bars.full_b[bb]));
-        mbar_arrive(bar(bars.full_a[S - 1]));
+        if (ok && !b_announced) {  // a warp without A digits (S < 3) still owes its share of B
+          asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+          asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+          mbar_arrive(bar(bars.full_b[bb]));
+        }
       }
     }
     if (!ok) atomicExch(&g_oz_tc_error, 1);
