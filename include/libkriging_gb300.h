@@ -53,6 +53,19 @@ int lkg_kriging_log_likelihood_fun(void* ptr, const double* theta, int theta_n, 
                                    double* ll_out, double* grad_out, double* hess_out);
 /* libkriging_c.h:126 lk_kriging_log_likelihood */
 double lkg_kriging_log_likelihood(void* ptr);
+/* libkriging_c.h:118-123 lk_kriging_leave_one_out_fun: LOO = |errorsLOO|^2 / n and dLOO/dtheta (theta_n = d) */
+int lkg_kriging_leave_one_out_fun(void* ptr, const double* theta, int theta_n, int return_grad, double* loo_out,
+                                  double* grad_out);
+/* libkriging_c.h:133 lk_kriging_leave_one_out: leaveOneOutFun at the model's theta */
+double lkg_kriging_leave_one_out(void* ptr);
+/* libkriging_c.h:136 lk_kriging_leave_one_out_vec: yhat_out[n] = y - errorsLOO, stderr_out[n] = sqrt(sigma2LOO sigma2) */
+int lkg_kriging_leave_one_out_vec(void* ptr, const double* theta, int theta_n, double* yhat_out, double* stderr_out);
+/* libkriging_c.h:125-130 lk_kriging_log_marg_post_fun: log marginal posterior and its gradient (theta_n = d, or d + 1
+ * with alpha for a NuggetKriging model; d alone takes the model's alpha) */
+int lkg_kriging_log_marg_post_fun(void* ptr, const double* theta, int theta_n, int return_grad, double* lmp_out,
+                                  double* grad_out);
+/* libkriging_c.h:134 lk_kriging_log_marg_post */
+double lkg_kriging_log_marg_post(void* ptr);
 /* No counterpart in the reference: k candidates (k x theta_n column-major) evaluated in one batched GPU pass;
  * ll_out[k], grad_out k x theta_n column-major. */
 int lkg_kriging_log_likelihood_fun_batch(void* ptr, const double* thetas, int k, int theta_n, int return_grad,

@@ -36,6 +36,11 @@ _SIGS = {
     "lkg_kriging_summary": (_cp, [_vp]),
     "lkg_kriging_log_likelihood_fun": (_i, [_vp, _dp, _i, _i, _i, _dp, _dp, _dp]),
     "lkg_kriging_log_likelihood": (_d, [_vp]),
+    "lkg_kriging_leave_one_out_fun": (_i, [_vp, _dp, _i, _i, _dp, _dp]),
+    "lkg_kriging_leave_one_out": (_d, [_vp]),
+    "lkg_kriging_leave_one_out_vec": (_i, [_vp, _dp, _i, _dp, _dp]),
+    "lkg_kriging_log_marg_post_fun": (_i, [_vp, _dp, _i, _i, _dp, _dp]),
+    "lkg_kriging_log_marg_post": (_d, [_vp]),
     "lkg_kriging_log_likelihood_fun_batch": (_i, [_vp, _dp, _i, _i, _i, _dp, _dp]),
     "lkg_kriging_log_likelihood_fun_bench": (_i, [_vp, _dp, _i, _i, _dp, _dp, ctypes.c_char_p, _i]),
     "lkg_kriging_kernel": (_cp, [_vp]),

@@ -239,6 +239,55 @@ double lkg_kriging_log_likelihood(void* ptr) {
   CATCH_RETURN_NAN
 }
 
+int lkg_kriging_leave_one_out_fun(void* ptr, const double* theta, int theta_n, int return_grad, double* loo_out,
+                                  double* grad_out) {
+  try {
+    std::vector<double> t(theta, theta + theta_n);
+    auto [loo, grad] = K(ptr)->leaveOneOutFun(t, return_grad != 0);
+    if (loo_out) *loo_out = loo;
+    if (grad_out && return_grad) std::memcpy(grad_out, grad.data(), sizeof(double) * grad.size());
+    return 0;
+  }
+  CATCH_RETURN
+}
+
+double lkg_kriging_leave_one_out(void* ptr) {
+  try {
+    return K(ptr)->leaveOneOut();
+  }
+  CATCH_RETURN_NAN
+}
+
+int lkg_kriging_leave_one_out_vec(void* ptr, const double* theta, int theta_n, double* yhat_out, double* stderr_out) {
+  try {
+    std::vector<double> t(theta, theta + theta_n);
+    auto [yhat, sd] = K(ptr)->leaveOneOutVec(t);
+    if (yhat_out) std::memcpy(yhat_out, yhat.data(), sizeof(double) * yhat.size());
+    if (stderr_out) std::memcpy(stderr_out, sd.data(), sizeof(double) * sd.size());
+    return 0;
+  }
+  CATCH_RETURN
+}
+
+int lkg_kriging_log_marg_post_fun(void* ptr, const double* theta, int theta_n, int return_grad, double* lmp_out,
+                                  double* grad_out) {
+  try {
+    std::vector<double> t(theta, theta + theta_n);
+    auto [lmp, grad] = K(ptr)->logMargPostFun(t, return_grad != 0);
+    if (lmp_out) *lmp_out = lmp;
+    if (grad_out && return_grad) std::memcpy(grad_out, grad.data(), sizeof(double) * grad.size());
+    return 0;
+  }
+  CATCH_RETURN
+}
+
+double lkg_kriging_log_marg_post(void* ptr) {
+  try {
+    return K(ptr)->logMargPost();
+  }
+  CATCH_RETURN_NAN
+}
+
 const char* lkg_kriging_kernel(void* ptr) {
   try {
     return K(ptr)->kernel().c_str();

@@ -145,7 +145,7 @@ Engine::Engine(int kernel, int n, int d, int p, int ndesign, const double* X, co
 
 Engine::~Engine() {
   for (double* p : {dX_, dY_, dF_, dA_, dDinv_, dW_, dRinv_, dFY_, dEstar_, dxv_, dtheta_, dfactor_, ddiag_, dgram_,
-                    dbeta_, drstar_, dsse_, dpart_, dadj_, dvec_, dcol_})
+                    dbeta_, drstar_, dsse_, dpart_, dadj_, dvec_, dcol_, dloo_m_, dloo_at_, dloo_vec_})
     if (p) cudaFree(p);
   if (dinfo_) cudaFree(dinfo_);
   if (dgls_info_) cudaFree(dgls_info_);
@@ -509,9 +509,16 @@ void Engine::evaluate(int batch, const double* thetas, const double* factors, bo
       wtw_lower(dW_, lda_, mstride_, n, dRinv_, lda_, mstride_, batch, st_);
     }
     tm.lap("R^-1 = L^-T * L^-1");
-    adjoint_sums(kernel_, n, d, dXb, xbs, dtheta_, dfactor_, dxv_, n, dRinv_, lda_, mstride_, dpart_, dadj_, batch,
-                 st_);
-    tm.lap("gradR computation [optimized]");
+    if (lmp_mode_ && p > 0) {  // B = R^-1 - A'A in the lower triangle of R^-1
+      build_At(batch);
+      sub_aat_lower(n, p, dloo_at_, (int64_t)n * p, dRinv_, lda_, mstride_, batch, st_);
+      tm.lap("B = R^-1 - RiF (F'RiF)^-1 F'Ri");
+    }
+    if (!skip_adjoint_) {
+      adjoint_sums(kernel_, n, d, dXb, xbs, dtheta_, dfactor_, dxv_, n, dRinv_, lda_, mstride_, dpart_, dadj_, batch,
+                   st_);
+      tm.lap("gradR computation [optimized]");
+    }
   }
 
   // ---- results to host ----
@@ -522,8 +529,12 @@ void Engine::evaluate(int batch, const double* thetas, const double* factors, bo
   LKG_CUDA(cudaMemcpyAsync(sse.data(), dsse_, sizeof(double) * batch, cudaMemcpyDeviceToHost, st_));
   LKG_CUDA(cudaMemcpyAsync(beta.data(), dbeta_, sizeof(double) * beta.size(), cudaMemcpyDeviceToHost, st_));
   LKG_CUDA(cudaMemcpyAsync(gls.data(), dgls_info_, sizeof(int) * batch, cudaMemcpyDeviceToHost, st_));
+  std::vector<double> rstar((size_t)p * p * batch);
+  if (p > 0)
+    LKG_CUDA(cudaMemcpyAsync(rstar.data(), drstar_, sizeof(double) * rstar.size(), cudaMemcpyDeviceToHost, st_));
   const int nacc = adjoint_nacc(d);
-  if (with_grad) {
+  const bool adj_out = with_grad && !skip_adjoint_;
+  if (adj_out) {
     adj.resize((size_t)nacc * batch);
     LKG_CUDA(cudaMemcpyAsync(adj.data(), dadj_, sizeof(double) * adj.size(), cudaMemcpyDeviceToHost, st_));
   }
@@ -538,10 +549,121 @@ void Engine::evaluate(int batch, const double* thetas, const double* factors, bo
     }
     o.logdet = 2.0 * gram[(size_t)b * gram_stride_ + (p + 1) * (p + 1)];
     o.sse = sse[b];
+    o.rstar_logdet = 0.0;
+    for (int j = 0; j < p; ++j) o.rstar_logdet += std::log(rstar[(size_t)b * p * p + j + (size_t)j * p]);
     o.beta.assign(beta.begin() + (size_t)b * std::max(p, 1), beta.begin() + (size_t)b * std::max(p, 1) + p);
-    if (with_grad) {
+    if (adj_out) {
       o.adj.assign(adj.begin() + (size_t)b * nacc, adj.begin() + (size_t)(b + 1) * nacc);
       o.adj[2 * d + 3] -= (double)(n - nv_entry[b]);  // padded R^-1 diagonal entries are exactly 1
+    }
+  }
+}
+
+void Engine::ensure_loo_buffers(bool with_product) {
+  if (!dloo_at_) dalloc(&dloo_at_, (size_t)cap_ * n_ * std::max(p_, 1));
+  if (with_product && !dloo_m_) {
+    dalloc(&dloo_m_, (size_t)mstride_);
+    dalloc(&dloo_vec_, (size_t)n_ * (2 * d_ + 2));
+  }
+}
+
+// A' = L^-T Q* with Q* = F* Rstar^-1 (the thin QR of F*; A'A does not depend on the signs of Q*'s columns)
+void Engine::build_At(int batch) {
+  const int n = n_, p = p_;
+  ensure_loo_buffers(false);
+  for (int b = 0; b < batch; ++b)
+    LKG_CUDA(cudaMemcpyAsync(dloo_at_ + (size_t)b * n * p, dFY_ + (size_t)b * fystride_, sizeof(double) * n * p,
+                             cudaMemcpyDeviceToDevice, st_));
+  trsm_lower_left_t(dA_, lda_, mstride_, n, dDinv_, dloo_at_, n, (int64_t)n * p, p, batch, st_);
+  right_solve_upper(n, p, dloo_at_, (int64_t)n * p, drstar_, batch, st_);
+}
+
+void Engine::evaluate_lmp(int batch, const double* thetas, const double* factors, bool with_grad,
+                          std::vector<EvalOut>& out) {
+  if (ndesign_ != 1) throw std::invalid_argument("evaluate_lmp: engine holds several designs");
+  lmp_mode_ = true;
+  try {
+    evaluate(batch, thetas, factors, with_grad, out, nullptr);
+  } catch (...) {
+    lmp_mode_ = false;
+    throw;
+  }
+  lmp_mode_ = false;
+}
+
+void Engine::leave_one_out(int batch, const double* thetas, const double* factors, bool want_grad,
+                           std::vector<LooOut>& out) {
+  if (ndesign_ != 1) throw std::invalid_argument("leave_one_out: engine holds several designs");
+  const int n = n_, d = d_, p = p_;
+  std::vector<EvalOut> ev;
+  const int saved_slices = slices_;
+  slices_ = 0;
+  skip_adjoint_ = true;
+  try {
+    evaluate(batch, thetas, factors, true, ev, nullptr);
+  } catch (...) {
+    slices_ = saved_slices;
+    skip_adjoint_ = false;
+    throw;
+  }
+  slices_ = saved_slices;
+  skip_adjoint_ = false;
+  ensure_loo_buffers(true);
+  if (p > 0) build_At(batch);
+  out.assign(batch, LooOut());
+  for (int b = 0; b < batch; ++b) {
+    LooOut& o = out[b];
+    o.ev = ev[b];
+    if (ev[b].status != 0) continue;
+    double* Bm = dW_ + (size_t)b * mstride_;     // L^-1 is not needed any more: B goes here
+    double* G = dRinv_ + (size_t)b * mstride_;   // R^-1 is consumed by B: G_k goes here
+    const double* By = dxv_ + (size_t)b * n;     // L^-T E*
+    double* vdiag = dloo_vec_;                   // diag(B)
+    double* vby = dloo_vec_ + n;                 // By
+    loo_build_B(n, p, G, lda_, dloo_at_ + (size_t)b * n * p, Bm, lda_, st_);
+    LKG_CUDA(cudaMemcpy2DAsync(vdiag, sizeof(double), Bm, sizeof(double) * (lda_ + 1), sizeof(double), n,
+                               cudaMemcpyDeviceToDevice, st_));
+    LKG_CUDA(cudaMemcpyAsync(vby, By, sizeof(double) * n, cudaMemcpyDeviceToDevice, st_));
+    if (want_grad) {
+      const double* th = dtheta_ + (size_t)b * d;
+      for (int k = 0; k < d; ++k) {
+        loo_gradR(kernel_, n, d, dX_, th, factors[b], k, G, lda_, st_);
+        gemm_tiles(n, n, n, 1.0, MatView{G, 1, lda_, 0}, MatView{Bm, 1, lda_, 0}, 0.0, dloo_m_, lda_, 0, 1, false,
+                   st_);
+        col_dot(n, Bm, lda_, dloo_m_, lda_, dloo_vec_ + (size_t)(2 + 2 * k) * n, st_);  // diag(B G_k B)
+        col_dot(n, By, 0, dloo_m_, lda_, dloo_vec_ + (size_t)(3 + 2 * k) * n, st_);     // (G_k B)' By
+      }
+    }
+    const int nvec = want_grad ? 2 * d + 2 : 2;
+    std::vector<double> hv((size_t)n * nvec);
+    LKG_CUDA(cudaMemcpyAsync(hv.data(), dloo_vec_, sizeof(double) * hv.size(), cudaMemcpyDeviceToHost, st_));
+    LKG_CUDA(cudaStreamSynchronize(st_));
+    // host assembly (Kriging.cpp:411-465), n-vectors only
+    const double* dg = hv.data();
+    const double* by = hv.data() + n;
+    o.s2.resize(n);
+    o.errors.resize(n);
+    double acc = 0.0;
+    for (int i = 0; i < n; ++i) {
+      o.s2[i] = 1.0 / dg[i];
+      o.errors[i] = o.s2[i] * by[i];
+      acc += o.errors[i] * o.errors[i];
+    }
+    o.loo = acc / n;
+    if (want_grad) {
+      o.grad.assign(d, 0.0);
+      for (int k = 0; k < d; ++k) {
+        const double* bgb = hv.data() + (size_t)(2 + 2 * k) * n;
+        const double* bgy = hv.data() + (size_t)(3 + 2 * k) * n;
+        double s = 0.0;
+        for (int i = 0; i < n; ++i) {
+          const double diagdB = -bgb[i];
+          const double ds2 = -o.s2[i] * o.s2[i] * diagdB;
+          const double derr = ds2 * by[i] - o.s2[i] * bgy[i];
+          s += o.errors[i] * derr;
+        }
+        o.grad[k] = 2.0 * s / n;
+      }
     }
   }
 }

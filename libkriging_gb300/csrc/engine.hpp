@@ -25,6 +25,15 @@ struct EvalOut {
   double rcond = -1.0;         // rcond(L)^2 of the accepted factor (when the check ran)
   int slices = 0;              // 0: FP64 path; > 0: tensor-core digit slices used for the O(n^3) products
   bool retreated = false;      // the mixed factorisation hit a non-positive pivot and was redone in FP64
+  double rstar_logdet = 0.0;   // sum log Rstar_jj, Rstar = chol_upper(F*'F*) (= chol(F' R^-1 F) of the LMP)
+};
+
+struct LooOut {
+  EvalOut ev;                  // the populate_Model part (status, beta, SSE, ...)
+  double loo = 0.0;            // sum(errors^2) / n
+  std::vector<double> grad;    // dLOO/dtheta (want_grad)
+  std::vector<double> errors;  // sigma2LOO * By
+  std::vector<double> s2;      // sigma2LOO = 1 / diag(B)
 };
 
 class Engine {
@@ -47,6 +56,19 @@ class Engine {
   // designs[b]; several entries may name the same design.
   void evaluate(int batch, const double* thetas, const double* factors, bool with_grad, std::vector<EvalOut>& out,
                 std::map<std::string, double>* bench = nullptr, const int* designs = nullptr);
+
+  // Leave-one-out objective (Kriging::_leaveOneOut, Kriging.cpp:353-468) at each theta with R = factor C + (1 -
+  // factor) I (factor 1 for NoiseModel None), on the FP64 path: By = L^-T E*, A' = L^-T F* Rstar^-1, B = R^-1 - A'A, sigma2LOO = 1 / diag(B),
+  // errors = sigma2LOO * By; with want_grad, per dimension k: G_k = R o dlnC_k (zero diagonal), M = G_k B,
+  // diag(B G_k B) = column dots of B and M, B G_k By = M' By.  One design only.  Leaves the factor of every
+  // entry in HBM like evaluate() (R^-1 and L^-1 are overwritten).
+  void leave_one_out(int batch, const double* thetas, const double* factors, bool want_grad,
+                     std::vector<LooOut>& out);
+
+  // evaluate() for the marginal-posterior objective (Kriging::_logMargPost, Kriging.cpp:487-652): with with_grad the
+  // adjoint sums are taken against B = R^-1 - R^-1 F (F' R^-1 F)^-1 F' R^-1 instead of R^-1, which turns
+  // T2_k into tr(G_k B) / 2 and U2 into tr(C B) / 2 (compute_lmp_theta_ans, KrigingImpl.cpp:887-921).
+  void evaluate_lmp(int batch, const double* thetas, const double* factors, bool with_grad, std::vector<EvalOut>& out);
 
   // Copies of the last evaluation's state for batch entry b (host, column-major):
   //   L (n x n lower, upper part zero), Fstar (n x p), ystar (n), Rstar (p x p upper), Estar (n)
@@ -85,12 +107,19 @@ class Engine {
 
  private:
   void ensure_grad_buffers();
+  void ensure_loo_buffers(bool with_product);
+  // A' = L^-T F* Rstar^-1 (n x p per entry, stride n p) into dloo_at_ for entries [0, batch)
+  void build_At(int batch);
   void ensure_mixed_buffers(bool with_grad);
   // rcond(L)^2 per entry, dtrcon('1') style estimate on each entry's first nvb[b] rows / columns
   void rcond_batch(int batch, std::vector<double>& rc2, const std::vector<int>& nvb);
 
   int kernel_, n_, d_, p_, cap_;
   int ndesign_ = 1;
+  bool skip_adjoint_ = false;                      // leave_one_out needs R^-1 but not the adjoint sums
+  bool lmp_mode_ = false;                          // evaluate_lmp: adjoint sums against B
+  double *dloo_m_ = nullptr, *dloo_at_ = nullptr;  // leave-one-out scratch: n x n product, A' (n x p per entry)
+  double* dloo_vec_ = nullptr;                     // diag(B), By and per-dimension column dots (n x (2 d + 2))
   bool plain_chol_ = false;
   double base_diag_ = 1.0;
   std::vector<int> nvalid_;               // valid points per design

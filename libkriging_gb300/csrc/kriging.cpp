@@ -124,7 +124,9 @@ struct EvalRequest {
   double factor = 1.0;
   bool want_grad = false;
   bool vecchia = false;  // evaluate the Vecchia likelihood instead of the exact one
+  int kind = 0;          // exact objectives: 0 LL, 1 LMP, 2 LOO
   EvalOut out;
+  LooOut lout;
   VecchiaOut vout;
   std::exception_ptr err;
   bool done = false;
@@ -304,6 +306,134 @@ double Kriging::logLikelihood() {
   return std::get<0>(logLikelihoodFun(g, false, false));
 }
 
+// ---- leave-one-out (Kriging.cpp:353-484) ----
+std::tuple<double, std::vector<double>> Kriging::leaveOneOutFun(const std::vector<double>& theta, bool return_grad) {
+  if (m_n == 0) throw std::runtime_error("Kriging model has no data: call fit() first");
+  if ((int)theta.size() != m_d)
+    throw std::invalid_argument("leaveOneOutFun: theta should have length " + std::to_string(m_d));
+  ensure_engine(1);
+  const double factor = (m_noise_model == NoiseModel::Nugget) ? m_alpha : 1.0;
+  std::vector<LooOut> out;
+  m_eval->leave_one_out(1, theta.data(), &factor, return_grad, out);
+  m_evals++;
+  if (out[0].ev.status != 0) throw std::runtime_error(out[0].ev.message);
+  return {out[0].loo, return_grad ? out[0].grad : std::vector<double>()};
+}
+
+std::tuple<std::vector<double>, std::vector<double>> Kriging::leaveOneOutVec(const std::vector<double>& theta) {
+  if (m_n == 0) throw std::runtime_error("Kriging model has no data: call fit() first");
+  if ((int)theta.size() != m_d)
+    throw std::invalid_argument("leaveOneOutVec: theta should have length " + std::to_string(m_d));
+  ensure_engine(1);
+  const double factor = (m_noise_model == NoiseModel::Nugget) ? m_alpha : 1.0;
+  std::vector<LooOut> out;
+  m_eval->leave_one_out(1, theta.data(), &factor, false, out);
+  m_evals++;
+  if (out[0].ev.status != 0) throw std::runtime_error(out[0].ev.message);
+  std::vector<double> yhat(m_n), sd(m_n);
+  const double s = std::sqrt(m_sigma2);
+  for (int i = 0; i < m_n; ++i) {
+    yhat[i] = m_y[i] - out[0].errors[i];
+    sd[i] = std::sqrt(out[0].s2[i]) * s;
+  }
+  return {yhat, sd};
+}
+
+double Kriging::leaveOneOut() { return std::get<0>(leaveOneOutFun(m_theta, false)); }
+
+// ---- log marginal posterior (Kriging.cpp:487-665, KrigingImpl.cpp:887-921) ----
+// With B = R^-1 - R^-1 F (F' R^-1 F)^-1 F' R^-1 and x = B y = L^-T E*, the reference's Wb_k = G_k B gives
+// tr(Wb_k) = 2 T2_k and y' Wb_k' Q_output = x' G_k x = 2 T1_k (adjoint sums against B), and for the nugget
+// direction U1, U2; S_2 = y' B y = SSE and chol(F' R^-1 F) = Rstar'.
+double Kriging::lmp_from(const EvalOut& o, const double* theta, double alpha, std::vector<double>* grad,
+                         int gdim) const {
+  if (o.status != 0) throw std::runtime_error(o.message);
+  const int n = m_n, d = m_d, p = m_p;
+  const bool nug = (m_noise_model == NoiseModel::Nugget);
+  double sigma2;
+  if (nug) {
+    if (m_est_sigma2 && m_est_nugget)
+      sigma2 = o.sse / (n - p);
+    else if (m_est_sigma2 || m_est_nugget)
+      sigma2 = m_sigma2 / alpha;
+    else
+      sigma2 = m_sigma2 + m_nugget;
+  } else if (m_est_sigma2) {
+    sigma2 = o.sse / (n - p);
+  } else {
+    sigma2 = m_sigma2;
+  }
+  const double log_S_2 = std::log(sigma2 * (n - p));
+  const double lml = -0.5 * o.logdet - o.rstar_logdet - (n - p) / 2.0 * log_S_2;
+  // default prior (RobustGaSP's approximate reference prior)
+  const double a = 0.2;
+  const double b = 1.0 / std::pow((double)n, 1.0 / d) * (a + d);
+  std::vector<double> CL(d);
+  double t = 0.0;
+  for (int k = 0; k < d; ++k) {
+    double mn = m_X[(size_t)k * n], mx = mn;
+    for (int i = 1; i < n; ++i) {
+      mn = std::min(mn, m_X[i + (size_t)k * n]);
+      mx = std::max(mx, m_X[i + (size_t)k * n]);
+    }
+    CL[k] = (mx - mn) / std::pow((double)n, 1.0 / d);
+    t += CL[k] / theta[k];
+  }
+  t += nug ? (1.0 - alpha) / alpha : 0.0;
+  const double lp = -b * t + a * std::log(t);
+  if (grad) {
+    grad->assign(gdim, 0.0);
+    const std::vector<double>& A = o.adj;  // [T1(d), T2(d), U1, U2, D1, D2] against B
+    for (int k = 0; k < d; ++k) {
+      const double ans = -A[d + k] + A[k] / sigma2;
+      (*grad)[k] = ans - (a * CL[k] / t - b * CL[k]) / (theta[k] * theta[k]);
+    }
+    if (nug && gdim > d) {
+      if (m_est_sigma2 || m_est_nugget) {
+        const double ans_d = -A[2 * d + 1] + A[2 * d] / sigma2;
+        (*grad)[d] = ans_d - (a / t - b) / std::pow(alpha, 2.0);
+      } else {
+        (*grad)[d] = 0.0;
+      }
+    }
+  }
+  return lml + lp;
+}
+
+std::tuple<double, std::vector<double>> Kriging::logMargPostFun(const std::vector<double>& gamma_in,
+                                                                bool return_grad) {
+  if (m_n == 0) throw std::runtime_error("Kriging model has no data: call fit() first");
+  const int d = m_d;
+  const bool nug = (m_noise_model == NoiseModel::Nugget);
+  std::vector<double> gamma = gamma_in;
+  if (nug && (int)gamma.size() == d) gamma.push_back(m_alpha);
+  const int gd = d + (nug ? 1 : 0);
+  if ((int)gamma.size() != gd)
+    throw std::invalid_argument("logMargPostFun: theta should have length " + std::to_string(d));
+  const double alpha = nug ? gamma[d] : 1.0;
+  const bool analytic = return_grad && m_est_sigma2;
+  ensure_engine(return_grad && !m_est_sigma2 ? d + 1 : 1);
+  std::vector<EvalOut> out;
+  m_eval->evaluate_lmp(1, gamma.data(), &alpha, analytic, out);
+  m_evals++;
+  std::vector<double> grad;
+  const double lmp = lmp_from(out[0], gamma.data(), alpha, analytic ? &grad : nullptr, gd);
+  if (return_grad && !m_est_sigma2) {  // forward differences, step 1e-6 in theta (Kriging.cpp:629-640)
+    const double eps = 1e-6;
+    std::vector<double> th((size_t)d * d), fac(d, alpha);
+    for (int k = 0; k < d; ++k)
+      for (int j = 0; j < d; ++j) th[(size_t)k * d + j] = gamma[j] + (j == k ? eps : 0.0);
+    std::vector<EvalOut> fd;
+    m_eval->evaluate_lmp(d, th.data(), fac.data(), false, fd);
+    m_evals += d;
+    grad.assign(gd, 0.0);
+    for (int k = 0; k < d; ++k) grad[k] = (lmp_from(fd[k], th.data() + (size_t)k * d, alpha, nullptr, gd) - lmp) / eps;
+  }
+  return {lmp, grad};
+}
+
+double Kriging::logMargPost() { return std::get<0>(logMargPostFun(m_theta, false)); }
+
 // commit the model at (theta, alpha): one exact evaluation kept in the model engine (KModel -> m_T, m_M, ...)
 void Kriging::commit(const std::vector<double>& theta, double alpha) {
   if (m_service) {  // batched with the other models' evaluations; no factor is kept (predict needs a plain commit)
@@ -332,9 +462,14 @@ void Kriging::fit(const std::vector<double>& y, const Mat& Xin, RegressionModel 
     throw std::runtime_error("Dimension of new data should be the same:\n X: (" + std::to_string(n) + "x" +
                              std::to_string(d) + "), y: (" + std::to_string(y.size()) + ")");
   const bool vecchia = objective.rfind("LLVecchia", 0) == 0;
-  if (!vecchia && objective != "LL")
+  if (!vecchia && objective != "LL" && objective != "LOO" && objective != "LMP")
     throw std::invalid_argument("Unsupported fit objective: " + objective +
-                                " (supported by the GPU build are: LL, LLVecchia, LLVecchia(m))");
+                                " (supported by the GPU build are: LL, LOO, LMP, LLVecchia, LLVecchia(m))");
+  const int obj_kind = (objective == "LMP") ? 1 : (objective == "LOO") ? 2 : 0;
+  if (obj_kind == 2 && m_noise_model != NoiseModel::None)  // Kriging.cpp:1471-1473
+    throw std::invalid_argument("LOO objective not supported for Nugget/Heterogeneous noise modes");
+  if (obj_kind != 0 && m_service)
+    throw std::invalid_argument("a shared evaluation service runs the LL objective only");
   if (vecchia) {
     parse_vll_m(objective);  // validate the spec early (throws on malformed), Kriging.cpp:1522-1524
     if (m_noise_model != NoiseModel::None)
@@ -618,28 +753,64 @@ void Kriging::fit(const std::vector<double>& y, const Mat& Xin, RegressionModel 
       g = g || dense[b]->want_grad;
     }
     std::vector<EvalOut> out;
+    if (obj_kind == 2) {
+      std::vector<LooOut> lo;
+      m_eval->leave_one_out(k, th.data(), fac.data(), g, lo);
+      m_evals += k;
+      for (int b = 0; b < k; ++b) dense[b]->lout = std::move(lo[b]);
+      return;
+    }
     if (m_service)
       m_service->evaluate(m_service_design, k, th.data(), fac.data(), g, out);
+    else if (obj_kind == 1)
+      m_eval->evaluate_lmp(k, th.data(), fac.data(), g, out);
     else
       m_eval->evaluate(k, th.data(), fac.data(), g, out, nullptr);
     m_evals += k;
     for (int b = 0; b < k; ++b) dense[b]->out = std::move(out[b]);
   });
+  // The objective to maximise (LL, LMP, or -LOO) and its gradient in theta (alpha) space.
   // exact_ll: the exact likelihood even under LLVecchia (the final exact-commit evaluation, Kriging.cpp:1532-1551)
   auto eval_ll = [&](const std::vector<double>& ta, bool want_grad, std::vector<double>* grad, bool exact_ll) {
     EvalRequest req;
     req.theta.assign(ta.begin(), ta.begin() + d);
     double extra = nug ? ta[d] : m_sigma2;
-    if (nug && !m_est_sigma2 && !m_est_nugget) extra = m_sigma2 / (m_sigma2 + m_nugget);
+    if (nug && obj_kind == 0 && !m_est_sigma2 && !m_est_nugget) extra = m_sigma2 / (m_sigma2 + m_nugget);
     req.factor = nug ? extra : 1.0;
-    req.want_grad = want_grad;
+    req.want_grad = want_grad && !(obj_kind == 1 && !m_est_sigma2);
     req.vecchia = vecchia && !exact_ll;
+    req.kind = obj_kind;
     batcher.submit(&req);
     if (req.err) std::rethrow_exception(req.err);
     if (req.vecchia) {
       if (req.vout.status != 0) throw std::runtime_error(req.vout.message);
       if (grad) *grad = req.vout.grad;
       return req.vout.vll;
+    }
+    if (obj_kind == 2) {  // maximise -LOO
+      if (req.lout.ev.status != 0) throw std::runtime_error(req.lout.ev.message);
+      if (grad) {
+        grad->assign(gd, 0.0);
+        for (int j = 0; j < d; ++j) (*grad)[j] = -req.lout.grad[j];
+      }
+      return -req.lout.loo;
+    }
+    if (obj_kind == 1) {
+      const double lmp = lmp_from(req.out, ta.data(), extra, req.want_grad ? grad : nullptr, gd);
+      if (want_grad && !req.want_grad) {  // sigma2 fixed: forward differences in theta (Kriging.cpp:629-640)
+        grad->assign(gd, 0.0);
+        for (int k = 0; k < d; ++k) {
+          EvalRequest r2;
+          r2.theta = req.theta;
+          r2.theta[k] += 1e-6;
+          r2.factor = req.factor;
+          r2.kind = 1;
+          batcher.submit(&r2);
+          if (r2.err) std::rethrow_exception(r2.err);
+          (*grad)[k] = (lmp_from(r2.out, r2.theta.data(), extra, nullptr, gd) - lmp) / 1e-6;
+        }
+      }
+      return lmp;
     }
     return loglik_from(req.out, extra, grad, gd);
   };
@@ -680,8 +851,10 @@ void Kriging::fit(const std::vector<double>& y, const Mat& Xin, RegressionModel 
       Lbfgsb opt(gd);
       opt.iprint = -1;
       opt.max_iter = cfg.max_iteration;
-      opt.pgtol = cfg.gradient_tolerance;
-      opt.factr = cfg.objective_rel_tolerance / 1e-13;
+      // LOO values scale like 1 / n^2 of the likelihood's (Kriging.cpp:1953-1958)
+      const double loo_scale = (obj_kind == 2) ? 1.0 / ((double)n * n) : 1.0;
+      opt.pgtol = cfg.gradient_tolerance * loo_scale;
+      opt.factr = cfg.objective_rel_tolerance / 1e-13 * loo_scale;
       std::vector<int> btype(gd, 2);
       int retry = 0;
       double best_f = std::numeric_limits<double>::infinity();
@@ -766,6 +939,7 @@ void Kriging::fit(const std::vector<double>& y, const Mat& Xin, RegressionModel 
       if (m_est_nugget) {
         const double total_var = m.sse / n;
         m_sigma2 = m_alpha * total_var;
+        if (obj_kind == 1) m_sigma2 = m_sigma2 * n / (n - m_p - 2);
         m_nugget = m_sigma2 / m_alpha - m_sigma2;
       } else {
         m_sigma2 = m_nugget * m_alpha / (1.0 - m_alpha);
@@ -774,7 +948,7 @@ void Kriging::fit(const std::vector<double>& y, const Mat& Xin, RegressionModel 
       if (m_est_nugget) m_nugget = m_sigma2 * (1.0 - m_alpha) / m_alpha;
     }
   } else if (m_est_sigma2) {
-    m_sigma2 = m.sse / n;
+    m_sigma2 = (obj_kind == 1) ? m.sse / (n - m_p) : m.sse / n;
   }
   m_last_fit_starts = multistart;
 }

@@ -71,6 +71,17 @@ class Kriging {
                              std::vector<double>& grad);
   double logLikelihood();
 
+  // leave-one-out (Kriging.hpp:135-143, Kriging.cpp:353-484, 666-668): theta only; R = C, or alpha C + (1 - alpha) I
+  // with the model's alpha for NoiseModel Nugget
+  std::tuple<double, std::vector<double>> leaveOneOutFun(const std::vector<double>& theta, bool return_grad);
+  // (y - errorsLOO, sqrt(sigma2LOO) sqrt(sigma2)) in the model's (normalised) units
+  std::tuple<std::vector<double>, std::vector<double>> leaveOneOutVec(const std::vector<double>& theta);
+  double leaveOneOut();
+  // log marginal posterior (Kriging.hpp:137-139, Kriging.cpp:487-665): gamma = theta, or [theta, alpha] (Nugget;
+  // theta alone takes the model's alpha)
+  std::tuple<double, std::vector<double>> logMargPostFun(const std::vector<double>& gamma, bool return_grad);
+  double logMargPost();
+
   // Vecchia (objective "LLVecchia" / "LLVecchia(m)"; Kriging.hpp:145-173, Kriging.cpp:718-924)
   std::tuple<double, std::vector<double>> logLikelihoodVecchiaFun(const std::vector<double>& theta, bool return_grad);
   void set_vecchia_exact_commit(bool b) { m_vecchia_exact_commit = b; }
@@ -138,6 +149,8 @@ class Kriging {
 
  private:
   double loglik_from(const EvalOut& o, double extra_param, std::vector<double>* grad, int gdim) const;
+  // log marginal posterior at (theta, alpha) from an evaluate_lmp result; grad (gdim) only when sigma2 is estimated
+  double lmp_from(const EvalOut& o, const double* theta, double alpha, std::vector<double>* grad, int gdim) const;
   void ensure_engine(int batch_cap);
   void commit(const std::vector<double>& theta, double alpha);
 

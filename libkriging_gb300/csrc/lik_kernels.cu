@@ -338,6 +338,100 @@ __global__ void k_lower_colsum_abs(int n, const double* __restrict__ L, int64_t 
   if (lane == 0) colsum[b * n + j] = s;
 }
 
+// ---- leave-one-out building blocks ----
+template <int K, int DM>
+__global__ void __launch_bounds__(256) k_loo_gradR(int n, int d, const double* __restrict__ X,
+                                                   const double* __restrict__ theta, double factor, int kdim,
+                                                   double* __restrict__ G, int64_t ldg) {
+  __shared__ double xi[DM][T], xj[DM][T], th[DM];
+  const int r0 = blockIdx.x * T, c0 = blockIdx.y * T, t = threadIdx.x;
+  for (int idx = t; idx < DM * T; idx += 256) {
+    const int k = idx / T, q = idx % T;
+    xi[k][q] = (k < d && r0 + q < n) ? X[(r0 + q) + (int64_t)k * n] : 0.0;
+    xj[k][q] = (k < d && c0 + q < n) ? X[(c0 + q) + (int64_t)k * n] : 0.0;
+  }
+  if (t < DM) th[t] = (t < d) ? theta[t] : 1.0;
+  __syncthreads();
+  const int ri = t & 63, i = r0 + ri;
+  if (i >= n) return;
+  for (int s = 0; s < 16; ++s) {
+    const int cj = (t >> 6) + 4 * s, j = c0 + cj;
+    if (j >= n) continue;
+    double v = 0.0;
+    if (j != i) {
+      double sum = 0.0, dk = 0.0;
+#pragma unroll
+      for (int k = 0; k < DM; ++k) {
+        if (k < d) {
+          const double dx = xj[k][cj] - xi[k][ri];
+          sum += cov_term<K>(dx, th[k]);
+          if (k == kdim) dk = dlncov_term<K>(dx, th[k]);
+        }
+      }
+      v = (cov_from_sum<K>(sum) * factor) * dk;
+    }
+    G[i + (int64_t)j * ldg] = v;
+  }
+}
+
+__global__ void k_loo_B(int n, int p, const double* __restrict__ Rinv, int64_t ldr, const double* __restrict__ At,
+                        double* __restrict__ B, int64_t ldb) {
+  const int i = blockIdx.x * 32 + (threadIdx.x & 31);
+  const int j = blockIdx.y * 8 + (threadIdx.x >> 5);
+  if (i >= n || j >= n) return;
+  double v = (i >= j) ? Rinv[i + (int64_t)j * ldr] : Rinv[j + (int64_t)i * ldr];
+  for (int k = 0; k < p; ++k) v -= At[i + (int64_t)k * n] * At[j + (int64_t)k * n];
+  B[i + (int64_t)j * ldb] = v;
+}
+
+__global__ void k_right_solve_upper(int n, int p, double* __restrict__ H, int64_t hstride,
+                                    const double* __restrict__ R) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  H += blockIdx.y * hstride;
+  R += (int64_t)blockIdx.y * p * p;
+  for (int j = 0; j < p; ++j) {
+    double v = H[i + (int64_t)j * n];
+    for (int l = 0; l < j; ++l) v -= H[i + (int64_t)l * n] * R[l + j * p];
+    H[i + (int64_t)j * n] = v / R[j + j * p];
+  }
+}
+
+__global__ void k_sub_aat_lower(int n, int p, const double* __restrict__ At, int64_t atstride, double* __restrict__ C,
+                                int64_t ldc, int64_t cstride) {
+  const int i = blockIdx.x * 32 + (threadIdx.x & 31);
+  const int j = blockIdx.y * 8 + (threadIdx.x >> 5);
+  if (i >= n || j > i) return;
+  const double* a = At + blockIdx.z * atstride;
+  double* c = C + blockIdx.z * cstride;
+  double v = c[i + (int64_t)j * ldc];
+  for (int k = 0; k < p; ++k) v -= a[i + (int64_t)k * n] * a[j + (int64_t)k * n];
+  c[i + (int64_t)j * ldc] = v;
+}
+
+__global__ void k_col_dot(int n, const double* __restrict__ B, int64_t ldb, const double* __restrict__ M,
+                          int64_t ldm, double* __restrict__ out) {
+  const int col = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (col >= n) return;
+  const double* b = B + (int64_t)col * ldb;
+  const double* m = M + (int64_t)col * ldm;
+  double s = 0.0;
+  for (int r = lane; r < n; r += 32) s = fma(b[r], m[r], s);
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) out[col] = s;
+}
+
+template <int K, int DM>
+struct LooGradRLaunch {
+  static void run(int n, int d, const double* X, const double* theta, double factor, int kdim, double* G,
+                  int64_t ldg, cudaStream_t st) {
+    LaunchTimer lt("k_loo_gradR", st, (double)n * n, 8.0 * n * n);
+    k_loo_gradR<K, DM><<<dim3(ceil_div(n, T), ceil_div(n, T), 1), 256, 0, st>>>(n, d, X, theta, factor, kdim, G,
+                                                                                           ldg);
+    LKG_LAUNCH("k_loo_gradR");
+  }
+};
+
 template <int K, int DM>
 struct CovLowerLaunch {
   static void run(int n, int d, const double* X, int64_t xb, const double* theta, const double* factor,
@@ -444,6 +538,42 @@ void lower_colsum_abs(int n, const double* L, int64_t ldl, int64_t lstride, doub
   LaunchTimer lt("k_lower_colsum_abs", st, 0.5 * n * (n + 1.0) * batch, 4.0 * n * (n + 1.0) * batch);
   k_lower_colsum_abs<<<dim3(ceil_div(n, 8), 1, batch), 256, 0, st>>>(n, L, ldl, lstride, colsum);
   LKG_LAUNCH("k_lower_colsum_abs");
+}
+
+void loo_gradR(int kernel, int n, int d, const double* X, const double* theta, double factor, int k, double* G,
+               int64_t ldg, cudaStream_t st) {
+  if (n <= 0) return;
+  dispatch_kd<LooGradRLaunch>(kernel, d, n, d, X, theta, factor, k, G, ldg, st);
+}
+
+void loo_build_B(int n, int p, const double* Rinv, int64_t ldr, const double* At, double* B, int64_t ldb,
+                 cudaStream_t st) {
+  if (n <= 0) return;
+  LaunchTimer lt("k_loo_B", st, 2.0 * n * n * p, 8.0 * n * n * 1.5);
+  k_loo_B<<<dim3(ceil_div(n, 32), ceil_div(n, 8), 1), 256, 0, st>>>(n, p, Rinv, ldr, At, B, ldb);
+  LKG_LAUNCH("k_loo_B");
+}
+
+void right_solve_upper(int n, int p, double* H, int64_t hstride, const double* Rstar, int batch, cudaStream_t st) {
+  if (n <= 0 || p <= 0) return;
+  LaunchTimer lt("k_right_solve_upper", st, (double)n * p * p * batch, 16.0 * n * p * batch);
+  k_right_solve_upper<<<dim3(ceil_div(n, 128), batch), 128, 0, st>>>(n, p, H, hstride, Rstar);
+  LKG_LAUNCH("k_right_solve_upper");
+}
+
+void sub_aat_lower(int n, int p, const double* At, int64_t atstride, double* C, int64_t ldc, int64_t cstride,
+                   int batch, cudaStream_t st) {
+  if (n <= 0 || p <= 0) return;
+  LaunchTimer lt("k_sub_aat_lower", st, (double)n * (n + 1.0) * p * batch, 8.0 * n * (n + 1.0) * batch);
+  k_sub_aat_lower<<<dim3(ceil_div(n, 32), ceil_div(n, 8), batch), 256, 0, st>>>(n, p, At, atstride, C, ldc, cstride);
+  LKG_LAUNCH("k_sub_aat_lower");
+}
+
+void col_dot(int n, const double* B, int64_t ldb, const double* M, int64_t ldm, double* out, cudaStream_t st) {
+  if (n <= 0) return;
+  LaunchTimer lt("k_col_dot", st, 2.0 * n * n, 16.0 * n * n);
+  k_col_dot<<<ceil_div(n, 8), 256, 0, st>>>(n, B, ldb, M, ldm, out);
+  LKG_LAUNCH("k_col_dot");
 }
 
 }  // namespace lkg

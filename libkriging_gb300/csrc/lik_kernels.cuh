@@ -54,4 +54,20 @@ void residual_sse(int n, int p, const double* FY, int64_t ldfy, int64_t fystride
 void lower_colsum_abs(int n, const double* L, int64_t ldl, int64_t lstride, double* colsum, int batch,
                       cudaStream_t st);
 
+// ---- leave-one-out (Kriging.cpp:353-468) ----
+// G(i, j) = R(i, j) dlnC/dtheta_k (x_i - x_j) for i != j with R(i, j) = factor C(x_i - x_j), G(i, i) = 0;
+// full n x n, ld ldg; the reference's formulas.
+void loo_gradR(int kernel, int n, int d, const double* X, const double* theta, double factor, int k, double* G,
+               int64_t ldg, cudaStream_t st);
+// full symmetric B = R^-1 - A'A from the lower triangle of R^-1 (ldr) and At = A' (n x p, column-major, ld n)
+void loo_build_B(int n, int p, const double* Rinv, int64_t ldr, const double* At, double* B, int64_t ldb,
+                 cudaStream_t st);
+// At = H Rstar^-1 in place (H n x p, ld n, batch stride hstride; Rstar p x p upper, column-major, batch stride p*p)
+void right_solve_upper(int n, int p, double* H, int64_t hstride, const double* Rstar, int batch, cudaStream_t st);
+// lower triangle of C (ldc, batch stride cstride) -= At At' (At n x p, ld n, batch stride atstride)
+void sub_aat_lower(int n, int p, const double* At, int64_t atstride, double* C, int64_t ldc, int64_t cstride,
+                   int batch, cudaStream_t st);
+// out[i] = sum_j B(j, i) M(j, i) (one warp per column, fixed order)
+void col_dot(int n, const double* B, int64_t ldb, const double* M, int64_t ldm, double* out, cudaStream_t st);
+
 }  // namespace lkg

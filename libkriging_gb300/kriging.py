@@ -140,6 +140,47 @@ class Kriging:
                 raise _lib.LibKrigingError(err)
         return v
 
+    def _nan_checked(self, v):
+        if np.isnan(v):
+            err = _lib.last_error()
+            if err:
+                raise _lib.LibKrigingError(err)
+        return v
+
+    # ---- leave-one-out and marginal posterior (Kriging.hpp:135-143) ----
+    def leaveOneOutFun(self, theta, return_grad=False):
+        """Kriging::leaveOneOutFun -> (loo, grad); grad is empty unless return_grad."""
+        t = np.ascontiguousarray(np.asarray(theta, dtype=np.float64).reshape(-1))
+        v = ctypes.c_double()
+        g = np.zeros(t.size) if return_grad else None
+        check(_lib.load().lkg_kriging_leave_one_out_fun(self._h, ptr(t), t.size, int(bool(return_grad)),
+                                                        ctypes.byref(v), ptr(g)))
+        return v.value, (g if return_grad else np.zeros(0))
+
+    def leaveOneOutVec(self, theta):
+        """Kriging::leaveOneOutVec -> (leave-one-out means, standard deviations) in the model's units."""
+        t = np.ascontiguousarray(np.asarray(theta, dtype=np.float64).reshape(-1))
+        n = self.y().size
+        yhat, sd = np.zeros(n), np.zeros(n)
+        check(_lib.load().lkg_kriging_leave_one_out_vec(self._h, ptr(t), t.size, ptr(yhat), ptr(sd)))
+        return yhat, sd
+
+    def leaveOneOut(self):
+        return self._nan_checked(_lib.load().lkg_kriging_leave_one_out(self._h))
+
+    def logMargPostFun(self, theta, return_grad=False):
+        """Kriging::logMargPostFun -> (lmp, grad)."""
+        t = np.ascontiguousarray(np.asarray(theta, dtype=np.float64).reshape(-1))
+        v = ctypes.c_double()
+        gd = t.size + (1 if (self.noise_model() == "nugget" and t.size == self.centerX().size) else 0)
+        g = np.zeros(gd) if return_grad else None
+        check(_lib.load().lkg_kriging_log_marg_post_fun(self._h, ptr(t), t.size, int(bool(return_grad)),
+                                                        ctypes.byref(v), ptr(g)))
+        return v.value, (g if return_grad else np.zeros(0))
+
+    def logMargPost(self):
+        return self._nan_checked(_lib.load().lkg_kriging_log_marg_post(self._h))
+
     def predict(self, X, return_stdev=True, return_cov=False, return_deriv=False):
         X = _as_X(X)
         m, d = X.shape

@@ -438,6 +438,110 @@ class OracleKriging:
                 grad[d] = 0.0
         return ll, grad
 
+    # Kriging.cpp:353-468 (_leaveOneOut, NoiseModel None): B = L^-T L^-1 - A'A with A = Q*' L^-1 (Q* the thin QR
+    # factor of F*), sigma2LOO = 1 / diag(B), errors = sigma2LOO * (L^-T E*), LOO = |errors|^2 / n; gradient per
+    # theta_k with gradR_k = R o dlnC_k (zero diagonal).  Returns (loo, grad or None, yhat, sigma2LOO).
+    def _gradR_all(self, R, theta):
+        """gradR_k = R o DlnCovDtheta_k over the strict lower triangle, mirrored, zero diagonal (Kriging.cpp:430-440)."""
+        n, d = self.X.shape
+        G = np.zeros((d, n, n))
+        for i in range(n):
+            for j in range(i):
+                g = R[i, j] * dlncov(self.kernel, self.X[i] - self.X[j], theta)
+                G[:, i, j] = g
+                G[:, j, i] = g
+        return G
+
+    def leave_one_out(self, theta, return_grad=True):
+        n, d = self.X.shape
+        theta = np.asarray(theta, dtype=np.float64).reshape(-1)
+        alpha = self.alpha if self.noise_model == "nugget" else 1.0
+        m = populate_model(self.kernel, self.X, self.y, self.F, theta, alpha, None, False, self.cfg)
+        Linv = solve_lower(m.L, np.eye(n))
+        By = Linv.T @ m.Estar
+        Qs, _ = np.linalg.qr(m.Fstar, mode="reduced")
+        A = Qs.T @ Linv
+        B = Linv.T @ Linv - A.T @ A
+        s2 = 1.0 / np.diag(B)
+        errors = s2 * By
+        loo = float(errors @ errors) / n
+        grad = None
+        if return_grad:
+            grad = np.zeros(d)
+            Gs = self._gradR_all(m.R, theta)
+            for k in range(d):
+                G = Gs[k]
+                diagdB = -np.einsum("ij,jk,ki->i", B, G, B)
+                ds2 = -s2 * s2 * diagdB
+                derr = ds2 * By - s2 * (B @ (G @ By))
+                grad[k] = 2.0 * float(errors @ derr) / n
+        return loo, grad, self.y - errors, s2
+
+    # Kriging.cpp:487-652 (_logMargPost, RobustGaSP's marginal likelihood + approximate reference prior) and
+    # KrigingImpl.cpp:887-921 (compute_lmp_theta_ans), in the reference's order of operations.
+    def log_marg_post(self, gamma, return_grad=True):
+        n, d = self.X.shape
+        p = self.F.shape[1]
+        gamma = np.asarray(gamma, dtype=np.float64).reshape(-1)
+        nug = self.noise_model == "nugget"
+        if nug and gamma.size == d:
+            gamma = np.append(gamma, self.alpha)
+        theta = gamma[:d]
+        alpha = float(gamma[d]) if nug else 1.0
+        m = populate_model(self.kernel, self.X, self.y, self.F, theta, alpha, None, False, self.cfg)
+        Rinv_X = solve_upper_t(m.L, m.Fstar)
+        Xt_Rinv_X = self.F.T @ Rinv_X
+        if p > 0:
+            LX, _ = safe_chol_lower(Xt_Rinv_X, self.cfg)
+            P = Rinv_X @ solve_upper_t(LX, solve_lower(LX, Rinv_X.T))
+        else:
+            LX, P = np.zeros((0, 0)), np.zeros((n, n))
+        yt_Rinv = solve_upper_t(m.L, m.ystar.reshape(-1, 1))[:, 0]
+        S_2 = float(yt_Rinv @ self.y - self.y @ P @ self.y)
+        if nug:
+            if self.est_sigma2 and self.est_nugget:
+                sigma2 = S_2 / (n - p)
+            elif self.est_sigma2 or self.est_nugget:
+                sigma2 = self.sigma2 / alpha
+            else:
+                sigma2 = self.sigma2 + self.nugget
+        elif self.est_sigma2:
+            sigma2 = S_2 / (n - p)
+        else:
+            sigma2 = self.sigma2
+        log_S_2 = math.log(sigma2 * (n - p))
+        lml = -np.sum(np.log(np.diag(m.L))) - np.sum(np.log(np.diag(LX))) - (n - p) / 2.0 * log_S_2
+        a = 0.2
+        b = 1.0 / n ** (1.0 / d) * (a + d)
+        CL = (self.X.max(axis=0) - self.X.min(axis=0)) / n ** (1.0 / d)
+        t = float(np.sum(CL / theta)) + ((1.0 - alpha) / alpha if nug else 0.0)
+        lp = -b * t + a * math.log(t)
+        value = float(lml + lp)
+        if not return_grad:
+            return value, None
+        grad = np.zeros(gamma.size)
+        if self.est_sigma2:
+            Q_output = yt_Rinv - P @ self.y
+            Gs = self._gradR_all(m.R, theta)
+            ans = np.zeros(d)
+            for k in range(d):
+                Wb = solve_upper_t(m.L, solve_lower(m.L, Gs[k])).T - Gs[k] @ P
+                ans[k] = -np.trace(Wb) / 2.0 + float(self.y @ Wb.T @ Q_output) / (2.0 * sigma2)
+            grad[:d] = ans - (a * CL / t - b * CL) / theta ** 2
+            if nug:
+                if self.est_sigma2 or self.est_nugget:
+                    gR = m.R / alpha
+                    np.fill_diagonal(gR, 0.0)
+                    Wb = solve_upper_t(m.L, solve_lower(m.L, gR)).T - gR @ P
+                    ans_d = -np.trace(Wb) / 2.0 + float(self.y @ Wb.T @ Q_output) / (2.0 * sigma2)
+                    grad[d] = ans_d - (a / t - b) / alpha ** 2
+        else:
+            for k in range(d):
+                ge = gamma.copy()
+                ge[k] += 1e-6
+                grad[k] = (self.log_marg_post(ge, False)[0] - value) / 1e-6
+        return value, grad
+
     # KrigingImpl.cpp:145-251, Kriging.cpp:2240-2285 (mean and stdev)
     def predict(self, Xn, theta, beta, sigma2, alpha=1.0, return_stdev=True, fixed_beta=False):
         """fixed_beta: beta is a given trend (is_beta_estim = false), so z = L \\ (y - F beta) (KrigingImpl.cpp:116)."""

@@ -1,6 +1,7 @@
 """Regenerate tests/golden/loglik_golden.json from the reference's own known-answer CSVs.
 
-The reference ships LL / dLL/dtheta known answers for a gauss kernel at theta = 0.3 * ones(d), constant
+The reference ships LL / dLL/dtheta known answers (and, for data1-scal, the leave-one-out value and its
+gradient, binding_consistency_test.py:46-72) for a gauss kernel at theta = 0.3 * ones(d), constant
 trend, no normalisation, NoiseModel None (bindings/Python/pylibkriging/tests/binding_consistency_test.py:46-121
 reads them from tests/references/). This script copies the inputs and answers verbatim (every CSV value
 parsed to float64) into one JSON fixture so that the tests can run where the reference tree is absent.
@@ -39,6 +40,8 @@ def main(ref_root):
         y=_csv(refs / f"{prefix}-y.csv").tolist(),
         ll=float(_csv(refs / f"{prefix}-result-logLikelihood.csv")[0]),
         grad=_csv(refs / f"{prefix}-result-logLikelihoodGrad.csv").tolist(),
+        loo=float(_csv(refs / f"{prefix}-result-leaveOneOut.csv")[0]),
+        loo_grad=_csv(refs / f"{prefix}-result-leaveOneOutGrad.csv").tolist(),
     ))
     out = dict(
         source="libKriging tests/references/{data2-grad-1..10,data1-scal}-*.csv",

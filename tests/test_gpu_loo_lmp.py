@@ -1,0 +1,190 @@
+"""GPU leave-one-out and log-marginal-posterior objectives against the oracle (Kriging.cpp:353-665,
+KrigingImpl.cpp:887-921), the reference's known LOO answer, and the reference's fit tests for both objectives
+(tests/KrigingFitTest.cpp:73-169, tests/NuggetKrigingFitTest.cpp:84-135 of libKriging)."""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+KERNELS = ["gauss", "exp", "matern3_2", "matern5_2"]
+
+
+def _data(n, d, seed):
+    rng = np.random.default_rng(seed)
+    X = rng.uniform(size=(n, d))
+    y = np.sin(2 * np.pi * X).sum(axis=1) + 0.5 * X[:, 0] * X[:, -1]
+    return X, y
+
+
+def _model(lk, y, X, kernel, theta, regmodel="constant", noise_model="none", params=None):
+    k = lk.Kriging(kernel, noise_model)
+    P = {"theta": np.asarray(theta, dtype=float).reshape(1, -1)}
+    P.update(params or {})
+    k.fit(y, X, regmodel, False, "none", "LL", P)
+    return k
+
+
+def test_loo_known_answer(gpu_lib, golden):
+    """data1-scal, gauss, theta = 0.3: the reference's LOO value and gradient (binding_consistency_test.py:46-68)."""
+    c = golden["cases"][-1]
+    X, y = np.array(c["X"]), np.array(c["y"])
+    k = _model(gpu_lib, y, X, "gauss", [0.3])
+    loo, g = k.leaveOneOutFun(np.array([0.3]), True)
+    assert rel_err(loo, c["loo"]) < 1e-10
+    assert rel_err(g, c["loo_grad"]) < 1e-10
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
+@pytest.mark.parametrize("regmodel", ["constant", "linear"])
+def test_loo_matches_oracle(gpu_lib, kernel, regmodel):
+    X, y = _data(120, 3, 11)
+    th = np.array([0.35, 0.5, 0.3]) if kernel != "gauss" else np.array([0.15, 0.2, 0.12])
+    k = _model(gpu_lib, y, X, kernel, th, regmodel)
+    loo, g = k.leaveOneOutFun(th, True)
+    ora = O.OracleKriging(y, X, kernel, regmodel)
+    loo_o, g_o, yhat_o, s2_o = ora.leave_one_out(th, True)
+    assert rel_err(loo, loo_o) < 1e-9
+    assert rel_err(g, g_o) < 1e-8
+    loo2, g2 = k.leaveOneOutFun(th, False)
+    assert loo2 == loo and g2.size == 0
+    yhat, sd = k.leaveOneOutVec(th)
+    assert rel_err(yhat, yhat_o) < 1e-10
+    assert rel_err(sd, np.sqrt(s2_o) * np.sqrt(k.sigma2())) < 1e-10
+
+
+def test_loo_nugget_model_uses_its_alpha(gpu_lib):
+    """leaveOneOutFun on a NuggetKriging model: R = alpha C + (1 - alpha) I with the model's alpha."""
+    X, y = _data(90, 2, 12)
+    th = np.array([0.3, 0.4])
+    k = _model(gpu_lib, y, X, "matern5_2", th, noise_model="nugget", params={"sigma2": 1.0, "nugget": 0.1})
+    alpha = 1.0 / 1.1
+    ora = O.OracleKriging(y, X, "matern5_2", noise_model="nugget", alpha=alpha)
+    loo_o, g_o, _, _ = ora.leave_one_out(th, True)
+    loo, g = k.leaveOneOutFun(th, True)
+    assert rel_err(loo, loo_o) < 1e-9
+    assert rel_err(g, g_o) < 1e-8
+
+
+def test_loo_gradient_fd_at_size(gpu_lib):
+    """n = 1000 (beyond the oracle's double loop): the analytic gradient against central differences of the GPU
+    LOO value."""
+    X, y = _data(1000, 4, 13)
+    th = np.array([0.4, 0.5, 0.45, 0.6])
+    k = _model(gpu_lib, y, X, "matern5_2", th)
+    loo, g = k.leaveOneOutFun(th, True)
+    for j in range(4):
+        e = np.zeros(4)
+        e[j] = 1e-4 * th[j]
+        fd = (k.leaveOneOutFun(th + e, False)[0] - k.leaveOneOutFun(th - e, False)[0]) / (2 * e[j])
+        assert abs(g[j] - fd) < 1e-5 * max(abs(fd), 1e-3 * np.abs(g).max()), (j, g[j], fd)
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_lmp_matches_oracle(gpu_lib, kernel):
+    X, y = _data(150, 3, 14)
+    th = np.array([0.35, 0.5, 0.3]) if kernel != "gauss" else np.array([0.15, 0.2, 0.12])
+    k = _model(gpu_lib, y, X, kernel, th, "linear")
+    v, g = k.logMargPostFun(th, True)
+    v_o, g_o = O.OracleKriging(y, X, kernel, "linear").log_marg_post(th, True)
+    assert rel_err(v, v_o) < 1e-10
+    assert rel_err(g, g_o) < 1e-8
+
+
+@pytest.mark.parametrize("est", ["both", "sigma2_fixed"])
+def test_lmp_nugget_matches_oracle(gpu_lib, est):
+    X, y = _data(100, 2, 15)
+    th = np.array([0.3, 0.4])
+    if est == "both":
+        k = _model(gpu_lib, y, X, "matern3_2", th, noise_model="nugget")
+        ora = O.OracleKriging(y, X, "matern3_2", noise_model="nugget")
+    else:
+        P = {"sigma2": 0.8, "is_sigma2_estim": False}
+        k = _model(gpu_lib, y, X, "matern3_2", th, noise_model="nugget", params=P)
+        ora = O.OracleKriging(y, X, "matern3_2", noise_model="nugget", est_sigma2=False, sigma2=0.8)
+    gam = np.array([0.3, 0.4, 0.85])
+    v, g = k.logMargPostFun(gam, True)
+    v_o, g_o = ora.log_marg_post(gam, True)
+    assert rel_err(v, v_o) < 1e-10
+    # fixed sigma2: forward differences of step 1e-6 on both sides, so rounding of the values shows at ~1e-10 / 1e-6
+    assert rel_err(g, g_o) < (1e-8 if est == "both" else 1e-3)
+
+
+def _branin(n, seed=123):
+    rng = np.random.default_rng(seed)
+    X = rng.uniform(size=(n, 2))
+    x1, x2 = X[:, 0], X[:, 1]
+    y = (x2 - 0.5 * x1 * x1 + 5 * x1 - 6) ** 2 + 10 * (1 - 0.1) * np.cos(x1) + 10
+    return X, y
+
+
+def test_fit_loo_bfgs10_beats_grid(gpu_lib):
+    """KrigingFitTest.cpp:73-121: a BFGS10 LOO fit reaches the best LOO of a 10 x 10 grid over [1e-6, 10]^2."""
+    X, y = _branin(20)
+    kg = gpu_lib.Kriging(y, X, "gauss", "constant", False, "BFGS", "LOO")
+    assert kg.objective() == "LOO"
+    grid = np.linspace(1e-6, 10.0, 10)
+    best = np.inf
+    for t1 in grid:
+        for t2 in grid:
+            try:
+                loo, _ = kg.leaveOneOutFun(np.array([t1, t2]), False)
+            except RuntimeError:
+                continue
+            best = min(best, loo)
+    kb = gpu_lib.Kriging(y, X, "gauss", "constant", False, "BFGS10", "LOO")
+    loo_b = kb.leaveOneOut()
+    assert loo_b <= best + 1e-3, (loo_b, best, kb.theta())
+    # committed sigma2 is SSE / n at theta_hat (Kriging.cpp:2196-2199)
+    ora = O.OracleKriging(y, X, "gauss")
+    m = O.populate_model("gauss", ora.X, ora.y, ora.F, kb.theta(), 1.0, None, False)
+    assert kb.sigma2() == pytest.approx(m.SSEstar / 20, rel=1e-8)
+
+
+def test_fit_lmp_bfgs10_beats_grid(gpu_lib):
+    """KrigingFitTest.cpp:123-169: a BFGS10 LMP fit within 1e-3 (relative) of the best LMP of the grid."""
+    X, y = _branin(20)
+    kg = gpu_lib.Kriging(y, X, "gauss", "constant", False, "BFGS", "LMP")
+    grid = np.linspace(1e-6, 10.0, 10)
+    best = -np.inf
+    for t1 in grid:
+        for t2 in grid:
+            try:
+                v, _ = kg.logMargPostFun(np.array([t1, t2]), False)
+            except RuntimeError:
+                continue
+            best = max(best, v)
+    kb = gpu_lib.Kriging(y, X, "gauss", "constant", False, "BFGS10", "LMP")
+    v_b = kb.logMargPost()
+    assert v_b >= best - abs(best) * 1e-3, (v_b, best, kb.theta())
+    ora = O.OracleKriging(y, X, "gauss")
+    m = O.populate_model("gauss", ora.X, ora.y, ora.F, kb.theta(), 1.0, None, False)
+    assert kb.sigma2() == pytest.approx(m.SSEstar / (20 - 1), rel=1e-8)  # SSE / (n - p) for LMP
+
+
+def test_fit_lmp_nugget_beats_grid(gpu_lib):
+    """NuggetKrigingFitTest.cpp:84-135: n = 25 with a nugget effect, a 5 x 5 x 4 grid of (theta, alpha)."""
+    rng = np.random.default_rng(123)
+    X = rng.uniform(size=(25, 2))
+    y = np.sin(4 * X[:, 0]) + np.cos(3 * X[:, 1]) + 0.05 * rng.standard_normal(25)
+    kg = gpu_lib.Kriging(y, X, "gauss", "constant", False, "BFGS", "LMP", noise_model="nugget")
+    best = -np.inf
+    for t1 in np.linspace(1e-6, 10.0, 5):
+        for t2 in np.linspace(1e-6, 10.0, 5):
+            for a in np.linspace(0.1, 0.9, 4):
+                try:
+                    v, _ = kg.logMargPostFun(np.array([t1, t2, a]), False)
+                except RuntimeError:
+                    continue
+                best = max(best, v)
+    kb = gpu_lib.Kriging(y, X, "gauss", "constant", False, "BFGS", "LMP", noise_model="nugget")
+    v_b = kb.logMargPost()
+    assert v_b >= best - abs(best) * 1e-3, (v_b, best, kb.theta())
+
+
+def test_fit_loo_rejects_nugget(gpu_lib):
+    X, y = _branin(20)
+    with pytest.raises(Exception, match="LOO objective not supported"):
+        gpu_lib.Kriging(y, X, "gauss", "constant", False, "BFGS", "LOO", noise_model="nugget")

@@ -102,3 +102,61 @@ def test_mt19937_stream_matches_std_uniform_real():
     # first raw outputs of std::mt19937 seeded with 123 (published reference sequence of the generator)
     raw = O.MT19937Stream(123).bg.random_raw(2)
     assert raw.tolist() == [2991312382, 3062119789]
+
+
+def test_oracle_loo_gradient_matches_fd():
+    """The restated _leaveOneOut gradient (Kriging.cpp:421-465) against central differences of the LOO value."""
+    rng = np.random.default_rng(5)
+    X = rng.uniform(size=(30, 2))
+    y = np.sin(3 * X[:, 0]) + np.cos(5 * X[:, 1]) + X[:, 0] * X[:, 1]
+    for kernel in ("gauss", "matern5_2"):
+        ora = O.OracleKriging(y, X, kernel)
+        th = np.array([0.3, 0.4])
+        loo, g, _, _ = ora.leave_one_out(th, True)
+        for k in range(2):
+            e = np.zeros(2)
+            e[k] = 1e-6
+            fd = (ora.leave_one_out(th + e, False)[0] - ora.leave_one_out(th - e, False)[0]) / 2e-6
+            assert abs(g[k] - fd) < 1e-5 * max(1.0, abs(fd)), (kernel, k, g[k], fd)
+
+
+def test_oracle_loo_matches_reference_known_answer(golden):
+    """LOO value and gradient for data1-scal at theta = 0.3 (binding_consistency_test.py:46-68)."""
+    c = golden["cases"][-1]
+    assert c["name"] == "data1-scal"
+    X, y = np.array(c["X"]), np.array(c["y"])
+    loo, g, _, _ = O.OracleKriging(y, X, "gauss").leave_one_out(golden["theta_value"] * np.ones(X.shape[1]), True)
+    assert rel_err(loo, c["loo"]) < TOL_GOLDEN
+    assert rel_err(g, c["loo_grad"]) < TOL_GOLDEN
+
+
+@pytest.mark.parametrize("kernel", ["gauss", "matern5_2"])
+def test_oracle_lmp_gradient_matches_fd(kernel):
+    """The restated _logMargPost gradient (Kriging.cpp:603-626, KrigingImpl.cpp:887-921) against central
+    differences, for NoiseModel None and Nugget (theta and alpha directions)."""
+    rng = np.random.default_rng(7)
+    X = rng.uniform(size=(30, 2))
+    y = np.sin(3 * X[:, 0]) + np.cos(5 * X[:, 1]) + X[:, 0] * X[:, 1]
+    cases = [(O.OracleKriging(y, X, kernel), np.array([0.3, 0.4])),
+             (O.OracleKriging(y, X, kernel, noise_model="nugget", alpha=0.9), np.array([0.3, 0.4, 0.9]))]
+    for ora, g0 in cases:
+        v, g = ora.log_marg_post(g0, True)
+        for k in range(g0.size):
+            e = np.zeros(g0.size)
+            e[k] = 1e-6
+            fd = (ora.log_marg_post(g0 + e, False)[0] - ora.log_marg_post(g0 - e, False)[0]) / 2e-6
+            assert abs(g[k] - fd) < 1e-5 * max(1.0, abs(fd)), (ora.noise_model, k, g[k], fd)
+
+
+def test_oracle_lmp_fixed_sigma2_forward_differences():
+    """sigma2 given: the reference takes forward differences with step 1e-6 (Kriging.cpp:629-640)."""
+    rng = np.random.default_rng(8)
+    X = rng.uniform(size=(25, 2))
+    y = np.sin(3 * X[:, 0]) + X[:, 1]
+    ora = O.OracleKriging(y, X, "gauss", est_sigma2=False, sigma2=0.5)
+    th = np.array([0.3, 0.5])
+    v, g = ora.log_marg_post(th, True)
+    for k in range(2):
+        e = np.zeros(2)
+        e[k] = 1e-6
+        assert g[k] == (ora.log_marg_post(th + e, False)[0] - v) / 1e-6
