@@ -265,7 +265,7 @@ def run_gpu(args):
     def roof(stats_, bound):
         name, s = max(stats_.items(), key=lambda kv: kv[1]["ms"])
         achieved = s["flops"] / (s["ms"] * 1e-3) / 1e12
-        if name.startswith("k_oz_tc"):
+        if name.startswith("k_oz_tc") or name.startswith("k_oz7"):
             pk, unit, src = tensor_peak, "TFLOP/s", "MEASURED_PEAKS.json bf16_tflops (burst, cuBLAS tcgen05)"
         elif name.startswith("k_oz"):
             pk, unit, src = tensor_peak, "TFLOP/s", ("MEASURED_PEAKS.json bf16_tflops (burst, cuBLAS tcgen05); this "
@@ -552,8 +552,9 @@ def main():
     ap.add_argument("--mixed", action="store_true", help="multistart / nested workloads on the mixed path")
     ap.add_argument("--nested-n", type=int, default=1_000_000, help="points of the nested workload")
     ap.add_argument("--nested-q", type=int, default=10_000, help="gPoE prediction points of the nested workload")
-    ap.add_argument("--tensor-path", type=int, default=None, choices=[0, 1, 2],
-                    help="digit-product kernels of the mixed path: 0 mma.sync, 1 tcgen05 (W^T W on mma.sync), 2 tcgen05 (default: the library's)")
+    ap.add_argument("--tensor-path", type=int, default=None, choices=[0, 1, 2, 3],
+                    help="digit-product kernels of the mixed path: 0 mma.sync, 1 tcgen05 (W^T W on mma.sync), 2 "
+                         "tcgen05, 3 tcgen05 on 7-bit digits in 256-wide k blocks (default: the library's)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -16,15 +16,15 @@
 extern "C" {
 #endif
 
-/* libkriging_c.h:9 lk_get_last_error -- message of the last failed call on this thread. */
+/* libkriging_c.h:10 lk_get_last_error -- message of the last failed call on this thread. */
 const char* lkg_get_last_error(void);
 
 /* ---------------------------------------------------------------- Kriging ---------------------------------------- */
 /* noise_model: "none" (or NULL) or "nugget".  "heterogeneous" is rejected (not part of this path). */
 
-/* libkriging_c.h:18 lk_kriging_new */
+/* libkriging_c.h:17 lk_kriging_new */
 void* lkg_kriging_new(const char* kernel, const char* noise_model);
-/* libkriging_c.h:19-41 lk_kriging_new_fit (theta: one starting point of length theta_n, as there) */
+/* libkriging_c.h:18-41 lk_kriging_new_fit (theta: one starting point of length theta_n, as there) */
 void* lkg_kriging_new_fit(const double* y, int n, const double* noise, int noise_n, const double* X, int nX, int d,
                           const char* kernel, const char* noise_model, const char* regmodel, int normalize,
                           const char* optim, const char* objective, const double* sigma2, int is_sigma2_estim,
@@ -46,12 +46,27 @@ int lkg_kriging_fit_params(void* ptr, const double* y, int n, const double* X, i
 int lkg_kriging_predict(void* ptr, const double* X_n, int m, int d, int return_stdev, int return_cov,
                         int return_deriv, double* mean_out, double* stdev_out, double* cov_out, double* mean_deriv_out,
                         double* stdev_deriv_out);
-/* libkriging_c.h:102 lk_kriging_summary */
+/* libkriging_c.h:43 lk_kriging_copy: a deep copy of the model (data, parameters and committed factor) */
+void* lkg_kriging_copy(void* ptr);
+/* libkriging_c.h:83-91 lk_kriging_update (Kriging.cpp:2433-2633): append n new points (X_u nX x d) in original units.
+ * refit with optim != "none": NoiseModel nugget refits on the joined data, NoiseModel none runs one warm-started
+ * L-BFGS-B from the current theta; otherwise theta is kept and the factor is extended by the incremental Cholesky on
+ * the GPU.  noise_u must be NULL / 0 (per-observation noise is not part of this path). */
+int lkg_kriging_update(void* ptr, const double* y_u, int n, const double* noise_u, int noise_n, const double* X_u,
+                       int nX, int d, int refit);
+/* libkriging_c.h:105 lk_kriging_save: libKriging's JSON model file, version 2 */
+int lkg_kriging_save(void* ptr, const char* filename);
+/* libkriging_c.h:106 lk_kriging_load: a model saved by lk_kriging_save or lkg_kriging_save (NULL on error) */
+void* lkg_kriging_load(const char* filename);
+/* libkriging_c.h:138 lk_kriging_cov_mat: cov_out (n1 x n2) = sigma2 C(X1, X2), X1 / X2 in original units */
+int lkg_kriging_cov_mat(void* ptr, const double* X1, int n1, int d1, const double* X2, int n2, int d2,
+                        double* cov_out);
+/* libkriging_c.h:107 lk_kriging_summary */
 const char* lkg_kriging_summary(void* ptr);
-/* libkriging_c.h:104-111 lk_kriging_log_likelihood_fun (return_hess is rejected; hess_out untouched) */
+/* libkriging_c.h:109-116 lk_kriging_log_likelihood_fun (return_hess is rejected; hess_out untouched) */
 int lkg_kriging_log_likelihood_fun(void* ptr, const double* theta, int theta_n, int return_grad, int return_hess,
                                    double* ll_out, double* grad_out, double* hess_out);
-/* libkriging_c.h:126 lk_kriging_log_likelihood */
+/* libkriging_c.h:132 lk_kriging_log_likelihood */
 double lkg_kriging_log_likelihood(void* ptr);
 /* libkriging_c.h:118-123 lk_kriging_leave_one_out_fun: LOO = |errorsLOO|^2 / n and dLOO/dtheta (theta_n = d) */
 int lkg_kriging_leave_one_out_fun(void* ptr, const double* theta, int theta_n, int return_grad, double* loo_out,
@@ -121,7 +136,7 @@ int lkg_kriging_predict_vecchia(void* ptr, const double* X_n, int q, int d, int 
  * device; on failure the message is stored like every other entry point's. */
 int lkg_vecchia_sets_noalloc(int n, int d, const double* X, int m, int* order, int* nbr, void* stream);
 
-/* getters, libkriging_c.h:141-166 */
+/* getters, libkriging_c.h:141-165 */
 const char* lkg_kriging_kernel(void* ptr);
 const char* lkg_kriging_optim(void* ptr);
 const char* lkg_kriging_objective(void* ptr);
@@ -133,6 +148,7 @@ int lkg_kriging_get_scaleX(void* ptr, double* out, int* d);
 int lkg_kriging_get_y(void* ptr, double* out, int* n);
 double lkg_kriging_get_centerY(void* ptr);
 double lkg_kriging_get_scaleY(void* ptr);
+int lkg_kriging_get_F(void* ptr, double* out, int* n, int* d);
 int lkg_kriging_get_T(void* ptr, double* out, int* n, int* d);
 int lkg_kriging_get_M(void* ptr, double* out, int* n, int* d);
 int lkg_kriging_get_z(void* ptr, double* out, int* n);
@@ -179,14 +195,23 @@ void lkg_stats_enable(int on);
 void lkg_stats_reset(void);
 int lkg_stats_report(char* out, int cap);
 /* No counterpart in the reference: C = A B^T (A M x K, B N x K, C M x N, column-major host buffers) through the
- * split-bf16 tensor-core GEMM with `slices` digits -- the check hook of the mixed path's emulated products. */
+ * split-bf16 tensor-core GEMM with `slices` digits -- the check hook of the mixed path's emulated products.  On
+ * tensor path 3, as in the engine, `slices` 8-bit slices become min(8, max(6, slices + 1)) 7-bit digits. */
 int lkg_ozaki_gemm_check(int M, int N, int K, const double* A, const double* B, int slices, double* C);
 /* No counterpart in the reference: the kernels of the mixed path's digit products -- 0 = mma.sync (warp-level),
- * 1 = tcgen05 (TMEM accumulators) for the Cholesky and triangular-inverse updates with W^T W on mma.sync (the
- * faster pair on this part; the default), 2 = tcgen05 for all three.  Returns the path now in effect; the
- * environment variable LK_OZAKI_TC sets the initial value. */
+ * 1 = tcgen05 (TMEM accumulators) for the Cholesky and triangular-inverse updates with W^T W on mma.sync, 2 =
+ * tcgen05 for all three, 3 = tcgen05 on 7-bit digits with one exponent per 256-wide k block and two-level (256 / 64)
+ * blocked Cholesky and triangular inverse, one digit more than the precision's slice count (the default: the
+ * fastest on this part).  Returns the path now in effect; the environment variable LK_OZAKI_TC sets the initial
+ * value. */
 int lkg_set_tensor_path(int tc);
 int lkg_get_tensor_path(void);
+/* No counterpart in the reference: one product of the 7-bit digit kernel on host data, S digits (6..8):
+ * mode 0: C (M x N) = A B^T (A M x K, B N x K); mode 1: C = A A^T lower (M x M); mode 2: C = W^T W lower with
+ * W = A (M x M, lower).  Returns 0, -1 (error text in lkg_get_last_error) or -2 when a wait of the kernel expired
+ * (where_out, 8 ints, receives where). */
+int lkg_oz7_mode_check(int mode, int M, int N, int K, const double* A, const double* B, int S, double* C,
+                       int* where_out);
 
 /* ------------------------------------------------------------- NestedKriging -------------------------------------- */
 /* libkriging_c.h:394-455 lk_nested_kriging_* (NestedKriging.hpp:63-105): partition (kmeans | random), submodel

@@ -34,6 +34,13 @@ _SIGS = {
                                     _dp, _i]),
     "lkg_kriging_predict": (_i, [_vp, _dp, _i, _i, _i, _i, _i, _dp, _dp, _dp, _dp, _dp]),
     "lkg_kriging_summary": (_cp, [_vp]),
+    "lkg_kriging_copy": (_vp, [_vp]),
+    "lkg_kriging_update": (_i, [_vp, _dp, _i, _dp, _i, _dp, _i, _i, _i]),
+    "lkg_kriging_save": (_i, [_vp, _cp]),
+    "lkg_kriging_load": (_vp, [_cp]),
+    "lkg_kriging_cov_mat": (_i, [_vp, _dp, _i, _i, _dp, _i, _i, _dp]),
+    "lkg_kriging_get_F": (_i, [_vp, _dp, _ip, _ip]),
+    "lkg_oz7_mode_check": (_i, [_i, _i, _i, _i, _dp, _dp, _i, _dp, _ip]),
     "lkg_kriging_log_likelihood_fun": (_i, [_vp, _dp, _i, _i, _i, _dp, _dp, _dp]),
     "lkg_kriging_log_likelihood": (_d, [_vp]),
     "lkg_kriging_leave_one_out_fun": (_i, [_vp, _dp, _i, _i, _dp, _dp]),

@@ -19,6 +19,11 @@ using lkg::Mat;
 
 static thread_local std::string g_last_error;
 
+namespace lkg {
+// the last-error text of this thread, for entry points implemented outside this file
+void set_last_error(const char* msg) { g_last_error = msg ? msg : ""; }
+}  // namespace lkg
+
 #define CATCH_RETURN                \
   catch (const std::exception& e) { \
     g_last_error = e.what();        \
@@ -170,6 +175,51 @@ int lkg_kriging_predict_vecchia(void* ptr, const double* X_n, int q, int d, int 
     auto [mean, sd] = K(ptr)->predictVecchia(mat_of(X_n, q, d), return_stdev != 0, m);
     if (mean_out) std::memcpy(mean_out, mean.data(), sizeof(double) * mean.size());
     if (stdev_out && return_stdev) std::memcpy(stdev_out, sd.data(), sizeof(double) * sd.size());
+    return 0;
+  }
+  CATCH_RETURN
+}
+
+void* lkg_kriging_copy(void* ptr) {
+  try {
+    return K(ptr)->copy().release();
+  }
+  CATCH_RETURN_NULL
+}
+
+int lkg_kriging_update(void* ptr, const double* y_u, int n, const double* noise_u, int noise_n, const double* X_u,
+                       int nX, int d, int refit) {
+  try {
+    if (noise_u && noise_n > 0) throw std::runtime_error("update(y, noise, X) requires NoiseModel::Heterogeneous");
+    std::vector<double> yv(y_u, y_u + n);
+    K(ptr)->update(yv, mat_of(X_u, nX, d), refit != 0);
+    return 0;
+  }
+  CATCH_RETURN
+}
+
+int lkg_kriging_save(void* ptr, const char* filename) {
+  try {
+    if (!filename) throw std::invalid_argument("save: null filename");
+    K(ptr)->save(filename);
+    return 0;
+  }
+  CATCH_RETURN
+}
+
+void* lkg_kriging_load(const char* filename) {
+  try {
+    if (!filename) throw std::invalid_argument("load: null filename");
+    return Kriging::load(filename).release();
+  }
+  CATCH_RETURN_NULL
+}
+
+int lkg_kriging_cov_mat(void* ptr, const double* X1, int n1, int d1, const double* X2, int n2, int d2,
+                        double* cov_out) {
+  try {
+    Mat R = K(ptr)->covMat(mat_of(X1, n1, d1), mat_of(X2, n2, d2));
+    if (cov_out) std::memcpy(cov_out, R.v.data(), sizeof(double) * R.v.size());
     return 0;
   }
   CATCH_RETURN
@@ -366,6 +416,17 @@ double lkg_kriging_get_scaleY(void* ptr) {
   }
   CATCH_RETURN_NAN
 }
+int lkg_kriging_get_F(void* ptr, double* out, int* n, int* d) {
+  try {
+    Kriging* k = K(ptr);
+    if (n) *n = k->n();
+    if (d) *d = k->p();
+    if (out) std::memcpy(out, k->F().data(), sizeof(double) * k->F().size());
+    return 0;
+  }
+  CATCH_RETURN
+}
+
 int lkg_kriging_get_T(void* ptr, double* out, int* n, int* d) {
   try {
     Mat T = K(ptr)->T();

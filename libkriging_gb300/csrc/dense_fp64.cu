@@ -281,9 +281,106 @@ __global__ void k_copy_dinv_block(const double* Dinv, int64_t dinv_bstride, int 
   }
 }
 
+// Inverses of the NB x NB diagonal blocks of an existing lower factor (one CTA per block): the same row wavefront as
+// k_potrf_diag, so a block inverted here equals the one the factorisation itself stored.
+__global__ void __launch_bounds__(NT) k_trtri_diag(const double* L, int64_t lda, int64_t mstride, int n, double* Dinv,
+                                                   int64_t dinv_bstride) {
+  extern __shared__ double tsm[];
+  double* s = tsm;
+  double* w = tsm + NB * DPAD;
+  const int64_t b = blockIdx.z;
+  const int blk = blockIdx.x, k0 = blk * NB, nb = min(NB, n - k0);
+  const double* Lb = L + b * mstride + k0 + (int64_t)k0 * lda;
+  const int t = threadIdx.x;
+  for (int idx = t; idx < NB * NB; idx += NT) {
+    const int i = idx & 63, j = idx >> 6;
+    s[i * DPAD + j] = (i < nb && j < nb && i >= j) ? Lb[i + (int64_t)j * lda] : 0.0;
+    w[i * DPAD + j] = 0.0;
+  }
+  __syncthreads();
+  const int c = t >> 2, q = t & 3;
+  for (int i = 0; i < nb; ++i) {
+    double sum = 0.0;
+    if (c <= i && c < nb)
+      for (int k = c + q; k < i; k += 4) sum = fma(s[i * DPAD + k], w[k * DPAD + c], sum);
+    sum += __shfl_xor_sync(0xffffffffu, sum, 1);
+    sum += __shfl_xor_sync(0xffffffffu, sum, 2);
+    if (q == 0 && c <= i && c < nb) w[i * DPAD + c] = ((i == c ? 1.0 : 0.0) - sum) / s[i * DPAD + i];
+    __syncthreads();
+  }
+  double* Db = Dinv + b * dinv_bstride + (int64_t)blk * NB * NB;
+  for (int idx = t; idx < NB * NB; idx += NT) {
+    const int i = idx & 63, j = idx >> 6;
+    Db[i + j * NB] = (i >= j) ? w[i * DPAD + j] : 0.0;
+  }
+}
+
+// D(c, r) = S(r, c) for an rows x cols block; 32 x 32 tiles through shared memory
+__global__ void k_transpose_copy(const double* __restrict__ S, int64_t lds, double* __restrict__ D, int64_t ldd,
+                                 int rows, int cols) {
+  __shared__ double tile[32][33];
+  const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
+  for (int k = ty; k < 32; k += 8) {
+    const int r = r0 + tx, c = c0 + k;
+    tile[k][tx] = (r < rows && c < cols) ? S[r + (int64_t)c * lds] : 0.0;
+  }
+  __syncthreads();
+  for (int k = ty; k < 32; k += 8) {
+    const int c = c0 + tx, r = r0 + k;  // D(c, r) with c contiguous
+    if (r < rows && c < cols) D[c + (int64_t)r * ldd] = tile[tx][k];
+  }
+}
+
+__global__ void k_add_diag(double* A, int64_t lda, int n, double v) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) A[i + (int64_t)i * lda] += v;
+}
+
+// zero the strictly upper part of an n x n block (column j: rows 0 .. j-1)
+__global__ void k_zero_upper(double* A, int64_t lda, int64_t mstride, int n) {
+  const int64_t b = blockIdx.z;
+  const int j = blockIdx.x;
+  double* col = A + b * mstride + (int64_t)j * lda;
+  for (int i = threadIdx.x; i < j && i < n; i += blockDim.x) col[i] = 0.0;
+}
+
 bool g_diag_attr_set = false;
+bool g_trtri_diag_attr_set = false;
 
 }  // namespace
+
+void trtri_diag_blocks(const double* L, int64_t lda, int64_t mstride, int n, double* Dinv, int batch,
+                       cudaStream_t st) {
+  const int nblk = ceil_div(n, NB);
+  const size_t smem = 2 * NB * DPAD * sizeof(double);
+  if (!g_trtri_diag_attr_set) {
+    LKG_CUDA(cudaFuncSetAttribute(k_trtri_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    g_trtri_diag_attr_set = true;
+  }
+  LaunchTimer lt("k_trtri_diag", st, (double)nblk * NB * NB * NB / 3.0 * batch, 16.0 * nblk * NB * NB * batch);
+  k_trtri_diag<<<dim3(nblk, 1, batch), NT, smem, st>>>(L, lda, mstride, n, Dinv, (int64_t)nblk * NB * NB);
+  LKG_LAUNCH("k_trtri_diag");
+}
+
+void transpose_copy(const double* S, int64_t lds, double* D, int64_t ldd, int rows, int cols, cudaStream_t st) {
+  if (rows <= 0 || cols <= 0) return;
+  LaunchTimer lt("k_transpose_copy", st, 0.0, 16.0 * rows * cols);
+  k_transpose_copy<<<dim3(ceil_div(rows, 32), ceil_div(cols, 32)), 256, 0, st>>>(S, lds, D, ldd, rows, cols);
+  LKG_LAUNCH("k_transpose_copy");
+}
+
+void add_diag(double* A, int64_t lda, int n, double v, cudaStream_t st) {
+  if (n <= 0) return;
+  k_add_diag<<<ceil_div(n, 256), 256, 0, st>>>(A, lda, n, v);
+  LKG_LAUNCH("k_add_diag");
+}
+
+void zero_upper(double* A, int64_t lda, int64_t mstride, int n, int batch, cudaStream_t st) {
+  if (n <= 1) return;
+  k_zero_upper<<<dim3(n, 1, batch), 128, 0, st>>>(A, lda, mstride, n);
+  LKG_LAUNCH("k_zero_upper");
+}
 
 void gemm_tiles(int M, int N, int K, double alpha, MatView A, MatView B, double beta, double* C, int64_t ldc,
                 int64_t c_batch, int batch, bool lower_only, cudaStream_t st) {

@@ -66,6 +66,17 @@ void trtri_blocked_mixed(const double* L, int64_t lda, int64_t mstride, int n, c
 void wtw_lower_mixed(const double* W, int64_t ldw, int64_t wstride, int n, double* C, int64_t ldc, int64_t cstride,
                      int batch, const MixedWorkspace& ws, cudaStream_t st);
 
+// Dinv blocks (nblk * NB * NB per matrix) of an existing lower factor L: the inverses of its NB x NB diagonal
+// blocks, computed exactly as potrf_diag computes them.
+void trtri_diag_blocks(const double* L, int64_t lda, int64_t mstride, int n, double* Dinv, int batch,
+                       cudaStream_t st);
+// D(c, r) = S(r, c) for r < rows, c < cols (column-major, leading dimensions lds, ldd)
+void transpose_copy(const double* S, int64_t lds, double* D, int64_t ldd, int rows, int cols, cudaStream_t st);
+// A(i, i) += v for i < n
+void add_diag(double* A, int64_t lda, int n, double v, cudaStream_t st);
+// A(i, j) = 0 for i < j < n in every batch matrix
+void zero_upper(double* A, int64_t lda, int64_t mstride, int n, int batch, cudaStream_t st);
+
 // Solve L X = B in place (B n x r column-major, ldb, batch stride bstride).
 void trsm_lower_left(const double* L, int64_t lda, int64_t mstride, int n, const double* Dinv, double* B,
                      int64_t ldb, int64_t bstride, int r, int batch, cudaStream_t st);

@@ -3,6 +3,7 @@
 // diagonal-block factorisations and inverses, the panel solves and the small row-block products stay FP64.
 #include "dense_fp64.cuh"
 #include "ozaki.cuh"
+#include "ozaki7.cuh"
 
 namespace lkg {
 
@@ -18,10 +19,96 @@ SplitBuf make_split(void* planes, int* exps, int S, int rows_cap, int K_cap) {
   return s;
 }
 
+// digits of the 7-bit split for a given count of 8-bit slices: the same operand precision, one digit more
+int oz7_digits(int slices) { return std::min(8, std::max(6, slices + 1)); }
+
+// Two-level blocked Cholesky: 256-wide panels factored with the 64-wide FP64 steps (diagonal block, panel solve and
+// the update of the panel's remaining columns), then one rank-256 trailing update on the tensor cores per panel.
+void potrf_blocked_mixed7(double* A, int64_t lda, int64_t mstride, int n, double* Dinv, int* info, int batch,
+                          const MixedWorkspace& ws, cudaStream_t st) {
+  const int nblk = ceil_div(n, NB);
+  const int64_t dstride = (int64_t)nblk * NB * NB;
+  LKG_CUDA(cudaMemsetAsync(info, 0, sizeof(int) * batch, st));
+  Split7 P = oz7_buffer(ws.panel, ws.panel_exp, oz7_digits(ws.slices), ws.n, OZ7_KB, OZ7_KB);
+  for (int K0 = 0; K0 < n; K0 += OZ7_KB) {
+    const int W = std::min(OZ7_KB, n - K0);
+    for (int k0 = K0; k0 < K0 + W; k0 += NB) {
+      const int nb = std::min(NB, n - k0), k = k0 / NB;
+      potrf_diag(A, lda, mstride, k0, nb, Dinv, dstride, k, info, batch, st);
+      const int M = n - k0 - nb;
+      if (M <= 0) continue;
+      double* A21 = A + (k0 + nb) + (int64_t)k0 * lda;
+      MatView a{A21, 1, lda, mstride};
+      MatView bt{Dinv + (int64_t)k * NB * NB, NB, 1, dstride};
+      gemm_tiles(M, nb, nb, 1.0, a, bt, 0.0, A21, lda, mstride, batch, false, st);
+      const int wr = K0 + W - (k0 + nb);  // panel columns right of this block
+      if (wr > 0) {
+        MatView l21t{A21, lda, 1, mstride};  // B(kk, c) = L21(c, kk)
+        gemm_tiles(M, wr, nb, -1.0, a, l21t, 1.0, A21 + (int64_t)nb * lda, lda, mstride, batch, true, st);
+      }
+    }
+    const int M2 = n - K0 - W;
+    if (M2 <= 0) continue;
+    // A22 -= P2 P2^T, P2 = L(K0+W:, K0:K0+W), one k block
+    double* P2 = A + (K0 + W) + (int64_t)K0 * lda;
+    oz7_split(M2, W, P2, 1, lda, mstride, batch, P, st);
+    oz7_gemm(M2, M2, 0, 1, -1.0, P, P, 1.0, P2 + (int64_t)W * lda, lda, mstride, batch, true, st);
+  }
+}
+
+// Two-level triangular inverse: inside a 256-row block the 64-wide FP64 steps; below it one rank-256 update of the
+// accumulated rows on the tensor cores.
+void trtri_blocked_mixed7(const double* L, int64_t lda, int64_t mstride, int n, const double* Dinv, double* W,
+                          int64_t ldw, int64_t wstride, int batch, const MixedWorkspace& ws, cudaStream_t st) {
+  const int nblk = ceil_div(n, NB);
+  const int64_t dstride = (int64_t)nblk * NB * NB;
+  for (int b = 0; b < batch; ++b)
+    LKG_CUDA(cudaMemset2DAsync(W + b * wstride, ldw * sizeof(double), 0, n * sizeof(double), n, st));
+  const int S = oz7_digits(ws.slices_inv);
+  Split7 SL = oz7_buffer(ws.panel, ws.panel_exp, S, ws.n, OZ7_KB, OZ7_KB);
+  Split7 SR = oz7_buffer(ws.rowblk, ws.rowblk_exp, S, ws.n, OZ7_KB, OZ7_KB);
+  for (int K0 = 0; K0 < n; K0 += OZ7_KB) {
+    const int Wd = std::min(OZ7_KB, n - K0);
+    for (int k0 = K0; k0 < K0 + Wd; k0 += NB) {
+      const int nb = std::min(NB, n - k0), k = k0 / NB;
+      copy_dinv_block(Dinv, dstride, k, W, ldw, wstride, k0, nb, batch, st);
+      if (k0 > 0) {  // W(k0:k0+nb, 0:k0) = -Dinv_k Acc(k0:k0+nb, 0:k0)
+        MatView d{Dinv + (int64_t)k * NB * NB, 1, NB, dstride};
+        MatView acc{W + k0, 1, ldw, wstride};
+        gemm_tiles(nb, k0, nb, -1.0, d, acc, 0.0, W + k0, ldw, wstride, batch, false, st);
+      }
+      const int mr = K0 + Wd - (k0 + nb);  // rows of this 256-row block below the 64-row one
+      if (mr > 0) {
+        MatView a{L + (k0 + nb) + (int64_t)k0 * lda, 1, lda, mstride};
+        MatView bw{W + k0, 1, ldw, wstride};
+        gemm_tiles(mr, k0 + nb, nb, 1.0, a, bw, 1.0, W + k0 + nb, ldw, wstride, batch, false, st);
+      }
+    }
+    const int M2 = n - K0 - Wd;
+    if (M2 <= 0) continue;
+    // Acc(K0+Wd:, 0:N) += L(K0+Wd:, K0:K0+Wd) W(K0:K0+Wd, 0:N), N = K0 + Wd
+    const int N = K0 + Wd;
+    oz7_split(M2, Wd, L + (K0 + Wd) + (int64_t)K0 * lda, 1, lda, mstride, batch, SL, st);
+    oz7_split(N, Wd, W + K0, ldw, 1, wstride, batch, SR, st);
+    oz7_gemm(M2, N, 0, 1, 1.0, SL, SR, 1.0, W + K0 + Wd, ldw, wstride, batch, false, st);
+  }
+}
+
+void wtw_lower_mixed7(const double* W, int64_t ldw, int64_t wstride, int n, double* C, int64_t ldc, int64_t cstride,
+                      int batch, const MixedWorkspace& ws, cudaStream_t st) {
+  Split7 SW = oz7_buffer(ws.wfull, ws.wfull_exp, oz7_digits(ws.slices_inv), ws.n, ws.n, OZ7_KB);
+  oz7_split(n, n, W, ldw, 1, wstride, batch, SW, st);  // rows of the split = columns of W, k = rows of W
+  oz7_wtw(n, SW, C, ldc, cstride, batch, st);
+}
+
 }  // namespace
 
 void potrf_blocked_mixed(double* A, int64_t lda, int64_t mstride, int n, double* Dinv, int* info, int batch,
                          const MixedWorkspace& ws, cudaStream_t st) {
+  if (ozaki_tensor_path() == 3) {
+    potrf_blocked_mixed7(A, lda, mstride, n, Dinv, info, batch, ws, st);
+    return;
+  }
   const int nblk = ceil_div(n, NB);
   const int64_t dstride = (int64_t)nblk * NB * NB;
   LKG_CUDA(cudaMemsetAsync(info, 0, sizeof(int) * batch, st));
@@ -43,6 +130,10 @@ void potrf_blocked_mixed(double* A, int64_t lda, int64_t mstride, int n, double*
 
 void trtri_blocked_mixed(const double* L, int64_t lda, int64_t mstride, int n, const double* Dinv, double* W,
                          int64_t ldw, int64_t wstride, int batch, const MixedWorkspace& ws, cudaStream_t st) {
+  if (ozaki_tensor_path() == 3) {
+    trtri_blocked_mixed7(L, lda, mstride, n, Dinv, W, ldw, wstride, batch, ws, st);
+    return;
+  }
   const int nblk = ceil_div(n, NB);
   const int64_t dstride = (int64_t)nblk * NB * NB;
   for (int b = 0; b < batch; ++b)
@@ -70,6 +161,10 @@ void trtri_blocked_mixed(const double* L, int64_t lda, int64_t mstride, int n, c
 
 void wtw_lower_mixed(const double* W, int64_t ldw, int64_t wstride, int n, double* C, int64_t ldc, int64_t cstride,
                      int batch, const MixedWorkspace& ws, cudaStream_t st) {
+  if (ozaki_tensor_path() == 3) {
+    wtw_lower_mixed7(W, ldw, wstride, n, C, ldc, cstride, batch, ws, st);
+    return;
+  }
   SplitBuf SW = make_split(ws.wfull, ws.wfull_exp, ws.slices_inv, ws.n, ws.n);
   // rows of the split = columns of W, k = rows of W
   ozaki_split(n, n, W, ldw, 1, wstride, batch, SW, st);

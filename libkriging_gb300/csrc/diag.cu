@@ -1,5 +1,6 @@
 // diag.cu -- device diagnostics exported through the C ABI: device name and the FP64 FMA throughput probe that
 // serves as the roofline denominator of the FP64 kernels (the published HBM and bf16 peaks do not cover the FP64 pipe).
+#include <algorithm>
 #include <string>
 
 #include "../../include/libkriging_gb300.h"
@@ -73,6 +74,11 @@ int lkg_probe_fp64_peak(double* tflops_out) {
 
 // ---- emulated-GEMM check entry point (host buffers) ----
 #include "ozaki.cuh"
+#include "ozaki7.cuh"
+
+namespace lkg {
+void set_last_error(const char* msg);
+}
 
 extern "C" int lkg_set_tensor_path(int tc) {
   lkg::ozaki_set_tensor_path(tc);
@@ -87,32 +93,51 @@ extern "C" int lkg_ozaki_gemm_check(int M, int N, int K, const double* A, const 
   void *pa = nullptr, *pb = nullptr;
   int *ea = nullptr, *eb = nullptr;
   int rc = -1;
+  lkg::set_last_error("");
   try {
     LKG_CUDA(cudaMalloc(&dA, sizeof(double) * M * K));
     LKG_CUDA(cudaMalloc(&dB, sizeof(double) * N * K));
     LKG_CUDA(cudaMalloc(&dC, sizeof(double) * M * N));
     LKG_CUDA(cudaMemcpy(dA, A, sizeof(double) * M * K, cudaMemcpyHostToDevice));
     LKG_CUDA(cudaMemcpy(dB, B, sizeof(double) * N * K, cudaMemcpyHostToDevice));
-    LKG_CUDA(cudaMalloc(&pa, lkg::split_plane_elems(M, K, slices) * 2));
-    LKG_CUDA(cudaMalloc(&pb, lkg::split_plane_elems(N, K, slices) * 2));
-    LKG_CUDA(cudaMalloc(&ea, lkg::split_exp_elems(M, K) * sizeof(int)));
-    LKG_CUDA(cudaMalloc(&eb, lkg::split_exp_elems(N, K) * sizeof(int)));
-    lkg::SplitBuf sa, sb;
-    sa.planes = static_cast<__nv_bfloat16*>(pa);
-    sa.exps = ea;
-    sa.S = slices;
-    sb.planes = static_cast<__nv_bfloat16*>(pb);
-    sb.exps = eb;
-    sb.S = slices;
-    lkg::ozaki_split(M, K, dA, 1, M, 0, 1, sa, 0);
-    lkg::ozaki_split(N, K, dB, 1, N, 0, 1, sb, 0);
-    lkg::ozaki_gemm(M, N, 0, sa.nchunk, 1.0, sa, 0, sb, 0, 0.0, dC, M, 0, 1, false, 0);
-    LKG_CUDA(cudaDeviceSynchronize());
-    LKG_CUDA(cudaMemcpy(C, dC, sizeof(double) * M * N, cudaMemcpyDeviceToHost));
-    rc = lkg::ozaki_tc_error_and_reset() ? -1 : 0;
-  } catch (const std::exception&) {
+    if (lkg::ozaki_tensor_path() == 3) {  // 7-bit digits, one more than the slices (6..8), 256-wide k blocks
+      const int kb = lkg::OZ7_KB;
+      slices = std::min(8, std::max(6, slices + 1));
+      LKG_CUDA(cudaMalloc(&pa, lkg::oz7_plane_elems(M, K, slices) * 2));
+      LKG_CUDA(cudaMalloc(&pb, lkg::oz7_plane_elems(N, K, slices) * 2));
+      LKG_CUDA(cudaMalloc(&ea, lkg::oz7_exp_elems(M, K, kb) * sizeof(int)));
+      LKG_CUDA(cudaMalloc(&eb, lkg::oz7_exp_elems(N, K, kb) * sizeof(int)));
+      lkg::Split7 sa = lkg::oz7_buffer(pa, ea, slices, M, K, kb), sb = lkg::oz7_buffer(pb, eb, slices, N, K, kb);
+      lkg::oz7_split(M, K, dA, 1, M, 0, 1, sa, 0);
+      lkg::oz7_split(N, K, dB, 1, N, 0, 1, sb, 0);
+      lkg::oz7_gemm(M, N, 0, sa.nblk, 1.0, sa, sb, 0.0, dC, M, 0, 1, false, 0);
+      LKG_CUDA(cudaDeviceSynchronize());
+      LKG_CUDA(cudaMemcpy(C, dC, sizeof(double) * M * N, cudaMemcpyDeviceToHost));
+      rc = lkg::oz7_error_and_reset() ? -1 : 0;
+    } else {
+      LKG_CUDA(cudaMalloc(&pa, lkg::split_plane_elems(M, K, slices) * 2));
+      LKG_CUDA(cudaMalloc(&pb, lkg::split_plane_elems(N, K, slices) * 2));
+      LKG_CUDA(cudaMalloc(&ea, lkg::split_exp_elems(M, K) * sizeof(int)));
+      LKG_CUDA(cudaMalloc(&eb, lkg::split_exp_elems(N, K) * sizeof(int)));
+      lkg::SplitBuf sa, sb;
+      sa.planes = static_cast<__nv_bfloat16*>(pa);
+      sa.exps = ea;
+      sa.S = slices;
+      sb.planes = static_cast<__nv_bfloat16*>(pb);
+      sb.exps = eb;
+      sb.S = slices;
+      lkg::ozaki_split(M, K, dA, 1, M, 0, 1, sa, 0);
+      lkg::ozaki_split(N, K, dB, 1, N, 0, 1, sb, 0);
+      lkg::ozaki_gemm(M, N, 0, sa.nchunk, 1.0, sa, 0, sb, 0, 0.0, dC, M, 0, 1, false, 0);
+      LKG_CUDA(cudaDeviceSynchronize());
+      LKG_CUDA(cudaMemcpy(C, dC, sizeof(double) * M * N, cudaMemcpyDeviceToHost));
+      rc = lkg::ozaki_tc_error_and_reset() ? -1 : 0;
+    }
+  } catch (const std::exception& e) {
+    lkg::set_last_error(e.what());
     rc = -1;
   }
+  if (rc != 0 && std::string(lkg_get_last_error()).empty()) lkg::set_last_error("tensor-core digit product timed out");
   cudaFree(dA);
   cudaFree(dB);
   cudaFree(dC);

@@ -18,6 +18,7 @@
 #include "dense_fp64.cuh"
 #include "lik_kernels.cuh"
 #include "ozaki.cuh"
+#include "ozaki7.cuh"
 
 namespace lkg {
 
@@ -177,7 +178,10 @@ void Engine::ensure_mixed_buffers(bool with_grad) {
       }
     mixed_alloc_slices_ = slices_;
   }
-  const size_t pe = split_plane_elems(n_, NB, slices_) * cap_, ee = split_exp_elems(n_, NB) * cap_;
+  // sized for both forms of the digit products: 8-bit digits in 64-wide chunks, or up to 8 7-bit digits in
+  // 256-wide blocks (ozaki7.cuh)
+  const size_t pe = std::max(split_plane_elems(n_, NB, slices_), oz7_plane_elems(n_, OZ7_KB, 8)) * cap_;
+  const size_t ee = std::max(split_exp_elems(n_, NB), oz7_exp_elems(n_, OZ7_KB, OZ7_KB)) * cap_;
   if (!dpanel_) {
     LKG_CUDA(cudaMalloc(&dpanel_, pe * 2));
     LKG_CUDA(cudaMalloc(&drowblk_, pe * 2));
@@ -185,8 +189,8 @@ void Engine::ensure_mixed_buffers(bool with_grad) {
     dalloc(&drowblk_exp_, ee);
   }
   if (with_grad && !dwfull_) {
-    LKG_CUDA(cudaMalloc(&dwfull_, split_plane_elems(n_, n_, slices_) * cap_ * 2));
-    dalloc(&dwfull_exp_, split_exp_elems(n_, n_) * cap_);
+    LKG_CUDA(cudaMalloc(&dwfull_, std::max(split_plane_elems(n_, n_, slices_), oz7_plane_elems(n_, n_, std::min(8, slices_ + 1))) * cap_ * 2));
+    dalloc(&dwfull_exp_, std::max(split_exp_elems(n_, n_), oz7_exp_elems(n_, n_, OZ7_KB)) * cap_);
   }
 }
 
@@ -206,11 +210,15 @@ void Engine::solve_lower_inplace(int b, double* dB, int64_t ldb, int r) const {
 // dtrcon('1', 'L', 'N') style estimate (LAPACK dlacn2 iteration of Hager / Higham) of rcond(L)^2 for every entry,
 // with the triangular solves of all entries batched into the same launches.
 void Engine::rcond_batch(int batch, std::vector<double>& rc2, const std::vector<int>& nvb) {
+  rcond_core(batch, rc2, nvb, dA_, lda_, mstride_, n_, dDinv_);
+}
+
+void Engine::rcond_core(int batch, std::vector<double>& rc2, const std::vector<int>& nvb, const double* A,
+                        int64_t lda, int64_t mstride, int n, const double* Dinv) {
   // every vector of the estimator lives on the entry's valid block (the padded identity stays out of it), so a
   // padded entry follows exactly the iteration of its unpadded matrix
-  const int n = n_;
   std::vector<double> colsum((size_t)n * batch);
-  lower_colsum_abs(n, dA_, lda_, mstride_, dcol_, batch, st_);
+  lower_colsum_abs(n, A, lda, mstride, dcol_, batch, st_);
   LKG_CUDA(cudaMemcpyAsync(colsum.data(), dcol_, sizeof(double) * n * batch, cudaMemcpyDeviceToHost, st_));
   LKG_CUDA(cudaStreamSynchronize(st_));
   std::vector<double> anorm(batch, 0.0);
@@ -259,9 +267,9 @@ void Engine::rcond_batch(int batch, std::vector<double>& rc2, const std::vector<
     const int kind = any1 ? 1 : 2;
     LKG_CUDA(cudaMemcpyAsync(dvec_, vec.data(), sizeof(double) * n * batch, cudaMemcpyHostToDevice, st_));
     if (kind == 1)
-      trsm_lower_left(dA_, lda_, mstride_, n, dDinv_, dvec_, n, n, 1, batch, st_);
+      trsm_lower_left(A, lda, mstride, n, Dinv, dvec_, n, n, 1, batch, st_);
     else
-      trsm_lower_left_t(dA_, lda_, mstride_, n, dDinv_, dvec_, n, n, 1, batch, st_);
+      trsm_lower_left_t(A, lda, mstride, n, Dinv, dvec_, n, n, 1, batch, st_);
     std::vector<double> res((size_t)n * batch);
     LKG_CUDA(cudaMemcpyAsync(res.data(), dvec_, sizeof(double) * n * batch, cudaMemcpyDeviceToHost, st_));
     LKG_CUDA(cudaStreamSynchronize(st_));
@@ -541,6 +549,8 @@ void Engine::evaluate(int batch, const double* thetas, const double* factors, bo
   LKG_CUDA(cudaStreamSynchronize(st_));
   if (slices_ > 0 && ozaki_tensor_path() && ozaki_tc_error_and_reset())
     throw std::runtime_error("mixed path: a tensor-core digit product did not complete (timed out)");
+  if (slices_ > 0 && ozaki_tensor_path() == 3 && oz7_error_and_reset())
+    throw std::runtime_error("mixed path: a tensor-core digit product did not complete (timed out)");
   for (int b = 0; b < batch; ++b) {
     EvalOut& o = out[b];
     if (o.status == 0 && gls[b] != 0) {
@@ -665,6 +675,163 @@ void Engine::leave_one_out(int batch, const double* thetas, const double* factor
         o.grad[k] = 2.0 * s / n;
       }
     }
+  }
+}
+
+void Engine::evaluate_update(const Engine& old, const double* theta, double factor, EvalOut& out) {
+  const int n = n_, d = d_, p = p_, no = old.n(), nu = n_ - old.n();
+  if (ndesign_ != 1 || old.ndesign() != 1 || nu < 1 || old.d() != d || old.p() != p || old.kernel() != kernel_)
+    throw std::invalid_argument("Engine::evaluate_update: the new design must extend the old one");
+  const Config& cfg = config();
+  out = EvalOut{};
+  const double one = base_diag_;
+  LKG_CUDA(cudaMemcpyAsync(dtheta_, theta, sizeof(double) * d, cudaMemcpyHostToDevice, st_));
+  LKG_CUDA(cudaMemcpyAsync(dfactor_, &factor, sizeof(double), cudaMemcpyHostToDevice, st_));
+  LKG_CUDA(cudaMemcpyAsync(ddiag_, &one, sizeof(double), cudaMemcpyHostToDevice, st_));
+  // R (lower) of the whole design; its leading block is then replaced by the old factor (update_cholCov restores
+  // R_old there and chol_block keeps L_oo)
+  cov_build_lower(kernel_, n, d, dX_, 0, dtheta_, dfactor_, ddiag_, dA_, lda_, mstride_, 1, st_, false, nullptr);
+  LKG_CUDA(cudaStreamSynchronize(old.stream()));
+  LKG_CUDA(cudaMemcpy2DAsync(dA_, sizeof(double) * lda_, old.dL(0), sizeof(double) * old.lda(), sizeof(double) * no,
+                             no, cudaMemcpyDeviceToDevice, st_));
+  double* Auo = dA_ + no;                       // rows no.., columns 0..no-1: C_uo, then L_uo
+  double* Auu = dA_ + no + (int64_t)no * lda_;  // trailing block: C_uu, then S, then L_uu
+  const int nbs = ceil_div(nu, NB);
+  double *dT = nullptr, *dS = nullptr, *dDs = nullptr;
+  struct Free {
+    double** p[3];
+    ~Free() {
+      for (double** q : p)
+        if (*q) cudaFree(*q);
+    }
+  } guard{{&dT, &dS, &dDs}};
+  LKG_CUDA(cudaMalloc(&dT, sizeof(double) * (size_t)no * nu));
+  LKG_CUDA(cudaMalloc(&dS, sizeof(double) * (size_t)nu * nu));
+  LKG_CUDA(cudaMalloc(&dDs, sizeof(double) * (size_t)nbs * NB * NB));
+  // Lou = L_oo \ C_ou (n_o x n_u), then L_uo = Lou'
+  transpose_copy(Auo, lda_, dT, no, nu, no, st_);
+  trsm_lower_left(old.dL(0), old.lda(), 0, no, old.dDinv(0), dT, no, 0, nu, 1, st_);
+  transpose_copy(dT, no, Auo, lda_, no, nu, st_);
+  // S = C_uu - L_uo L_uo'
+  MatView a{Auo, 1, lda_, 0}, bt{Auo, lda_, 1, 0};
+  gemm_tiles(nu, nu, no, -1.0, a, bt, 1.0, Auu, lda_, 0, 1, true, st_);
+  LKG_CUDA(cudaMemcpy2DAsync(dS, sizeof(double) * nu, Auu, sizeof(double) * lda_, sizeof(double) * nu, nu,
+                             cudaMemcpyDeviceToDevice, st_));
+  // L_uu = safe_chol_lower(S): cumulative 1e-10 * 10^k jitter on S's diagonal (LinearAlgebra.cpp:68-98)
+  const bool rcond_check = cfg.chol_rcond_check && !plain_chol_;
+  double jitter = 0.0;
+  int inc = 0, info = 0;
+  double rc2 = -1.0;
+  bool fallback = false;
+  for (;;) {
+    if (inc > 0) {
+      LKG_CUDA(cudaMemcpy2DAsync(Auu, sizeof(double) * lda_, dS, sizeof(double) * nu, sizeof(double) * nu, nu,
+                                 cudaMemcpyDeviceToDevice, st_));
+      add_diag(Auu, lda_, nu, jitter, st_);
+    }
+    potrf_blocked(Auu, lda_, 0, nu, dDs, dinfo_, 1, st_);
+    LKG_CUDA(cudaMemcpyAsync(&info, dinfo_, sizeof(int), cudaMemcpyDeviceToHost, st_));
+    LKG_CUDA(cudaStreamSynchronize(st_));
+    rc2 = -1.0;
+    if (info == 0 && rcond_check) {
+      std::vector<double> r;
+      rcond_core(1, r, std::vector<int>{nu}, Auu, lda_, 0, nu, dDs);
+      rc2 = r[0];
+    }
+    const bool wrong = rcond_check && info == 0 && rc2 < cfg.min_rcond;
+    if (info == 0 && !wrong) break;
+    if (plain_chol_ || inc > cfg.max_inc_choldiag || cfg.num_nugget <= 0.0) {
+      fallback = true;
+      break;
+    }
+    jitter += cfg.num_nugget * std::pow(10.0, inc);
+    inc++;
+  }
+  if (fallback) {  // chol_block: "falling back to a full Cholesky factorization"
+    std::vector<EvalOut> o;
+    evaluate(1, theta, &factor, false, o, nullptr);
+    out = o[0];
+    return;
+  }
+  zero_upper(dA_, lda_, mstride_, n, 1, st_);
+  trtri_diag_blocks(dA_, lda_, mstride_, n, dDinv_, 1, st_);
+  out.nugget_increments = inc;
+  out.rcond = rc2;
+  entry_design_.assign(1, 0);
+  // [F* y*] = L \ [F y], GLS, E*, SSE (as in evaluate)
+  if (p > 0) LKG_CUDA(cudaMemcpyAsync(dFY_, dF_, sizeof(double) * n * p, cudaMemcpyDeviceToDevice, st_));
+  LKG_CUDA(cudaMemcpyAsync(dFY_ + (size_t)n * p, dY_, sizeof(double) * n, cudaMemcpyDeviceToDevice, st_));
+  trsm_lower_left(dA_, lda_, mstride_, n, dDinv_, dFY_, n, fystride_, p + 1, 1, st_);
+  gram_and_logdet(n, p + 1, dFY_, n, fystride_, dA_, lda_, mstride_, dgram_, gram_stride_, 1, st_);
+  if (p > 0)
+    gls_solve(p, dgram_, gram_stride_, dbeta_, p, drstar_, p * p, dgls_info_, 1, st_);
+  else
+    LKG_CUDA(cudaMemsetAsync(dgls_info_, 0, sizeof(int), st_));
+  residual_sse(n, p, dFY_, n, fystride_, dbeta_, std::max(p, 1), dEstar_, n, dsse_, 1, 1, st_);
+  std::vector<double> gram((size_t)gram_stride_), beta((size_t)std::max(p, 1)), rstar((size_t)p * p);
+  int gls = 0;
+  LKG_CUDA(cudaMemcpyAsync(gram.data(), dgram_, sizeof(double) * gram.size(), cudaMemcpyDeviceToHost, st_));
+  LKG_CUDA(cudaMemcpyAsync(&out.sse, dsse_, sizeof(double), cudaMemcpyDeviceToHost, st_));
+  LKG_CUDA(cudaMemcpyAsync(beta.data(), dbeta_, sizeof(double) * beta.size(), cudaMemcpyDeviceToHost, st_));
+  LKG_CUDA(cudaMemcpyAsync(&gls, dgls_info_, sizeof(int), cudaMemcpyDeviceToHost, st_));
+  if (p > 0)
+    LKG_CUDA(cudaMemcpyAsync(rstar.data(), drstar_, sizeof(double) * rstar.size(), cudaMemcpyDeviceToHost, st_));
+  LKG_CUDA(cudaStreamSynchronize(st_));
+  if (gls != 0) {
+    out.status = 2;
+    out.message = "chol(): decomposition failed (F*'F* not positive definite)";
+  }
+  out.logdet = 2.0 * gram[(size_t)(p + 1) * (p + 1)];
+  for (int j = 0; j < p; ++j) out.rstar_logdet += std::log(rstar[j + (size_t)j * p]);
+  out.beta.assign(beta.begin(), beta.begin() + p);
+}
+
+void Engine::adopt_model(const double* L, const double* Fstar, const double* ystar, const double* Rstar,
+                         const double* Estar) {
+  if (ndesign_ != 1) throw std::invalid_argument("Engine::adopt_model: one design only");
+  const int n = n_, p = p_;
+  LKG_CUDA(cudaMemcpy2DAsync(dA_, sizeof(double) * lda_, L, sizeof(double) * n, sizeof(double) * n, n,
+                             cudaMemcpyHostToDevice, st_));
+  zero_upper(dA_, lda_, mstride_, n, 1, st_);
+  trtri_diag_blocks(dA_, lda_, mstride_, n, dDinv_, 1, st_);
+  if (p > 0) {
+    LKG_CUDA(cudaMemcpyAsync(dFY_, Fstar, sizeof(double) * n * p, cudaMemcpyHostToDevice, st_));
+    LKG_CUDA(cudaMemcpyAsync(drstar_, Rstar, sizeof(double) * p * p, cudaMemcpyHostToDevice, st_));
+  }
+  LKG_CUDA(cudaMemcpyAsync(dFY_ + (size_t)n * p, ystar, sizeof(double) * n, cudaMemcpyHostToDevice, st_));
+  LKG_CUDA(cudaMemcpyAsync(dEstar_, Estar, sizeof(double) * n, cudaMemcpyHostToDevice, st_));
+  entry_design_.assign(1, 0);
+  LKG_CUDA(cudaStreamSynchronize(st_));
+}
+
+void Engine::model_matrices(const double* theta, double factor, std::vector<double>* R, std::vector<double>* Rinv) {
+  if (ndesign_ != 1) throw std::invalid_argument("Engine::model_matrices: one design only");
+  const int n = n_;
+  ensure_grad_buffers();
+  auto mirror = [n](std::vector<double>& M) {  // lower triangle -> full symmetric
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < j; ++i) M[i + (size_t)j * n] = M[j + (size_t)i * n];
+  };
+  if (R) {
+    const double one = 1.0;
+    LKG_CUDA(cudaMemcpyAsync(dtheta_, theta, sizeof(double) * d_, cudaMemcpyHostToDevice, st_));
+    LKG_CUDA(cudaMemcpyAsync(dfactor_, &factor, sizeof(double), cudaMemcpyHostToDevice, st_));
+    LKG_CUDA(cudaMemcpyAsync(ddiag_, &one, sizeof(double), cudaMemcpyHostToDevice, st_));
+    cov_build_lower(kernel_, n, d_, dX_, 0, dtheta_, dfactor_, ddiag_, dW_, lda_, mstride_, 1, st_, false, nullptr);
+    R->assign((size_t)n * n, 0.0);
+    LKG_CUDA(cudaMemcpy2DAsync(R->data(), sizeof(double) * n, dW_, sizeof(double) * lda_, sizeof(double) * n, n,
+                               cudaMemcpyDeviceToHost, st_));
+    LKG_CUDA(cudaStreamSynchronize(st_));
+    mirror(*R);
+  }
+  if (Rinv) {
+    trtri_blocked(dA_, lda_, mstride_, n, dDinv_, dW_, lda_, mstride_, 1, st_);
+    wtw_lower(dW_, lda_, mstride_, n, dRinv_, lda_, mstride_, 1, st_);
+    Rinv->assign((size_t)n * n, 0.0);
+    LKG_CUDA(cudaMemcpy2DAsync(Rinv->data(), sizeof(double) * n, dRinv_, sizeof(double) * lda_, sizeof(double) * n,
+                               n, cudaMemcpyDeviceToHost, st_));
+    LKG_CUDA(cudaStreamSynchronize(st_));
+    mirror(*Rinv);
   }
 }
 

@@ -70,6 +70,23 @@ class Engine {
   // T2_k into tr(G_k B) / 2 and U2 into tr(C B) / 2 (compute_lmp_theta_ans, KrigingImpl.cpp:887-921).
   void evaluate_lmp(int batch, const double* thetas, const double* factors, bool with_grad, std::vector<EvalOut>& out);
 
+  // populate_Model with the incremental factor of update_cholCov / chol_block (src/lib/LinearAlgebra.cpp:206-299).
+  // The first n_o = old.n() points of this engine's design are old's, and old's entry 0 holds the factor L_oo of
+  // the same (theta, factor).  L_uo = C_uo L_oo^-T; S = C_uu - L_uo L_uo^T is factored with the retry rules of
+  // safe_chol_lower applied to S alone; when S cannot be factored within the retry budget the whole matrix is
+  // factored from scratch instead (chol_block's fallback).  One entry, no gradient; the factor stays in entry 0
+  // like evaluate().  The O(n^3) work shrinks to O(n_u n_o^2 + n_u^2 n_o + n_u^3) for n_u = n - n_o new points.
+  void evaluate_update(const Engine& old, const double* theta, double factor, EvalOut& out);
+
+  // Entry 0 takes a committed model given on the host (a loaded model file): L (n x n lower, column-major), F* (n x
+  // p), y* (n), R* (p x p upper), E* (n).  The diagonal-block inverses are recomputed from L.
+  void adopt_model(const double* L, const double* Fstar, const double* ystar, const double* Rstar,
+                   const double* Estar);
+
+  // Model matrices of a saved model file (host, n x n, full symmetric): R = factor C(X; theta) with unit diagonal,
+  // and R^-1 = (L^-1)' L^-1 from entry 0's factor (FP64 path).
+  void model_matrices(const double* theta, double factor, std::vector<double>* R, std::vector<double>* Rinv);
+
   // Copies of the last evaluation's state for batch entry b (host, column-major):
   //   L (n x n lower, upper part zero), Fstar (n x p), ystar (n), Rstar (p x p upper), Estar (n)
   void copy_model(int b, std::vector<double>* L, std::vector<double>* Fstar, std::vector<double>* ystar,
@@ -113,6 +130,9 @@ class Engine {
   void ensure_mixed_buffers(bool with_grad);
   // rcond(L)^2 per entry, dtrcon('1') style estimate on each entry's first nvb[b] rows / columns
   void rcond_batch(int batch, std::vector<double>& rc2, const std::vector<int>& nvb);
+  // the same estimate for the n x n lower factors at A (lda, mstride) with diagonal-block inverses Dinv
+  void rcond_core(int batch, std::vector<double>& rc2, const std::vector<int>& nvb, const double* A, int64_t lda,
+                  int64_t mstride, int n, const double* Dinv);
 
   int kernel_, n_, d_, p_, cap_;
   int ndesign_ = 1;

@@ -651,7 +651,9 @@ void Kriging::fit(const std::vector<double>& y, const Mat& Xin, RegressionModel 
     }
   }
   rng_engine().seed(rng_seed());  // Random::init()
-  int multistart = parse_method(optim, "BFGS").second;
+  // a warm restart (update) runs one L-BFGS-B from the given theta, without restarts (Kriging.cpp:2583-2590)
+  int multistart = m_warm ? 1 : parse_method(optim, "BFGS").second;
+  const int max_restart = m_warm ? 0 : cfg.max_restart;
   Mat U = randu_mat(multistart, d);
   Mat theta0_rand;
   theta0_rand.rows = multistart;
@@ -661,7 +663,7 @@ void Kriging::fit(const std::vector<double>& y, const Mat& Xin, RegressionModel 
     for (int j = 0; j < d; ++j) theta0_rand(i, j) = theta_lower[j] + U(i, j) * (theta_upper[j] - theta_lower[j]);
   Mat starts;
   if (parameters.theta.has_value()) {
-    multistart = std::max(multistart, theta0.rows);
+    if (!m_warm) multistart = std::max(multistart, theta0.rows);
     starts.rows = multistart;
     starts.cols = d;
     starts.v.resize((size_t)multistart * d);
@@ -859,7 +861,7 @@ void Kriging::fit(const std::vector<double>& y, const Mat& Xin, RegressionModel 
       int retry = 0;
       double best_f = std::numeric_limits<double>::infinity();
       std::vector<double> best_gamma = gamma_tmp;
-      while (retry <= cfg.max_restart) {
+      while (retry <= max_restart) {
         LbfgsbResult r = opt.minimize(
             [&](const std::vector<double>& x, std::vector<double>& g) { return fit_ofn(x, &g); }, gamma_tmp,
             lo.data(), hi.data(), btype.data());
@@ -870,7 +872,7 @@ void Kriging::fit(const std::vector<double>& y, const Mat& Xin, RegressionModel 
         std::vector<double> tp = reparam_from(gamma_tmp);
         double sol_to_lb = std::numeric_limits<double>::infinity();
         for (int j = 0; j < d; ++j) sol_to_lb = std::min(sol_to_lb, std::fabs(tp[j] - theta_lower[j]));
-        if (retry < cfg.max_restart &&
+        if (retry < max_restart &&
             (r.task.rfind("ABNORMAL_TERMINATION_IN_LNSRCH", 0) == 0 || r.num_iters <= 2 ||
              sol_to_lb < std::numeric_limits<double>::epsilon() || r.f_opt > best_f)) {
           std::vector<double> rt(d);

@@ -99,6 +99,21 @@ class Kriging {
   std::tuple<std::vector<double>, std::vector<double>> predictVecchia(const Mat& X_n, bool return_stdev = true,
                                                                       int m = 0);
 
+  // update (Kriging.hpp:255-257, Kriging.cpp:2433-2633): append (X_u, y_u) in the model's original units.
+  //   refit and optim != "none", NoiseModel Nugget: a full fit on the joined data with the model's parameters;
+  //   refit and optim != "none", NoiseModel None: one L-BFGS-B run warm-started at the current theta, bounds from
+  //     the joined data, the normalisation kept;
+  //   otherwise: theta kept, the factor extended by the incremental Cholesky (chol_block) on the GPU, beta and
+  //     sigma2 = SSE / n re-estimated when they are estimated (KrigingImpl.cpp:576-635).
+  void update(const std::vector<double>& y_u, const Mat& X_u, bool refit = true);
+  // libKriging's JSON model file, version 2 (Kriging.cpp:2691-2749, KrigingImpl.cpp:644-711)
+  void save(const std::string& filename) const;
+  static std::unique_ptr<Kriging> load(const std::string& filename);
+  // sigma2 * C(X1, X2) in the original units (KrigingImpl.cpp:60-71); X1 n1 x d, X2 n2 x d -> n1 x n2
+  Mat covMat(const Mat& X1, const Mat& X2) const;
+  // deep copy (Kriging(const Kriging&, ExplicitCopySpecifier)): the data, parameters and committed model
+  std::unique_ptr<Kriging> copy() const;
+
   // accessors (KrigingImpl.hpp:40-60, Kriging.hpp:94-97)
   const std::string& kernel() const { return m_covType; }
   NoiseModel noise_model() const { return m_noise_model; }
@@ -120,6 +135,7 @@ class Kriging {
   int p() const { return m_p; }
   const std::vector<double>& X() const { return m_X; }
   const std::vector<double>& y() const { return m_y; }
+  const std::vector<double>& F() const { return m_F; }
   const std::vector<double>& centerX() const { return m_centerX; }
   const std::vector<double>& scaleX() const { return m_scaleX; }
   double centerY() const { return m_centerY; }
@@ -152,6 +168,9 @@ class Kriging {
   // log marginal posterior at (theta, alpha) from an evaluate_lmp result; grad (gdim) only when sigma2 is estimated
   double lmp_from(const EvalOut& o, const double* theta, double alpha, std::vector<double>* grad, int gdim) const;
   void ensure_engine(int batch_cap);
+  // fit() on data that is already normalised with the model's centre / scale, restarted from theta_warm only
+  // (update's warm restart, Kriging.cpp:2467-2625): one start, no restarts, normalisation kept
+  bool m_warm = false;
   void commit(const std::vector<double>& theta, double alpha);
 
   std::string m_covType;

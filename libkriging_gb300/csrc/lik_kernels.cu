@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(256) k_cov_lower(int n, int d, const double* _
 template <int K, int DM>
 __global__ void __launch_bounds__(256) k_cov_cross(int n_o, int q, int d, const double* __restrict__ Xo,
                                                    const double* __restrict__ Xn, const double* __restrict__ theta,
-                                                   double factor, double* __restrict__ R) {
+                                                   double factor, double* __restrict__ R, bool snap) {
   __shared__ double xo[DM][T], xn[DM][T], th[DM];
   const int r0 = blockIdx.x * T, c0 = blockIdx.y * T, t = threadIdx.x;
   for (int idx = t; idx < DM * T; idx += 256) {
@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(256) k_cov_cross(int n_o, int q, int d, const 
         sum += cov_term<K>(dx, th[k]);
       }
     }
-    R[i + (int64_t)j * n_o] = coincident ? 1.0 : cov_from_sum<K>(sum) * factor;
+    R[i + (int64_t)j * n_o] = (snap && coincident) ? 1.0 : cov_from_sum<K>(sum) * factor;
   }
 }
 
@@ -453,10 +453,10 @@ struct CovLowerLaunch {
 template <int K, int DM>
 struct CovCrossLaunch {
   static void run(int n_o, int q, int d, const double* Xo, const double* Xn, const double* theta, double factor,
-                  double* R, cudaStream_t st) {
+                  double* R, bool snap, cudaStream_t st) {
     LaunchTimer lt("k_cov_cross", st, (double)n_o * q, 8.0 * n_o * q);
     k_cov_cross<K, DM><<<dim3(ceil_div(n_o, T), ceil_div(q, T), 1), 256, 0, st>>>(n_o, q, d, Xo, Xn, theta, factor,
-                                                                                   R);
+                                                                                   R, snap);
     LKG_LAUNCH("k_cov_cross");
   }
 };
@@ -484,9 +484,9 @@ void cov_build_lower(int kernel, int n, int d, const double* X, int64_t x_bstrid
 }
 
 void cov_cross(int kernel, int n_o, int q, int d, const double* Xo, const double* Xn, const double* theta,
-               double factor, double* R, cudaStream_t st) {
+               double factor, double* R, cudaStream_t st, bool snap_coincident) {
   if (n_o <= 0 || q <= 0) return;
-  dispatch_kd<CovCrossLaunch>(kernel, d, n_o, q, d, Xo, Xn, theta, factor, R, st);
+  dispatch_kd<CovCrossLaunch>(kernel, d, n_o, q, d, Xo, Xn, theta, factor, R, snap_coincident, st);
 }
 
 size_t adjoint_partials_size(int n, int d, int batch) {

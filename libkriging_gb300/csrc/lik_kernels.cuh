@@ -24,9 +24,10 @@ void cov_build_lower(int kernel, int n, int d, const double* X, int64_t x_bstrid
                      cudaStream_t st, bool fast = false, const int* nvalid = nullptr);
 
 // Rectangular cross-correlation R_on(i, j) = factor * C(Xo_i - Xn_j) (n_o x q, column-major, ldr = n_o);
-// coincident points (all |dx| <= eps) get 1.0 as in KrigingImpl::predict_impl.
+// with snap_coincident, coincident points (all |dx| <= eps) get 1.0 as in KrigingImpl::predict_impl; without it
+// every entry is the formula (LinearAlgebra::covMat_rect).
 void cov_cross(int kernel, int n_o, int q, int d, const double* Xo, const double* Xn, const double* theta,
-               double factor, double* R, cudaStream_t st);
+               double factor, double* R, cudaStream_t st, bool snap_coincident = true);
 
 // Adjoint partial sums over the strict lower triangle (+ diagonal terms), one partial per 64x64 tile,
 // then a deterministic fixed-order reduction into out[b * nacc + a].

@@ -301,17 +301,17 @@ size_t split_plane_elems(int rows, int K, int S) {
 
 size_t split_exp_elems(int rows, int K) { return (size_t)ceil_div(K, OZ_CHUNK) * ceil_div(rows, 128) * 128; }
 
-// default 1: tcgen05 for the Cholesky and triangular-inverse updates, mma.sync for W^T W (the fastest measured pair:
-// 865 ms against 1040 ms per n = 16384 evaluation on the mma.sync kernels alone)
+// default 3: 7-bit digits in 256-wide k blocks on tcgen05 with two-level blocked factorisations (527 ms per n = 16384
+// LL + gradient evaluation, against 866 ms for path 1: tcgen05 64-wide updates with W^T W on mma.sync)
 int& oz_tc_flag() {
   static int f = [] {
     const char* e = std::getenv("LK_OZAKI_TC");
-    return e ? std::atoi(e) : 1;
+    return e ? std::atoi(e) : 3;
   }();
   return f;
 }
 
-void ozaki_set_tensor_path(int tc) { oz_tc_flag() = (tc < 0 || tc > 2) ? 1 : tc; }
+void ozaki_set_tensor_path(int tc) { oz_tc_flag() = (tc < 0 || tc > 3) ? 1 : tc; }
 int ozaki_tensor_path() { return oz_tc_flag(); }
 
 void ozaki_split(int rows, int K, const double* p, int64_t s_r, int64_t s_k, int64_t bstride, int batch, SplitBuf& out,

@@ -105,6 +105,45 @@ class Kriging:
             int(P.get("is_nugget_estim", True))))
         return self
 
+    def update(self, y_u, X_u, refit=True):
+        """Kriging::update (Kriging.cpp:2433-2633): append (X_u, y_u) in original units; refit as the reference."""
+        X = _as_X(X_u)
+        y = np.ascontiguousarray(np.asarray(y_u, dtype=np.float64).reshape(-1))
+        check(_lib.load().lkg_kriging_update(self._h, ptr(y), y.size, None, 0, ptr(X), X.shape[0], X.shape[1],
+                                             int(bool(refit))))
+        return self
+
+    def save(self, filename):
+        """libKriging's JSON model file, version 2 (Kriging.cpp:2691-2717)."""
+        check(_lib.load().lkg_kriging_save(self._h, cstr(str(filename))))
+
+    @staticmethod
+    def load(filename):
+        """A model saved by save() or by libKriging's Kriging::save (Kriging.cpp:2719-2749)."""
+        L = _lib.load()
+        h = L.lkg_kriging_load(cstr(str(filename)))
+        if not h:
+            raise _lib.LibKrigingError(_lib.last_error())
+        k = Kriging.__new__(Kriging)
+        k._h = h
+        return k
+
+    def copy(self):
+        h = _lib.load().lkg_kriging_copy(self._h)
+        if not h:
+            raise _lib.LibKrigingError(_lib.last_error())
+        k = Kriging.__new__(Kriging)
+        k._h = h
+        return k
+
+    def covMat(self, X1, X2):
+        """sigma2 C(X1, X2) in original units (KrigingImpl.cpp:60-71)."""
+        A, B = _as_X(X1), _as_X(X2)
+        out = np.zeros((A.shape[0], B.shape[0]), order="F")
+        check(_lib.load().lkg_kriging_cov_mat(self._h, ptr(A), A.shape[0], A.shape[1], ptr(B), B.shape[0],
+                                              B.shape[1], ptr(out)))
+        return out
+
     def logLikelihoodFun(self, theta, return_grad=False, want_hess=False, bench=False):
         if want_hess:
             raise ValueError("logLikelihoodFun: the Hessian is not supported by the GPU build")
@@ -292,6 +331,9 @@ class Kriging:
 
     def scaleY(self):
         return _lib.load().lkg_kriging_get_scaleY(self._h)
+
+    def F(self):
+        return self._mat(_lib.load().lkg_kriging_get_F)
 
     def T(self):
         return self._mat(_lib.load().lkg_kriging_get_T)

@@ -228,6 +228,48 @@ def predict_vecchia(kernel, X, y, F, beta, theta, sigma2, Xn, Fn, m, cfg: Config
     return mean, sd
 
 
+def chol_block(C, Loo, cfg: Config = CONFIG):
+    """LinearAlgebra::chol_block (LinearAlgebra.cpp:254-299): the factor of C given the factor Loo of its leading
+    block.  Lou = Loo \\ C_ou, L_uo = Lou', L_uu = safe_chol_lower(C_uu - Lou' Lou) (the retry jitter lands on the
+    Schur complement only); when that exceeds the retry budget, the whole C is factored instead.
+    Returns (L, increments used by the accepted factorisation, True when the fallback ran)."""
+    C = np.asarray(C, dtype=np.float64)
+    n, no = C.shape[0], Loo.shape[0]
+    Lou = solve_lower(Loo, np.asfortranarray(C[:no, no:]))
+    L = np.zeros((n, n), order="F")
+    L[:no, :no] = np.tril(Loo)
+    L[no:, :no] = Lou.T
+    try:
+        Luu, inc = safe_chol_lower(C[no:, no:] - Lou.T @ Lou, cfg)
+    except CholeskyError:
+        Lf, inc = safe_chol_lower(C, cfg)
+        return np.asfortranarray(np.tril(Lf)), inc, True
+    L[no:, no:] = np.tril(Luu)
+    return L, inc, False
+
+
+def update_no_refit(kernel, X_old, L_old, X_new, y_all, F_all, theta, alpha=1.0, cfg: Config = CONFIG):
+    """KrigingImpl::update_no_refit_impl with update_cholCov (LinearAlgebra.cpp:206-252) and populate_Model's GLS
+    (KrigingImpl.cpp:73-125) in normalised units: R of the joined design (factor alpha off the diagonal, unit
+    diagonal), L = chol_block(R, L_old), then F*, y*, R*, beta, E*, SSE.  Returns (KModel, fallback_used)."""
+    X = np.vstack([np.asarray(X_old, dtype=np.float64), np.asarray(X_new, dtype=np.float64)])
+    R = build_R(kernel, X, theta, alpha, None)
+    L, inc, fb = chol_block(R, L_old, cfg)
+    Fstar = solve_lower(L, F_all)
+    ystar = solve_lower(L, y_all.reshape(-1, 1))[:, 0]
+    FtF = Fstar.T @ Fstar
+    if FtF.shape[0] > 0:
+        Rstar, info = lapack.dpotrf(FtF, lower=0, clean=1)
+        assert info == 0
+        rhs = Fstar.T @ ystar
+        beta = lapack.dtrtrs(Rstar, lapack.dtrtrs(Rstar, rhs.reshape(-1, 1), lower=0, trans=1)[0], lower=0)[0][:, 0]
+    else:
+        Rstar = np.zeros((0, 0))
+        beta = np.zeros(0)
+    Estar = solve_lower(L, (y_all - F_all @ beta).reshape(-1, 1))[:, 0]
+    return KModel(R, L, None, Fstar, ystar, Rstar, beta, Estar, float(Estar @ Estar), inc), fb
+
+
 def solve_lower(L, B):
     x, info = lapack.dtrtrs(L, np.asfortranarray(B, dtype=np.float64), lower=1, trans=0)
     assert info == 0

@@ -59,3 +59,34 @@ def test_call_on_unfitted_model_fails_loudly(so):
     assert rc == -1
     assert "fit" in lk._lib.last_error()
     L.lkg_kriging_delete(h)
+
+
+def test_load_errors_follow_reference(so, tmp_path):
+    """Kriging::load (Kriging.cpp:2719-2731): version 2 and content "Kriging" required, with the reference's
+    messages; the file is parsed before any device work, so these run without a GPU."""
+    L = lk.load()
+    f = tmp_path / "m.json"
+    f.write_text('{"version": 3, "content": "Kriging"}')
+    assert L.lkg_kriging_load(str(f).encode()) is None
+    assert "Bad version to load from '%s'; found 3, requires 2" % f in lk._lib.last_error()
+    f.write_text('{"version": 2, "content": "WarpKriging"}')
+    assert L.lkg_kriging_load(str(f).encode()) is None
+    assert "Bad content to load from '%s'; found 'WarpKriging', requires 'Kriging'" % f in lk._lib.last_error()
+    f.write_text('{"version": 2, "content": "Kriging", ')
+    assert L.lkg_kriging_load(str(f).encode()) is None
+    assert "JSON parse error" in lk._lib.last_error()
+    assert L.lkg_kriging_load(str(tmp_path / "missing.json").encode()) is None
+    assert "cannot open" in lk._lib.last_error()
+
+
+def test_update_rejects_noise_like_reference(so):
+    """lk_kriging_update with a noise vector calls update(y, noise, X), which requires NoiseModel Heterogeneous
+    (Kriging.cpp:2639-2640)."""
+    L = lk.load()
+    h = L.lkg_kriging_new(b"gauss", None)
+    y = (ctypes.c_double * 1)(1.0)
+    x = (ctypes.c_double * 2)(0.1, 0.2)
+    rc = L.lkg_kriging_update(h, y, 1, y, 1, x, 1, 2, 0)
+    assert rc == -1
+    assert "requires NoiseModel::Heterogeneous" in lk._lib.last_error()
+    L.lkg_kriging_delete(h)

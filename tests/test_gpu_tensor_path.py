@@ -52,6 +52,23 @@ def test_tc_gemm_matches_fp64_and_mma_sync(gpu_lib, tensor_path, S, shape):
         assert err < (4e-15 if S == 7 else 2e-15), err
 
 
+@pytest.mark.parametrize("S", [6, 7])
+@pytest.mark.parametrize("shape", [(64, 64, 64), (200, 130, 257), (129, 300, 64), (384, 256, 512), (300, 70, 1000)])
+def test_oz7_gemm_matches_fp64(gpu_lib, tensor_path, S, shape):
+    """Tensor path 3: 7-bit digits with one exponent per 256-wide k block; several k blocks are summed in FP64.
+    S = 7 slices -> 8 digits (56-bit operands) reaches FP64-level products, S = 6 -> 7 digits (49 bits) the precision
+    of the inverse."""
+    M, N, K = shape
+    rng = np.random.default_rng(M + N + K + S)
+    A = rng.standard_normal((M, K)) * np.exp(rng.uniform(-5, 5, size=(M, 1)))
+    B = rng.standard_normal((N, K))
+    assert tensor_path.lkg_set_tensor_path(3) == 3
+    C = _emulated(gpu_lib, A, B, S)
+    scale = np.abs(A) @ np.abs(B).T
+    err = np.max(np.abs(C - A @ B.T) / scale)
+    assert err < (4e-15 if S == 7 else 5e-13), err
+
+
 def _config2_like(n, d=8, seed=123):
     rng = np.random.default_rng(seed)
     X = rng.uniform(size=(n, d))
@@ -60,8 +77,8 @@ def _config2_like(n, d=8, seed=123):
     return X, y, theta
 
 
-@pytest.mark.parametrize("path", [1, 2])
-@pytest.mark.parametrize("n", [640, 2048])
+@pytest.mark.parametrize("path", [1, 2, 3])
+@pytest.mark.parametrize("n", [640, 2048, 1000])
 def test_tc_mixed_loglik(gpu_lib, tensor_path, n, path):
     X, y, theta = _config2_like(n)
     alpha = 1.0 / (1.0 + 1e-6)
@@ -77,5 +94,6 @@ def test_tc_mixed_loglik(gpu_lib, tensor_path, n, path):
     ll_t, g_t, _ = k.logLikelihoodFun(g, True)
     assert abs(ll_t - ll64) / abs(ll64) < 1e-8
     assert rel_err(g_t, g64) < 1e-6
-    assert abs(ll_t - ll_s) / abs(ll_s) < 1e-12
-    assert rel_err(g_t, g_s) < 1e-10
+    if path < 3:  # the same digits as the mma.sync kernels
+        assert abs(ll_t - ll_s) / abs(ll_s) < 1e-12
+        assert rel_err(g_t, g_s) < 1e-10

@@ -160,3 +160,33 @@ def test_oracle_lmp_fixed_sigma2_forward_differences():
         e = np.zeros(2)
         e[k] = 1e-6
         assert g[k] == (ora.log_marg_post(th + e, False)[0] - v) / 1e-6
+
+
+@pytest.mark.parametrize("no,nu", [(40, 1), (37, 13), (64, 64)])
+def test_oracle_chol_block_equals_full_factor(no, nu):
+    """chol_block (LinearAlgebra.cpp:254-299) on a well-conditioned matrix: the block factor is the Cholesky factor
+    of the whole matrix (to rounding), no jitter is added and the fallback does not run."""
+    rng = np.random.default_rng(7)
+    X = rng.uniform(size=(no + nu, 3))
+    C = O.build_R("matern5_2", X, np.array([0.3, 0.4, 0.5]), 1.0)
+    Loo, _ = O.safe_chol_lower(C[:no, :no])
+    L, inc, fb = O.chol_block(C, Loo)
+    Lf, _ = O.safe_chol_lower(C)
+    assert inc == 0 and not fb
+    assert np.max(np.abs(L - np.tril(Lf))) < 1e-12
+    assert np.max(np.abs(np.triu(L, 1))) == 0.0
+
+
+def test_oracle_chol_block_jitters_the_schur_block_only():
+    """A new point that duplicates an old one makes the Schur complement singular: safe_chol_lower's jitter goes on
+    that block's diagonal (LinearAlgebra.cpp:286-297), so the old block of L is untouched."""
+    rng = np.random.default_rng(8)
+    Xo = rng.uniform(size=(30, 2))
+    X = np.vstack([Xo, Xo[3:4]])
+    C = O.build_R("gauss", X, np.array([0.4, 0.4]), 1.0)
+    Loo, inc0 = O.safe_chol_lower(C[:30, :30])
+    L, inc, fb = O.chol_block(C, Loo)
+    assert not fb and inc >= 1
+    assert np.array_equal(L[:30, :30], np.tril(Loo))
+    Lf, incf = O.safe_chol_lower(C)  # the full factor would have jittered every diagonal entry
+    assert incf >= 1
