@@ -178,9 +178,11 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def _timed_steps(k, lib, gamma, steps, local):
+def _timed_steps(k, lib, gamma, steps, local, label):
     """K LL+grad steps; returns (mean device ms per step from the CUDA-event stage timings, last (ll, grad),
-    per-kernel stats, clock record)."""
+    per-kernel stats, clock record).  Each step is an NVTX range named `label` (a profiler can select one path's
+    launches with it)."""
+    import torch
     lib.lkg_stats_reset()
     lib.lkg_stats_enable(1)
     clocks = ClockSampler(local)
@@ -188,7 +190,9 @@ def _timed_steps(k, lib, gamma, steps, local):
     dev_ms = []
     ll = g = None
     for _ in range(steps):
+        torch.cuda.nvtx.range_push(label)
         ll, g, _ = k.logLikelihoodFun(gamma, True, False, bench=True)
+        torch.cuda.nvtx.range_pop()
         dev_ms.append(sum(k.last_bench.values()))
     clk = clocks.stop()
     lib.lkg_stats_enable(0)
@@ -238,7 +242,7 @@ def run_gpu(args):
     for _ in range(args.warmup):
         k.logLikelihoodFun(gamma, True, False, bench=True)
     barrier()
-    fp64_ms, (ll64, g64), st64, clk64, stage64 = _timed_steps(k, lib, gamma, args.steps, local)
+    fp64_ms, (ll64, g64), st64, clk64, stage64 = _timed_steps(k, lib, gamma, args.steps, local, "fp64_step")
     barrier()
     # ---- mixed path (headline) ----
     k.set_precision(args.slices)
@@ -246,7 +250,7 @@ def run_gpu(args):
         k.logLikelihoodFun(gamma, True, False, bench=True)
     barrier()
     t0 = time.perf_counter()
-    mix_ms, (llm, gm), stats, clk, stage = _timed_steps(k, lib, gamma, args.steps, local)
+    mix_ms, (llm, gm), stats, clk, stage = _timed_steps(k, lib, gamma, args.steps, local, "mixed_step")
     barrier()
     wall_value = time.perf_counter() - t0
     used = k.last_slices()

@@ -104,66 +104,147 @@ __global__ void __launch_bounds__(NT) k_gemm_tiles(int M, int N, int K, double a
 // ---- diagonal block: Cholesky + inverse in shared memory (one CTA per batch entry) ----
 constexpr int DPAD = NB + 1;
 
+constexpr int PB = 16;  // panel width inside a diagonal block
+
+// Inverse of the 16 x 16 lower block of s at (jb, jb) into the same block of w: lane c < 16 substitutes column c,
+// with the reciprocals of the diagonal (one division per row).
+__device__ __forceinline__ void diag16_inverse(const double* s, double* w, int jb, int lane) {
+  if (lane >= PB) return;
+  const int c = lane;
+  for (int i = c; i < PB; ++i) {
+    double sum = (i == c) ? 1.0 : 0.0;
+    for (int k = c; k < i; ++k) sum = fma(-s[(jb + i) * DPAD + jb + k], w[(jb + k) * DPAD + jb + c], sum);
+    w[(jb + i) * DPAD + jb + c] = sum * (1.0 / s[(jb + i) * DPAD + jb + i]);
+  }
+}
+
+// The off-diagonal 16 x 16 blocks of the inverse from the diagonal ones, by block diagonals:
+// W_ij = -W_ii sum_{k=j}^{i-1} L_ik W_kj.  scratch: 3 x 16 x 16 doubles.  Ends with a barrier.
+__device__ __forceinline__ void assemble_inverse(const double* s, double* w, double* scratch, int t) {
+  constexpr int NPB = NB / PB;
+  for (int dist = 1; dist < NPB; ++dist) {
+    const int npair = NPB - dist;
+    for (int it = t; it < npair * PB * PB; it += NT) {  // T = sum_k L_ik W_kj
+      const int pr = it / (PB * PB), r = (it / PB) % PB, c = it % PB;
+      const int bi = (pr + dist) * PB, bj = pr * PB;
+      double acc = 0.0;
+      for (int k = bj; k < bi; ++k) acc = fma(s[(bi + r) * DPAD + k], w[k * DPAD + bj + c], acc);
+      scratch[it] = acc;
+    }
+    __syncthreads();
+    for (int it = t; it < npair * PB * PB; it += NT) {  // W_ij = -W_ii T
+      const int pr = it / (PB * PB), r = (it / PB) % PB, c = it % PB;
+      const int bi = (pr + dist) * PB, bj = pr * PB;
+      double acc = 0.0;
+      for (int m = 0; m <= r; ++m) acc = fma(w[(bi + r) * DPAD + bi + m], scratch[pr * PB * PB + m * PB + c], acc);
+      w[(bi + r) * DPAD + bj + c] = -acc;
+    }
+    __syncthreads();
+  }
+}
+
+// Cholesky factor and inverse of one nb x nb diagonal block (nb <= 64) in shared memory.  16-column block steps:
+// update the block column with the columns left of it, factor and invert its 16 x 16 diagonal block in one warp,
+// then solve the rows below with that inverse; the full inverse is assembled from the diagonal inverses.  A ragged
+// block is padded with the identity.
 __global__ void __launch_bounds__(NT) k_potrf_diag(double* A, int64_t lda, int64_t mstride, int k0, int nb,
                                                    double* Dinv, int64_t dinv_bstride, int blk, int* info) {
   const int64_t b = blockIdx.z;
   if (info[b] != 0) return;  // an earlier block of this matrix already failed
   extern __shared__ double dsm[];
-  double* s = dsm;                 // [NB][DPAD]  s[i*DPAD + j] = L(i, j)
-  double* w = dsm + NB * DPAD;     // [NB][DPAD]  w[i*DPAD + j] = L^-1(i, j)
+  double* s = dsm;                   // [NB][DPAD]  s[i*DPAD + j] = L(i, j)
+  double* w = dsm + NB * DPAD;       // [NB][DPAD]  w[i*DPAD + j] = L^-1(i, j)
+  double* scratch = w + NB * DPAD;   // [3][PB][PB]
   __shared__ int failed;
   double* Ab = A + b * mstride + k0 + (int64_t)k0 * lda;
-  const int t = threadIdx.x;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   if (t == 0) failed = 0;
   for (int idx = t; idx < NB * NB; idx += NT) {
     const int i = idx & 63, j = idx >> 6;
-    s[i * DPAD + j] = (i < nb && j < nb && i >= j) ? Ab[i + (int64_t)j * lda] : 0.0;
+    double v = 0.0;
+    if (i < nb && j < nb) {
+      if (i >= j) v = Ab[i + (int64_t)j * lda];
+    } else if (i == j) {
+      v = 1.0;
+    }
+    s[i * DPAD + j] = v;
     w[i * DPAD + j] = 0.0;
   }
   __syncthreads();
-  for (int j = 0; j < nb; ++j) {
-    if (t == 0) {
-      const double dj = s[j * DPAD + j];
-      if (!(dj > 0.0)) {  // non-positive or NaN pivot
-        failed = 1;
-        info[b] = k0 + j + 1;
-      } else {
-        s[j * DPAD + j] = sqrt(dj);
+  for (int jb = 0; jb < NB; jb += PB) {
+    // (1) columns jb .. jb+15, rows i >= c: subtract the columns 0 .. jb-1
+    if (jb > 0) {
+      for (int it = t; it < (NB - jb) * PB; it += NT) {
+        const int c = jb + (it % PB), i = jb + it / PB;
+        if (i >= c) {
+          double acc = s[i * DPAD + c];
+          for (int k = 0; k < jb; ++k) acc = fma(-s[i * DPAD + k], s[c * DPAD + k], acc);
+          s[i * DPAD + c] = acc;
+        }
       }
+      __syncthreads();
+    }
+    // (2) the 16 x 16 diagonal block: right-looking Cholesky, lane = row (column scaling by the reciprocal of the
+    // pivot, as LAPACK's dpotf2 does), then its inverse, lane = column
+    if (warp == 0) {
+      const int r = jb + lane;
+      bool bad = false;
+      for (int j = 0; j < PB; ++j) {
+        const int cj = jb + j;
+        const double piv = s[cj * DPAD + cj];
+        if (!(piv > 0.0)) {  // non-positive or NaN pivot
+          bad = true;
+          if (lane == 0) {
+            failed = 1;
+            info[b] = k0 + cj + 1;
+          }
+          break;
+        }
+        const double d = sqrt(piv), rd = 1.0 / d;
+        __syncwarp();
+        if (lane == 0) s[cj * DPAD + cj] = d;
+        if (lane > j && lane < PB) s[r * DPAD + cj] *= rd;
+        __syncwarp();
+        if (lane > j && lane < PB) {
+          const double lrj = s[r * DPAD + cj];
+          for (int c = j + 1; c <= lane; ++c) s[r * DPAD + jb + c] = fma(-lrj, s[(jb + c) * DPAD + cj], s[r * DPAD + jb + c]);
+        }
+        __syncwarp();
+      }
+      if (!bad) diag16_inverse(s, w, jb, lane);
     }
     __syncthreads();
     if (failed) return;
-    const double ljj = s[j * DPAD + j];
-    for (int i = j + 1 + t; i < nb; i += NT) s[i * DPAD + j] /= ljj;
-    __syncthreads();
-    // trailing update of columns c in (j, nb): 64 columns x 4 row groups
+    // (3) rows below: L(i, jb..jb+15) = A(i, jb..jb+15) W_dd^T, computed into registers, then stored
     {
-      const int c = j + 1 + (t & 63);
-      if (c < nb) {
-        const double lcj = s[c * DPAD + j];
-        for (int i = c + (t >> 6); i < nb; i += 4) s[i * DPAD + c] -= s[i * DPAD + j] * lcj;
+      const int nrow = NB - jb - PB;
+      double out[3];
+#pragma unroll
+      for (int u = 0; u < 3; ++u) {
+        const int it = t + u * NT;
+        out[u] = 0.0;
+        if (it < nrow * PB) {
+          const int i = jb + PB + it / PB, c = it % PB;
+          double acc = 0.0;
+          for (int k = 0; k <= c; ++k) acc = fma(s[i * DPAD + jb + k], w[(jb + c) * DPAD + jb + k], acc);
+          out[u] = acc;
+        }
       }
-    }
-    __syncthreads();
-  }
-  // inverse by row wavefront: w(i, c) = (delta_ic - sum_{k=c}^{i-1} L(i,k) w(k,c)) / L(i,i), 4 lanes per column
-  {
-    const int c = t >> 2, q = t & 3;
-    for (int i = 0; i < nb; ++i) {
-      double sum = 0.0;
-      if (c <= i && c < nb)
-        for (int k = c + q; k < i; k += 4) sum = fma(s[i * DPAD + k], w[k * DPAD + c], sum);
-      sum += __shfl_xor_sync(0xffffffffu, sum, 1);
-      sum += __shfl_xor_sync(0xffffffffu, sum, 2);
-      if (q == 0 && c <= i && c < nb) w[i * DPAD + c] = ((i == c ? 1.0 : 0.0) - sum) / s[i * DPAD + i];
+      __syncthreads();
+#pragma unroll
+      for (int u = 0; u < 3; ++u) {
+        const int it = t + u * NT;
+        if (it < nrow * PB) s[(jb + PB + it / PB) * DPAD + jb + it % PB] = out[u];
+      }
       __syncthreads();
     }
   }
+  assemble_inverse(s, w, scratch, t);
   double* Db = Dinv + b * dinv_bstride + (int64_t)blk * NB * NB;
   for (int idx = t; idx < NB * NB; idx += NT) {
     const int i = idx & 63, j = idx >> 6;
     if (i < nb && j < nb && i >= j) Ab[i + (int64_t)j * lda] = s[i * DPAD + j];
-    Db[i + j * NB] = (i >= j) ? w[i * DPAD + j] : 0.0;  // zero above the diagonal and in the ragged padding
+    Db[i + j * NB] = (i >= j && i < nb && j < nb) ? w[i * DPAD + j] : 0.0;  // zero above the diagonal and padding
   }
 }
 
@@ -288,30 +369,30 @@ __global__ void __launch_bounds__(NT) k_trtri_diag(const double* L, int64_t lda,
   extern __shared__ double tsm[];
   double* s = tsm;
   double* w = tsm + NB * DPAD;
+  double* scratch = w + NB * DPAD;
   const int64_t b = blockIdx.z;
   const int blk = blockIdx.x, k0 = blk * NB, nb = min(NB, n - k0);
   const double* Lb = L + b * mstride + k0 + (int64_t)k0 * lda;
-  const int t = threadIdx.x;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   for (int idx = t; idx < NB * NB; idx += NT) {
     const int i = idx & 63, j = idx >> 6;
-    s[i * DPAD + j] = (i < nb && j < nb && i >= j) ? Lb[i + (int64_t)j * lda] : 0.0;
+    double v = 0.0;
+    if (i < nb && j < nb) {
+      if (i >= j) v = Lb[i + (int64_t)j * lda];
+    } else if (i == j) {
+      v = 1.0;
+    }
+    s[i * DPAD + j] = v;
     w[i * DPAD + j] = 0.0;
   }
   __syncthreads();
-  const int c = t >> 2, q = t & 3;
-  for (int i = 0; i < nb; ++i) {
-    double sum = 0.0;
-    if (c <= i && c < nb)
-      for (int k = c + q; k < i; k += 4) sum = fma(s[i * DPAD + k], w[k * DPAD + c], sum);
-    sum += __shfl_xor_sync(0xffffffffu, sum, 1);
-    sum += __shfl_xor_sync(0xffffffffu, sum, 2);
-    if (q == 0 && c <= i && c < nb) w[i * DPAD + c] = ((i == c ? 1.0 : 0.0) - sum) / s[i * DPAD + i];
-    __syncthreads();
-  }
+  if (warp < NB / PB) diag16_inverse(s, w, warp * PB, lane);
+  __syncthreads();
+  assemble_inverse(s, w, scratch, t);
   double* Db = Dinv + b * dinv_bstride + (int64_t)blk * NB * NB;
   for (int idx = t; idx < NB * NB; idx += NT) {
     const int i = idx & 63, j = idx >> 6;
-    Db[i + j * NB] = (i >= j) ? w[i * DPAD + j] : 0.0;
+    Db[i + j * NB] = (i >= j && i < nb && j < nb) ? w[i * DPAD + j] : 0.0;
   }
 }
 
@@ -353,7 +434,7 @@ bool g_trtri_diag_attr_set = false;
 void trtri_diag_blocks(const double* L, int64_t lda, int64_t mstride, int n, double* Dinv, int batch,
                        cudaStream_t st) {
   const int nblk = ceil_div(n, NB);
-  const size_t smem = 2 * NB * DPAD * sizeof(double);
+  const size_t smem = (2 * NB * DPAD + 3 * PB * PB) * sizeof(double);
   if (!g_trtri_diag_attr_set) {
     LKG_CUDA(cudaFuncSetAttribute(k_trtri_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     g_trtri_diag_attr_set = true;
@@ -395,7 +476,7 @@ void gemm_tiles(int M, int N, int K, double alpha, MatView A, MatView B, double 
 
 void potrf_diag(double* A, int64_t lda, int64_t mstride, int k0, int nb, double* Dinv, int64_t dinv_bstride, int blk,
                 int* info, int batch, cudaStream_t st) {
-  const size_t smem = 2 * NB * DPAD * sizeof(double);
+  const size_t smem = (2 * NB * DPAD + 3 * PB * PB) * sizeof(double);
   if (!g_diag_attr_set) {
     LKG_CUDA(cudaFuncSetAttribute(k_potrf_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     g_diag_attr_set = true;

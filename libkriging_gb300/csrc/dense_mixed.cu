@@ -22,14 +22,18 @@ SplitBuf make_split(void* planes, int* exps, int S, int rows_cap, int K_cap) {
 // digits of the 7-bit split for a given count of 8-bit slices: the same operand precision, one digit more
 int oz7_digits(int slices) { return std::min(8, std::max(6, slices + 1)); }
 
-// Two-level blocked Cholesky: 256-wide panels factored with the 64-wide FP64 steps (diagonal block, panel solve and
-// the update of the panel's remaining columns), then one rank-256 trailing update on the tensor cores per panel.
+// Two-level blocked Cholesky: 256-wide panels factored in 64-wide steps (FP64 diagonal block; panel solve and the update
+// of the panel's remaining columns as 64-deep digit products), then one rank-256 trailing update per panel.  Every
+// product reads split copies of its operands, so the in-place ones (the panel solve) are safe.
 void potrf_blocked_mixed7(double* A, int64_t lda, int64_t mstride, int n, double* Dinv, int* info, int batch,
                           const MixedWorkspace& ws, cudaStream_t st) {
   const int nblk = ceil_div(n, NB);
   const int64_t dstride = (int64_t)nblk * NB * NB;
   LKG_CUDA(cudaMemsetAsync(info, 0, sizeof(int) * batch, st));
-  Split7 P = oz7_buffer(ws.panel, ws.panel_exp, oz7_digits(ws.slices), ws.n, OZ7_KB, OZ7_KB);
+  const int S = oz7_digits(ws.slices);
+  Split7 P = oz7_buffer(ws.panel, ws.panel_exp, S, ws.n, OZ7_KB, OZ7_KB);
+  Split7 SA = oz7_buffer(ws.panel, ws.panel_exp, S, ws.n, NB, NB);
+  Split7 SD = oz7_buffer(ws.rowblk, ws.rowblk_exp, S, ws.n, NB, NB);
   for (int K0 = 0; K0 < n; K0 += OZ7_KB) {
     const int W = std::min(OZ7_KB, n - K0);
     for (int k0 = K0; k0 < K0 + W; k0 += NB) {
@@ -38,26 +42,27 @@ void potrf_blocked_mixed7(double* A, int64_t lda, int64_t mstride, int n, double
       const int M = n - k0 - nb;
       if (M <= 0) continue;
       double* A21 = A + (k0 + nb) + (int64_t)k0 * lda;
-      MatView a{A21, 1, lda, mstride};
-      MatView bt{Dinv + (int64_t)k * NB * NB, NB, 1, dstride};
-      gemm_tiles(M, nb, nb, 1.0, a, bt, 0.0, A21, lda, mstride, batch, false, st);
+      // L21 = A21 Dinv_k^T: B rows are the rows of Dinv_k
+      oz7_split(M, nb, A21, 1, lda, mstride, batch, SA, st);
+      oz7_split(nb, nb, Dinv + (int64_t)k * NB * NB, 1, NB, dstride, batch, SD, st);
+      oz7_gemm(M, nb, 0, 1, 1.0, SA, SD, 0.0, A21, lda, mstride, batch, false, st);
       const int wr = K0 + W - (k0 + nb);  // panel columns right of this block
-      if (wr > 0) {
-        MatView l21t{A21, lda, 1, mstride};  // B(kk, c) = L21(c, kk)
-        gemm_tiles(M, wr, nb, -1.0, a, l21t, 1.0, A21 + (int64_t)nb * lda, lda, mstride, batch, true, st);
+      if (wr > 0) {  // A(k0+nb:, k0+nb:K0+W) -= L21 L21(0:wr, :)^T (the strict upper part written is never read)
+        oz7_split(M, nb, A21, 1, lda, mstride, batch, SA, st);
+        oz7_gemm(M, wr, 0, 1, -1.0, SA, SA, 1.0, A21 + (int64_t)nb * lda, lda, mstride, batch, false, st);
       }
     }
     const int M2 = n - K0 - W;
     if (M2 <= 0) continue;
-    // A22 -= P2 P2^T, P2 = L(K0+W:, K0:K0+W), one k block
+    // A22 -= P2 P2^T, P2 = L(K0+W:, K0:K0+W), one 256-wide k block
     double* P2 = A + (K0 + W) + (int64_t)K0 * lda;
     oz7_split(M2, W, P2, 1, lda, mstride, batch, P, st);
     oz7_gemm(M2, M2, 0, 1, -1.0, P, P, 1.0, P2 + (int64_t)W * lda, lda, mstride, batch, true, st);
   }
 }
 
-// Two-level triangular inverse: inside a 256-row block the 64-wide FP64 steps; below it one rank-256 update of the
-// accumulated rows on the tensor cores.
+// Two-level triangular inverse: inside a 256-row block the 64-wide steps, below it one rank-256 update of the
+// accumulated rows; every product on the digit kernel.
 void trtri_blocked_mixed7(const double* L, int64_t lda, int64_t mstride, int n, const double* Dinv, double* W,
                           int64_t ldw, int64_t wstride, int batch, const MixedWorkspace& ws, cudaStream_t st) {
   const int nblk = ceil_div(n, NB);
@@ -67,21 +72,23 @@ void trtri_blocked_mixed7(const double* L, int64_t lda, int64_t mstride, int n, 
   const int S = oz7_digits(ws.slices_inv);
   Split7 SL = oz7_buffer(ws.panel, ws.panel_exp, S, ws.n, OZ7_KB, OZ7_KB);
   Split7 SR = oz7_buffer(ws.rowblk, ws.rowblk_exp, S, ws.n, OZ7_KB, OZ7_KB);
+  Split7 SA = oz7_buffer(ws.panel, ws.panel_exp, S, ws.n, NB, NB);
+  Split7 SB = oz7_buffer(ws.rowblk, ws.rowblk_exp, S, ws.n, NB, NB);
   for (int K0 = 0; K0 < n; K0 += OZ7_KB) {
     const int Wd = std::min(OZ7_KB, n - K0);
     for (int k0 = K0; k0 < K0 + Wd; k0 += NB) {
       const int nb = std::min(NB, n - k0), k = k0 / NB;
       copy_dinv_block(Dinv, dstride, k, W, ldw, wstride, k0, nb, batch, st);
-      if (k0 > 0) {  // W(k0:k0+nb, 0:k0) = -Dinv_k Acc(k0:k0+nb, 0:k0)
-        MatView d{Dinv + (int64_t)k * NB * NB, 1, NB, dstride};
-        MatView acc{W + k0, 1, ldw, wstride};
-        gemm_tiles(nb, k0, nb, -1.0, d, acc, 0.0, W + k0, ldw, wstride, batch, false, st);
+      if (k0 > 0) {  // W(k0:k0+nb, 0:k0) = -Dinv_k Acc(k0:k0+nb, 0:k0): B rows are the columns of Acc
+        oz7_split(nb, nb, Dinv + (int64_t)k * NB * NB, 1, NB, dstride, batch, SA, st);
+        oz7_split(k0, nb, W + k0, ldw, 1, wstride, batch, SB, st);
+        oz7_gemm(nb, k0, 0, 1, -1.0, SA, SB, 0.0, W + k0, ldw, wstride, batch, false, st);
       }
       const int mr = K0 + Wd - (k0 + nb);  // rows of this 256-row block below the 64-row one
-      if (mr > 0) {
-        MatView a{L + (k0 + nb) + (int64_t)k0 * lda, 1, lda, mstride};
-        MatView bw{W + k0, 1, ldw, wstride};
-        gemm_tiles(mr, k0 + nb, nb, 1.0, a, bw, 1.0, W + k0 + nb, ldw, wstride, batch, false, st);
+      if (mr > 0) {  // Acc(k0+nb:K0+Wd, 0:k0+nb) += L(k0+nb:K0+Wd, k0:k0+nb) W(k0:k0+nb, 0:k0+nb)
+        oz7_split(mr, nb, L + (k0 + nb) + (int64_t)k0 * lda, 1, lda, mstride, batch, SA, st);
+        oz7_split(k0 + nb, nb, W + k0, ldw, 1, wstride, batch, SB, st);
+        oz7_gemm(mr, k0 + nb, 0, 1, 1.0, SA, SB, 1.0, W + k0 + nb, ldw, wstride, batch, false, st);
       }
     }
     const int M2 = n - K0 - Wd;

@@ -36,10 +36,19 @@ void set_last_error(const char* msg);
 namespace {
 
 constexpr int TM = 128, TN = 64;
-constexpr int NA = 4;                          // A ring stages
+constexpr int NA_MAX = 7;                      // A ring stages at most (S = 7)
 constexpr uint32_t A_BYTES = TM * 128;         // one digit of a 128-row tile, one 64-wide sub-chunk: 16 KB
 constexpr uint32_t B_BYTES = TN * 128;         // 64-row tile: 8 KB
 constexpr uint64_t kWaitNs = 200000000ull;     // an mbarrier wait gives up after 200 ms
+
+// A ring depth for S digits: what 227 KB of shared memory holds beside the two B buffers (6 for S = 8, 7 for S = 7);
+// a deep ring keeps enough digit images in flight to cover the L2 latency at the rate the MMAs consume them
+template <int S>
+constexpr int ring_depth() {
+  return (int)((227u * 1024u - 1024u - 2u * S * B_BYTES) / A_BYTES) < NA_MAX
+             ? (int)((227u * 1024u - 1024u - 2u * S * B_BYTES) / A_BYTES)
+             : NA_MAX;
+}
 constexpr int NTHREADS = 576;                  // 18 warps
 
 __device__ int g_oz7_error;
@@ -248,9 +257,10 @@ struct Tile {
 
 __device__ __forceinline__ bool tile_of(const Oz7Args& g, long long t, Tile& T) {
   if (g.lower || g.wtw) {  // lower tiles in row-major order: row block I holds column blocks 0 .. 2 I + 1
-    int I = (int)((sqrt(4.0 * (double)t + 1.0) - 1.0) * 0.5);
+    // I = floor((sqrt(4 t + 1) - 1) / 2) from an FP32 estimate and integer corrections (FP64 is scarce here)
+    int I = (int)((sqrtf(4.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
     while ((long long)(I + 1) * (I + 2) <= t) ++I;
-    while ((long long)I * (I + 1) > t) --I;
+    while (I > 0 && (long long)I * (I + 1) > t) --I;
     T.m0 = I * TM;
     T.n0 = (int)(t - (long long)I * (I + 1)) * TN;
   } else {
@@ -271,12 +281,14 @@ __device__ __forceinline__ bool tile_of(const Oz7Args& g, long long t, Tile& T) 
 }
 
 struct Bars {
-  uint64_t a_full[NA], a_empty[NA], b_full[2], b_empty[2], acc_full, acc_empty, drain;
+  uint64_t a_full[NA_MAX], a_empty[NA_MAX], b_full[2], b_empty[2], acc_full, acc_empty, drain;
 };
 
 template <int S>
 __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long ntiles) {
   static_assert(S >= 6 && S <= 8, "digit count");
+  constexpr int NA = ring_depth<S>();
+  static_assert(NA >= 2 && NA <= NA_MAX, "A ring depth");
   constexpr uint32_t B_BUF = S * B_BYTES;
   extern __shared__ unsigned char oz7_raw[];
   __shared__ Bars bars;
@@ -394,7 +406,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
               break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            const uint32_t bbase = sB + bb * B_BUF;
+            // descriptors advance with the address: +2 per 32-byte (16-element) step along k, +B_BYTES / 16 per B
+            // digit, so each MMA costs one add and one issue (an N = 64 MMA runs ~30 clocks at the tensor rate)
+            const uint64_t bdesc0 = sdesc(sB + bb * B_BUF);
+#pragma unroll
             for (int i = 1; i <= S; ++i) {
               const int st = ua % NA;
               if (!mbar_wait(bar(bars.a_full[st]), (ua / NA) & 1)) {
@@ -403,13 +418,15 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
                 break;
               }
               asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-              const uint32_t a0 = sA + st * A_BYTES;
+              const uint64_t adesc0 = sdesc(sA + st * A_BYTES);
+#pragma unroll
               for (int j = 1; j <= S + 1 - i; ++j) {
                 const uint32_t d = tmem + (uint32_t)((i + j - 2) * TN);
-                const uint32_t b0 = bbase + (j - 1) * B_BYTES;
+                const uint64_t bdesc = bdesc0 + (uint64_t)((j - 1) * (B_BYTES >> 4));
 #pragma unroll
                 for (int kk = 0; kk < 4; ++kk)
-                  mma_issue(d, sdesc(a0 + kk * 32u), sdesc(b0 + kk * 32u), (!first_sub || i > 1 || kk > 0) ? 1u : 0u);
+                  mma_issue(d, adesc0 + (uint64_t)(2 * kk), bdesc + (uint64_t)(2 * kk),
+                            (!first_sub || i > 1 || kk > 0) ? 1u : 0u);
               }
               mma_commit(bar(bars.a_empty[st]));
               issued = true;
@@ -446,7 +463,21 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
       for (int kb = T.kb0; kb < T.kb1 && ok; ++kb) {
         const bool first = (kb == T.kb0);
         const bool need_c = !(first && g.beta == 0.0);
+        // operands of the update, loaded while the block's products run: the column exponents and the first four
+        // C values (each group then prefetches the next group's C)
         const int er = ea[(int64_t)kb * g.SA.rows_pad + row];
+        const int* ebk = eb + (int64_t)kb * g.SB.rows_pad;
+        double cnext[4];
+        int enext[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int col = col0 + q;
+          enext[q] = (col < g.N) ? ebk[col] : 0;
+          cnext[q] = (need_c && row < g.M && col < g.N && (!tri || row >= col)) ? Cb[row + (int64_t)col * g.ldc] : 0.0;
+        }
+        // C = beta C + alpha P in one FP64 operation where the coefficients allow it
+        const int upd = !need_c ? (g.alpha == 1.0 ? 0 : 1)
+                                : ((!first || g.beta == 1.0) ? (g.alpha == -1.0 ? 2 : (g.alpha == 1.0 ? 3 : 4)) : 5);
         const bool got = mbar_wait(bar(bars.acc_full), uacc & 1);
         if (!__all_sync(0xffffffffu, got)) {
           if (lane == 0) record_expiry(6 + 16 * w, ti, kb, -1, -1, 0, 0, uacc);
@@ -454,15 +485,23 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-#pragma unroll 1
+#pragma unroll
         for (int q0 = 0; q0 < 16; q0 += 4) {
           double cold[4];
-          bool in[4];
+          int ec[4];
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
-            const int col = col0 + q0 + q;
-            in[q] = row < g.M && col < g.N && (!tri || row >= col);
-            cold[q] = (in[q] && need_c) ? Cb[row + (int64_t)col * g.ldc] : 0.0;
+            cold[q] = cnext[q];
+            ec[q] = enext[q];
+          }
+          if (q0 + 4 < 16) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              const int col = col0 + q0 + 4 + q;
+              enext[q] = (col < g.N) ? ebk[col] : 0;
+              cnext[q] = (need_c && row < g.M && col < g.N && (!tri || row >= col)) ? Cb[row + (int64_t)col * g.ldc]
+                                                                                     : 0.0;
+            }
           }
           uint32_t v[S][4];
 #pragma unroll
@@ -482,19 +521,21 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
               else
                 h2 = h2 * 128 + iv;
             }
-            if (in[q]) {
+            const int col = col0 + q0 + q;
+            if (row < g.M && col < g.N && (!tri || row >= col)) {
               // H = h1 128^(S-4) + h2: the block's exact product in units 2^(er + ec - 7 (S + 1))
-              const int col = col0 + q0 + q;
-              const int ec = eb[(int64_t)kb * g.SB.rows_pad + col];
               const __int128 H = ((__int128)h1 << (7 * (S - 4))) + (__int128)h2;
-              const double val = i128_to_double(H, er + ec - 7 * (S + 1));
-              double* cp = Cb + row + (int64_t)col * g.ldc;
-              if (!need_c)
-                *cp = g.alpha * val;
-              else if (first)
-                *cp = fma(g.alpha, val, g.beta * cold[q]);
-              else
-                *cp = fma(g.alpha, val, cold[q]);
+              const double val = i128_to_double(H, er + ec[q] - 7 * (S + 1));
+              double out;
+              switch (upd) {
+                case 0: out = val; break;
+                case 1: out = g.alpha * val; break;
+                case 2: out = cold[q] - val; break;
+                case 3: out = cold[q] + val; break;
+                case 4: out = fma(g.alpha, val, cold[q]); break;
+                default: out = fma(g.alpha, val, g.beta * cold[q]); break;
+              }
+              Cb[row + (int64_t)col * g.ldc] = out;
             }
           }
         }
@@ -513,7 +554,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
 
 template <int S>
 void launch_oz7(const Oz7Args& a, long long ntiles, int batch, cudaStream_t st) {
-  const size_t smem = (size_t)NA * A_BYTES + 2 * S * B_BYTES + 1024;
+  const size_t smem = (size_t)ring_depth<S>() * A_BYTES + 2 * S * B_BYTES + 1024;
   static bool attr = false;
   if (!attr) {
     LKG_CUDA(cudaFuncSetAttribute(k_oz7_gemm<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -112,5 +112,7 @@ def test_retry_semantics_duplicated_point(gpu_lib):
     k = gpu_lib.Kriging("gauss")
     k.fit(y, x, "constant", False, "none", "LL", {"theta": th.reshape(1, -1)})
     ll, g, _ = k.logLikelihoodFun(th, True)
-    assert rel_err(ll, ll_o) < 1e-7  # cond(R) ~ 1e11 after the increment
-    assert rel_err(g, g_o) < 1e-5
+    # cond(R) ~ 1e11 after the increment: agreement is limited to ~1e11 eps; a branch without the increment would
+    # move LL by ~2 % (log det of the near-null direction), far outside this tolerance
+    assert rel_err(ll, ll_o) < 1e-5
+    assert rel_err(g, g_o) < 1e-4
