@@ -54,8 +54,11 @@ constexpr int NTHREADS = 576;                  // 18 warps
 __device__ int g_oz7_error;
 __device__ int g_oz7_where[8];  // first expired wait: role, tile, k block, sub-chunk, digit, and the role's counters
 
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TN >> 3) << 17) |
-                            ((uint32_t)(TM >> 4) << 24);
+// instruction descriptor of tcgen05.mma kind::f16: D FP32, A and B bf16, both K-major, M = 128, N = 64 k (the B
+// digits j .. j + k - 1 side by side, up to N = 256)
+__host__ __device__ constexpr uint32_t idesc_n(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
+}
 
 __device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -122,11 +125,11 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t
       : "memory");
 }
 
-__device__ __forceinline__ void mma_issue(uint32_t d, uint64_t a, uint64_t b, uint32_t accumulate) {
+__device__ __forceinline__ void mma_issue(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
   asm volatile(
       "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate));
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
 }
 
 __device__ __forceinline__ void mma_commit(uint32_t mbar) {
@@ -419,13 +422,17 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
               }
               asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
               const uint64_t adesc0 = sdesc(sA + st * A_BYTES);
+              // A digit i meets B digits 1 .. S + 1 - i: those are adjacent 64-row blocks of one K-major operand and
+              // their diagonals i + j adjacent 64-column blocks of TMEM, so up to 4 of them form one N = 256 MMA
 #pragma unroll
-              for (int j = 1; j <= S + 1 - i; ++j) {
-                const uint32_t d = tmem + (uint32_t)((i + j - 2) * TN);
-                const uint64_t bdesc = bdesc0 + (uint64_t)((j - 1) * (B_BYTES >> 4));
+              for (int j0 = 1; j0 <= S + 1 - i; j0 += 4) {
+                const int k = (S + 1 - i - j0 + 1) < 4 ? (S + 1 - i - j0 + 1) : 4;
+                const uint32_t d = tmem + (uint32_t)((i + j0 - 2) * TN);
+                const uint64_t bdesc = bdesc0 + (uint64_t)((j0 - 1) * (B_BYTES >> 4));
+                const uint32_t idesc = idesc_n(TN * k);
 #pragma unroll
                 for (int kk = 0; kk < 4; ++kk)
-                  mma_issue(d, adesc0 + (uint64_t)(2 * kk), bdesc + (uint64_t)(2 * kk),
+                  mma_issue(d, adesc0 + (uint64_t)(2 * kk), bdesc + (uint64_t)(2 * kk), idesc,
                             (!first_sub || i > 1 || kk > 0) ? 1u : 0u);
               }
               mma_commit(bar(bars.a_empty[st]));
