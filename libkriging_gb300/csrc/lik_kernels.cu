@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(256) k_adjoint(int n, int d, const double* __r
   lower_tile_of(blockIdx.x, I, J);
   const int64_t b = blockIdx.z;
   constexpr int NA = 2 * DM + 4;
-  __shared__ double xi[DM][T], xj[DM][T], th[DM], vi[T], vj[T];
+  __shared__ double xi[DM][T], xj[DM][T], th[DM], cks[DM], vi[T], vj[T];
   __shared__ double red[NA][8];
   const int r0 = I * T, c0 = J * T, t = threadIdx.x;
   const double* Xb = X + b * xb;
@@ -146,7 +146,10 @@ __global__ void __launch_bounds__(256) k_adjoint(int n, int d, const double* __r
     vi[t] = (r0 + t < n) ? xv[b * xvb + r0 + t] : 0.0;
     vj[t] = (c0 + t < n) ? xv[b * xvb + c0 + t] : 0.0;
   }
-  if (t < DM) th[t] = (t < d) ? theta[b * d + t] : 1.0;
+  if (t < DM) {
+    th[t] = (t < d) ? theta[b * d + t] : 1.0;
+    cks[t] = cov_scale<K>() / th[t];
+  }
   __syncthreads();
   const double f = factor[b];
   double t1[DM], t2[DM];
@@ -156,14 +159,15 @@ __global__ void __launch_bounds__(256) k_adjoint(int n, int d, const double* __r
   const int ri = t & 63, i = r0 + ri;
   const double* Rb = Rinv + b * rstride;
   if (i < n) {
-    // the gradient sums use the division- and log1p-free forms of the kernel and of dlnC/dtheta (common.cuh)
-    double xr[DM], inv[DM], ck[DM];
-#pragma unroll
-    for (int k = 0; k < DM; ++k) {
-      xr[k] = xi[k][ri];
-      inv[k] = 1.0 / th[k];
-      ck[k] = cov_scale<K>() * inv[k];
-    }
+    // Division-free gradient sums.  With t_m = s |dx_m| / theta_m (s = 1, sqrt 3, sqrt 5), p_m the Matern polynomial
+    // factor and E = factor exp(-sum_m t_m):
+    //   gauss      r dlnC/dtheta_k = r v_k^2           / theta_k,  v_k = dx_k / theta_k
+    //   exp        r dlnC/dtheta_k = r t_k             / theta_k
+    //   matern3_2  r dlnC/dtheta_k = E t_k^2           prod_{m != k} p_m / theta_k
+    //   matern5_2  r dlnC/dtheta_k = E t_k^2 (1 + t_k) prod_{m != k} p_m / (3 theta_k)
+    // The Matern products over m != k come from prefix products and a running suffix product, so no term needs a
+    // division; the 1 / theta_k (and 1/3) factor is applied once per accumulator after the pair loop.  The row's
+    // coordinates and the scales stay in shared memory (the loop is bound by the FP64 pipe, not by its loads).
     const double x_i = vi[ri];
     for (int s = 0; s < 16; ++s) {
       const int cj = (t >> 6) + 4 * s, j = c0 + cj;
@@ -174,26 +178,90 @@ __global__ void __launch_bounds__(256) k_adjoint(int n, int d, const double* __r
         d2 += rinv;
         continue;
       }
-      double dxk[DM];
-      double sum = 0.0, prod = 1.0;
-#pragma unroll
-      for (int k = 0; k < DM; ++k) {
-        dxk[k] = xj[k][cj] - xr[k];
-        if (k < d) cov_fast_term<K>(dxk[k], ck[k], sum, prod);
-      }
-      const double c = cov_fast_finish<K>(sum, prod);
-      const double rij = c * f;
       const double wx = x_i * vj[cj];
-      u1 += wx * c;
-      u2 += rinv * c;
+      double tk[DM], sum = 0.0;
 #pragma unroll
       for (int k = 0; k < DM; ++k) {
+        tk[k] = 0.0;
         if (k < d) {
-          const double g = rij * dlncov_fast<K>(dxk[k], inv[k], ck[k]);
-          t1[k] += wx * g;
-          t2[k] += rinv * g;
+          const double dx = xj[k][cj] - xi[k][ri];
+          if constexpr (K == KGAUSS) {
+            tk[k] = dx * cks[k];
+            sum = fma(tk[k], tk[k], sum);
+          } else {
+            tk[k] = fabs(dx) * cks[k];
+            sum += tk[k];
+          }
         }
       }
+      if constexpr (K == KGAUSS || K == KEXP) {
+        const double c = exp(K == KGAUSS ? -0.5 * sum : -sum);
+        const double rij = c * f;
+        u1 = fma(wx, c, u1);
+        u2 = fma(rinv, c, u2);
+#pragma unroll
+        for (int k = 0; k < DM; ++k) {
+          if (k < d) {
+            const double g = rij * (K == KGAUSS ? tk[k] * tk[k] : tk[k]);
+            t1[k] = fma(wx, g, t1[k]);
+            t2[k] = fma(rinv, g, t2[k]);
+          }
+        }
+      } else {
+        auto poly = [](double tt) { return (K == KMATERN32) ? 1.0 + tt : fma(tt, fma(tt, 1.0 / 3.0, 1.0), 1.0); };
+        if constexpr (DM <= 16) {
+          // prefix products pre[k] = prod_{m <= k} p_m and a running suffix product
+          double pk[DM], pre[DM];
+#pragma unroll
+          for (int k = 0; k < DM; ++k) {
+            pk[k] = poly(tk[k]);
+            pre[k] = (k == 0) ? pk[0] : ((k < d) ? pre[k - 1] * pk[k] : pre[k - 1]);
+          }
+          const double ex = exp(-sum);
+          const double c = pre[DM - 1] * ex;
+          u1 = fma(wx, c, u1);
+          u2 = fma(rinv, c, u2);
+          double suf = ex * f;  // E prod_{m > k} p_m
+#pragma unroll
+          for (int k = DM - 1; k >= 0; --k) {
+            if (k < d) {
+              const double t2k = tk[k] * tk[k];
+              const double q = (K == KMATERN32) ? t2k : fma(t2k, tk[k], t2k);
+              const double g = (k > 0) ? q * (pre[k - 1] * suf) : q * suf;
+              t1[k] = fma(wx, g, t1[k]);
+              t2[k] = fma(rinv, g, t2[k]);
+              suf *= pk[k];
+            }
+          }
+        } else {
+          // d > 16: the prefix array would not fit in registers; divide by p_k instead
+          double prod = 1.0;
+#pragma unroll
+          for (int k = 0; k < DM; ++k)
+            if (k < d) prod *= poly(tk[k]);
+          const double ex = exp(-sum);
+          const double c = prod * ex;
+          const double rij = c * f;
+          u1 = fma(wx, c, u1);
+          u2 = fma(rinv, c, u2);
+#pragma unroll
+          for (int k = 0; k < DM; ++k) {
+            if (k < d) {
+              const double t2k = tk[k] * tk[k];
+              const double q = (K == KMATERN32) ? t2k : fma(t2k, tk[k], t2k);
+              const double g = rij * q / poly(tk[k]);
+              t1[k] = fma(wx, g, t1[k]);
+              t2[k] = fma(rinv, g, t2[k]);
+            }
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < DM; ++k) {
+      const double sc = (K == KMATERN52 ? 1.0 / 3.0 : 1.0) / th[k];
+      t1[k] *= sc;
+      t2[k] *= sc;
     }
   }
   // deterministic block reduction of the NA accumulators
