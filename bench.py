@@ -5,7 +5,7 @@ y = sum_j sin(2 pi x_j) + 0.1 N(0,1), matern5_2 kernel, NuggetKriging with alpha
 (nugget = 1e-6 sigma2), theta ~ U[0.2, 1.5]^8, all drawn from numpy's PCG64 with seed 123.  One step = one
 logLikelihoodFun(gamma = [theta, alpha], return_grad = true) -- covariance build, blocked Cholesky, solves, GLS,
 R^-1 and the adjoint gradient.  The headline line is the mixed-precision path (O(n^3) products as error-free bf16
-digit products on the tensor cores, 7 digits for the Cholesky, 6 for the inverse); the same line carries the FP64
+digit products on the tensor cores, 8 digits for the Cholesky, 5 for the inverse); the same line carries the FP64
 path's figures ("fp64"), the speed-up and the relative LL / gradient difference between the two.
 
   value  device throughput: evaluations / s from the CUDA-event stage timings of each step (design resident)
@@ -97,6 +97,14 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def _digits_note(lib, slices):
+    """Operand precision of the mixed path for `slices` (the engine runs the inverse two slices lower)."""
+    inv = max(4, slices - 2)
+    if lib.lkg_get_tensor_path() == 3:  # 7-bit digits: slices + 1 (6..8) for the Cholesky, slices (5..8) inverse
+        return "Cholesky %d 7-bit digits, inverse %d" % (min(8, max(6, slices + 1)), min(8, max(5, inv)))
+    return "Cholesky %d 8-bit slices, inverse %d" % (slices, inv)
+
+
 def kernel_stats(lib):
     need = lib.lkg_stats_report(None, 0)
     buf = ctypes.create_string_buffer(max(need, 1))
@@ -181,10 +189,11 @@ def run_reference(args):
 def _timed_steps(k, lib, gamma, steps, local, label):
     """K LL+grad steps; returns (mean device ms per step from the CUDA-event stage timings, last (ll, grad),
     per-kernel stats, clock record).  Each step is an NVTX range named `label` (a profiler can select one path's
-    launches with it)."""
+    launches with it).  The timed steps run without per-launch events (which cost host time on every launch and
+    would hold back the short launches of the solves); K further steps with per-launch events give the per-kernel
+    statistics."""
     import torch
-    lib.lkg_stats_reset()
-    lib.lkg_stats_enable(1)
+    lib.lkg_stats_enable(0)
     clocks = ClockSampler(local)
     clocks.start()
     dev_ms = []
@@ -195,8 +204,13 @@ def _timed_steps(k, lib, gamma, steps, local, label):
         torch.cuda.nvtx.range_pop()
         dev_ms.append(sum(k.last_bench.values()))
     clk = clocks.stop()
+    stage = dict(k.last_bench)
+    lib.lkg_stats_reset()
+    lib.lkg_stats_enable(1)
+    for _ in range(steps):
+        k.logLikelihoodFun(gamma, True, False, bench=True)
     lib.lkg_stats_enable(0)
-    return float(np.mean(dev_ms)), (ll, np.asarray(g)), kernel_stats(lib), clk, dict(k.last_bench)
+    return float(np.mean(dev_ms)), (ll, np.asarray(g)), kernel_stats(lib), clk, stage
 
 
 def _e2e(lk, lib, k, gamma, steps, barrier):
@@ -299,8 +313,7 @@ def run_gpu(args):
                 data="synthetic (seeded PCG64, seed 123)",
                 config=dict(workload="dense LL+grad, n=%d, d=8, matern5_2, nugget 1e-6" % args.n,
                             precision="mixed: O(n^3) products on bf16 tensor cores by error-free digit splitting "
-                                      "(Cholesky %d digits, inverse %d), FP64 panels and reductions"
-                                      % (used, max(4, used - 1)),
+                                      "(%s), FP64 panels and reductions" % _digits_note(lib, used),
                             digit_products="tcgen05" if lib.lkg_get_tensor_path() else "mma.sync",
                             parallelism="replicas" if world > 1 else "single GPU",
                             l2="inputs larger than L2 (R, L^-1, R^-1: 3 x %.2f GB)" % (8.0 * args.n * args.n / 1e9)),

@@ -206,7 +206,7 @@ int lkg_ozaki_gemm_check(int M, int N, int K, const double* A, const double* B, 
  * value. */
 int lkg_set_tensor_path(int tc);
 int lkg_get_tensor_path(void);
-/* No counterpart in the reference: one product of the 7-bit digit kernel on host data, S digits (6..8):
+/* No counterpart in the reference: one product of the 7-bit digit kernel on host data, S digits (5..8):
  * mode 0: C (M x N) = A B^T (A M x K, B N x K); mode 1: C = A A^T lower (M x M); mode 2: C = W^T W lower with
  * W = A (M x M, lower).  Returns 0, -1 (error text in lkg_get_last_error) or -2 when a wait of the kernel expired
  * (where_out, 8 ints, receives where). */

@@ -106,16 +106,36 @@ constexpr int DPAD = NB + 1;
 
 constexpr int PB = 16;  // panel width inside a diagonal block
 
-// Inverse of the 16 x 16 lower block of s at (jb, jb) into the same block of w: lane c < 16 substitutes column c,
-// with the reciprocals of the diagonal (one division per row).
+// Inverse of the 16 x 16 lower block of s at (jb, jb) into the same block of w, one warp, row by row: row i is scaled
+// by 1 / L_ii, then subtracted from the rows below it, w(r, c) -= L(r, i) w(i, c) for c <= i < r, with the (r, c)
+// pairs spread over the lanes.  Each entry accumulates its terms in ascending i from the identity and is scaled
+// last: the same operations, in the same order, as forward substitution column by column.
 __device__ __forceinline__ void diag16_inverse(const double* s, double* w, int jb, int lane) {
-  if (lane >= PB) return;
-  const int c = lane;
-  for (int i = c; i < PB; ++i) {
-    double sum = (i == c) ? 1.0 : 0.0;
-    for (int k = c; k < i; ++k) sum = fma(-s[(jb + i) * DPAD + jb + k], w[(jb + k) * DPAD + jb + c], sum);
-    w[(jb + i) * DPAD + jb + c] = sum * (1.0 / s[(jb + i) * DPAD + jb + i]);
+  const double rdl = (lane < PB) ? __drcp_rn(s[(jb + lane) * DPAD + jb + lane]) : 0.0;
+  for (int e = lane; e < PB * PB; e += 32) {
+    const int r = e / PB, c = e % PB;
+    if (c <= r) w[(jb + r) * DPAD + jb + c] = (r == c) ? 1.0 : 0.0;
   }
+  __syncwarp();
+  for (int i = 0; i < PB; ++i) {
+    const double rd = __shfl_sync(0xffffffffu, rdl, i);
+    if (lane <= i) w[(jb + i) * DPAD + jb + lane] *= rd;
+    __syncwarp();
+    const int ncol = i + 1, nel = (PB - 1 - i) * ncol;
+    for (int e = lane; e < nel; e += 32) {
+      const int r = jb + i + 1 + e / ncol, c = jb + e % ncol;
+      w[r * DPAD + c] = fma(-s[r * DPAD + jb + i], w[(jb + i) * DPAD + c], w[r * DPAD + c]);
+    }
+    __syncwarp();
+  }
+}
+
+// (row, column) of entry e of a lower triangle enumerated row by row: e = r (r + 1) / 2 + c, c <= r
+__device__ __forceinline__ void tri_index(int e, int& r, int& c) {
+  r = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
+  if ((r + 1) * (r + 2) / 2 <= e) ++r;
+  if (r * (r + 1) / 2 > e) --r;
+  c = e - r * (r + 1) / 2;
 }
 
 // The off-diagonal 16 x 16 blocks of the inverse from the diagonal ones, by block diagonals:
@@ -159,16 +179,19 @@ __global__ void __launch_bounds__(NT) k_potrf_diag(double* A, int64_t lda, int64
   double* Ab = A + b * mstride + k0 + (int64_t)k0 * lda;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   if (t == 0) failed = 0;
-  for (int idx = t; idx < NB * NB; idx += NT) {
-    const int i = idx & 63, j = idx >> 6;
-    double v = 0.0;
-    if (i < nb && j < nb) {
-      if (i >= j) v = Ab[i + (int64_t)j * lda];
-    } else if (i == j) {
-      v = 1.0;
+  {  // all 16 loads of a thread in flight before the shared-memory stores
+    double v[NB * NB / NT];
+#pragma unroll
+    for (int u = 0; u < NB * NB / NT; ++u) {
+      const int idx = t + u * NT, i = idx & 63, j = idx >> 6;
+      v[u] = (i < nb && j < nb) ? ((i >= j) ? Ab[i + (int64_t)j * lda] : 0.0) : (i == j ? 1.0 : 0.0);
     }
-    s[i * DPAD + j] = v;
-    w[i * DPAD + j] = 0.0;
+#pragma unroll
+    for (int u = 0; u < NB * NB / NT; ++u) {
+      const int idx = t + u * NT, i = idx & 63, j = idx >> 6;
+      s[i * DPAD + j] = v[u];
+      w[i * DPAD + j] = 0.0;
+    }
   }
   __syncthreads();
   for (int jb = 0; jb < NB; jb += PB) {
@@ -184,8 +207,8 @@ __global__ void __launch_bounds__(NT) k_potrf_diag(double* A, int64_t lda, int64
       }
       __syncthreads();
     }
-    // (2) the 16 x 16 diagonal block: right-looking Cholesky, lane = row (column scaling by the reciprocal of the
-    // pivot, as LAPACK's dpotf2 does), then its inverse, lane = column
+    // (2) the 16 x 16 diagonal block: right-looking Cholesky (column scaling by the reciprocal of the pivot, as
+    // LAPACK's dpotf2 does), then its inverse
     if (warp == 0) {
       const int r = jb + lane;
       bool bad = false;
@@ -200,14 +223,18 @@ __global__ void __launch_bounds__(NT) k_potrf_diag(double* A, int64_t lda, int64
           }
           break;
         }
-        const double d = sqrt(piv), rd = 1.0 / d;
+        const double d = sqrt(piv), rd = __drcp_rn(d);
         __syncwarp();
         if (lane == 0) s[cj * DPAD + cj] = d;
         if (lane > j && lane < PB) s[r * DPAD + cj] *= rd;
         __syncwarp();
-        if (lane > j && lane < PB) {
-          const double lrj = s[r * DPAD + cj];
-          for (int c = j + 1; c <= lane; ++c) s[r * DPAD + jb + c] = fma(-lrj, s[(jb + c) * DPAD + cj], s[r * DPAD + jb + c]);
+        // trailing update s(r, c) -= L(r, j) L(c, j), j < c <= r < 16, the (r, c) pairs spread over the lanes
+        const int m = PB - 1 - j;
+        for (int e = lane; e < m * (m + 1) / 2; e += 32) {
+          int rr, cc;
+          tri_index(e, rr, cc);
+          const int ra = jb + j + 1 + rr, ca = jb + j + 1 + cc;
+          s[ra * DPAD + ca] = fma(-s[ra * DPAD + cj], s[ca * DPAD + cj], s[ra * DPAD + ca]);
         }
         __syncwarp();
       }
@@ -270,95 +297,195 @@ __global__ void __launch_bounds__(NT) k_wtw(const double* W, int64_t ldw, int64_
   tile_store(n - r0, n - c0, 1.0, 0.0, C + b * cstride + r0 + (int64_t)c0 * ldc, ldc, 0, 0, I == J, acc);
 }
 
-// ---- small-RHS helpers ----
-// B_k (nb x r, ldb) <- D (nb x nb, lower, NB-strided) * B_k   (trans: D^T * B_k)
-__global__ void k_small_apply(const double* Dinv, int64_t dinv_bstride, int blk, double* B, int64_t ldb,
-                              int64_t bstride, int k0, int nb, int r, bool trans) {
-  const int64_t b = blockIdx.z;
-  const double* D = Dinv + b * dinv_bstride + (int64_t)blk * NB * NB;
-  double* Bk = B + b * bstride + k0;
-  extern __shared__ double xs[];  // nb * r
-  for (int idx = threadIdx.x; idx < nb * r; idx += blockDim.x) {
-    const int i = idx % nb, c = idx / nb;
-    xs[idx] = Bk[i + (int64_t)c * ldb];
+// ---- small-RHS solves: one launch per diagonal block ----
+// Step k of the blocked substitution with X_k = Dinv_k B_k (TRANS: Dinv_k^T B_k).  The update CTAs (blockIdx.x < nupd)
+// each form X_k in shared memory from the untouched B_k and apply it to their own rows of B:
+//   forward   B(k0+nb+i, :) -= L(k0+nb+i, k0:k0+nb) X_k     64 rows per CTA
+//   TRANS     B(j, :)       -= L(k0:k0+nb, j)^T X_k          64 columns j < k0 per CTA
+// The last CTA (blockIdx.x == nupd, when kw >= 0) overwrites block kw -- the block of the previous step, which no
+// other CTA of this step reads or writes -- with X_kw = Dinv_kw B_kw.  A solve is nblk + 1 such launches.
+constexpr int TS_THREADS = 128;
+constexpr int TS_ROWS = 64;
+constexpr int TS_LD = NB + 1;  // padded row of the staged L tile (TRANS)
+
+// Dinv_k staged column-major with a padded leading dimension (conflict-free for both access orders)
+// (loads batched in registers ahead of the shared-memory stores, so that a thread keeps 16 loads in flight)
+__device__ __forceinline__ void ts_stage_dinv(const double* __restrict__ D, double* ds) {
+#pragma unroll
+  for (int h = 0; h < NB * NB / TS_THREADS; h += 16) {
+    double v[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) v[u] = D[threadIdx.x + (h + u) * TS_THREADS];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      const int idx = threadIdx.x + (h + u) * TS_THREADS;
+      ds[(idx / NB) * TS_LD + idx % NB] = v[u];
+    }
   }
-  __syncthreads();
+}
+
+// xs = Dinv_k bs (trans: Dinv_k^T bs) from the staged block
+__device__ __forceinline__ void ts_block_apply(const double* ds, const double* bs, double* xs, int nb, int r,
+                                               bool trans) {
   for (int idx = threadIdx.x; idx < nb * r; idx += blockDim.x) {
     const int i = idx % nb, c = idx / nb;
-    double s = 0.0;
+    double sum = 0.0;
     if (!trans) {
-      for (int k = 0; k <= i; ++k) s = fma(D[i + k * NB], xs[k + c * nb], s);
+      for (int kk = 0; kk <= i; ++kk) sum = fma(ds[kk * TS_LD + i], bs[kk + c * nb], sum);
     } else {
-      for (int k = i; k < nb; ++k) s = fma(D[k + i * NB], xs[k + c * nb], s);
+      for (int kk = i; kk < nb; ++kk) sum = fma(ds[i * TS_LD + kk], bs[kk + c * nb], sum);
     }
-    Bk[i + (int64_t)c * ldb] = s;
+    xs[idx] = sum;
   }
 }
 
-// B(k0+nb+i, c) -= sum_kk L(k0+nb+i, k0+kk) X(kk, c)   thread per row
-__global__ void k_panel_update(const double* L, int64_t lda, int64_t mstride, double* B, int64_t ldb,
-                               int64_t bstride, int k0, int nb, int M, int r) {
+// RC: right-hand sides per pass of the update (1, 2, 4 or 8), so that no FP64 issue slot goes to a masked column
+template <bool TRANS, int RC>
+__global__ void __launch_bounds__(TS_THREADS) k_trsv_step(const double* L, int64_t lda, int64_t mstride,
+                                                          const double* Dinv, int64_t dstride, double* B, int64_t ldb,
+                                                          int64_t bstride, int n, int k, int kw, int r, int nupd) {
+  extern __shared__ double tsm[];
+  const int rs = max(r, 8);                     // B_k's slot also holds the [TS_ROWS][8] partial sums
+  double* bs = tsm;                             // nb x r: B_k (or B_kw)
+  double* xs = tsm + NB * rs;                   // nb x r: X_k
+  double* ds = tsm + 2 * NB * rs;               // [NB][TS_LD]: Dinv_k, ds[c * TS_LD + r] = Dinv_k(r, c)
+  double* ls = tsm + 2 * NB * rs + NB * TS_LD;  // TRANS: [TS_ROWS][TS_LD], ls[j * TS_LD + kk] = L(k0 + kk, j0 + j)
   const int64_t b = blockIdx.z;
-  extern __shared__ double xs[];  // nb * r
-  const double* Lb = L + b * mstride;
+  const int t = threadIdx.x;
   double* Bb = B + b * bstride;
-  for (int idx = threadIdx.x; idx < nb * r; idx += blockDim.x) {
-    const int i = idx % nb, c = idx / nb;
-    xs[idx] = Bb[k0 + i + (int64_t)c * ldb];
+  const double* Db = Dinv + b * dstride;
+  if ((int)blockIdx.x == nupd) {  // writer: X_kw over B_kw
+    const int w0 = kw * NB, nbw = min(NB, n - w0);
+    for (int idx = t; idx < nbw * r; idx += TS_THREADS) bs[idx] = Bb[w0 + idx % nbw + (int64_t)(idx / nbw) * ldb];
+    ts_stage_dinv(Db + (int64_t)kw * NB * NB, ds);
+    __syncthreads();
+    ts_block_apply(ds, bs, xs, nbw, r, TRANS);
+    __syncthreads();
+    for (int idx = t; idx < nbw * r; idx += TS_THREADS) Bb[w0 + idx % nbw + (int64_t)(idx / nbw) * ldb] = xs[idx];
+    return;
+  }
+  const int k0 = k * NB, nb = min(NB, n - k0);
+  for (int idx = t; idx < nb * r; idx += TS_THREADS) bs[idx] = Bb[k0 + idx % nb + (int64_t)(idx / nb) * ldb];
+  ts_stage_dinv(Db + (int64_t)k * NB * NB, ds);
+  const double* Lb = L + b * mstride;
+  const int half = t >> 6, q = t & 63;  // two threads per row (column): kk halves
+  const int kh0 = half * (NB / 2);
+  if constexpr (TRANS) {
+    // stage L(k0:k0+nb, j0:j0+64) with lanes along kk (contiguous in memory)
+    const int j0 = blockIdx.x * TS_ROWS;
+#pragma unroll
+    for (int h = 0; h < TS_ROWS * NB / TS_THREADS; h += 16) {
+      double v[16];
+#pragma unroll
+      for (int u = 0; u < 16; ++u) {
+        const int idx = t + (h + u) * TS_THREADS, kk = idx % NB, j = idx / NB;
+        v[u] = (kk < nb && j0 + j < k0) ? Lb[(k0 + kk) + (int64_t)(j0 + j) * lda] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < 16; ++u) {
+        const int idx = t + (h + u) * TS_THREADS;
+        ls[(idx / NB) * TS_LD + idx % NB] = v[u];
+      }
+    }
   }
   __syncthreads();
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= M) return;
-  const int row = k0 + nb + i;
-  double acc[8];
-  for (int c0 = 0; c0 < r; c0 += 8) {
-    const int rc = min(8, r - c0);
-#pragma unroll
-    for (int c = 0; c < 8; ++c) acc[c] = 0.0;
-    for (int kk = 0; kk < nb; ++kk) {
-      const double l = Lb[row + (int64_t)(k0 + kk) * lda];
-#pragma unroll
-      for (int c = 0; c < 8; ++c)
-        if (c < rc) acc[c] = fma(l, xs[kk + (c0 + c) * nb], acc[c]);
-    }
-#pragma unroll
-    for (int c = 0; c < 8; ++c)
-      if (c < rc) Bb[row + (int64_t)(c0 + c) * ldb] -= acc[c];
-  }
-}
-
-// B(j, c) -= sum_kk L(k0+kk, j) X(kk, c)  for j < k0; one warp per column j
-__global__ void k_panel_update_t(const double* L, int64_t lda, int64_t mstride, double* B, int64_t ldb,
-                                 int64_t bstride, int k0, int nb, int r) {
-  const int64_t b = blockIdx.z;
-  extern __shared__ double xs[];  // nb * r
-  const double* Lb = L + b * mstride;
-  double* Bb = B + b * bstride;
-  for (int idx = threadIdx.x; idx < nb * r; idx += blockDim.x) {
-    const int i = idx % nb, c = idx / nb;
-    xs[idx] = Bb[k0 + i + (int64_t)c * ldb];
-  }
+  ts_block_apply(ds, bs, xs, nb, r, TRANS);
   __syncthreads();
-  const int lane = threadIdx.x & 31;
-  const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (j >= k0) return;
-  for (int c = 0; c < r; ++c) {
-    double s = 0.0;
-    for (int kk = lane; kk < nb; kk += 32) s = fma(Lb[k0 + kk + (int64_t)j * lda], xs[kk + c * nb], s);
+  double* red = bs;  // B_k is no longer needed: partial sums of the upper kk half, [TS_ROWS][8]
+  int row;
+  if constexpr (TRANS) row = blockIdx.x * TS_ROWS + q;  // column j of L = row j of B
+  else row = k0 + nb + blockIdx.x * TS_ROWS + q;
+  const bool active = TRANS ? (row < k0) : (row < n);
+  const double* Lrow = Lb + row + (int64_t)k0 * lda;
+  for (int c0 = 0; c0 < r; c0 += RC) {
+    const int rc = min(RC, r - c0);
+    double acc[RC];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) Bb[j + (int64_t)c * ldb] -= s;
+    for (int c = 0; c < RC; ++c) acc[c] = 0.0;
+    if (active) {
+#pragma unroll
+      for (int u0 = 0; u0 < NB / 2; u0 += 16) {
+        double lv[16];
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+          const int kk = kh0 + u0 + u;
+          if constexpr (TRANS) lv[u] = ls[q * TS_LD + kk];
+          else lv[u] = (kk < nb) ? Lrow[(int64_t)kk * lda] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+          const int kk = kh0 + u0 + u;
+          if (kk < nb) {
+#pragma unroll
+            for (int c = 0; c < RC; ++c)
+              if (c < rc) acc[c] = fma(lv[u], xs[kk + (c0 + c) * nb], acc[c]);
+          }
+        }
+      }
+    }
+    if (half == 1) {
+#pragma unroll
+      for (int c = 0; c < RC; ++c) red[q * RC + c] = acc[c];
+    }
+    __syncthreads();
+    if (half == 0 && active) {
+#pragma unroll
+      for (int c = 0; c < RC; ++c)
+        if (c < rc) Bb[row + (int64_t)(c0 + c) * ldb] -= acc[c] + red[q * RC + c];
+    }
+    __syncthreads();
   }
 }
 
-__global__ void k_copy_dinv_block(const double* Dinv, int64_t dinv_bstride, int blk, double* W, int64_t ldw,
-                                  int64_t wstride, int k0, int nb) {
+size_t trsv_smem(int r, bool trans) {
+  return sizeof(double) * ((size_t)2 * NB * std::max(r, 8) + (size_t)NB * TS_LD + (trans ? (size_t)TS_ROWS * TS_LD : 0));
+}
+
+template <bool TRANS, int RC>
+void trsv_launch_rc(const double* L, int64_t lda, int64_t mstride, const double* Dinv, int64_t dstride, double* B,
+                    int64_t ldb, int64_t bstride, int n, int k, int kw, int r, int nupd, int batch, cudaStream_t st) {
+  static bool attr_set = false;  // one flag per instantiation
+  if (!attr_set) {
+    LKG_CUDA(cudaFuncSetAttribute(k_trsv_step<TRANS, RC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)trsv_smem(16, TRANS)));
+    attr_set = true;
+  }
+  const int grid = nupd + (kw >= 0 ? 1 : 0);
+  const double rows = (double)nupd * TS_ROWS;
+  const char* name = TRANS ? "k_trsv_step_t" : "k_trsv_step";
+  LaunchTimer lt(name, st, 2.0 * rows * NB * r * batch, 8.0 * (rows * NB + 2.0 * rows * r) * batch);
+  k_trsv_step<TRANS, RC><<<dim3(grid, 1, batch), TS_THREADS, trsv_smem(r, TRANS), st>>>(
+      L, lda, mstride, Dinv, dstride, B, ldb, bstride, n, k, kw, r, nupd);
+  LKG_LAUNCH(name);
+}
+
+template <bool TRANS>
+void trsv_launch(const double* L, int64_t lda, int64_t mstride, const double* Dinv, int64_t dstride, double* B,
+                 int64_t ldb, int64_t bstride, int n, int k, int kw, int r, int nupd, int batch, cudaStream_t st) {
+  if (nupd + (kw >= 0 ? 1 : 0) == 0) return;
+  if (r == 1)
+    trsv_launch_rc<TRANS, 1>(L, lda, mstride, Dinv, dstride, B, ldb, bstride, n, k, kw, r, nupd, batch, st);
+  else if (r == 2)
+    trsv_launch_rc<TRANS, 2>(L, lda, mstride, Dinv, dstride, B, ldb, bstride, n, k, kw, r, nupd, batch, st);
+  else if (r <= 4)
+    trsv_launch_rc<TRANS, 4>(L, lda, mstride, Dinv, dstride, B, ldb, bstride, n, k, kw, r, nupd, batch, st);
+  else
+    trsv_launch_rc<TRANS, 8>(L, lda, mstride, Dinv, dstride, B, ldb, bstride, n, k, kw, r, nupd, batch, st);
+}
+
+__global__ void __launch_bounds__(256) k_copy_dinv_block(const double* __restrict__ Dinv, int64_t dinv_bstride,
+                                                         int blk, double* W, int64_t ldw, int64_t wstride, int k0,
+                                                         int nb) {
   const int64_t b = blockIdx.z;
   const double* D = Dinv + b * dinv_bstride + (int64_t)blk * NB * NB;
   double* Wb = W + b * wstride + k0 + (int64_t)k0 * ldw;
-  for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
-    const int i = idx % nb, j = idx / nb;
-    Wb[i + (int64_t)j * ldw] = D[i + j * NB];
+  double v[NB * NB / 256];
+#pragma unroll
+  for (int u = 0; u < NB * NB / 256; ++u) v[u] = D[threadIdx.x + u * 256];
+#pragma unroll
+  for (int u = 0; u < NB * NB / 256; ++u) {
+    const int idx = threadIdx.x + u * 256, i = idx % NB, j = idx / NB;
+    if (i < nb && j < nb) Wb[i + (int64_t)j * ldw] = v[u];
   }
 }
 
@@ -374,16 +501,19 @@ __global__ void __launch_bounds__(NT) k_trtri_diag(const double* L, int64_t lda,
   const int blk = blockIdx.x, k0 = blk * NB, nb = min(NB, n - k0);
   const double* Lb = L + b * mstride + k0 + (int64_t)k0 * lda;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  for (int idx = t; idx < NB * NB; idx += NT) {
-    const int i = idx & 63, j = idx >> 6;
-    double v = 0.0;
-    if (i < nb && j < nb) {
-      if (i >= j) v = Lb[i + (int64_t)j * lda];
-    } else if (i == j) {
-      v = 1.0;
+  {  // all 16 loads of a thread in flight before the shared-memory stores
+    double v[NB * NB / NT];
+#pragma unroll
+    for (int u = 0; u < NB * NB / NT; ++u) {
+      const int idx = t + u * NT, i = idx & 63, j = idx >> 6;
+      v[u] = (i < nb && j < nb) ? ((i >= j) ? Lb[i + (int64_t)j * lda] : 0.0) : (i == j ? 1.0 : 0.0);
     }
-    s[i * DPAD + j] = v;
-    w[i * DPAD + j] = 0.0;
+#pragma unroll
+    for (int u = 0; u < NB * NB / NT; ++u) {
+      const int idx = t + u * NT, i = idx & 63, j = idx >> 6;
+      s[i * DPAD + j] = v[u];
+      w[i * DPAD + j] = 0.0;
+    }
   }
   __syncthreads();
   if (warp < NB / PB) diag16_inverse(s, w, warp * PB, lane);
@@ -555,11 +685,10 @@ void trsm_lower_left(const double* L, int64_t lda, int64_t mstride, int n, const
   const int64_t dstride = (int64_t)nblk * NB * NB;
   if (r > 16 && batch != 1 && mstride == 0)
     throw std::invalid_argument("trsm_lower_left: shared factor with many right-hand sides is not supported");
-  const size_t smem = sizeof(double) * NB * r;
-  for (int k = 0; k < nblk; ++k) {
-    const int k0 = k * NB, nb = std::min(NB, n - k0);
-    const int M = n - k0 - nb;
-    if (r > 16) {  // many right-hand sides: tile GEMMs (X_k = Dinv_k B_k in place per column tile, then update)
+  if (r > 16) {  // many right-hand sides: tile GEMMs (X_k = Dinv_k B_k in place per column tile, then update)
+    for (int k = 0; k < nblk; ++k) {
+      const int k0 = k * NB, nb = std::min(NB, n - k0);
+      const int M = n - k0 - nb;
       MatView d{Dinv + (int64_t)k * NB * NB, 1, NB, dstride};
       MatView bk{B + k0, 1, ldb, bstride};
       gemm_tiles(nb, r, nb, 1.0, d, bk, 0.0, B + k0, ldb, bstride, batch, false, st);
@@ -567,19 +696,15 @@ void trsm_lower_left(const double* L, int64_t lda, int64_t mstride, int n, const
         MatView a{L + (k0 + nb) + (int64_t)k0 * lda, 1, lda, mstride};
         gemm_tiles(M, r, nb, -1.0, a, bk, 1.0, B + k0 + nb, ldb, bstride, batch, false, st);
       }
-      continue;
     }
-    {
-      LaunchTimer lt("k_small_apply", st, (double)nb * nb * r * batch, 16.0 * nb * r * batch);
-      k_small_apply<<<dim3(1, 1, batch), 256, smem, st>>>(Dinv, dstride, k, B, ldb, bstride, k0, nb, r, false);
-    }
-    LKG_LAUNCH("k_small_apply");
-    if (M > 0) {
-      LaunchTimer lt("k_panel_update", st, 2.0 * M * nb * r * batch, 8.0 * ((double)M * nb + 2.0 * M * r) * batch);
-      k_panel_update<<<dim3(ceil_div(M, 128), 1, batch), 128, smem, st>>>(L, lda, mstride, B, ldb, bstride, k0, nb, M,
-                                                                          r);
-      LKG_LAUNCH("k_panel_update");
-    }
+    return;
+  }
+  // step k updates the rows below block k and writes X_{k-1}; the extra step writes the last block
+  for (int k = 0; k <= nblk; ++k) {
+    const int k0 = k * NB;
+    const int M = (k < nblk) ? n - k0 - std::min(NB, n - k0) : 0;
+    trsv_launch<false>(L, lda, mstride, Dinv, dstride, B, ldb, bstride, n, k, k - 1, r, ceil_div(M, TS_ROWS), batch,
+                       st);
   }
 }
 
@@ -589,10 +714,9 @@ void trsm_lower_left_t(const double* L, int64_t lda, int64_t mstride, int n, con
   const int64_t dstride = (int64_t)nblk * NB * NB;
   if (r > 16 && batch != 1 && mstride == 0)
     throw std::invalid_argument("trsm_lower_left_t: shared factor with many right-hand sides is not supported");
-  const size_t smem = sizeof(double) * NB * r;
-  for (int k = nblk - 1; k >= 0; --k) {
-    const int k0 = k * NB, nb = std::min(NB, n - k0);
-    if (r > 16) {  // many right-hand sides: X_k = Dinv_k^T B_k in place, then B_0:k0 -= L(k0:k0+nb, 0:k0)^T X_k
+  if (r > 16) {  // many right-hand sides: X_k = Dinv_k^T B_k in place, then B_0:k0 -= L(k0:k0+nb, 0:k0)^T X_k
+    for (int k = nblk - 1; k >= 0; --k) {
+      const int k0 = k * NB, nb = std::min(NB, n - k0);
       MatView dt{Dinv + (int64_t)k * NB * NB, NB, 1, dstride};  // (i, kk) = Dinv_k(kk, i)
       MatView bk{B + k0, 1, ldb, bstride};
       gemm_tiles(nb, r, nb, 1.0, dt, bk, 0.0, B + k0, ldb, bstride, batch, false, st);
@@ -600,19 +724,14 @@ void trsm_lower_left_t(const double* L, int64_t lda, int64_t mstride, int n, con
         MatView lt{L + k0, lda, 1, mstride};  // (i, kk) = L(k0 + kk, i)
         gemm_tiles(k0, r, nb, -1.0, lt, bk, 1.0, B, ldb, bstride, batch, false, st);
       }
-      continue;
     }
-    {
-      LaunchTimer lt("k_small_apply", st, (double)nb * nb * r * batch, 16.0 * nb * r * batch);
-      k_small_apply<<<dim3(1, 1, batch), 256, smem, st>>>(Dinv, dstride, k, B, ldb, bstride, k0, nb, r, true);
-    }
-    LKG_LAUNCH("k_small_apply");
-    if (k0 > 0) {
-      LaunchTimer lt("k_panel_update_t", st, 2.0 * k0 * nb * r * batch, 8.0 * ((double)k0 * nb + 2.0 * k0 * r) * batch);
-      k_panel_update_t<<<dim3(ceil_div(k0, 8), 1, batch), 256, smem, st>>>(L, lda, mstride, B, ldb, bstride, k0, nb,
-                                                                           r);
-      LKG_LAUNCH("k_panel_update_t");
-    }
+    return;
+  }
+  // step k (descending) updates the rows above block k and writes X_{k+1}; the extra step writes block 0
+  for (int k = nblk - 1; k >= -1; --k) {
+    const int nupd = (k >= 0) ? ceil_div(k * NB, TS_ROWS) : 0;
+    trsv_launch<true>(L, lda, mstride, Dinv, dstride, B, ldb, bstride, n, k, (k + 1 < nblk) ? k + 1 : -1, r, nupd,
+                      batch, st);
   }
 }
 

@@ -19,8 +19,12 @@ SplitBuf make_split(void* planes, int* exps, int S, int rows_cap, int K_cap) {
   return s;
 }
 
-// digits of the 7-bit split for a given count of 8-bit slices: the same operand precision, one digit more
+// digits of the 7-bit split of the factorisation for a given count of 8-bit slices: the same operand precision, one
+// digit more (6 .. 8)
 int oz7_digits(int slices) { return std::min(8, std::max(6, slices + 1)); }
+// digits of the triangular inverse and of W^T W, which feed only the gradient: as many 7-bit digits as the inverse
+// has 8-bit slices (5 .. 8)
+int oz7_inv_digits(int slices_inv) { return std::min(8, std::max(5, slices_inv)); }
 
 // Two-level blocked Cholesky: 256-wide panels factored in 64-wide steps (FP64 diagonal block; panel solve and the update
 // of the panel's remaining columns as 64-deep digit products), then one rank-256 trailing update per panel.  Every
@@ -69,7 +73,7 @@ void trtri_blocked_mixed7(const double* L, int64_t lda, int64_t mstride, int n, 
   const int64_t dstride = (int64_t)nblk * NB * NB;
   for (int b = 0; b < batch; ++b)
     LKG_CUDA(cudaMemset2DAsync(W + b * wstride, ldw * sizeof(double), 0, n * sizeof(double), n, st));
-  const int S = oz7_digits(ws.slices_inv);
+  const int S = oz7_inv_digits(ws.slices_inv);
   Split7 SL = oz7_buffer(ws.panel, ws.panel_exp, S, ws.n, OZ7_KB, OZ7_KB);
   Split7 SR = oz7_buffer(ws.rowblk, ws.rowblk_exp, S, ws.n, OZ7_KB, OZ7_KB);
   Split7 SA = oz7_buffer(ws.panel, ws.panel_exp, S, ws.n, NB, NB);
@@ -103,7 +107,7 @@ void trtri_blocked_mixed7(const double* L, int64_t lda, int64_t mstride, int n, 
 
 void wtw_lower_mixed7(const double* W, int64_t ldw, int64_t wstride, int n, double* C, int64_t ldc, int64_t cstride,
                       int batch, const MixedWorkspace& ws, cudaStream_t st) {
-  Split7 SW = oz7_buffer(ws.wfull, ws.wfull_exp, oz7_digits(ws.slices_inv), ws.n, ws.n, OZ7_KB);
+  Split7 SW = oz7_buffer(ws.wfull, ws.wfull_exp, oz7_inv_digits(ws.slices_inv), ws.n, ws.n, OZ7_KB);
   oz7_split(n, n, W, ldw, 1, wstride, batch, SW, st);  // rows of the split = columns of W, k = rows of W
   oz7_wtw(n, SW, C, ldc, cstride, batch, st);
 }

@@ -100,9 +100,9 @@ extern "C" int lkg_ozaki_gemm_check(int M, int N, int K, const double* A, const 
     LKG_CUDA(cudaMalloc(&dC, sizeof(double) * M * N));
     LKG_CUDA(cudaMemcpy(dA, A, sizeof(double) * M * K, cudaMemcpyHostToDevice));
     LKG_CUDA(cudaMemcpy(dB, B, sizeof(double) * N * K, cudaMemcpyHostToDevice));
-    if (lkg::ozaki_tensor_path() == 3) {  // 7-bit digits, one more than the slices (6..8), 256-wide k blocks
+    if (lkg::ozaki_tensor_path() == 3) {  // 7-bit digits, one more than the slices (5..8), 256-wide k blocks
       const int kb = lkg::OZ7_KB;
-      slices = std::min(8, std::max(6, slices + 1));
+      slices = std::min(8, std::max(5, slices + 1));
       LKG_CUDA(cudaMalloc(&pa, lkg::oz7_plane_elems(M, K, slices) * 2));
       LKG_CUDA(cudaMalloc(&pb, lkg::oz7_plane_elems(N, K, slices) * 2));
       LKG_CUDA(cudaMalloc(&ea, lkg::oz7_exp_elems(M, K, kb) * sizeof(int)));

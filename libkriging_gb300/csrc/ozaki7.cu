@@ -289,7 +289,7 @@ struct Bars {
 
 template <int S>
 __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long ntiles) {
-  static_assert(S >= 6 && S <= 8, "digit count");
+  static_assert(S >= 5 && S <= 8, "digit count");
   constexpr int NA = ring_depth<S>();
   static_assert(NA >= 2 && NA <= NA_MAX, "A ring depth");
   constexpr uint32_t B_BUF = S * B_BYTES;
@@ -580,10 +580,11 @@ void launch_oz7(const Oz7Args& a, long long ntiles, int batch, cudaStream_t st) 
 
 void dispatch(int S, const Oz7Args& a, long long ntiles, int batch, cudaStream_t st) {
   switch (S) {
+    case 5: launch_oz7<5>(a, ntiles, batch, st); break;
     case 6: launch_oz7<6>(a, ntiles, batch, st); break;
     case 7: launch_oz7<7>(a, ntiles, batch, st); break;
     case 8: launch_oz7<8>(a, ntiles, batch, st); break;
-    default: throw std::invalid_argument("ozaki7: number of digits must be 6, 7 or 8");
+    default: throw std::invalid_argument("ozaki7: number of digits must be 5 .. 8");
   }
 }
 
@@ -612,7 +613,7 @@ void oz7_split(int rows, int K, const double* p, int64_t s_r, int64_t s_k, int64
                cudaStream_t st) {
   if (rows <= 0 || K <= 0) return;
   if (out.sub_per_blk < 1 || out.sub_per_blk > OZ7_MAX_SPB) throw std::invalid_argument("oz7_split: bad k block");
-  if (out.S < 6 || out.S > 8) throw std::invalid_argument("oz7_split: digits must be 6, 7 or 8");
+  if (out.S < 5 || out.S > 8) throw std::invalid_argument("oz7_split: digits must be 5 .. 8");
   out.rows_pad = ceil_div(rows, TM) * TM;
   out.nsub = ceil_div(K, OZ7_SUB);
   out.nblk = ceil_div(out.nsub, out.sub_per_blk);
