@@ -8,8 +8,8 @@
 // of a block stays below S * 256 * 2^12 <= 2^23: every FP32 tensor-core accumulator is an exact integer.  Products
 // with i + j <= S + 1 are formed (S (S + 1) / 2 bf16 GEMMs per block), one accumulator per diagonal g, and the S
 // diagonals are folded into FP64 once per block: Horner in base 128 over g = 2..5 and g = 6..S+1 (int64), one
-// 128-bit integer, one correctly rounded conversion.  S = 8 gives 56-bit operands (FP64-level products); S = 7 is
-// used where 49 bits suffice (the triangular inverse and W^T W, which feed only the gradient).
+// 128-bit integer, one correctly rounded conversion.  S = 8 gives 56-bit operands (FP64-level products); S = 5
+// (35 bits) serves the triangular inverse and W^T W, which feed only the gradient.
 //
 // Data layout: the split writes each (digit, 64-wide k sub-chunk, 128-row tile) as the 16 KB shared-memory image of
 // a K-major tile with the 128-byte swizzle (16-byte chunk c of row r at chunk c ^ (r & 7)), so the kernel moves it
@@ -17,9 +17,10 @@
 //
 // k_oz7_gemm (one persistent CTA per SM, 18 warps):
 //   warp 0        one thread streams the digit images: per sub-chunk all S digits of B (64 rows, double-buffered),
-//                 then the S digits of A (128 rows) through a 4-stage ring; bulk copies complete on mbarriers
+//                 then the S digits of A (128 rows) through a 6-7-stage ring; bulk copies complete on mbarriers
 //   warp 1        TMEM allocation (512 columns = S diagonals x 64 columns); one thread issues tcgen05.mma
-//                 (M 128, N 64, K 16) digit-major and releases each A stage and B buffer with tcgen05.commit
+//                 (M 128, N 64 k, K 16): A digit i against up to 4 adjacent B digits at once, and releases each A
+//                 stage and B buffer with tcgen05.commit
 //   warps 2..17   epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 (rows) and 16 columns, 4 at a time:
 //                 Horner-folds the S diagonals, converts to FP64 and updates C, then releases TMEM to the next
 //                 block (18 warps leave 96 registers a thread: a sub-partition holds 5 warps of its 16K registers)
@@ -168,7 +169,15 @@ __device__ __forceinline__ double i128_to_double(__int128 H, int E) {
 }
 
 // ---------------------------------------------------------------------------------------------------------------
+// bf16 bit pattern of a small integer d (|d| <= 64): 1.5 2^23 + d is exact in FP32, so subtracting 1.5 2^23 gives d
+// as a float whose low 16 bits are zero (at most 7 significant bits), and its high half is the bf16 value
+__device__ __forceinline__ uint32_t bf16_bits_of_small(int d) {
+  const float f = __int_as_float(0x4B400000 + d) - 12582912.0f;
+  return (uint32_t)__float_as_int(f) >> 16;
+}
+
 // split: one warp per (row, k block); lane l holds the column pairs 2 l, 2 l + 1 of every 64-wide sub-chunk
+template <int S>
 __global__ void __launch_bounds__(256) k_oz7_split(int rows, int K, const double* __restrict__ p, int64_t s_r,
                                                    int64_t s_k, int64_t bstride, Split7 out) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -206,7 +215,6 @@ __global__ void __launch_bounds__(256) k_oz7_split(int rows, int K, const double
     const int E = bx ? bx - 1022 : (64 - __clzll((long long)(bm & 0xFFFFFFFFFFFFFull))) - 1074;
     e = E + 1;
   }
-  const int S = out.S;
   const int ntile = out.rows_pad / 128, t = r >> 7, rr = r & 127;
   __nv_bfloat16* base = out.planes + b * out.plane_bstride;
 #pragma unroll
@@ -235,19 +243,18 @@ __global__ void __launch_bounds__(256) k_oz7_split(int rows, int K, const double
     }
     const int kk = 2 * lane, c = kk >> 3, e8 = kk & 7;
     const int64_t off = (int64_t)rr * 64 + ((c ^ (rr & 7)) << 3) + e8;
-    for (int i = S - 1; i >= 0; --i) {  // least significant digit first; the top digit keeps the rest (|d| <= 64)
-      long long d0 = V[0], d1 = V[1];
-      if (i > 0) {
-        d0 = ((V[0] + 64) & 127) - 64;
-        d1 = ((V[1] + 64) & 127) - 64;
-        V[0] = (V[0] - d0) >> 7;
-        V[1] = (V[1] - d1) >> 7;
-      }
-      __nv_bfloat162 pr2;
-      pr2.x = __float2bfloat16_rn((float)d0);
-      pr2.y = __float2bfloat16_rn((float)d1);
-      __nv_bfloat16* img = base + (((int64_t)i * out.nsub + s) * ntile + t) * (TM * 64);
-      *reinterpret_cast<__nv_bfloat162*>(img + off) = pr2;
+    // balanced base-128 digits in closed form: with U = V + 64 (1 + 128 + ... + 128^(S-2)), digit k (least
+    // significant first) is ((U >> 7 k) & 127) - 64 for k < S - 1 and the top digit is U >> 7 (S - 1) (|d| <= 64)
+    constexpr long long C = 64ll * ((1ll << (7 * (S - 1))) - 1) / 127;
+    const long long U0 = V[0] + C, U1 = V[1] + C;
+    const int64_t plane = (int64_t)out.nsub * ntile * (TM * 64);  // elements between digit images
+    uint32_t* img = reinterpret_cast<uint32_t*>(base + ((int64_t)s * ntile + t) * (TM * 64) + off);
+#pragma unroll
+    for (int k = 0; k < S; ++k) {
+      const int i = S - 1 - k;  // digit index, 0 = most significant
+      const int d0 = (k < S - 1) ? (int)((U0 >> (7 * k)) & 127) - 64 : (int)(U0 >> (7 * k));
+      const int d1 = (k < S - 1) ? (int)((U1 >> (7 * k)) & 127) - 64 : (int)(U1 >> (7 * k));
+      img[(i * plane) >> 1] = bf16_bits_of_small(d0) | (bf16_bits_of_small(d1) << 16);
     }
   }
   if (lane == 0) out.exps[b * out.exp_bstride + (int64_t)kb * out.rows_pad + r] = e;
@@ -622,7 +629,12 @@ void oz7_split(int rows, int K, const double* p, int64_t s_r, int64_t s_k, int64
     throw std::logic_error("oz7_split: operand larger than its buffer");
   dim3 grid(out.rows_pad / 8, out.nblk, batch);
   LaunchTimer lt("k_oz7_split", st, 0.0, ((double)rows * K * (8.0 + 2.0 * out.S)) * batch);
-  k_oz7_split<<<grid, 256, 0, st>>>(rows, K, p, s_r, s_k, bstride, out);
+  switch (out.S) {
+    case 5: k_oz7_split<5><<<grid, 256, 0, st>>>(rows, K, p, s_r, s_k, bstride, out); break;
+    case 6: k_oz7_split<6><<<grid, 256, 0, st>>>(rows, K, p, s_r, s_k, bstride, out); break;
+    case 7: k_oz7_split<7><<<grid, 256, 0, st>>>(rows, K, p, s_r, s_k, bstride, out); break;
+    default: k_oz7_split<8><<<grid, 256, 0, st>>>(rows, K, p, s_r, s_k, bstride, out); break;
+  }
   LKG_LAUNCH("k_oz7_split");
 }
 
