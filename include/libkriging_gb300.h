@@ -89,6 +89,10 @@ int lkg_kriging_log_likelihood_fun_batch(void* ptr, const double* thetas, int k,
  * as "key<TAB>value<LF>" lines; keys are the reference's Bench keys (src/lib/KrigingImpl.cpp:96-124). */
 int lkg_kriging_log_likelihood_fun_bench(void* ptr, const double* theta, int theta_n, int return_grad, double* ll_out,
                                          double* grad_out, char* bench_out, int bench_cap);
+/* No counterpart in the reference: lkg_kriging_log_likelihood_fun_batch writing the batched pass's per-stage
+ * timings (ms, CUDA events on the model's stream, summed over the k candidates) like the entry point above. */
+int lkg_kriging_log_likelihood_fun_batch_bench(void* ptr, const double* thetas, int k, int theta_n, int return_grad,
+                                               double* ll_out, double* grad_out, char* bench_out, int bench_cap);
 
 /* No counterpart in the reference (it has only the FP64 LAPACK path): precision of this model's objective
  * evaluations.  slices = 0 selects the FP64 path (default); 4..8 the mixed path, where the O(n^3) products of the
@@ -98,6 +102,11 @@ int lkg_kriging_log_likelihood_fun_bench(void* ptr, const double* theta, int the
 int lkg_kriging_set_precision(void* ptr, int slices);
 int lkg_kriging_get_precision(void* ptr);
 int lkg_kriging_last_slices(void* ptr);
+
+/* No counterpart in the reference: objective evaluations this model has run since it was created, and the GPU
+ * evaluation launches they took (a multistart fit runs every start's evaluation of one optimiser round as one
+ * batched launch, so rounds < evaluations there).  Either pointer may be NULL. */
+int lkg_kriging_eval_counts(void* ptr, long long* evaluations, long long* rounds);
 
 /* Vecchia approximation (objective "LLVecchia" / "LLVecchia(m)" of lkg_kriging_fit[_params]).  The reference
  * exposes these through its C++ Kriging class only (Kriging.hpp:145-173; no lk_* counterpart):
@@ -130,10 +139,13 @@ int lkg_kriging_predict_vecchia(void* ptr, const double* X_n, int q, int d, int 
  * limited to n * (2 d + 1) + 768 <= 1048576 (d = 3: n <= 149686; d = 8: n <= 61635), with 1 <= d <= 8 and
  * 0 <= m <= 32; larger or malformed calls fail with -1 and a message before any work is queued.  Nothing in that
  * array has to start at zero: every word is written before it is read within a call.  The first call on each device
- * resolves the array's address (cudaGetSymbolAddress, which may load the module) and should come before any
- * stream capture begins.  Calls that overlap on one device -- from two threads, or on two streams that are not
- * ordered with each other -- share the array and race: order them.  On success no memory is allocated, host or
- * device; on failure the message is stored like every other entry point's. */
+ * (and the first after that device's context was reset) resolves the array's address with cudaGetSymbolAddress and
+ * loads every kernel the entry point launches, whatever its m; loading a module can make the driver allocate, so
+ * make that first call before any stream capture begins and outside any memory budget.  Later calls in the same
+ * context load and resolve nothing.  Calls that overlap on one device -- from two threads, or on two streams that
+ * are not ordered with each other -- share the array and race: order them.  The entry point calls no cudaMalloc,
+ * cudaFree or allocating library routine and allocates no device memory; on failure the message is stored like
+ * every other entry point's. */
 int lkg_vecchia_sets_noalloc(int n, int d, const double* X, int m, int* order, int* nbr, void* stream);
 
 /* getters, libkriging_c.h:141-165 */

@@ -1071,8 +1071,22 @@ namespace {
 constexpr int SETS_MAX_DEVICES = 64;
 constexpr long long SETS_FIXED_DOUBLES = 768;  // block maxima and their indices
 std::mutex g_sets_mu;
-double* g_sets_addr[SETS_MAX_DEVICES];  // g_sets_scratch's address on each device, resolved on first use
+// g_sets_scratch's address on each device, with the ID of the context it was resolved in.  A context reset
+// (cudaDeviceReset, a primary-context reset by another library) reloads the module and may move the array, so
+// the address is resolved again whenever the current context's ID differs from the recorded one.
+struct SetsSlot {
+  unsigned long long ctx_id;
+  double* addr;
+};
+SetsSlot g_sets_slot[SETS_MAX_DEVICES];
 thread_local char g_sets_msg[320];
+
+// driver entry points for the current context's ID, looked up through the runtime (the library does not link
+// libcuda directly); the types mirror cuCtxGetCurrent / cuCtxGetId with opaque handles
+using CtxGetCurrentFn = int (*)(void** ctx);
+using CtxGetIdFn = int (*)(void* ctx, unsigned long long* id);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
 
 const char* sets_msg_cuda(const char* what, cudaError_t e) {
   std::snprintf(g_sets_msg, sizeof g_sets_msg, "lkg_vecchia_sets_noalloc: %s failed: %s", what,
@@ -1168,14 +1182,52 @@ const char* vecchia_sets_noalloc(int n, int d, const double* X, int m, int32_t* 
   double* base;
   {
     std::lock_guard<std::mutex> lock(g_sets_mu);
-    if (!g_sets_addr[dev]) {
+    if (!g_ctx_get_current || !g_ctx_get_id) {
+      void* f1 = nullptr;
+      void* f2 = nullptr;
+      cudaDriverEntryPointQueryResult q1, q2;
+      e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1);
+      if (e != cudaSuccess || q1 != cudaDriverEntryPointSuccess || !f1)
+        return e != cudaSuccess ? sets_msg_cuda("cudaGetDriverEntryPointByVersion", e)
+                                : "lkg_vecchia_sets_noalloc: the driver has no cuCtxGetCurrent";
+      e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+      if (e != cudaSuccess || q2 != cudaDriverEntryPointSuccess || !f2)
+        return e != cudaSuccess ? sets_msg_cuda("cudaGetDriverEntryPointByVersion", e)
+                                : "lkg_vecchia_sets_noalloc: the driver has no cuCtxGetId";
+      g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+      g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f2);
+    }
+    void* ctx = nullptr;
+    unsigned long long ctx_id = 0;
+    if (g_ctx_get_current(&ctx) == 0 && !ctx) {
+      // the caller's buffers live in this device's primary context; make it current on this thread
+      e = cudaSetDevice(dev);
+      if (e != cudaSuccess) return sets_msg_cuda("cudaSetDevice", e);
+      g_ctx_get_current(&ctx);
+    }
+    if (!ctx || g_ctx_get_id(ctx, &ctx_id) != 0)
+      return "lkg_vecchia_sets_noalloc: no current CUDA context on this thread";
+    SetsSlot& slot = g_sets_slot[dev];
+    if (!slot.addr || slot.ctx_id != ctx_id) {
+      // first call in this context: resolve the array and load every kernel the call may launch, so that later
+      // calls load nothing (with lazy module loading a kernel is otherwise loaded at its first launch)
       void* p = nullptr;
       e = cudaGetSymbolAddress(&p, g_sets_scratch);
       if (e != cudaSuccess) return sets_msg_cuda("cudaGetSymbolAddress", e);
-      g_sets_addr[dev] = static_cast<double*>(p);
+      cudaFuncAttributes fa;
+      const void* kernels[] = {(const void*)k_gather_points, (const void*)k_sets_prepare,
+                               (const void*)k_maxmin_step, (const void*)k_knn_earlier};
+      for (const void* k : kernels) {
+        e = cudaFuncGetAttributes(&fa, k);
+        if (e != cudaSuccess) return sets_msg_cuda("cudaFuncGetAttributes", e);
+      }
+      slot.addr = static_cast<double*>(p);
+      slot.ctx_id = ctx_id;
     }
-    base = g_sets_addr[dev];
+    base = slot.addr;
   }
+  // an error left by an earlier, unrelated runtime call on this thread must not be reported as this call's
+  (void)cudaGetLastError();
   double* Xp = base;
   double* Xo = Xp + (int64_t)n * d;
   double* mind2 = Xo + (int64_t)n * d;

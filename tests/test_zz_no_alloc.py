@@ -70,12 +70,19 @@ def test_noalloc_sets_allocate_no_device_memory(gpu_lib):
             ctypes.c_void_p(nbr.data_ptr()), ctypes.c_void_p(0))
     assert lib.lkg_vecchia_sets_noalloc(*args) == 0, last_error()  # first call resolves the scratch
     torch.cuda.synchronize()
-    free0, _ = torch.cuda.mem_get_info()
+    # cudaMemGetInfo is device-wide: another context on the same GPU can move it between the two readings, so
+    # only a drop seen on every one of three attempts counts as an allocation by the entry point
+    drops = []
     for _ in range(3):
-        assert lib.lkg_vecchia_sets_noalloc(*args) == 0, last_error()
-    torch.cuda.synchronize()
-    free1, _ = torch.cuda.mem_get_info()
-    assert free1 == free0
+        free0, _ = torch.cuda.mem_get_info()
+        for _ in range(3):
+            assert lib.lkg_vecchia_sets_noalloc(*args) == 0, last_error()
+        torch.cuda.synchronize()
+        free1, _ = torch.cuda.mem_get_info()
+        drops.append(free0 - free1)
+        if free1 >= free0:
+            break
+    assert min(drops) <= 0, "device free memory dropped on every attempt: %s bytes" % drops
 
 
 def test_noalloc_sets_reject_before_any_work(gpu_lib):
