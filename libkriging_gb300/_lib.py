@@ -50,6 +50,7 @@ _SIGS = {
     "lkg_kriging_log_marg_post": (_d, [_vp]),
     "lkg_kriging_log_likelihood_fun_batch": (_i, [_vp, _dp, _i, _i, _i, _dp, _dp]),
     "lkg_kriging_log_likelihood_fun_bench": (_i, [_vp, _dp, _i, _i, _dp, _dp, ctypes.c_char_p, _i]),
+    "lkg_kriging_log_likelihood_fun_batch_bench": (_i, [_vp, _dp, _i, _i, _i, _dp, _dp, ctypes.c_char_p, _i]),
     "lkg_kriging_kernel": (_cp, [_vp]),
     "lkg_kriging_optim": (_cp, [_vp]),
     "lkg_kriging_objective": (_cp, [_vp]),
@@ -94,6 +95,7 @@ _SIGS = {
     "lkg_kriging_set_precision": (_i, [_vp, _i]),
     "lkg_kriging_get_precision": (_i, [_vp]),
     "lkg_kriging_last_slices": (_i, [_vp]),
+    "lkg_kriging_eval_counts": (_i, [_vp, _vp, _vp]),
     "lkg_ozaki_gemm_check": (_i, [_i, _i, _i, _dp, _dp, _i, _dp]),
     "lkg_kriging_log_likelihood_vecchia_fun": (_i, [_vp, _dp, _i, _i, _dp, _dp]),
     "lkg_kriging_set_vecchia_exact_commit": (_i, [_vp, _i]),

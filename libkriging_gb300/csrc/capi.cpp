@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <memory>
 #include <sstream>
 #include <string>
 
@@ -24,30 +25,35 @@ namespace lkg {
 void set_last_error(const char* msg) { g_last_error = msg ? msg : ""; }
 }  // namespace lkg
 
-#define CATCH_RETURN                \
-  catch (const std::exception& e) { \
-    g_last_error = e.what();        \
-    return -1;                      \
+// Runs the body of one entry point.  A C++ exception never crosses the C boundary: its text becomes this thread's
+// last error and the entry point returns its failure value (-1, NULL or NaN, as the header states per function).
+template <class R, class Body>
+R run_entry(R failure, Body&& body) noexcept {
+  try {
+    return body();
+  } catch (const std::exception& e) {
+    g_last_error = e.what();
+  } catch (...) {
+    g_last_error = "unexpected non-standard C++ exception";
   }
-#define CATCH_RETURN_NULL           \
-  catch (const std::exception& e) { \
-    g_last_error = e.what();        \
-    return nullptr;                 \
-  }
-#define CATCH_RETURN_NAN                             \
-  catch (const std::exception& e) {                  \
-    g_last_error = e.what();                         \
-    return std::numeric_limits<double>::quiet_NaN(); \
-  }
+  return failure;
+}
 
 namespace {
 
-Kriging::NoiseModel parse_noise_model(const char* s) {
-  if (!s || std::string(s) == "none") return Kriging::NoiseModel::None;
-  if (std::string(s) == "nugget") return Kriging::NoiseModel::Nugget;
-  if (std::string(s) == "heterogeneous")
+// NoiseModel names as the reference's bindings spell them; NULL means the default ("none")
+Kriging::NoiseModel parse_noise_model(const char* name) {
+  const std::string key = name ? name : "none";
+  struct Entry {
+    const char* text;
+    Kriging::NoiseModel model;
+  };
+  static const Entry known[] = {{"none", Kriging::NoiseModel::None}, {"nugget", Kriging::NoiseModel::Nugget}};
+  for (const Entry& e : known)
+    if (key == e.text) return e.model;
+  if (key == "heterogeneous")
     throw std::invalid_argument("noise_model 'heterogeneous' is not supported by the GPU build");
-  throw std::runtime_error(std::string("Unknown noise_model: ") + s);
+  throw std::runtime_error("Unknown noise_model: " + key);
 }
 
 Kriging* K(void* p) {
@@ -91,10 +97,9 @@ extern "C" {
 const char* lkg_get_last_error(void) { return g_last_error.c_str(); }
 
 void* lkg_kriging_new(const char* kernel, const char* noise_model) {
-  try {
+  return run_entry<void*>(nullptr, [&]() -> void* {
     return new Kriging(kernel ? kernel : "matern3_2", parse_noise_model(noise_model));
-  }
-  CATCH_RETURN_NULL
+  });
 }
 
 void* lkg_kriging_new_fit(const double* y, int n, const double* noise, int noise_n, const double* X, int nX, int d,
@@ -102,38 +107,32 @@ void* lkg_kriging_new_fit(const double* y, int n, const double* noise, int noise
                           const char* optim, const char* objective, const double* sigma2, int is_sigma2_estim,
                           const double* theta, int theta_n, int is_theta_estim, const double* beta, int beta_n,
                           int is_beta_estim, const double* nugget, int is_nugget_estim) {
-  Kriging* kr = nullptr;
-  try {
+  return run_entry<void*>(nullptr, [&]() -> void* {
     if (noise && noise_n > 0) throw std::invalid_argument("per-observation noise is not supported by the GPU build");
     if (n != nX) throw std::runtime_error("Dimension of new data should be the same");
-    kr = new Kriging(kernel ? kernel : "matern3_2", parse_noise_model(noise_model));
+    std::unique_ptr<Kriging> kr(new Kriging(kernel ? kernel : "matern3_2", parse_noise_model(noise_model)));
     // theta: one starting point (1 x theta_n), as in the reference C ABI
     lkg::Parameters P = make_params(sigma2, is_sigma2_estim, theta, (theta && theta_n > 0) ? 1 : 0, theta_n,
                                     is_theta_estim, beta, beta_n, is_beta_estim, nugget, is_nugget_estim);
     std::vector<double> yv(y, y + n);
     kr->fit(yv, mat_of(X, nX, d), lkg::regmodel_from_string(regmodel ? regmodel : "constant"), normalize != 0,
             optim ? optim : "BFGS", objective ? objective : "LL", P);
-    return kr;
-  } catch (const std::exception& e) {
-    g_last_error = e.what();
-    delete kr;
-    return nullptr;
-  }
+    return kr.release();  // a failed fit frees the model on the way out
+  });
 }
 
 void lkg_kriging_delete(void* ptr) { delete static_cast<Kriging*>(ptr); }
 
 int lkg_kriging_fit(void* ptr, const double* y, int n, const double* noise, int noise_n, const double* X, int nX,
                     int d, const char* regmodel, int normalize, const char* optim, const char* objective) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     if (noise && noise_n > 0) throw std::invalid_argument("per-observation noise is not supported by the GPU build");
     if (n != nX) throw std::runtime_error("Dimension of new data should be the same");
     std::vector<double> yv(y, y + n);
     K(ptr)->fit(yv, mat_of(X, nX, d), lkg::regmodel_from_string(regmodel ? regmodel : "constant"), normalize != 0,
                 optim ? optim : "BFGS", objective ? objective : "LL", {});
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 int lkg_kriging_fit_params(void* ptr, const double* y, int n, const double* X, int nX, int d, const char* regmodel,
@@ -141,7 +140,7 @@ int lkg_kriging_fit_params(void* ptr, const double* y, int n, const double* X, i
                            int is_sigma2_estim, const double* theta, int theta_rows, int is_theta_estim,
                            const double* beta, int beta_n, int is_beta_estim, const double* nugget,
                            int is_nugget_estim) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     if (n != nX) throw std::runtime_error("Dimension of new data should be the same");
     lkg::Parameters P = make_params(sigma2, is_sigma2_estim, theta, theta_rows, d, is_theta_estim, beta, beta_n,
                                     is_beta_estim, nugget, is_nugget_estim);
@@ -149,14 +148,13 @@ int lkg_kriging_fit_params(void* ptr, const double* y, int n, const double* X, i
     K(ptr)->fit(yv, mat_of(X, nX, d), lkg::regmodel_from_string(regmodel ? regmodel : "constant"), normalize != 0,
                 optim ? optim : "BFGS", objective ? objective : "LL", P);
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 int lkg_kriging_predict(void* ptr, const double* X_n, int m, int d, int return_stdev, int return_cov,
                         int return_deriv, double* mean_out, double* stdev_out, double* cov_out, double* mean_deriv_out,
                         double* stdev_deriv_out) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     (void)mean_deriv_out;
     (void)stdev_deriv_out;
     auto [mean, sd, cov, md, sdd] = K(ptr)->predict(mat_of(X_n, m, d), return_stdev != 0, return_cov != 0,
@@ -165,78 +163,70 @@ int lkg_kriging_predict(void* ptr, const double* X_n, int m, int d, int return_s
     if (stdev_out && return_stdev) std::memcpy(stdev_out, sd.data(), sizeof(double) * sd.size());
     if (cov_out && return_cov) std::memcpy(cov_out, cov.v.data(), sizeof(double) * cov.v.size());
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 int lkg_kriging_predict_vecchia(void* ptr, const double* X_n, int q, int d, int return_stdev, int m,
                                 double* mean_out, double* stdev_out) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     auto [mean, sd] = K(ptr)->predictVecchia(mat_of(X_n, q, d), return_stdev != 0, m);
     if (mean_out) std::memcpy(mean_out, mean.data(), sizeof(double) * mean.size());
     if (stdev_out && return_stdev) std::memcpy(stdev_out, sd.data(), sizeof(double) * sd.size());
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 void* lkg_kriging_copy(void* ptr) {
-  try {
+  return run_entry<void*>(nullptr, [&]() -> void* {
     return K(ptr)->copy().release();
-  }
-  CATCH_RETURN_NULL
+  });
 }
 
 int lkg_kriging_update(void* ptr, const double* y_u, int n, const double* noise_u, int noise_n, const double* X_u,
                        int nX, int d, int refit) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     if (noise_u && noise_n > 0) throw std::runtime_error("update(y, noise, X) requires NoiseModel::Heterogeneous");
     std::vector<double> yv(y_u, y_u + n);
     K(ptr)->update(yv, mat_of(X_u, nX, d), refit != 0);
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 int lkg_kriging_save(void* ptr, const char* filename) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     if (!filename) throw std::invalid_argument("save: null filename");
     K(ptr)->save(filename);
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 void* lkg_kriging_load(const char* filename) {
-  try {
+  return run_entry<void*>(nullptr, [&]() -> void* {
     if (!filename) throw std::invalid_argument("load: null filename");
     return Kriging::load(filename).release();
-  }
-  CATCH_RETURN_NULL
+  });
 }
 
 int lkg_kriging_cov_mat(void* ptr, const double* X1, int n1, int d1, const double* X2, int n2, int d2,
                         double* cov_out) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     Mat R = K(ptr)->covMat(mat_of(X1, n1, d1), mat_of(X2, n2, d2));
     if (cov_out) std::memcpy(cov_out, R.v.data(), sizeof(double) * R.v.size());
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 const char* lkg_kriging_summary(void* ptr) {
-  try {
+  return run_entry<const char*>(nullptr, [&]() -> const char* {
     static thread_local std::string buf;
     buf = K(ptr)->summary();
     return buf.c_str();
-  }
-  CATCH_RETURN_NULL
+  });
 }
 
 int lkg_kriging_log_likelihood_fun(void* ptr, const double* theta, int theta_n, int return_grad, int return_hess,
                                    double* ll_out, double* grad_out, double* hess_out) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     (void)hess_out;
     if (return_hess) throw std::invalid_argument("logLikelihoodFun: return_hess is not supported by the GPU build");
     std::vector<double> g(theta, theta + theta_n);
@@ -244,33 +234,48 @@ int lkg_kriging_log_likelihood_fun(void* ptr, const double* theta, int theta_n, 
     if (ll_out) *ll_out = ll;
     if (grad_out && return_grad) std::memcpy(grad_out, grad.data(), sizeof(double) * grad.size());
     return 0;
-  }
-  CATCH_RETURN
+  });
+}
+
+static void write_bench(const Kriging* k, char* bench_out, int bench_cap) {
+  if (!bench_out || bench_cap <= 0) return;
+  std::ostringstream o;
+  o.precision(17);
+  for (auto& kv : k->last_bench()) o << kv.first << "\t" << kv.second << "\n";
+  const std::string s = o.str();
+  std::strncpy(bench_out, s.c_str(), bench_cap - 1);
+  bench_out[bench_cap - 1] = 0;
 }
 
 int lkg_kriging_log_likelihood_fun_bench(void* ptr, const double* theta, int theta_n, int return_grad, double* ll_out,
                                          double* grad_out, char* bench_out, int bench_cap) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     std::vector<double> g(theta, theta + theta_n);
     auto [ll, grad] = K(ptr)->logLikelihoodFun(g, return_grad != 0, true);
     if (ll_out) *ll_out = ll;
     if (grad_out && return_grad) std::memcpy(grad_out, grad.data(), sizeof(double) * grad.size());
-    if (bench_out && bench_cap > 0) {
-      std::ostringstream o;
-      o.precision(17);
-      for (auto& kv : K(ptr)->last_bench()) o << kv.first << "\t" << kv.second << "\n";
-      const std::string s = o.str();
-      std::strncpy(bench_out, s.c_str(), bench_cap - 1);
-      bench_out[bench_cap - 1] = 0;
-    }
+    write_bench(K(ptr), bench_out, bench_cap);
     return 0;
-  }
-  CATCH_RETURN
+  });
+}
+
+int lkg_kriging_log_likelihood_fun_batch_bench(void* ptr, const double* thetas, int k, int theta_n, int return_grad,
+                                               double* ll_out, double* grad_out, char* bench_out, int bench_cap) {
+  return run_entry<int>(-1, [&]() -> int {
+    std::vector<double> ll, grad;
+    K(ptr)->logLikelihoodFunBatch(mat_of(thetas, k, theta_n), return_grad != 0, ll, grad, bench_out != nullptr);
+    if (ll_out) std::memcpy(ll_out, ll.data(), sizeof(double) * k);
+    if (grad_out && return_grad)
+      for (int b = 0; b < k; ++b)
+        for (int j = 0; j < theta_n; ++j) grad_out[b + (size_t)j * k] = grad[(size_t)b * theta_n + j];
+    write_bench(K(ptr), bench_out, bench_cap);
+    return 0;
+  });
 }
 
 int lkg_kriging_log_likelihood_fun_batch(void* ptr, const double* thetas, int k, int theta_n, int return_grad,
                                          double* ll_out, double* grad_out) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     std::vector<double> ll, grad;
     K(ptr)->logLikelihoodFunBatch(mat_of(thetas, k, theta_n), return_grad != 0, ll, grad);
     if (ll_out) std::memcpy(ll_out, ll.data(), sizeof(double) * k);
@@ -278,98 +283,86 @@ int lkg_kriging_log_likelihood_fun_batch(void* ptr, const double* thetas, int k,
       for (int b = 0; b < k; ++b)
         for (int j = 0; j < theta_n; ++j) grad_out[b + (size_t)j * k] = grad[(size_t)b * theta_n + j];
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 double lkg_kriging_log_likelihood(void* ptr) {
-  try {
+  return run_entry<double>(std::numeric_limits<double>::quiet_NaN(), [&]() -> double {
     return K(ptr)->logLikelihood();
-  }
-  CATCH_RETURN_NAN
+  });
 }
 
 int lkg_kriging_leave_one_out_fun(void* ptr, const double* theta, int theta_n, int return_grad, double* loo_out,
                                   double* grad_out) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     std::vector<double> t(theta, theta + theta_n);
     auto [loo, grad] = K(ptr)->leaveOneOutFun(t, return_grad != 0);
     if (loo_out) *loo_out = loo;
     if (grad_out && return_grad) std::memcpy(grad_out, grad.data(), sizeof(double) * grad.size());
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 double lkg_kriging_leave_one_out(void* ptr) {
-  try {
+  return run_entry<double>(std::numeric_limits<double>::quiet_NaN(), [&]() -> double {
     return K(ptr)->leaveOneOut();
-  }
-  CATCH_RETURN_NAN
+  });
 }
 
 int lkg_kriging_leave_one_out_vec(void* ptr, const double* theta, int theta_n, double* yhat_out, double* stderr_out) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     std::vector<double> t(theta, theta + theta_n);
     auto [yhat, sd] = K(ptr)->leaveOneOutVec(t);
     if (yhat_out) std::memcpy(yhat_out, yhat.data(), sizeof(double) * yhat.size());
     if (stderr_out) std::memcpy(stderr_out, sd.data(), sizeof(double) * sd.size());
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 int lkg_kriging_log_marg_post_fun(void* ptr, const double* theta, int theta_n, int return_grad, double* lmp_out,
                                   double* grad_out) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     std::vector<double> t(theta, theta + theta_n);
     auto [lmp, grad] = K(ptr)->logMargPostFun(t, return_grad != 0);
     if (lmp_out) *lmp_out = lmp;
     if (grad_out && return_grad) std::memcpy(grad_out, grad.data(), sizeof(double) * grad.size());
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 double lkg_kriging_log_marg_post(void* ptr) {
-  try {
+  return run_entry<double>(std::numeric_limits<double>::quiet_NaN(), [&]() -> double {
     return K(ptr)->logMargPost();
-  }
-  CATCH_RETURN_NAN
+  });
 }
 
 const char* lkg_kriging_kernel(void* ptr) {
-  try {
+  return run_entry<const char*>(nullptr, [&]() -> const char* {
     return K(ptr)->kernel().c_str();
-  }
-  CATCH_RETURN_NULL
+  });
 }
 const char* lkg_kriging_optim(void* ptr) {
-  try {
+  return run_entry<const char*>(nullptr, [&]() -> const char* {
     return K(ptr)->optim().c_str();
-  }
-  CATCH_RETURN_NULL
+  });
 }
 const char* lkg_kriging_objective(void* ptr) {
-  try {
+  return run_entry<const char*>(nullptr, [&]() -> const char* {
     return K(ptr)->objective().c_str();
-  }
-  CATCH_RETURN_NULL
+  });
 }
 int lkg_kriging_is_normalize(void* ptr) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     return K(ptr)->is_normalize() ? 1 : 0;
-  }
-  CATCH_RETURN
+  });
 }
 const char* lkg_kriging_regmodel(void* ptr) {
-  try {
+  return run_entry<const char*>(nullptr, [&]() -> const char* {
     return lkg::regmodel_to_string(K(ptr)->regmodel());
-  }
-  CATCH_RETURN_NULL
+  });
 }
 int lkg_kriging_get_X(void* ptr, double* out, int* n, int* d) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     Kriging* k = K(ptr);
     if (n) *n = k->n();
     if (d) *d = k->d();
@@ -379,133 +372,114 @@ int lkg_kriging_get_X(void* ptr, double* out, int* n, int* d) {
           out[i + (size_t)j * k->n()] = k->X()[i + (size_t)j * k->n()] * k->scaleX()[j] + k->centerX()[j];
     }
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 int lkg_kriging_get_centerX(void* ptr, double* out, int* d) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     return copy_vec(K(ptr)->centerX(), out, d);
-  }
-  CATCH_RETURN
+  });
 }
 int lkg_kriging_get_scaleX(void* ptr, double* out, int* d) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     return copy_vec(K(ptr)->scaleX(), out, d);
-  }
-  CATCH_RETURN
+  });
 }
 int lkg_kriging_get_y(void* ptr, double* out, int* n) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     Kriging* k = K(ptr);
     if (n) *n = k->n();
     if (out)
       for (int i = 0; i < k->n(); ++i) out[i] = k->y()[i] * k->scaleY() + k->centerY();
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 double lkg_kriging_get_centerY(void* ptr) {
-  try {
+  return run_entry<double>(std::numeric_limits<double>::quiet_NaN(), [&]() -> double {
     return K(ptr)->centerY();
-  }
-  CATCH_RETURN_NAN
+  });
 }
 double lkg_kriging_get_scaleY(void* ptr) {
-  try {
+  return run_entry<double>(std::numeric_limits<double>::quiet_NaN(), [&]() -> double {
     return K(ptr)->scaleY();
-  }
-  CATCH_RETURN_NAN
+  });
 }
 int lkg_kriging_get_F(void* ptr, double* out, int* n, int* d) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     Kriging* k = K(ptr);
     if (n) *n = k->n();
     if (d) *d = k->p();
     if (out) std::memcpy(out, k->F().data(), sizeof(double) * k->F().size());
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 int lkg_kriging_get_T(void* ptr, double* out, int* n, int* d) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     Mat T = K(ptr)->T();
     if (n) *n = T.rows;
     if (d) *d = T.cols;
     if (out) std::memcpy(out, T.v.data(), sizeof(double) * T.v.size());
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 int lkg_kriging_get_M(void* ptr, double* out, int* n, int* d) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     Mat M = K(ptr)->M();
     if (n) *n = M.rows;
     if (d) *d = M.cols;
     if (out) std::memcpy(out, M.v.data(), sizeof(double) * M.v.size());
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 int lkg_kriging_get_z(void* ptr, double* out, int* n) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     return copy_vec(K(ptr)->z(), out, n);
-  }
-  CATCH_RETURN
+  });
 }
 int lkg_kriging_get_beta(void* ptr, double* out, int* n) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     return copy_vec(K(ptr)->beta(), out, n);
-  }
-  CATCH_RETURN
+  });
 }
 int lkg_kriging_is_beta_estim(void* ptr) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     return K(ptr)->is_beta_estim() ? 1 : 0;
-  }
-  CATCH_RETURN
+  });
 }
 int lkg_kriging_get_theta(void* ptr, double* out, int* n) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     return copy_vec(K(ptr)->theta(), out, n);
-  }
-  CATCH_RETURN
+  });
 }
 int lkg_kriging_is_theta_estim(void* ptr) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     return K(ptr)->is_theta_estim() ? 1 : 0;
-  }
-  CATCH_RETURN
+  });
 }
 double lkg_kriging_get_sigma2(void* ptr) {
-  try {
+  return run_entry<double>(std::numeric_limits<double>::quiet_NaN(), [&]() -> double {
     return K(ptr)->sigma2();
-  }
-  CATCH_RETURN_NAN
+  });
 }
 int lkg_kriging_is_sigma2_estim(void* ptr) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     return K(ptr)->is_sigma2_estim() ? 1 : 0;
-  }
-  CATCH_RETURN
+  });
 }
 const char* lkg_kriging_noise_model(void* ptr) {
-  try {
+  return run_entry<const char*>(nullptr, [&]() -> const char* {
     return K(ptr)->noise_model() == Kriging::NoiseModel::Nugget ? "nugget" : "none";
-  }
-  CATCH_RETURN_NULL
+  });
 }
 double lkg_kriging_get_nugget(void* ptr) {
-  try {
+  return run_entry<double>(std::numeric_limits<double>::quiet_NaN(), [&]() -> double {
     return K(ptr)->nugget();
-  }
-  CATCH_RETURN_NAN
+  });
 }
 int lkg_kriging_is_nugget_estim(void* ptr) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     return K(ptr)->is_nugget_estim() ? 1 : 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 void lkg_set_num_nugget(double nugget) { lkg::config().num_nugget = nugget; }
@@ -528,25 +502,31 @@ void lkg_optim_set_max_restart(int m) { lkg::config().max_restart = m; }
 extern "C" {
 
 int lkg_kriging_set_precision(void* ptr, int slices) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     K(ptr)->set_precision(slices);
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 int lkg_kriging_get_precision(void* ptr) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     return K(ptr)->precision();
-  }
-  CATCH_RETURN
+  });
 }
 
 int lkg_kriging_last_slices(void* ptr) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     return K(ptr)->last_slices();
-  }
-  CATCH_RETURN
+  });
+}
+
+int lkg_kriging_eval_counts(void* ptr, long long* evaluations, long long* rounds) {
+  return run_entry<int>(-1, [&]() -> int {
+    const Kriging* k = K(ptr);
+    if (evaluations) *evaluations = k->evaluations();
+    if (rounds) *rounds = k->rounds();
+    return 0;
+  });
 }
 
 }  // extern "C"
@@ -556,40 +536,36 @@ extern "C" {
 
 int lkg_kriging_log_likelihood_vecchia_fun(void* ptr, const double* theta, int theta_n, int return_grad,
                                            double* vll_out, double* grad_out) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     std::vector<double> t(theta, theta + theta_n);
     auto [vll, grad] = K(ptr)->logLikelihoodVecchiaFun(t, return_grad != 0);
     if (vll_out) *vll_out = vll;
     if (grad_out && return_grad) std::memcpy(grad_out, grad.data(), sizeof(double) * grad.size());
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 int lkg_kriging_set_vecchia_exact_commit(void* ptr, int b) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     K(ptr)->set_vecchia_exact_commit(b != 0);
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 int lkg_kriging_vecchia_neighbors(void* ptr) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     return K(ptr)->vecchia_neighbors();
-  }
-  CATCH_RETURN
+  });
 }
 
 int lkg_kriging_is_vecchia_light(void* ptr) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     return K(ptr)->is_vecchia_light() ? 1 : 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 int lkg_kriging_get_vecchia_sets(void* ptr, int* order_out, int* nbr_out, int* n, int* m) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     const auto& o = K(ptr)->vecchia_order();
     const auto& nb = K(ptr)->vecchia_nbr();
     const int nn = (int)o.size();
@@ -599,17 +575,15 @@ int lkg_kriging_get_vecchia_sets(void* ptr, int* order_out, int* nbr_out, int* n
     if (order_out) std::memcpy(order_out, o.data(), sizeof(int) * o.size());
     if (nbr_out) std::memcpy(nbr_out, nb.data(), sizeof(int) * nb.size());
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 int lkg_vecchia_sets(int n, int d, const double* X, int m, int* order_out, int* nbr_out) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     if (n < 1 || d < 1 || m < 0) throw std::invalid_argument("lkg_vecchia_sets: bad sizes");
     lkg::vecchia_sets_gpu(n, d, X, m, order_out, nbr_out);
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 int lkg_vecchia_sets_noalloc(int n, int d, const double* X, int m, int* order, int* nbr, void* stream) {
@@ -648,7 +622,7 @@ void reject_warping(int n_warping) {
 extern "C" {
 
 void* lkg_nested_kriging_new(const char* kernel, const char* aggregation, const char* partition, int seed) {
-  try {
+  return run_entry<void*>(nullptr, [&]() -> void* {
     auto* nk = new lkg::NestedKriging(kernel ? kernel : "matern3_2");
     try {
       nk->set_aggregation(lkg::NestedKriging::aggregation_from_string(aggregation ? aggregation : "NK"));
@@ -659,8 +633,7 @@ void* lkg_nested_kriging_new(const char* kernel, const char* aggregation, const 
       throw;
     }
     return nk;
-  }
-  CATCH_RETURN_NULL
+  });
 }
 
 void* lkg_nested_kriging_new_fit(const double* y, int n, const double* X, int nX, int d, const char* kernel,
@@ -668,7 +641,7 @@ void* lkg_nested_kriging_new_fit(const double* y, int n, const double* X, int nX
                                  const char** warping, int n_warping, const char* regmodel, const char* optim,
                                  const char* objective, const double* sigma2, int is_sigma2_estim, const double* theta,
                                  int theta_n, int is_theta_estim, const double* beta, int beta_n, int is_beta_estim) {
-  try {
+  return run_entry<void*>(nullptr, [&]() -> void* {
     (void)warping;
     reject_warping(n_warping);
     auto* nk = new lkg::NestedKriging(kernel ? kernel : "matern3_2");
@@ -686,8 +659,7 @@ void* lkg_nested_kriging_new_fit(const double* y, int n, const double* X, int nX
       throw;
     }
     return nk;
-  }
-  CATCH_RETURN_NULL
+  });
 }
 
 void lkg_nested_kriging_delete(void* ptr) { delete static_cast<lkg::NestedKriging*>(ptr); }
@@ -696,7 +668,7 @@ int lkg_nested_kriging_fit(void* ptr, const double* y, int n, const double* X, i
                            const char** warping, int n_warping, const char* regmodel, const char* optim,
                            const char* objective, const double* sigma2, int is_sigma2_estim, const double* theta,
                            int theta_n, int is_theta_estim, const double* beta, int beta_n, int is_beta_estim) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     (void)warping;
     reject_warping(n_warping);
     std::vector<double> yv(y, y + n);
@@ -705,8 +677,7 @@ int lkg_nested_kriging_fit(void* ptr, const double* y, int n, const double* X, i
                  make_params(sigma2, is_sigma2_estim, theta, (theta && theta_n > 0) ? 1 : 0, theta_n, is_theta_estim,
                              beta, beta_n, is_beta_estim, nullptr, 1));
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 int lkg_nested_kriging_fit_groups(void* ptr, const double* y, int n, const double* X, int nX, int d,
@@ -714,7 +685,7 @@ int lkg_nested_kriging_fit_groups(void* ptr, const double* y, int n, const doubl
                                   const char* objective, const double* sigma2, int is_sigma2_estim,
                                   const double* theta, int theta_n, int is_theta_estim, const double* beta,
                                   int beta_n, int is_beta_estim) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     if (!labels || nb_groups < 1) throw std::invalid_argument("fit_groups: labels and nb_groups >= 1 required");
     std::vector<std::vector<int>> groups(nb_groups);
     for (int i = 0; i < nX; ++i) {
@@ -728,76 +699,67 @@ int lkg_nested_kriging_fit_groups(void* ptr, const double* y, int n, const doubl
                         make_params(sigma2, is_sigma2_estim, theta, (theta && theta_n > 0) ? 1 : 0, theta_n,
                                     is_theta_estim, beta, beta_n, is_beta_estim, nullptr, 1));
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 int lkg_nested_kriging_predict(void* ptr, const double* X_n, int m, int d, int return_stdev, double* mean_out,
                                double* stdev_out) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     auto [mean, sd] = NK(ptr)->predict(mat_of(X_n, m, d), return_stdev != 0);
     if (mean_out) std::memcpy(mean_out, mean.data(), sizeof(double) * mean.size());
     if (stdev_out && return_stdev) std::memcpy(stdev_out, sd.data(), sizeof(double) * sd.size());
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 const char* lkg_nested_kriging_summary(void* ptr) {
-  try {
+  return run_entry<const char*>(nullptr, [&]() -> const char* {
     static thread_local std::string buf;
     buf = NK(ptr)->summary();
     return buf.c_str();
-  }
-  CATCH_RETURN_NULL
+  });
 }
 
 const char* lkg_nested_kriging_kernel(void* ptr) {
-  try {
+  return run_entry<const char*>(nullptr, [&]() -> const char* {
     return NK(ptr)->kernel().c_str();
-  }
-  CATCH_RETURN_NULL
+  });
 }
 
 const char* lkg_nested_kriging_aggregation(void* ptr) {
-  try {
+  return run_entry<const char*>(nullptr, [&]() -> const char* {
     static thread_local std::string buf;
     buf = lkg::NestedKriging::aggregation_to_string(NK(ptr)->aggregation());
     return buf.c_str();
-  }
-  CATCH_RETURN_NULL
+  });
 }
 
 int lkg_nested_kriging_nb_groups(void* ptr) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     return NK(ptr)->nb_groups();
-  }
-  CATCH_RETURN
+  });
 }
 
 int lkg_nested_kriging_get_theta(void* ptr, double* out, int* n) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     return copy_vec(NK(ptr)->theta(), out, n);
-  }
-  CATCH_RETURN
+  });
 }
 
 double lkg_nested_kriging_get_sigma2(void* ptr) {
-  try {
+  return run_entry<double>(std::numeric_limits<double>::quiet_NaN(), [&]() -> double {
     return NK(ptr)->sigma2();
-  }
-  CATCH_RETURN_NAN
+  });
 }
 
 double lkg_nested_kriging_get_beta0(void* ptr) {
-  try {
+  return run_entry<double>(std::numeric_limits<double>::quiet_NaN(), [&]() -> double {
     return NK(ptr)->beta0();
-  }
-  CATCH_RETURN_NAN
+  });
 }
 
 int lkg_nested_kriging_get_groups(void* ptr, int* labels_out, int* n) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     const auto& G = NK(ptr)->groups();
     int total = 0;
     for (const auto& g : G) total += (int)g.size();
@@ -806,28 +768,25 @@ int lkg_nested_kriging_get_groups(void* ptr, int* labels_out, int* n) {
       for (size_t k = 0; k < G.size(); ++k)
         for (int i : G[k]) labels_out[i] = (int)k;
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 void* lkg_nested_kriging_submodel(void* ptr, int i) {
-  try {
+  return run_entry<void*>(nullptr, [&]() -> void* {
     return &NK(ptr)->submodel(i);
-  }
-  CATCH_RETURN_NULL
+  });
 }
 
 int lkg_nested_kriging_set_precision(void* ptr, int slices) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     NK(ptr)->set_precision(slices);
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 int lkg_nested_kriging_log_likelihood_groups(void* ptr, const double* thetas, int p, int d, int return_grad,
                                              double* ll_out, double* grad_out) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     lkg::Mat T;
     T.rows = p;
     T.cols = d;
@@ -839,13 +798,12 @@ int lkg_nested_kriging_log_likelihood_groups(void* ptr, const double* thetas, in
     if (ll_out) std::memcpy(ll_out, ll.data(), sizeof(double) * ll.size());
     if (grad_out && return_grad) std::memcpy(grad_out, grad.data(), sizeof(double) * grad.size());
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 int lkg_nested_kriging_get_group_estimates(void* ptr, double* theta_out, double* sigma2_out, double* beta0_out,
                                            int* p, int* d) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     auto* nk = NK(ptr);
     const auto& th = nk->group_theta();
     const int np = (int)nk->group_sigma2().size();
@@ -855,16 +813,14 @@ int lkg_nested_kriging_get_group_estimates(void* ptr, double* theta_out, double*
     if (sigma2_out && np) std::memcpy(sigma2_out, nk->group_sigma2().data(), sizeof(double) * np);
     if (beta0_out && np) std::memcpy(beta0_out, nk->group_beta0().data(), sizeof(double) * np);
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 int lkg_nested_kriging_set_predict_chunk(void* ptr, int chunk) {
-  try {
+  return run_entry<int>(-1, [&]() -> int {
     NK(ptr)->set_predict_chunk(chunk);
     return 0;
-  }
-  CATCH_RETURN
+  });
 }
 
 }  // extern "C"

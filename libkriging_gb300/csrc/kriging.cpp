@@ -268,6 +268,7 @@ std::tuple<double, std::vector<double>> Kriging::logLikelihoodFun(const std::vec
   m_bench.clear();
   m_eval->evaluate(1, gamma.data(), &factor, return_grad, out, bench ? &m_bench : nullptr);
   m_evals++;
+  m_rounds++;
   m_last_slices = out[0].slices;
   std::vector<double> grad;
   const double ll = loglik_from(out[0], extra, return_grad ? &grad : nullptr, (int)gamma.size());
@@ -275,7 +276,7 @@ std::tuple<double, std::vector<double>> Kriging::logLikelihoodFun(const std::vec
 }
 
 void Kriging::logLikelihoodFunBatch(const Mat& gammas, bool return_grad, std::vector<double>& ll,
-                                    std::vector<double>& grad) {
+                                    std::vector<double>& grad, bool bench) {
   const int k = gammas.rows, gd = gammas.cols, d = m_d;
   if (gd != d && !(gd == d + 1 && m_noise_model == NoiseModel::Nugget))
     throw std::invalid_argument("logLikelihoodFunBatch: gamma rows should have length " + std::to_string(d));
@@ -289,8 +290,10 @@ void Kriging::logLikelihoodFunBatch(const Mat& gammas, bool return_grad, std::ve
     fac[b] = (m_noise_model == NoiseModel::Nugget) ? e : 1.0;
   }
   std::vector<EvalOut> out;
-  m_eval->evaluate(k, th.data(), fac.data(), return_grad, out, nullptr);
+  m_bench.clear();
+  m_eval->evaluate(k, th.data(), fac.data(), return_grad, out, bench ? &m_bench : nullptr);
   m_evals += k;
+  m_rounds++;
   ll.assign(k, 0.0);
   grad.assign(return_grad ? (size_t)k * gd : 0, 0.0);
   for (int b = 0; b < k; ++b) {
@@ -316,6 +319,7 @@ std::tuple<double, std::vector<double>> Kriging::leaveOneOutFun(const std::vecto
   std::vector<LooOut> out;
   m_eval->leave_one_out(1, theta.data(), &factor, return_grad, out);
   m_evals++;
+  m_rounds++;
   if (out[0].ev.status != 0) throw std::runtime_error(out[0].ev.message);
   return {out[0].loo, return_grad ? out[0].grad : std::vector<double>()};
 }
@@ -329,6 +333,7 @@ std::tuple<std::vector<double>, std::vector<double>> Kriging::leaveOneOutVec(con
   std::vector<LooOut> out;
   m_eval->leave_one_out(1, theta.data(), &factor, false, out);
   m_evals++;
+  m_rounds++;
   if (out[0].ev.status != 0) throw std::runtime_error(out[0].ev.message);
   std::vector<double> yhat(m_n), sd(m_n);
   const double s = std::sqrt(m_sigma2);
@@ -416,6 +421,7 @@ std::tuple<double, std::vector<double>> Kriging::logMargPostFun(const std::vecto
   std::vector<EvalOut> out;
   m_eval->evaluate_lmp(1, gamma.data(), &alpha, analytic, out);
   m_evals++;
+  m_rounds++;
   std::vector<double> grad;
   const double lmp = lmp_from(out[0], gamma.data(), alpha, analytic ? &grad : nullptr, gd);
   if (return_grad && !m_est_sigma2) {  // forward differences, step 1e-6 in theta (Kriging.cpp:629-640)
@@ -426,6 +432,7 @@ std::tuple<double, std::vector<double>> Kriging::logMargPostFun(const std::vecto
     std::vector<EvalOut> fd;
     m_eval->evaluate_lmp(d, th.data(), fac.data(), false, fd);
     m_evals += d;
+    m_rounds++;
     grad.assign(gd, 0.0);
     for (int k = 0; k < d; ++k) grad[k] = (lmp_from(fd[k], th.data() + (size_t)k * d, alpha, nullptr, gd) - lmp) / eps;
   }
@@ -740,6 +747,7 @@ void Kriging::fit(const std::vector<double>& y, const Mat& Xin, RegressionModel 
         r->vout = m_vecchia->evaluate(r->theta.data(), r->want_grad, m_est_beta || (int)m_beta.size() != m_p,
                                       m_beta.data());
         m_evals++;
+        m_rounds++;
       } else {
         dense.push_back(r);
       }
@@ -759,6 +767,7 @@ void Kriging::fit(const std::vector<double>& y, const Mat& Xin, RegressionModel 
       std::vector<LooOut> lo;
       m_eval->leave_one_out(k, th.data(), fac.data(), g, lo);
       m_evals += k;
+      m_rounds++;
       for (int b = 0; b < k; ++b) dense[b]->lout = std::move(lo[b]);
       return;
     }
@@ -769,6 +778,7 @@ void Kriging::fit(const std::vector<double>& y, const Mat& Xin, RegressionModel 
     else
       m_eval->evaluate(k, th.data(), fac.data(), g, out, nullptr);
     m_evals += k;
+    m_rounds++;
     for (int b = 0; b < k; ++b) dense[b]->out = std::move(out[b]);
   });
   // The objective to maximise (LL, LMP, or -LOO) and its gradient in theta (alpha) space.
@@ -990,6 +1000,7 @@ std::tuple<double, std::vector<double>> Kriging::logLikelihoodVecchiaFun(const s
   VecchiaOut vo = m_vecchia->evaluate(theta.data(), return_grad, m_est_beta || (int)m_beta.size() != m_p,
                                       m_beta.data());
   m_evals++;
+  m_rounds++;
   if (vo.status != 0) throw std::runtime_error(vo.message);
   return {vo.vll, return_grad ? vo.grad : std::vector<double>()};
 }

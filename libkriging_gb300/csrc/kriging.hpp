@@ -67,8 +67,9 @@ class Kriging {
   std::tuple<double, std::vector<double>> logLikelihoodFun(const std::vector<double>& gamma, bool return_grad,
                                                            bool bench);
   // Batched objective: gammas rows = candidates (k x gdim).  ll[k], grad[k x gdim] (row-major per candidate).
+  // bench = true records the per-stage timings of the batched pass (last_bench()).
   void logLikelihoodFunBatch(const Mat& gammas, bool return_grad, std::vector<double>& ll,
-                             std::vector<double>& grad);
+                             std::vector<double>& grad, bool bench = false);
   double logLikelihood();
 
   // leave-one-out (Kriging.hpp:135-143, Kriging.cpp:353-484, 666-668): theta only; R = C, or alpha C + (1 - alpha) I
@@ -150,6 +151,8 @@ class Kriging {
   const std::map<std::string, double>& last_bench() const { return m_bench; }
   // total evaluations performed by the engine since construction (objective calls, batched entries counted once each)
   long long evaluations() const { return m_evals; }
+  // GPU evaluation launches since construction: a batched round of a multistart fit counts once
+  long long rounds() const { return m_rounds; }
   // 0: FP64 path (default); 4..8: mixed path with that many bf16 digit slices for the O(n^3) products of the
   // objective evaluations (logLikelihoodFun and the fit); the committed model used by predict stays FP64.
   void set_precision(int slices);
@@ -191,6 +194,7 @@ class Kriging {
   std::unique_ptr<Engine> m_model;  // committed model (predict)
   std::map<std::string, double> m_bench;
   long long m_evals = 0;
+  long long m_rounds = 0;
   EvalOut m_last_commit;
   int m_last_fit_starts = 0;
   int m_slices = 0;

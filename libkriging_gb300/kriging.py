@@ -161,14 +161,22 @@ class Kriging:
                                                              ctypes.byref(ll), ptr(g), None))
         return ll.value, (g if return_grad else np.zeros(0)), np.zeros((0, 0))
 
-    def logLikelihoodFunBatch(self, thetas, return_grad=True):
-        """k candidate gammas (rows) in one batched GPU evaluation -> (ll[k], grad[k, gdim])."""
+    def logLikelihoodFunBatch(self, thetas, return_grad=True, bench=False):
+        """k candidate gammas (rows) in one batched GPU evaluation -> (ll[k], grad[k, gdim]); bench=True stores the
+        pass's per-stage timings (ms) in self.last_bench."""
         T = f64(np.atleast_2d(np.asarray(thetas, dtype=np.float64)))
         k, gd = T.shape
         ll = np.zeros(k)
         g = np.zeros((k, gd), order="F") if return_grad else None
-        check(_lib.load().lkg_kriging_log_likelihood_fun_batch(self._h, ptr(T), k, gd, int(bool(return_grad)),
-                                                               ptr(ll), ptr(g)))
+        if bench:
+            buf = ctypes.create_string_buffer(4096)
+            check(_lib.load().lkg_kriging_log_likelihood_fun_batch_bench(
+                self._h, ptr(T), k, gd, int(bool(return_grad)), ptr(ll), ptr(g), buf, 4096))
+            self.last_bench = {kv.split("\t")[0]: float(kv.split("\t")[1])
+                               for kv in buf.value.decode().split("\n") if kv}
+        else:
+            check(_lib.load().lkg_kriging_log_likelihood_fun_batch(self._h, ptr(T), k, gd, int(bool(return_grad)),
+                                                                   ptr(ll), ptr(g)))
         return ll, (np.ascontiguousarray(g) if return_grad else None)
 
     def logLikelihood(self):
@@ -279,6 +287,12 @@ class Kriging:
 
     def last_slices(self):
         return _lib.load().lkg_kriging_last_slices(self._h)
+
+    def eval_counts(self):
+        """(objective evaluations, GPU evaluation launches) since this model was created."""
+        ev, ro = ctypes.c_longlong(), ctypes.c_longlong()
+        check(_lib.load().lkg_kriging_eval_counts(self._h, ctypes.byref(ev), ctypes.byref(ro)))
+        return int(ev.value), int(ro.value)
 
     def summary(self):
         s = _lib.load().lkg_kriging_summary(self._h)

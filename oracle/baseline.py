@@ -1,29 +1,32 @@
-"""CPU baseline: the reference's LL + gradient evaluation path restated on the host cores, timed on bounded samples.
+"""CPU baseline: the reference's LL + gradient evaluation path restated on the host cores, timed in full.
 
-TEST / BENCH INFRASTRUCTURE ONLY (used by bench.py's CPU-baseline leg and its ``--impl reference`` arm).
+TEST / BENCH INFRASTRUCTURE ONLY (used by bench.py's CPU-baseline legs and its ``--impl reference`` arm).
 
 The reference cannot be compiled here (its Armadillo / lbfgsb_cpp submodules are empty), so the baseline is the
-oracle's restatement of the path the reference runs for one ``logLikelihoodFun(gamma, return_grad=true)``:
+oracle's restatement of the path the reference runs for one ``logLikelihoodFun(gamma, return_grad=true)``, every
+stage at the full problem size (nothing sampled, nothing scaled):
 
-1. ``LinearAlgebra::cholCov`` pair loop, serial (src/lib/LinearAlgebra.cpp:150-155)       -> oracle C, 1 thread
-2. ``arma::chol`` = LAPACK dpotrf, then ``rcond_chol`` = dtrcon                             -> OpenBLAS, all cores
-3. ``inv_sympd`` = two triangular solves against the n x n identity (:708-710)            -> dtrsm, all cores
-4. ``F* = L \\ F``, ``y* = L \\ y``, GLS, ``E* = L \\ (y - F b)``, ``x = L' \\ E*``         -> dtrsm / numpy
-5. ``compute_ll_grad_theta_vecs`` pair loop, serial (src/lib/KrigingImpl.cpp:863-884)     -> oracle C, 1 thread
+1. ``LinearAlgebra::cholCov`` pair loop (src/lib/LinearAlgebra.cpp:150-161)               -> oracle C, `threads`
+2. ``arma::chol`` = LAPACK dpotrf, then ``rcond_chol`` = dtrcon (:43-115)                  -> OpenBLAS, all cores
+3. ``inv_sympd`` = two triangular solves against the n x n identity (:708-710)            -> dtrtrs, all cores
+4. ``F* = L \\ F``, ``y* = L \\ y``, GLS, ``E* = L \\ (y - F b)`` (src/lib/KrigingImpl.cpp:73-125)
+5. the nugget alpha terms (src/lib/Kriging.cpp:307-326) and ``x = L' \\ E*``
+6. ``compute_ll_grad_theta_vecs`` pair loop (src/lib/KrigingImpl.cpp:855-885)            -> oracle C, `threads`
 
-At the full problem size each stage is timed on a bounded sample and scaled by its exact work ratio:
-stages 1 and 5 on the last rows of the pair loop (a fixed fraction of the n(n-1)/2 pairs), stage 3 on a block of
-identity columns (dtrsm's work is linear in the number of right-hand sides), stages 2 and 4 in full.  Stage 5
-reads R in place of R^-1 (the loop's cost does not depend on the values).  The dX cube of compute_dX (n^2 d
-doubles) is not materialised: differences are recomputed per pair with the same subtraction.
+The reference runs the two pair loops in one thread; here they run over `threads` OpenMP threads with the identical
+per-pair arithmetic (a stronger baseline than the reference as built).  The dX cube of compute_dX (n^2 d doubles,
+17 GB at n = 16384, d = 8) is not materialised: differences are recomputed per pair with the same subtraction.
+The LL and gradient it returns are the oracle's values at the full size (the gradient's pair sums in per-thread
+order, equal to the serial loop's up to summation order).
 """
 from __future__ import annotations
 
+import math
 import os
 import time
 
 import numpy as np
-from scipy.linalg import blas, lapack
+from scipy.linalg import lapack
 
 from . import oracle as O
 
@@ -32,70 +35,98 @@ def _dp(a):
     return O._dp(a)
 
 
-def dense_eval_sample(X, y, theta, factor=1.0, kernel="matern5_2", pair_fraction=0.125, rhs_fraction=1.0 / 16):
-    """Time one reference-restated LL+gradient evaluation.  Returns (seconds_scaled, detail dict)."""
+def host_threads():
+    """Threads the CPU legs use: OMP_NUM_THREADS when set, else every host core."""
+    v = os.environ.get("OMP_NUM_THREADS")
+    if v:
+        try:
+            return max(1, int(v))
+        except ValueError:
+            pass
+    return os.cpu_count() or 1
+
+
+def eval_full(X, y, theta, kernel="matern5_2", alpha=None, fixed_var=None, threads=None, with_grad=True):
+    """One reference-restated ``logLikelihoodFun`` evaluation with constant trend, timed per stage
+    (Kriging.cpp:214-341):
+
+    * ``alpha=None``: NoiseModel None, sigma2 estimated (gamma = theta);
+    * ``alpha`` given, ``fixed_var=None``: Nugget mode with sigma2 and nugget estimated (gamma = [theta, alpha]);
+    * ``alpha`` and ``fixed_var=(sigma2, nugget)``: Nugget mode with both fixed (alpha = sigma2 / (sigma2 + nugget),
+      the alpha-gradient is zero).
+
+    Returns (ll, grad, seconds, detail)."""
+    threads = threads or host_threads()
     X = O._colmajor(X)
+    y = np.ascontiguousarray(y, dtype=np.float64)
     n, d = X.shape
     th = np.ascontiguousarray(theta, dtype=np.float64)
     L_ = O.lib()
     kid = O.KERNELS[kernel]
-    # set-up (not timed): the full covariance matrix, built over all host threads
-    R = np.empty((n, n), order="F")
-    L_.ora_build_R_parallel(kid, n, d, _dp(X), _dp(th), float(factor), _dp(R))
-    total_pairs = n * (n - 1) / 2.0
-    i0 = int(n * np.sqrt(1.0 - pair_fraction))
-    sample_pairs = (n * (n - 1) - i0 * (i0 - 1)) / 2.0
-    scale_pairs = total_pairs / sample_pairs
+    factor = 1.0 if alpha is None else float(alpha)
     st = {}
-    # 1. covariance pair loop (rows i0..n), scaled; then R *= factor and the diagonal
-    Rw = np.empty((n, n), order="F")
+    t_all = time.perf_counter()
+    # 1. covariance build: R(i, j) = factor * Cov(x_i - x_j) off the diagonal, 1 on it
     t = time.perf_counter()
-    L_.ora_build_R_rows(kid, n, d, _dp(X), _dp(th), i0, n, _dp(Rw))
-    st["cov_pairs"] = (time.perf_counter() - t) * scale_pairs
-    del Rw
+    R = np.empty((n, n), order="F")
+    L_.ora_build_R_mt(kid, n, d, _dp(X), _dp(th), factor, None, _dp(R), int(threads))
+    st["cov_pairs"] = time.perf_counter() - t
+    # 2. safe_chol_lower: dpotrf + dtrcon (and the nugget retries, if any)
     t = time.perf_counter()
-    R *= 1.0  # the in-place scaling pass of "R *= factor" (factor already applied in the set-up build)
-    R[np.diag_indices(n)] = 1.0
-    st["cov_scale_diag"] = time.perf_counter() - t
-    # 2. dpotrf + dtrcon
-    t = time.perf_counter()
-    Lf, info = lapack.dpotrf(R, lower=1, clean=1, overwrite_a=0)
-    rc, _ = lapack.dtrcon(Lf, norm="1", uplo="L", diag="N")
+    L, inc = O.safe_chol_lower(R)
     st["chol_rcond"] = time.perf_counter() - t
-    if info != 0:
-        raise RuntimeError("CPU baseline: dpotrf failed (info=%d)" % info)
-    # 3. inv_sympd on a block of identity columns, scaled
-    w = max(1, int(n * rhs_fraction))
-    E = np.zeros((n, w), order="F")
-    E[np.arange(w), np.arange(w)] = 1.0
-    t = time.perf_counter()
-    Z = blas.dtrsm(1.0, Lf, E, side=0, lower=1, trans_a=0, diag=0)
-    Z = blas.dtrsm(1.0, Lf, Z, side=0, lower=1, trans_a=1, diag=0)
-    st["inv_sympd"] = (time.perf_counter() - t) * (n / w)
-    del E, Z
-    # 4. whitening, GLS, residual, x
+    # 3. inv_sympd as coded: two full triangular solves against I
+    Rinv = None
+    if with_grad:
+        t = time.perf_counter()
+        Rinv = O.inv_sympd(L)
+        st["inv_sympd"] = time.perf_counter() - t
+    # 4. whitening, GLS, residual
     t = time.perf_counter()
     F = np.ones((n, 1), order="F")
-    Fs = blas.dtrsm(1.0, Lf, F, side=0, lower=1)
-    ys = blas.dtrsm(1.0, Lf, np.asfortranarray(y.reshape(-1, 1)), side=0, lower=1)[:, 0]
-    G = Fs.T @ Fs
-    beta = np.linalg.solve(G, Fs.T @ ys)
-    Es = blas.dtrsm(1.0, Lf, np.asfortranarray((y - F @ beta).reshape(-1, 1)), side=0, lower=1)[:, 0]
-    sse = float(Es @ Es)
-    x = blas.dtrsm(1.0, Lf, np.asfortranarray(Es.reshape(-1, 1)), side=0, lower=1, trans_a=1)[:, 0]
-    logdet = 2.0 * np.sum(np.log(np.diag(Lf)))
+    Fstar = O.solve_lower(L, F)
+    ystar = O.solve_lower(L, y.reshape(-1, 1))[:, 0]
+    Rstar, info = lapack.dpotrf(Fstar.T @ Fstar, lower=0, clean=1)
+    if info != 0:
+        raise RuntimeError("CPU baseline: chol(F*'F*) failed")
+    rhs = Fstar.T @ ystar
+    beta = lapack.dtrtrs(Rstar, lapack.dtrtrs(Rstar, rhs.reshape(-1, 1), lower=0, trans=1)[0], lower=0)[0][:, 0]
+    Estar = O.solve_lower(L, (y - F @ beta).reshape(-1, 1))[:, 0]
+    sse = float(Estar @ Estar)
+    logdet = 2.0 * float(np.sum(np.log(np.diag(L))))
+    if alpha is None:
+        var = sse / n
+        ll = -0.5 * (n * math.log(2 * math.pi * var) + logdet + n)
+    elif fixed_var is None:
+        var = sse / n
+        ll = -0.5 * (n * math.log(2 * math.pi * var) + logdet + sse / var)
+    else:
+        var = float(fixed_var[0]) + float(fixed_var[1])
+        ll = -0.5 * (n * math.log(2 * math.pi * var) + logdet + sse / var)
     st["solves_gls"] = time.perf_counter() - t
-    # 5. gradient pair loop (rows i0..n), scaled
-    t1 = np.zeros(d)
-    t2 = np.zeros(d)
-    t = time.perf_counter()
-    L_.ora_grad_terms_rows(kid, n, d, _dp(X), _dp(th), _dp(R), _dp(R), _dp(np.ascontiguousarray(x)), i0, n, _dp(t1),
-                           _dp(t2))
-    st["grad_pairs"] = (time.perf_counter() - t) * scale_pairs
-    total = sum(st.values())
-    detail = dict(stages_s=st, n=n, d=d, pair_fraction=sample_pairs / total_pairs, rhs_fraction=w / n,
-                  sse=sse, logdet=logdet, rcond=float(rc), blas_threads=blas_threads(), host_cores=os.cpu_count())
-    return total, detail
+    grad = None
+    if with_grad:
+        # 5. x = L' \ E* and, for the estimated nugget, the alpha terms
+        t = time.perf_counter()
+        x = np.ascontiguousarray(O.solve_upper_t(L, Estar.reshape(-1, 1))[:, 0])
+        out = np.zeros(2)
+        if alpha is not None and fixed_var is None:
+            L_.ora_alpha_terms_mt(n, _dp(R), _dp(Rinv), _dp(x), factor, 0.0, _dp(out), int(threads))
+        st["solve_x_alpha_terms"] = time.perf_counter() - t
+        # 6. gradient pair loop
+        t = time.perf_counter()
+        t1 = np.zeros(d)
+        t2 = np.zeros(d)
+        L_.ora_grad_terms_mt(kid, n, d, _dp(X), _dp(th), _dp(R), _dp(Rinv), _dp(x), _dp(t1), _dp(t2), int(threads))
+        st["grad_pairs"] = time.perf_counter() - t
+        grad = np.zeros(d + (0 if alpha is None else 1))
+        grad[:d] = (t1 / var + t2) / 2.0
+        if alpha is not None and fixed_var is None:
+            grad[d] = -0.5 * (-out[0] / var + out[1])
+    total = time.perf_counter() - t_all
+    detail = dict(stages_s={k: round(v, 4) for k, v in st.items()}, n=n, d=d, threads=int(threads),
+                  blas_threads=blas_threads(), host_cores=os.cpu_count(), nugget_increments=int(inc))
+    return ll, grad, total, detail
 
 
 def blas_threads():

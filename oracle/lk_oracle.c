@@ -21,6 +21,9 @@
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 enum { ORA_GAUSS = 0, ORA_EXP = 1, ORA_MATERN32 = 2, ORA_MATERN52 = 3 };
 
@@ -184,6 +187,96 @@ void ora_grad_terms(int kernel, int n, int d, const double* X, const double* the
       }
     }
   }
+}
+
+/* The same pair loops spread over `threads` OpenMP threads, for the timed CPU baseline (the reference runs them in
+ * one thread; every entry of R is computed with the identical per-pair arithmetic, so R is bit-identical to
+ * ora_build_R's).  The gradient sums are per-thread partial sums over a static row schedule, added in thread order:
+ * deterministic for a given thread count, equal to the serial loop's up to summation order. */
+void ora_build_R_mt(int kernel, int n, int d, const double* X, const double* theta, double factor,
+                    const double* diag, double* R, int threads) {
+#pragma omp parallel for schedule(dynamic, 8) num_threads(threads)
+  for (int i = 0; i < n; i++) {
+    double dx[64];
+    for (int j = 0; j < i; j++) {
+      pair_dx(n, d, X, i, j, dx);
+      double c = ora_cov(kernel, dx, theta, d) * factor;
+      R[i + (size_t)j * n] = c;
+      R[j + (size_t)i * n] = c;
+    }
+    R[i + (size_t)i * n] = diag ? diag[i] : 1.0;
+  }
+}
+
+void ora_grad_terms_mt(int kernel, int n, int d, const double* X, const double* theta, const double* R,
+                       const double* Rinv, const double* x, double* term1, double* term2, int threads) {
+  double part[256][2][16];
+  if (threads > 256) threads = 256;
+  if (d > 16) return;
+#pragma omp parallel num_threads(threads)
+  {
+    int tid = 0, nt = 1;
+#ifdef _OPENMP
+    tid = omp_get_thread_num();
+    nt = omp_get_num_threads();
+#endif
+    double t1[16] = {0}, t2[16] = {0}, dx[64], dln[64];
+    /* rows dealt round-robin in pairs (i, n-1-i) so that every thread gets the same number of pairs */
+    for (int r = tid; r < (n + 1) / 2; r += nt) {
+      for (int half = 0; half < 2; half++) {
+        int i = half ? n - 1 - r : r;
+        if (half && i == r) break;
+        for (int j = 0; j < i; j++) {
+          pair_dx(n, d, X, i, j, dx);
+          ora_dlncov(kernel, dx, theta, d, dln);
+          double R_ij = R[i + (size_t)j * n];
+          double x_i = x[i], x_j = x[j];
+          double Rinv_ij = Rinv[i + (size_t)j * n];
+          for (int k = 0; k < d; k++) {
+            double g = R_ij * dln[k];
+            t1[k] += 2.0 * x_i * g * x_j;
+            t2[k] -= 2.0 * Rinv_ij * g;
+          }
+        }
+      }
+    }
+    for (int k = 0; k < d; k++) {
+      part[tid][0][k] = t1[k];
+      part[tid][1][k] = t2[k];
+    }
+#pragma omp barrier
+#pragma omp single
+    for (int q = 0; q < nt; q++)
+      for (int k = 0; k < d; k++) {
+        term1[k] += part[q][0][k];
+        term2[k] += part[q][1][k];
+      }
+  }
+}
+
+/* ora_alpha_terms over `threads` threads: per-column partial sums, combined in column order. */
+void ora_alpha_terms_mt(int n, const double* R, const double* Rinv, const double* x, double alpha,
+                        double diag_value, double* out, int threads) {
+  double* colv = (double*)malloc(sizeof(double) * 2 * (size_t)n);
+#pragma omp parallel for schedule(static) num_threads(threads)
+  for (int j = 0; j < n; j++) {
+    double v = 0.0, dot = 0.0;
+    for (int i = 0; i < n; i++) {
+      double a = (i == j) ? diag_value : R[i + (size_t)j * n] / alpha;
+      v += x[i] * a;
+      dot += Rinv[i + (size_t)j * n] * a;
+    }
+    colv[j] = v * x[j];
+    colv[n + j] = dot;
+  }
+  double xtAx = 0.0, dot = 0.0;
+  for (int j = 0; j < n; j++) {
+    xtAx += colv[j];
+    dot += colv[n + j];
+  }
+  free(colv);
+  out[0] = xtAx;
+  out[1] = dot;
 }
 
 /* Kriging.cpp:307-326 building blocks: with dRdv = R/alpha (diagonal replaced by diag_value),

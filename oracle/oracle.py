@@ -82,6 +82,15 @@ def lib():
         L.ora_grad_terms_rows.restype = None
         L.ora_grad_terms_rows.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp, dp, dp, ctypes.c_int,
                                           ctypes.c_int, dp, dp]
+        L.ora_build_R_mt.restype = None
+        L.ora_build_R_mt.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, ctypes.c_double, dp, dp,
+                                     ctypes.c_int]
+        L.ora_grad_terms_mt.restype = None
+        L.ora_grad_terms_mt.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp, dp, dp, dp, dp, dp,
+                                        ctypes.c_int]
+        L.ora_alpha_terms_mt.restype = None
+        L.ora_alpha_terms_mt.argtypes = [ctypes.c_int, dp, dp, dp, ctypes.c_double, ctypes.c_double, dp,
+                                         ctypes.c_int]
         L.ora_alpha_terms.restype = None
         L.ora_alpha_terms.argtypes = [ctypes.c_int, dp, dp, dp, ctypes.c_double, ctypes.c_double, dp]
         L.ora_vecchia_sets.restype = None

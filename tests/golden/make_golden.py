@@ -6,7 +6,7 @@ trend, no normalisation, NoiseModel None (bindings/Python/pylibkriging/tests/bin
 reads them from tests/references/). This script copies the inputs and answers verbatim (every CSV value
 parsed to float64) into one JSON fixture so that the tests can run where the reference tree is absent.
 
-Usage:  python tests/golden/make_golden.py [path/to/reference]
+Usage:  python tests/golden/make_golden.py path/to/libKriging-source-tree
 """
 import json
 import sys
@@ -55,4 +55,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py path/to/libKriging-source-tree")
+    main(sys.argv[1])

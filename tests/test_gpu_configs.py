@@ -1,0 +1,102 @@
+"""GPU parity at the sizes of the benchmark configurations, against the oracle's full-size evaluation.
+
+* Dense LL + gradient, n = 4096, d = 8, matern5_2, NuggetKriging with nugget 1e-6 sigma2 (the headline workload at a
+  quarter of its size; it runs the 256-wide two-level panels and many 256-wide k blocks of the mixed path): the
+  FP64 path within 1e-10 (LL) / 1e-7 (gradient) of the oracle, the mixed path within 1e-8 / 1e-6.
+* Batched multistart, n = 2048, d = 6, gauss, Nugget mode with sigma2 and nugget fixed (alpha = 1 / (1 + 1e-8)):
+  LL and gradient at several starting points against the oracle, within a tolerance scaled by cond(R) (these
+  matrices reach cond(R) ~ 1e11, where any two backward-stable FP64 evaluations differ by ~cond * eps), and the
+  reference's multistart invariant (src/lib/Kriging.cpp:2086-2091): a BFGS16 fit equals, bit for bit, the best of
+  16 separate BFGS1 fits from the same starting points.
+
+The oracle side is ``oracle.baseline.eval_full``: the oracle's restatement with its pair loops spread over the host
+cores (equal to ``OracleKriging.log_likelihood`` up to the gradient's summation order; see tests/test_oracle.py).
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from oracle import baseline as B
+
+pytestmark = pytest.mark.gpu
+
+EPS = np.finfo(np.float64).eps
+
+
+def _config2(n, d=8, seed=123):
+    rng = np.random.default_rng(seed)
+    X = rng.uniform(size=(n, d))
+    y = np.sin(2 * np.pi * X).sum(axis=1) + 0.1 * rng.standard_normal(n)
+    theta = rng.uniform(0.2, 1.5, size=d)
+    return X, y, theta, 1.0 / (1.0 + 1e-6)
+
+
+def _config3(n=2048, d=6, starts=64, seed=123):
+    rng = np.random.default_rng(seed)
+    X = rng.uniform(size=(n, d))
+    y = (np.cos(3 * X) * X).sum(axis=1) + 0.1 * rng.standard_normal(n)
+    thetas = rng.uniform(0.1, 2.0, size=(starts, d))
+    s2 = float(np.var(y))
+    return X, y, thetas, s2, 1e-8 * s2
+
+
+@pytest.fixture(scope="module")
+def config2_n4096():
+    X, y, theta, alpha = _config2(4096)
+    ll_o, g_o, _, _ = B.eval_full(X, y, theta, "matern5_2", alpha=alpha)
+    return X, y, theta, alpha, ll_o, g_o
+
+
+@pytest.mark.parametrize("slices", [0, 7])
+def test_config2_n4096_vs_oracle(gpu_lib, config2_n4096, slices):
+    X, y, theta, alpha, ll_o, g_o = config2_n4096
+    k = gpu_lib.Kriging("matern5_2", "nugget")
+    k.fit(y, X, "constant", False, "none", "LL", {"theta": theta.reshape(1, -1), "sigma2": 1.0, "nugget": 1e-6})
+    k.set_precision(slices)
+    ll, g, _ = k.logLikelihoodFun(np.concatenate([theta, [alpha]]), True)
+    tol_ll, tol_g = (1e-10, 1e-7) if slices == 0 else (1e-8, 1e-6)
+    if slices:
+        assert k.last_slices() == slices  # the mixed factorisation was kept (no retreat to FP64)
+    assert rel_err(ll, ll_o) <= tol_ll, (ll, ll_o)
+    assert rel_err(g, g_o) <= tol_g, (g, g_o)
+
+
+def _cond_tol(X, theta, alpha, floor):
+    from oracle import oracle as O
+    w = np.linalg.eigvalsh(O.build_R("gauss", X, theta, alpha))
+    return max(floor, 64.0 * EPS * w[-1] / w[0])
+
+
+@pytest.mark.parametrize("start", [2, 4, 0])
+def test_config3_loglik_vs_oracle(gpu_lib, start):
+    X, y, thetas, s2, nu = _config3()
+    alpha = s2 / (s2 + nu)
+    th = thetas[start]
+    k = gpu_lib.Kriging("gauss", "nugget")
+    k.fit(y, X, "constant", False, "none", "LL",
+          {"theta": th.reshape(1, -1), "sigma2": s2, "is_sigma2_estim": False, "nugget": nu,
+           "is_nugget_estim": False})
+    ll, g, _ = k.logLikelihoodFun(th, True)
+    ll_o, g_o, _, _ = B.eval_full(X, y, th, "gauss", alpha=alpha, fixed_var=(s2, nu))
+    tol_ll = _cond_tol(X, th, alpha, 1e-10)
+    assert rel_err(ll, ll_o) <= tol_ll, (ll, ll_o, tol_ll)
+    assert rel_err(g[:6], g_o[:6]) <= max(1e-7, tol_ll), (g, g_o, tol_ll)
+    # sigma2 and the nugget fixed: the reference zeroes the alpha direction (Kriging.cpp:324-326)
+    assert g.size == 6 or g[6] == 0.0
+
+
+def test_config3_batched_equals_best_of_single_starts(gpu_lib):
+    """BFGS16 == best of 16 x BFGS1 from the same starting points, bit for bit (Kriging.cpp:2086-2091)."""
+    X, y, thetas, s2, nu = _config3(starts=16)
+    params = {"sigma2": s2, "is_sigma2_estim": False, "nugget": nu, "is_nugget_estim": False}
+    kb = gpu_lib.Kriging("gauss", "nugget")
+    kb.fit(y, X, "constant", False, "BFGS16", "LL", dict(params, theta=thetas))
+    best = None
+    for i in range(thetas.shape[0]):
+        k1 = gpu_lib.Kriging("gauss", "nugget")
+        k1.fit(y, X, "constant", False, "BFGS", "LL", dict(params, theta=thetas[i:i + 1]))
+        ll1 = k1.logLikelihood()
+        if best is None or ll1 > best[0]:  # strict: the first of equal optima, as the reference's min_ofn scan
+            best = (ll1, k1.theta(), i)
+    assert kb.logLikelihood() == best[0], (kb.logLikelihood(), best)
+    assert np.array_equal(kb.theta(), best[1]), (kb.theta(), best[1], best[2])

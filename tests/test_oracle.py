@@ -190,3 +190,36 @@ def test_oracle_chol_block_jitters_the_schur_block_only():
     assert np.array_equal(L[:30, :30], np.tril(Loo))
     Lf, incf = O.safe_chol_lower(C)  # the full factor would have jittered every diagonal entry
     assert incf >= 1
+
+
+@pytest.mark.parametrize("mode", ["none", "nugget", "nugget_fixed"])
+def test_full_baseline_evaluation_equals_oracle(mode):
+    """oracle.baseline.eval_full (the timed CPU baseline, pair loops over all host threads) computes the oracle's
+    LL exactly and its gradient up to the pair sums' order, for the three noise settings the benchmarks use."""
+    from oracle import baseline as B
+    rng = np.random.default_rng(21)
+    n, d = 300, 4
+    X = rng.uniform(size=(n, d))
+    y = np.sin(2 * np.pi * X).sum(axis=1) + 0.1 * rng.standard_normal(n)
+    th = rng.uniform(0.2, 1.0, size=d)
+    if mode == "none":
+        ll, g, _, _ = B.eval_full(X, y, th, "matern3_2")
+        ll_o, g_o = O.OracleKriging(y, X, "matern3_2").log_likelihood(th)
+    elif mode == "nugget":
+        a = 1.0 / (1.0 + 1e-6)
+        ll, g, _, _ = B.eval_full(X, y, th, "matern5_2", alpha=a)
+        ll_o, g_o = O.OracleKriging(y, X, "matern5_2", noise_model="nugget").log_likelihood(np.r_[th, a])
+    else:
+        s2, nu = 0.8, 0.8e-8
+        a = s2 / (s2 + nu)
+        ll, g, _, _ = B.eval_full(X, y, th, "gauss", alpha=a, fixed_var=(s2, nu))
+        ora = O.OracleKriging(y, X, "gauss", noise_model="nugget", est_sigma2=False, sigma2=s2, est_nugget=False,
+                              nugget=nu)
+        ll_o, g_o = ora.log_likelihood(th)
+        g_o = g_o[:d]
+        g = g[:d]
+    assert ll == ll_o
+    # the fixed-variance gradient is a difference of two large pair sums (cond(R) ~ 1e9 here): summation order
+    # alone moves it by ~1e-9 relative
+    tol = 1e-8 if mode == "nugget_fixed" else 1e-12
+    assert np.max(np.abs(g - g_o)) <= tol * np.max(np.abs(g_o))
