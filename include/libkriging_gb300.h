@@ -148,6 +148,25 @@ int lkg_kriging_predict_vecchia(void* ptr, const double* X_n, int q, int d, int 
  * every other entry point's. */
 int lkg_vecchia_sets_noalloc(int n, int d, const double* X, int m, int* order, int* nbr, void* stream);
 
+/* Sharded Vecchia likelihood: no counterpart in the reference, whose _logLikelihoodVecchia (Kriging.cpp:806-924)
+ * sums per-point terms over all ordered points in one loop.  Each rank owns the ordered positions [t0, t1) of the
+ * same sets (X n x d, y n, F n x p column-major, normalised as the model holds them; order[n], nbr[n x m]):
+ *   1. lkg_vecchia_shard_sums1: s1 = [A (p x p row-major), b (p), sum log v] over its positions, A = sum W W'/v,
+ *      b = sum W u / v; failed_points counts conditionals that stayed non-SPD after the nugget increments;
+ *   2. the ranks sum s1 (an all-reduce) and lkg_vecchia_gls_beta solves (A + num_nugget I) beta = b;
+ *   3. lkg_vecchia_shard_sums2: s2 = [Q, dQ_k (d), sum dv_k / v (d)] at that beta;
+ *   4. the ranks sum s2 and lkg_vecchia_finish gives sigma2 = Q / n, the VLL and its gradient (d).
+ * The single-GPU evaluation runs the same four steps on one range. */
+void* lkg_vecchia_shard_new(const char* kernel, int n, int d, int p, const double* X, const double* y,
+                            const double* F, const int* order, const int* nbr, int m, int t0, int t1);
+void lkg_vecchia_shard_delete(void* h);
+int lkg_vecchia_shard_sums1(void* h, const double* theta, int with_grad, double* s1_out, long long* nugget_points,
+                            int* failed_points);
+int lkg_vecchia_shard_sums2(void* h, const double* beta, int with_grad, double* s2_out);
+int lkg_vecchia_gls_beta(int p, const double* s1, double* beta_out);
+int lkg_vecchia_finish(int n, int d, double slogv, const double* s2, int with_grad, double* vll_out,
+                       double* sigma2_out, double* grad_out);
+
 /* getters, libkriging_c.h:141-165 */
 const char* lkg_kriging_kernel(void* ptr);
 const char* lkg_kriging_optim(void* ptr);

@@ -8,7 +8,8 @@ single GPU launches), the Vecchia likelihood and predict.  All compute goes thro
 """
 from ._lib import LibKrigingError, header_symbols
 from ._lib import load as _load_library
-from .kriging import Kriging, Optim, check_chol_rcond, get_num_nugget, set_num_nugget, vecchia_sets
+from .kriging import (Kriging, Optim, VecchiaShard, check_chol_rcond, get_num_nugget, set_num_nugget,
+                      vecchia_sets)
 from .nested import NestedKriging
 
 
@@ -20,5 +21,5 @@ def load(filename=None):
     return Kriging.load(filename)
 
 
-__all__ = ["Kriging", "NestedKriging", "Optim", "vecchia_sets", "set_num_nugget", "get_num_nugget",
+__all__ = ["Kriging", "NestedKriging", "Optim", "VecchiaShard", "vecchia_sets", "set_num_nugget", "get_num_nugget",
            "check_chol_rcond", "LibKrigingError", "load", "header_symbols"]

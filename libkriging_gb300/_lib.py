@@ -107,6 +107,12 @@ _SIGS = {
     "lkg_set_tensor_path": (_i, [_i]),
     "lkg_get_tensor_path": (_i, []),
     "lkg_vecchia_sets_noalloc": (_i, [_i, _i, _vp, _i, _vp, _vp, _vp]),
+    "lkg_vecchia_shard_new": (_vp, [_cp, _i, _i, _i, _dp, _dp, _dp, _ip, _ip, _i, _i, _i]),
+    "lkg_vecchia_shard_delete": (None, [_vp]),
+    "lkg_vecchia_shard_sums1": (_i, [_vp, _dp, _i, _dp, _vp, _ip]),
+    "lkg_vecchia_shard_sums2": (_i, [_vp, _dp, _i, _dp]),
+    "lkg_vecchia_gls_beta": (_i, [_i, _dp, _dp]),
+    "lkg_vecchia_finish": (_i, [_i, _i, ctypes.c_double, _dp, _i, _dp, _dp, _dp]),
     "lkg_nested_kriging_new_fit": (_vp, [_dp, _i, _dp, _i, _i, _cp, _i, _cp, _cp, _i, _vp, _i, _cp, _cp, _cp, _dp, _i,
                                          _dp, _i, _i, _dp, _i, _i]),
     "lkg_nested_kriging_delete": (None, [_vp]),

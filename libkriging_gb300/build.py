@@ -20,8 +20,11 @@ BUILD = PKG / "_build"
 SO = BUILD / "liblkgpu.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code is built without floating-point contraction (-ffp-contract=off): GCC contracts a * b + c into one fused
+# operation by default where the target has one (the Arm hosts do), which would change host-side sums that must
+# round like the reference's
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
-              "-Xcompiler", "-O2", "-Xptxas", "-O3"]
+              "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-O3"]
 
 
 def _nvcc() -> str:

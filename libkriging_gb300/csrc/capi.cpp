@@ -11,8 +11,10 @@
 #include <string>
 
 #include "../../include/libkriging_gb300.h"
+#include "common.cuh"
 #include "config.hpp"
 #include "kriging.hpp"
+#include "vecchia.hpp"
 #include "nested.hpp"
 
 using lkg::Kriging;
@@ -582,6 +584,66 @@ int lkg_vecchia_sets(int n, int d, const double* X, int m, int* order_out, int* 
   return run_entry<int>(-1, [&]() -> int {
     if (n < 1 || d < 1 || m < 0) throw std::invalid_argument("lkg_vecchia_sets: bad sizes");
     lkg::vecchia_sets_gpu(n, d, X, m, order_out, nbr_out);
+    return 0;
+  });
+}
+
+void* lkg_vecchia_shard_new(const char* kernel, int n, int d, int p, const double* X, const double* y,
+                            const double* F, const int* order, const int* nbr, int m, int t0, int t1) {
+  return run_entry<void*>(nullptr, [&]() -> void* {
+    if (n < 1 || d < 1 || p < 0 || m < 0) throw std::invalid_argument("lkg_vecchia_shard_new: bad sizes");
+    std::unique_ptr<lkg::VecchiaEngine> e(new lkg::VecchiaEngine(lkg::kernel_from_name(kernel ? kernel : ""), n, d, p,
+                                                                 X, y, F, order, nbr, m));
+    e->set_range(t0, t1);
+    return e.release();
+  });
+}
+
+void lkg_vecchia_shard_delete(void* h) { delete static_cast<lkg::VecchiaEngine*>(h); }
+
+int lkg_vecchia_shard_sums1(void* h, const double* theta, int with_grad, double* s1_out, long long* nugget_points,
+                            int* failed_points) {
+  return run_entry<int>(-1, [&]() -> int {
+    if (!h) throw std::invalid_argument("null Vecchia shard handle");
+    auto* e = static_cast<lkg::VecchiaEngine*>(h);
+    std::vector<double> s1;
+    long long np = 0;
+    const int failed = e->partial_sums1(theta, with_grad != 0, s1, &np);
+    std::memcpy(s1_out, s1.data(), sizeof(double) * s1.size());
+    if (nugget_points) *nugget_points = np;
+    if (failed_points) *failed_points = failed;
+    return 0;
+  });
+}
+
+int lkg_vecchia_shard_sums2(void* h, const double* beta, int with_grad, double* s2_out) {
+  return run_entry<int>(-1, [&]() -> int {
+    if (!h) throw std::invalid_argument("null Vecchia shard handle");
+    std::vector<double> s2;
+    static_cast<lkg::VecchiaEngine*>(h)->partial_sums2(beta, with_grad != 0, s2);
+    std::memcpy(s2_out, s2.data(), sizeof(double) * s2.size());
+    return 0;
+  });
+}
+
+int lkg_vecchia_gls_beta(int p, const double* s1, double* beta_out) {
+  return run_entry<int>(-1, [&]() -> int {
+    std::vector<double> v(s1, s1 + p * p + p + 1), beta;
+    if (lkg::vecchia_gls_beta(p, v, beta) != 0)
+      throw std::runtime_error("solve(): GLS system of the Vecchia likelihood is not positive definite");
+    std::memcpy(beta_out, beta.data(), sizeof(double) * p);
+    return 0;
+  });
+}
+
+int lkg_vecchia_finish(int n, int d, double slogv, const double* s2, int with_grad, double* vll_out,
+                       double* sigma2_out, double* grad_out) {
+  return run_entry<int>(-1, [&]() -> int {
+    lkg::VecchiaOut o;
+    lkg::vecchia_finish(n, d, slogv, std::vector<double>(s2, s2 + 1 + 2 * d), with_grad != 0, o);
+    if (vll_out) *vll_out = o.vll;
+    if (sigma2_out) *sigma2_out = o.sigma2;
+    if (grad_out && with_grad) std::memcpy(grad_out, o.grad.data(), sizeof(double) * d);
     return 0;
   });
 }

@@ -36,14 +36,15 @@ void set_last_error(const char* msg);
 
 namespace {
 
-constexpr int TM = 128, TN = 64;
-constexpr int NA_MAX = 7;                      // A ring stages at most (S = 7)
+constexpr int TM = 128, TN = 32;
+constexpr int NA_MAX = 10;                     // A ring stages at most
 constexpr uint32_t A_BYTES = TM * 128;         // one digit of a 128-row tile, one 64-wide sub-chunk: 16 KB
-constexpr uint32_t B_BYTES = TN * 128;         // 64-row tile: 8 KB
+constexpr uint32_t B_BYTES = TN * 128;         // 32-row tile: 4 KB
 constexpr uint64_t kWaitNs = 200000000ull;     // an mbarrier wait gives up after 200 ms
+constexpr uint32_t TMEM_SET = 256;             // two accumulator sets of S x 32 columns (S <= 8) in 512 columns
 
-// A ring depth for S digits: what 227 KB of shared memory holds beside the two B buffers (6 for S = 8, 7 for S = 7);
-// a deep ring keeps enough digit images in flight to cover the L2 latency at the rate the MMAs consume them
+// A ring depth for S digits: what 227 KB of shared memory holds beside the two B buffers (10 for S = 8); a deep ring
+// keeps enough digit images in flight to cover the L2 latency at the rate the MMAs consume them
 template <int S>
 constexpr int ring_depth() {
   return (int)((227u * 1024u - 1024u - 2u * S * B_BYTES) / A_BYTES) < NA_MAX
@@ -55,8 +56,8 @@ constexpr int NTHREADS = 576;                  // 18 warps
 __device__ int g_oz7_error;
 __device__ int g_oz7_where[8];  // first expired wait: role, tile, k block, sub-chunk, digit, and the role's counters
 
-// instruction descriptor of tcgen05.mma kind::f16: D FP32, A and B bf16, both K-major, M = 128, N = 64 k (the B
-// digits j .. j + k - 1 side by side, up to N = 256)
+// instruction descriptor of tcgen05.mma kind::f16: D FP32, A and B bf16, both K-major, M = 128, N = 32 k (the B
+// digits 1 .. k side by side, up to N = 256)
 __host__ __device__ constexpr uint32_t idesc_n(int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
 }
@@ -266,13 +267,13 @@ struct Tile {
 };
 
 __device__ __forceinline__ bool tile_of(const Oz7Args& g, long long t, Tile& T) {
-  if (g.lower || g.wtw) {  // lower tiles in row-major order: row block I holds column blocks 0 .. 2 I + 1
-    // I = floor((sqrt(4 t + 1) - 1) / 2) from an FP32 estimate and integer corrections (FP64 is scarce here)
-    int I = (int)((sqrtf(4.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
-    while ((long long)(I + 1) * (I + 2) <= t) ++I;
-    while (I > 0 && (long long)I * (I + 1) > t) --I;
+  if (g.lower || g.wtw) {  // lower tiles in row-major order: row block I holds the 32-wide column blocks 0 .. 4 I + 3
+    // I = max { I : 2 I (I + 1) <= t } from an FP32 estimate and integer corrections (FP64 is scarce here)
+    int I = (int)((sqrtf(2.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+    while (2ll * (I + 1) * (I + 2) <= t) ++I;
+    while (I > 0 && 2ll * I * (I + 1) > t) --I;
     T.m0 = I * TM;
-    T.n0 = (int)(t - (long long)I * (I + 1)) * TN;
+    T.n0 = (int)(t - 2ll * I * (I + 1)) * TN;
   } else {
     const int tx = (g.M + TM - 1) / TM;
     T.m0 = (int)(t % tx) * TM;
@@ -291,7 +292,7 @@ __device__ __forceinline__ bool tile_of(const Oz7Args& g, long long t, Tile& T) 
 }
 
 struct Bars {
-  uint64_t a_full[NA_MAX], a_empty[NA_MAX], b_full[2], b_empty[2], acc_full, acc_empty, drain;
+  uint64_t a_full[NA_MAX], a_empty[NA_MAX], b_full[2], b_empty[2], acc_full[2], acc_empty[2], drain;
 };
 
 template <int S>
@@ -325,8 +326,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
       mbar_init(bar(bars.b_full[i]), 1);
       mbar_init(bar(bars.b_empty[i]), 1);
     }
-    mbar_init(bar(bars.acc_full), 1);
-    mbar_init(bar(bars.acc_empty), 16);
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(bar(bars.acc_full[i]), 1);
+      mbar_init(bar(bars.acc_empty[i]), 16);
+    }
     mbar_init(bar(bars.drain), 1);
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
@@ -400,12 +403,16 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
         Tile T;
         if (!tile_of(g, ti, T)) continue;
         for (int kb = T.kb0; kb < T.kb1 && ok; ++kb) {
-          if (!mbar_wait(bar(bars.acc_empty), (uacc & 1) ^ 1)) {
+          // accumulator set uacc & 1: the epilogue releases set s after folding the block that used it, so the
+          // products of this block overlap the fold of the previous one
+          const int set = uacc & 1;
+          if (!mbar_wait(bar(bars.acc_empty[set]), ((uacc >> 1) & 1) ^ 1)) {
             record_expiry(3, ti, kb, -1, -1, ua, ub, uacc);
             ok = false;
             break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+          const uint32_t tset = tmem + (uint32_t)set * TMEM_SET;
           const int s1 = min((kb + 1) * spb, g.SA.nsub);
           for (int s = kb * spb; s < s1 && ok; ++s) {
             const bool first_sub = (s == kb * spb);
@@ -416,8 +423,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
               break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            // descriptors advance with the address: +2 per 32-byte (16-element) step along k, +B_BYTES / 16 per B
-            // digit, so each MMA costs one add and one issue (an N = 64 MMA runs ~30 clocks at the tensor rate)
+            // descriptors advance with the address: +2 per 32-byte (16-element) step along k, so each MMA costs one
+            // add and one issue
             const uint64_t bdesc0 = sdesc(sB + bb * B_BUF);
 #pragma unroll
             for (int i = 1; i <= S; ++i) {
@@ -429,19 +436,14 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
               }
               asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
               const uint64_t adesc0 = sdesc(sA + st * A_BYTES);
-              // A digit i meets B digits 1 .. S + 1 - i: those are adjacent 64-row blocks of one K-major operand and
-              // their diagonals i + j adjacent 64-column blocks of TMEM, so up to 4 of them form one N = 256 MMA
+              // A digit i meets B digits 1 .. S + 1 - i: adjacent 32-row blocks of one K-major operand, whose
+              // diagonals i + 1 .. S + 1 are adjacent 32-column blocks of TMEM -- one MMA of N = 32 (S + 1 - i)
+              const uint32_t d = tset + (uint32_t)((i - 1) * TN);
+              const uint32_t idesc = idesc_n(TN * (S + 1 - i));
 #pragma unroll
-              for (int j0 = 1; j0 <= S + 1 - i; j0 += 4) {
-                const int k = (S + 1 - i - j0 + 1) < 4 ? (S + 1 - i - j0 + 1) : 4;
-                const uint32_t d = tmem + (uint32_t)((i + j0 - 2) * TN);
-                const uint64_t bdesc = bdesc0 + (uint64_t)((j0 - 1) * (B_BYTES >> 4));
-                const uint32_t idesc = idesc_n(TN * k);
-#pragma unroll
-                for (int kk = 0; kk < 4; ++kk)
-                  mma_issue(d, adesc0 + (uint64_t)(2 * kk), bdesc + (uint64_t)(2 * kk), idesc,
-                            (!first_sub || i > 1 || kk > 0) ? 1u : 0u);
-              }
+              for (int kk = 0; kk < 4; ++kk)
+                mma_issue(d, adesc0 + (uint64_t)(2 * kk), bdesc0 + (uint64_t)(2 * kk), idesc,
+                          (!first_sub || i > 1 || kk > 0) ? 1u : 0u);
               mma_commit(bar(bars.a_empty[st]));
               issued = true;
               ++ua;
@@ -451,7 +453,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
             ++ub;
           }
           if (!ok) break;
-          mma_commit(bar(bars.acc_full));
+          mma_commit(bar(bars.acc_full[set]));
           ++uacc;
         }
       }
@@ -463,18 +465,21 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
     }
   } else {
     // ------------------------------- epilogue -------------------------------
-    // 16 warps: warp w owns TMEM lanes 32 (w % 4) .. +31 (rows) and the 16 columns 16 cg .. +15, taken 4 at a time:
+    // 16 warps: warp w owns TMEM lanes 32 (w % 4) .. +31 (rows) and the 8 columns 8 cg .. +7, taken 4 at a time:
     // the S diagonals of 4 columns are loaded together, Horner-folded, converted and added into C.
+    constexpr int CPW = TN / 4;  // columns per epilogue warp
     const int quarter = w & 3, cg = (w - 2) >> 2;
-    const uint32_t tl = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(cg * 16);
+    const uint32_t tl0 = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(cg * CPW);
     double* Cb = g.C + bz * g.c_batch;
     const bool tri = g.lower || g.wtw;
     uint32_t uacc = 0;
     for (long long ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
       Tile T;
       if (!tile_of(g, ti, T)) continue;
-      const int row = T.m0 + 32 * quarter + lane, col0 = T.n0 + cg * 16;
+      const int row = T.m0 + 32 * quarter + lane, col0 = T.n0 + cg * CPW;
       for (int kb = T.kb0; kb < T.kb1 && ok; ++kb) {
+        const int set = uacc & 1;
+        const uint32_t tl = tl0 + (uint32_t)set * TMEM_SET;
         const bool first = (kb == T.kb0);
         const bool need_c = !(first && g.beta == 0.0);
         // operands of the update, loaded while the block's products run: the column exponents and the first four
@@ -492,7 +497,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
         // C = beta C + alpha P in one FP64 operation where the coefficients allow it
         const int upd = !need_c ? (g.alpha == 1.0 ? 0 : 1)
                                 : ((!first || g.beta == 1.0) ? (g.alpha == -1.0 ? 2 : (g.alpha == 1.0 ? 3 : 4)) : 5);
-        const bool got = mbar_wait(bar(bars.acc_full), uacc & 1);
+        const bool got = mbar_wait(bar(bars.acc_full[set]), (uacc >> 1) & 1);
         if (!__all_sync(0xffffffffu, got)) {
           if (lane == 0) record_expiry(6 + 16 * w, ti, kb, -1, -1, 0, 0, uacc);
           ok = false;
@@ -500,7 +505,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
         }
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
 #pragma unroll
-        for (int q0 = 0; q0 < 16; q0 += 4) {
+        for (int q0 = 0; q0 < CPW; q0 += 4) {
           double cold[4];
           int ec[4];
 #pragma unroll
@@ -508,7 +513,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
             cold[q] = cnext[q];
             ec[q] = enext[q];
           }
-          if (q0 + 4 < 16) {
+          if (q0 + 4 < CPW) {
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
               const int col = col0 + q0 + 4 + q;
@@ -555,7 +560,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
         }
         asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
         __syncwarp();
-        if (lane == 0) mbar_arrive(bar(bars.acc_empty));
+        if (lane == 0) mbar_arrive(bar(bars.acc_empty[set]));
         ++uacc;
       }
     }
@@ -650,7 +655,7 @@ void oz7_gemm(int M, int N, int kb0, int kb1, double alpha, const Split7& SA, co
   long long ntiles = tx * ty;
   if (lower) {
     if (M != N) throw std::invalid_argument("oz7_gemm: lower products are square");
-    ntiles = tx * (tx + 1);  // row block I holds 2 I + 2 column blocks
+    ntiles = 2 * tx * (tx + 1);  // row block I holds 4 I + 4 column blocks of 32
   }
   const double K = std::min<double>((double)(kb1 - kb0) * SA.sub_per_blk * OZ7_SUB,
                                     (double)(SA.nsub - kb0 * SA.sub_per_blk) * OZ7_SUB);
@@ -666,7 +671,7 @@ void oz7_wtw(int n, const Split7& SW, double* C, int64_t ldc, int64_t cstride, i
   // executed work: tile (I, J) sums the k blocks from the one holding row 128 I
   LaunchTimer lt("k_oz7_wtw", st, (double)n * (n + 1.0) * (n + 2.0) / 3.0 * batch * SW.S * (SW.S + 1) / 2.0,
                  8.0 * n * (n + 1.0) * batch);
-  dispatch(SW.S, a, I * (I + 1), batch, st);
+  dispatch(SW.S, a, 2 * I * (I + 1), batch, st);
 }
 
 int oz7_error_and_reset(int* where) {

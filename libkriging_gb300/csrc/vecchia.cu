@@ -146,6 +146,7 @@ __device__ double wrcond2(const double* L, int mi, int lane) {
 
 struct VPointArgs {
   int n, d, p, m;
+  int t0, t1;  // ordered positions evaluated: [t0, t1)
   const double *X, *y, *F, *theta;
   const int32_t *order, *nbr;
   double num_nugget, min_rcond;
@@ -162,8 +163,8 @@ __global__ void __launch_bounds__(WPB * 32) k_vecchia_points(VPointArgs a) {
   double* LN = RN + 32 * LDP;
   double* xs = LN + 32 * LDP;  // [32][DM]
   double* sa = xs + 32 * DM;   // [32]
-  const int t = blockIdx.x * WPB + w;
-  if (t >= a.n) return;
+  const int t = a.t0 + blockIdx.x * WPB + w;
+  if (t >= a.t1) return;
   const int n = a.n, d = a.d, p = a.p;
   const int oi = a.order[t];
   const int nbv = (lane < a.m) ? a.nbr[(int64_t)t * a.m + lane] : -1;
@@ -296,11 +297,12 @@ __device__ double bsum(double v, double* red) {
 }
 
 // stage 1: [A (p x p, row a col b), b (p), sum log v] partials per block
-__global__ void k_vsum1(int n, int p, const double* __restrict__ u, const double* __restrict__ v,
+__global__ void k_vsum1(int t0, int t1, int p, const double* __restrict__ u, const double* __restrict__ v,
                         const double* __restrict__ W, double* __restrict__ part) {
   __shared__ double red[8];
   const int P = p * p + p + 1;
-  const int64_t lo = (int64_t)n * blockIdx.x / gridDim.x, hi = (int64_t)n * (blockIdx.x + 1) / gridDim.x;
+  const int64_t cnt = t1 - t0;
+  const int64_t lo = t0 + cnt * blockIdx.x / gridDim.x, hi = t0 + cnt * (blockIdx.x + 1) / gridDim.x;
   for (int e = 0; e < P; ++e) {
     double s = 0.0;
     for (int64_t t = lo + threadIdx.x; t < hi; t += blockDim.x) {
@@ -319,13 +321,14 @@ __global__ void k_vsum1(int n, int p, const double* __restrict__ u, const double
 }
 
 // stage 2: [Q, dQ_k (d), sum dv_k / v (d)] partials per block, given beta
-__global__ void k_vsum2(int n, int p, int d, const double* __restrict__ u, const double* __restrict__ v,
+__global__ void k_vsum2(int t0, int t1, int p, int d, const double* __restrict__ u, const double* __restrict__ v,
                         const double* __restrict__ W, const double* __restrict__ du, const double* __restrict__ dv,
                         const double* __restrict__ dW, const double* __restrict__ beta, int with_grad,
                         double* __restrict__ part) {
   __shared__ double red[8];
   const int P = 1 + 2 * d;
-  const int64_t lo = (int64_t)n * blockIdx.x / gridDim.x, hi = (int64_t)n * (blockIdx.x + 1) / gridDim.x;
+  const int64_t cnt = t1 - t0;
+  const int64_t lo = t0 + cnt * blockIdx.x / gridDim.x, hi = t0 + cnt * (blockIdx.x + 1) / gridDim.x;
   for (int e = 0; e < (with_grad ? P : 1); ++e) {
     double s = 0.0;
     for (int64_t t = lo + threadIdx.x; t < hi; t += blockDim.x) {
@@ -361,10 +364,10 @@ __global__ void k_vsum_final(int nblocks, int stride, int count, const double* _
   }
 }
 
-__global__ void k_count_status(int n, const int* __restrict__ status, int* __restrict__ out) {
+__global__ void k_count_status(int t0, int t1, const int* __restrict__ status, int* __restrict__ out) {
   // out[0] = number of failed points, out[1] = number of points that needed nugget increments
   int f = 0, c = 0;
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+  for (int t = t0 + blockIdx.x * blockDim.x + threadIdx.x; t < t1; t += gridDim.x * blockDim.x) {
     f += status[t] < 0;
     c += status[t] > 0;
   }
@@ -387,7 +390,7 @@ struct VPointLaunch {
       LKG_CUDA(cudaFuncSetAttribute(k_vecchia_points<K, DM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       attr = true;
     }
-    k_vecchia_points<K, DM><<<ceil_div(a.n, WPB), WPB * 32, smem, st>>>(a);
+    k_vecchia_points<K, DM><<<ceil_div(a.t1 - a.t0, WPB), WPB * 32, smem, st>>>(a);
     LKG_LAUNCH("k_vecchia_points");
   }
 };
@@ -627,6 +630,8 @@ VecchiaEngine::VecchiaEngine(int kernel, int n, int d, int p, const double* X, c
   nblk_red_ = RED_BLOCKS;
   valloc(&dpart_, (size_t)nblk_red_ * (VPMAX * VPMAX + VPMAX + 1 + 2 * 8 + 1) + 512);
   valloc(&dbeta_, VPMAX);
+  t0_ = 0;
+  t1_ = n;
   LKG_CUDA(cudaStreamSynchronize(st_));
 }
 
@@ -639,51 +644,109 @@ VecchiaEngine::~VecchiaEngine() {
   if (st_) cudaStreamDestroy(st_);
 }
 
-VecchiaOut VecchiaEngine::evaluate(const double* theta, bool with_grad, bool est_beta, const double* beta_fixed) {
+void VecchiaEngine::set_range(int t0, int t1) {
+  if (t0 < 0 || t1 > n_ || t0 > t1) throw std::invalid_argument("VecchiaEngine::set_range: need 0 <= t0 <= t1 <= n");
+  t0_ = t0;
+  t1_ = t1;
+}
+
+int VecchiaEngine::partial_sums1(const double* theta, bool with_grad, std::vector<double>& s1,
+                                 long long* nugget_points) {
   const Config& cfg = config();
   const int n = n_, d = d_, p = p_;
-  VecchiaOut out;
+  const int P1 = p * p + p + 1;
+  s1.assign(P1, 0.0);
+  if (t1_ <= t0_) return 0;
   LKG_CUDA(cudaMemcpyAsync(dth_, theta, sizeof(double) * d, cudaMemcpyHostToDevice, st_));
-  VPointArgs a{n, d, p, m_, dX_, dY_, dF_, dth_, dorder_, dnbr_, cfg.num_nugget, cfg.min_rcond,
+  VPointArgs a{n, d, p, m_, t0_, t1_, dX_, dY_, dF_, dth_, dorder_, dnbr_, cfg.num_nugget, cfg.min_rcond,
                cfg.chol_rcond_check ? 1 : 0, cfg.max_inc_choldiag, with_grad ? 1 : 0, du_, dv_, dW_, ddu_, ddv_,
                ddW_, dstatus_};
+  const double cnt = t1_ - t0_;
   {
-    LaunchTimer lt("k_vecchia_points", st_, (double)n * m_ * (m_ + 1) / 2.0, 8.0 * n * (1.0 + d) * m_);
+    LaunchTimer lt("k_vecchia_points", st_, cnt * m_ * (m_ + 1) / 2.0, 8.0 * cnt * (1.0 + d) * m_);
     launch_points(kernel_, a, st_);
   }
   int* dcount = dstatus_ + n;
   LKG_CUDA(cudaMemsetAsync(dcount, 0, 2 * sizeof(int), st_));
   {
-    LaunchTimer lt("k_count_status", st_, 0.0, 4.0 * n);
-    k_count_status<<<152, 256, 0, st_>>>(n, dstatus_, dcount);
+    LaunchTimer lt("k_count_status", st_, 0.0, 4.0 * cnt);
+    k_count_status<<<152, 256, 0, st_>>>(t0_, t1_, dstatus_, dcount);
     LKG_LAUNCH("k_count_status");
   }
-  const int P1 = p * p + p + 1;
   double* fin = dpart_ + (size_t)nblk_red_ * (VPMAX * VPMAX + VPMAX + 1 + 2 * 8 + 1);
   {
-    LaunchTimer lt("k_vsum1", st_, 0.0, 8.0 * n * (2.0 + p));
-    k_vsum1<<<nblk_red_, 256, 0, st_>>>(n, p, du_, dv_, dW_, dpart_);
+    LaunchTimer lt("k_vsum1", st_, 0.0, 8.0 * cnt * (2.0 + p));
+    k_vsum1<<<nblk_red_, 256, 0, st_>>>(t0_, t1_, p, du_, dv_, dW_, dpart_);
     LKG_LAUNCH("k_vsum1");
     k_vsum_final<<<1, 256, 0, st_>>>(nblk_red_, P1, P1, dpart_, fin);
     LKG_LAUNCH("k_vsum_final");
   }
-  std::vector<double> s1(P1);
   int counts[2];
   LKG_CUDA(cudaMemcpyAsync(s1.data(), fin, sizeof(double) * P1, cudaMemcpyDeviceToHost, st_));
   LKG_CUDA(cudaMemcpyAsync(counts, dcount, 2 * sizeof(int), cudaMemcpyDeviceToHost, st_));
   LKG_CUDA(cudaStreamSynchronize(st_));
-  if (counts[0] > 0) {
+  if (nugget_points) *nugget_points += counts[1];
+  return counts[0];
+}
+
+void VecchiaEngine::partial_sums2(const double* beta, bool with_grad, std::vector<double>& s2) {
+  const int d = d_, p = p_;
+  const int P2 = 1 + 2 * d;
+  s2.assign(P2, 0.0);
+  if (t1_ <= t0_) return;
+  if (p > 0) LKG_CUDA(cudaMemcpyAsync(dbeta_, beta, sizeof(double) * p, cudaMemcpyHostToDevice, st_));
+  double* fin = dpart_ + (size_t)nblk_red_ * (VPMAX * VPMAX + VPMAX + 1 + 2 * 8 + 1);
+  const double cnt = t1_ - t0_;
+  {
+    LaunchTimer lt("k_vsum2", st_, 0.0, 8.0 * cnt * (2.0 + p) * (with_grad ? 1.0 + d : 1.0));
+    k_vsum2<<<nblk_red_, 256, 0, st_>>>(t0_, t1_, p, d, du_, dv_, dW_, ddu_, ddv_, ddW_, dbeta_, with_grad ? 1 : 0,
+                                        dpart_);
+    LKG_LAUNCH("k_vsum2");
+    k_vsum_final<<<1, 256, 0, st_>>>(nblk_red_, P2, with_grad ? P2 : 1, dpart_, fin);
+    LKG_LAUNCH("k_vsum_final");
+  }
+  LKG_CUDA(cudaMemcpyAsync(s2.data(), fin, sizeof(double) * (with_grad ? P2 : 1), cudaMemcpyDeviceToHost, st_));
+  LKG_CUDA(cudaStreamSynchronize(st_));
+}
+
+std::string vecchia_failure_message() {
+  const Config& cfg = config();
+  return "[ERROR] Exceed max numerical nugget (" + std::to_string(cfg.max_inc_choldiag + 1) + " x 1e" +
+         std::to_string(std::log10(cfg.num_nugget)) + ") added to force chol matrix";
+}
+
+int vecchia_gls_beta(int p, const std::vector<double>& s1, std::vector<double>& beta) {
+  const Config& cfg = config();
+  std::vector<double> A(s1.begin(), s1.begin() + p * p), b(s1.begin() + p * p, s1.begin() + p * p + p);
+  for (int q = 0; q < p; ++q) A[q * p + q] += cfg.num_nugget;  // Kriging.cpp:898
+  beta.assign(p, 0.0);
+  return (p == 0 || small_spd_solve(p, A, b, beta)) ? 0 : -1;
+}
+
+void vecchia_finish(int n, int d, double slogv, const std::vector<double>& s2, bool with_grad, VecchiaOut& out) {
+  const double Q = s2[0];
+  const double sigma2 = Q / n;
+  out.sigma2 = sigma2;
+  out.vll = -0.5 * n * std::log(2 * M_PI * sigma2) - 0.5 * slogv - 0.5 * n;
+  if (with_grad) {
+    out.grad.resize(d);
+    for (int k = 0; k < d; ++k) out.grad[k] = -0.5 * n * s2[1 + k] / Q - 0.5 * s2[1 + d + k];
+  }
+}
+
+VecchiaOut VecchiaEngine::evaluate(const double* theta, bool with_grad, bool est_beta, const double* beta_fixed) {
+  const int n = n_, d = d_, p = p_;
+  VecchiaOut out;
+  std::vector<double> s1, s2;
+  const int failed = partial_sums1(theta, with_grad, s1, &out.nugget_points);
+  if (failed > 0) {
     out.status = 1;
-    out.message = "[ERROR] Exceed max numerical nugget (" + std::to_string(cfg.max_inc_choldiag + 1) + " x 1e" +
-                  std::to_string(std::log10(cfg.num_nugget)) + ") added to force chol matrix";
+    out.message = vecchia_failure_message();
     return out;
   }
-  out.nugget_points = counts[1];
   std::vector<double> beta(p, 0.0);
   if (est_beta || beta_fixed == nullptr) {
-    std::vector<double> A(s1.begin(), s1.begin() + p * p), b(s1.begin() + p * p, s1.begin() + p * p + p);
-    for (int q = 0; q < p; ++q) A[q * p + q] += cfg.num_nugget;
-    if (p > 0 && !small_spd_solve(p, A, b, beta)) {
+    if (vecchia_gls_beta(p, s1, beta) != 0) {
       out.status = 2;
       out.message = "solve(): GLS system of the Vecchia likelihood is not positive definite";
       return out;
@@ -691,28 +754,9 @@ VecchiaOut VecchiaEngine::evaluate(const double* theta, bool with_grad, bool est
   } else {
     beta.assign(beta_fixed, beta_fixed + p);
   }
-  const double slogv = s1[p * p + p];
-  if (p > 0) LKG_CUDA(cudaMemcpyAsync(dbeta_, beta.data(), sizeof(double) * p, cudaMemcpyHostToDevice, st_));
-  const int P2 = 1 + 2 * d;
-  {
-    LaunchTimer lt("k_vsum2", st_, 0.0, 8.0 * n * (2.0 + p) * (with_grad ? 1.0 + d : 1.0));
-    k_vsum2<<<nblk_red_, 256, 0, st_>>>(n, p, d, du_, dv_, dW_, ddu_, ddv_, ddW_, dbeta_, with_grad ? 1 : 0, dpart_);
-    LKG_LAUNCH("k_vsum2");
-    k_vsum_final<<<1, 256, 0, st_>>>(nblk_red_, P2, with_grad ? P2 : 1, dpart_, fin);
-    LKG_LAUNCH("k_vsum_final");
-  }
-  std::vector<double> s2(P2, 0.0);
-  LKG_CUDA(cudaMemcpyAsync(s2.data(), fin, sizeof(double) * (with_grad ? P2 : 1), cudaMemcpyDeviceToHost, st_));
-  LKG_CUDA(cudaStreamSynchronize(st_));
-  const double Q = s2[0];
-  const double sigma2 = Q / n;
-  out.sigma2 = sigma2;
+  partial_sums2(beta.data(), with_grad, s2);
   out.beta = beta;
-  out.vll = -0.5 * n * std::log(2 * M_PI * sigma2) - 0.5 * slogv - 0.5 * n;
-  if (with_grad) {
-    out.grad.resize(d);
-    for (int k = 0; k < d; ++k) out.grad[k] = -0.5 * n * s2[1 + k] / Q - 0.5 * s2[1 + d + k];
-  }
+  vecchia_finish(n, d, s1[p * p + p], s2, with_grad, out);
   return out;
 }
 
@@ -772,7 +816,7 @@ __global__ void k_maxmin_step(int n, int d, const double* __restrict__ Xp, doubl
         double s = 0.0;
         for (int k = 0; k < d; ++k) {
           const double dk = Xp[i * d + k] - nx[k];
-          s += dk * dk;
+          s = __dadd_rn(s, __dmul_rn(dk, dk));  // no fused multiply-add, as the reference's loop
         }
         if (s < m) m = s;
       }
@@ -803,53 +847,6 @@ __global__ void k_maxmin_step(int n, int d, const double* __restrict__ Xp, doubl
   }
 }
 
-// mind2[i] = |x_i - x_first|^2, then the first step's block maxima
-__global__ void k_maxmin_init(int n, int d, const double* __restrict__ Xp, int first, double* __restrict__ mind2,
-                              double* __restrict__ pv, int* __restrict__ pi) {
-  __shared__ double sv[256];
-  __shared__ int si[256];
-  const int nb = gridDim.x;
-  const int64_t lo = (int64_t)n * blockIdx.x / nb, hi = (int64_t)n * (blockIdx.x + 1) / nb;
-  double bv = -INFINITY;
-  int bi = 0x7fffffff;
-  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-    double m;
-    if (i == first) {
-      m = -INFINITY;
-    } else {
-      double s = 0.0;
-      for (int k = 0; k < d; ++k) {
-        const double dk = Xp[i * d + k] - Xp[(int64_t)first * d + k];
-        s += dk * dk;
-      }
-      m = s;
-    }
-    mind2[i] = m;
-    if (m > bv || (m == bv && (int)i < bi)) {
-      bv = m;
-      bi = (int)i;
-    }
-  }
-  sv[threadIdx.x] = bv;
-  si[threadIdx.x] = bi;
-  __syncthreads();
-  for (int s = 128; s > 0; s >>= 1) {
-    if (threadIdx.x < s) {
-      const double ov = sv[threadIdx.x + s];
-      const int oi = si[threadIdx.x + s];
-      if (ov > sv[threadIdx.x] || (ov == sv[threadIdx.x] && oi < si[threadIdx.x])) {
-        sv[threadIdx.x] = ov;
-        si[threadIdx.x] = oi;
-      }
-    }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    pv[blockIdx.x] = sv[0];
-    pi[blockIdx.x] = si[0];
-  }
-}
-
 // m nearest earlier-ordered points of ordered point t, one warp per t: brute force over positions [0, t) with a
 // sorted per-warp list of the m best (squared distance, global index) keys
 __global__ void __launch_bounds__(256) k_knn_earlier(int n, int d, int m, const double* __restrict__ Xo,
@@ -873,7 +870,7 @@ __global__ void __launch_bounds__(256) k_knn_earlier(int n, int d, int m, const 
       double s = 0.0;
       for (int q = 0; q < d; ++q) {
         const double dq = xt[q] - Xo[(int64_t)j * d + q];
-        s += dq * dq;
+        s = __dadd_rn(s, __dmul_rn(dq, dq));
       }
       dj = s;
       ij = order[j];
@@ -929,22 +926,14 @@ void vecchia_sets_gpu(int n, int d, const double* X, int m, int32_t* order, int3
   const int mm = std::min(m, n - 1);
   cudaStream_t st;
   LKG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-  double *dX, *dXp, *dXo, *dmind, *pv;
-  int *pi;
+  double* dX;
   int32_t *dorder, *dnbr;
   valloc(&dX, (size_t)n * d);
-  valloc(&dXp, (size_t)n * d);
-  valloc(&dXo, (size_t)n * d);
-  valloc(&dmind, n);
-  const int nb = std::min(256, std::max(1, ceil_div(n, 1024)));
-  valloc(&pv, 2 * nb);
-  valloc(&pi, 2 * nb);
   valloc(&dorder, n);
   valloc(&dnbr, (size_t)n * std::max(m, 1));
   LKG_CUDA(cudaMemcpyAsync(dX, X, sizeof(double) * n * d, cudaMemcpyHostToDevice, st));
-  k_gather_points<<<ceil_div(n, 256), 256, 0, st>>>(n, d, dX, nullptr, nullptr, dXp);
-  LKG_LAUNCH("k_gather_points");
-  // first point: closest to the centroid (index_min: first minimum), computed on the host in FP64
+  // first point: closest to the centroid (index_min: first minimum), computed on the host in FP64 with the
+  // reference's sequential sums (the host code is built without floating-point contraction)
   std::vector<double> cen(d, 0.0);
   for (int q = 0; q < d; ++q) {
     double s = 0.0;
@@ -964,25 +953,7 @@ void vecchia_sets_gpu(int n, int d, const double* X, int m, int32_t* order, int3
       first = i;
     }
   }
-  LKG_CUDA(cudaMemcpyAsync(dorder, &first, sizeof(int), cudaMemcpyHostToDevice, st));
-  {
-    LaunchTimer lt("k_maxmin_init", st, 3.0 * n * d, 8.0 * n * d);
-    k_maxmin_init<<<nb, 256, 0, st>>>(n, d, dXp, first, dmind, pv, pi);
-    LKG_LAUNCH("k_maxmin_init");
-  }
-  for (int t = 1; t < n; ++t) {
-    const int in = (t - 1) & 1, outb = t & 1;
-    k_maxmin_step<<<nb, 256, 0, st>>>(n, d, dXp, dmind, pv + in * nb, pi + in * nb, pv + outb * nb, pi + outb * nb,
-                                      dorder, t);
-  }
-  LKG_LAUNCH("k_maxmin_step");
-  k_gather_points<<<ceil_div(n, 256), 256, 0, st>>>(n, d, dX, dorder, dXo, dXp);
-  LKG_LAUNCH("k_gather_points");
-  if (m > 0) {
-    LaunchTimer lt("k_knn_earlier", st, 1.5 * n * (double)n * d, 4.0 * n * (double)n * d);
-    k_knn_earlier<<<ceil_div(n, 8), 256, 0, st>>>(n, d, mm, dXo, dorder, dnbr);
-    LKG_LAUNCH("k_knn_earlier");
-  }
+  vecchia_sets_grid(n, d, X, dX, first, m, dorder, dnbr, st);
   LKG_CUDA(cudaMemcpyAsync(order, dorder, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
   std::vector<int32_t> tmp((size_t)n * std::max(mm, 1));
   if (mm > 0)
@@ -990,8 +961,7 @@ void vecchia_sets_gpu(int n, int d, const double* X, int m, int32_t* order, int3
   LKG_CUDA(cudaStreamSynchronize(st));
   for (int t = 0; t < n; ++t)
     for (int a = 0; a < m; ++a) nbr[(size_t)t * m + a] = (a < mm) ? tmp[(size_t)t * mm + a] : -1;
-  for (double* p : {dX, dXp, dXo, dmind, pv}) cudaFree(p);
-  cudaFree(pi);
+  cudaFree(dX);
   cudaFree(dorder);
   cudaFree(dnbr);
   cudaStreamDestroy(st);
@@ -1106,7 +1076,7 @@ bool on_device(const void* p, int dev) {
 
 // first point of the maxmin order (closest to the centroid, lowest index on ties -- the host computation of
 // vecchia_sets_gpu moved to one block), min squared distances set to +inf, and step-0 block maxima that all name
-// that point, so that k_maxmin_step at t = 0 records it and computes the distances k_maxmin_init would
+// that point, so that k_maxmin_step at t = 0 records it and computes the distances to that point
 __global__ void __launch_bounds__(1024) k_sets_prepare(int n, int d, const double* __restrict__ X, int nb,
                                                        double* __restrict__ mind2, double* __restrict__ pv,
                                                        int* __restrict__ pi) {

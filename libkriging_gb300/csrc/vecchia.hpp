@@ -34,6 +34,16 @@ class VecchiaEngine {
 
   // est_beta = false uses beta_fixed (p values), as the reference when m_est_beta is false and m_beta has p entries
   VecchiaOut evaluate(const double* theta, bool with_grad, bool est_beta, const double* beta_fixed);
+
+  // One share of a sharded evaluation (Kriging.cpp:895-922 sums over the ordered points, split by position):
+  // evaluate only the ordered positions [t0, t1) (default: all).
+  void set_range(int t0, int t1);
+  // stage 1 over the range: s1 = [A (p x p, row-major), b (p), sum log v] with A = sum W W'/v, b = sum W u / v;
+  // returns the number of points whose conditional stayed non-SPD after the nugget increments and adds the points
+  // that needed increments to *nugget_points
+  int partial_sums1(const double* theta, bool with_grad, std::vector<double>& s1, long long* nugget_points);
+  // stage 2 over the range, given beta (the last partial_sums1's theta): s2 = [Q, dQ_k (d), sum dv_k / v (d)]
+  void partial_sums2(const double* beta, bool with_grad, std::vector<double>& s2);
   int n() const { return n_; }
   int m() const { return m_; }
   cudaStream_t stream() const { return st_; }
@@ -47,12 +57,26 @@ class VecchiaEngine {
   int* dstatus_ = nullptr;
   double *dpart_ = nullptr, *dbeta_ = nullptr;
   int nblk_red_ = 0;
+  int t0_ = 0, t1_ = 0;
 };
+
+// the host steps between and after the partial sums (shared by evaluate and the sharded form): the GLS beta from the
+// summed stage-1 sums (A + num_nugget I) beta = b (0, or -1 when not positive definite); sigma2 = Q / n, VLL and its
+// gradient from the summed sums; the reference's message for a conditional that stayed non-SPD
+int vecchia_gls_beta(int p, const std::vector<double>& s1, std::vector<double>& beta);
+void vecchia_finish(int n, int d, double slogv, const std::vector<double>& s2, bool with_grad, VecchiaOut& out);
+std::string vecchia_failure_message();
 
 // GPU construction of the Vecchia sets, same definition as make_vecchia_sets: maxmin ordering from the point closest
 // to the centroid (argmin / argmax ties -> lowest index), then the min(m, t) nearest earlier-ordered points by
 // (squared distance, index).  X n x d column-major on the host; outputs host arrays order[n], nbr[n * m].
 void vecchia_sets_gpu(int n, int d, const double* X, int m, int32_t* order, int32_t* nbr);
+
+// The same sets from X on the device (n x d column-major; hX its host copy, for the grids' bounding box) with the
+// maxmin order started at `first`, on uniform grids (vecchia_grid.cu): dorder[n], dnbr[n x min(m, n - 1)].
+// Synchronises `st` before returning (its temporary buffers are freed).
+void vecchia_sets_grid(int n, int d, const double* hX, const double* dX, int first, int m, int32_t* dorder,
+                       int32_t* dnbr, cudaStream_t st);
 
 // predictVecchia's local kriging (Kriging.cpp:950-1022) on the GPU: for each of the q points of Xq (q x d
 // column-major, normalised), the m nearest of the n observations X (n x d column-major) by (squared distance,

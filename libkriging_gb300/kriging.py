@@ -446,3 +446,67 @@ def vecchia_sets(X, m):
     ip = ctypes.POINTER(ctypes.c_int)
     check(_lib.load().lkg_vecchia_sets(n, d, ptr(X), m, order.ctypes.data_as(ip), nbr.ctypes.data_as(ip)))
     return order, nbr
+
+
+class VecchiaShard:
+    """One rank's share of a sharded Vecchia likelihood: the ordered positions [t0, t1) of the sets (order, nbr) of
+    the normalised design (X n x d, y n, F n x p).  See lkg_vecchia_shard_* in the C header."""
+
+    def __init__(self, kernel, X, y, F, order, nbr, t0, t1):
+        L = _lib.load()
+        X = _as_X(X)
+        n, d = X.shape
+        y = f64(np.asarray(y, dtype=np.float64).reshape(-1))
+        F = f64(np.asarray(F, dtype=np.float64).reshape(n, -1))
+        self.d, self.p = d, F.shape[1]
+        self._order = np.ascontiguousarray(order, dtype=np.int32)
+        self._nbr = np.ascontiguousarray(nbr, dtype=np.int32)
+        m = self._nbr.shape[1] if self._nbr.ndim == 2 else 0
+        ip = ctypes.POINTER(ctypes.c_int)
+        self._h = L.lkg_vecchia_shard_new(cstr(kernel), n, d, self.p, ptr(X), ptr(y), ptr(F),
+                                          self._order.ctypes.data_as(ip), self._nbr.ctypes.data_as(ip), m, int(t0),
+                                          int(t1))
+        if not self._h:
+            raise _lib.LibKrigingError(_lib.last_error())
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                _lib.load().lkg_vecchia_shard_delete(h)
+            except Exception:
+                pass
+
+    def sums1(self, theta, return_grad=True):
+        t = np.ascontiguousarray(theta, dtype=np.float64)
+        s1 = np.zeros(self.p * self.p + self.p + 1)
+        npts = ctypes.c_longlong()
+        failed = ctypes.c_int()
+        check(_lib.load().lkg_vecchia_shard_sums1(self._h, ptr(t), int(bool(return_grad)), ptr(s1),
+                                                  ctypes.byref(npts), ctypes.byref(failed)))
+        return s1, int(failed.value), int(npts.value)
+
+    def sums2(self, beta, return_grad=True):
+        b = np.ascontiguousarray(beta, dtype=np.float64)
+        s2 = np.zeros(1 + 2 * self.d)
+        check(_lib.load().lkg_vecchia_shard_sums2(self._h, ptr(b) if b.size else None, int(bool(return_grad)),
+                                                  ptr(s2)))
+        return s2
+
+
+def vecchia_gls_beta(p, s1):
+    """The GLS beta of the summed stage-1 sums: (A + num_nugget I) beta = b (Kriging.cpp:895-905)."""
+    s1 = np.ascontiguousarray(s1, dtype=np.float64)
+    beta = np.zeros(p)
+    check(_lib.load().lkg_vecchia_gls_beta(int(p), ptr(s1), ptr(beta) if p else None))
+    return beta
+
+
+def vecchia_finish(n, d, slogv, s2, return_grad=True):
+    """(vll, sigma2, grad) from the summed stage-2 sums (Kriging.cpp:906-922)."""
+    s2 = np.ascontiguousarray(s2, dtype=np.float64)
+    vll, s2o = ctypes.c_double(), ctypes.c_double()
+    g = np.zeros(d)
+    check(_lib.load().lkg_vecchia_finish(int(n), int(d), float(slogv), ptr(s2), int(bool(return_grad)),
+                                         ctypes.byref(vll), ctypes.byref(s2o), ptr(g)))
+    return vll.value, s2o.value, (g if return_grad else None)

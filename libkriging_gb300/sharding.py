@@ -1,4 +1,4 @@
-"""Multi-GPU sharding of the paths that shard: multistart fits and NestedKriging submodels.
+"""Multi-GPU sharding of the paths that shard: multistart fits, NestedKriging submodels and the Vecchia likelihood.
 
 One process per GPU (torch.distributed, one rank per device).  The units are independent, so there is no data-path
 collective: each rank evaluates its contiguous share of the units on its own GPU, and the host exchanges a few
@@ -47,6 +47,7 @@ def fit_multistart_sharded(make_model, y, X, thetas, regmodel="constant", normal
 
     make_model() -> a fresh model exposing fit(...), theta(), logLikelihood() (a libkriging_gb300.Kriging).
     Every rank returns the same committed model: the best start over all ranks, refitted with optim="none".
+    The returned index is the first start of the winning rank's share.
     """
     import torch.distributed as dist
     rank, world = dist.get_rank(group), dist.get_world_size(group)
@@ -54,14 +55,17 @@ def fit_multistart_sharded(make_model, y, X, thetas, regmodel="constant", normal
     lo, hi = shard_range(thetas.shape[0], rank, world)
     local = []
     P = dict(parameters or {})
-    for i in range(lo, hi):
+    if hi > lo:
+        # the rank's share as ONE multistart fit: every optimiser round of its starts is one batched GPU evaluation,
+        # and the fit keeps the first of its best starts (the reference's strict '<' scan); across ranks the lowest
+        # objective wins with ties to the lowest rank, whose starts come first -- the global first-best start
         m = make_model()
         try:
-            P["theta"] = thetas[i:i + 1]
-            m.fit(y, X, regmodel, normalize, "BFGS", "LL", P)
-            local.append((i, -m.logLikelihood(), np.asarray(m.theta())))
-        except Exception:  # a failed start, as the reference's per-start try/catch
-            local.append((i, float("inf"), None))
+            P["theta"] = thetas[lo:hi]
+            m.fit(y, X, regmodel, normalize, "BFGS%d" % (hi - lo), "LL", P)
+            local.append((lo, -m.logLikelihood(), np.asarray(m.theta())))
+        except Exception:  # every start of the share failed
+            local.append((lo, float("inf"), None))
     idx, obj, theta = select_best(local, group)
     best = make_model()
     P["theta"] = np.asarray(theta).reshape(1, -1)
@@ -177,3 +181,28 @@ def allreduce_sums(values, group=None):
     t = torch.as_tensor(np.asarray(values, dtype=np.float64))
     dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
     return t.numpy()
+
+
+def vecchia_ll_sharded(make_shard, n, d, p, theta, return_grad=True, group=None):
+    """Vecchia log-likelihood (Kriging.cpp:806-924) with the ordered points split over the ranks of `group`.
+
+    make_shard(t0, t1) -> an object with sums1(theta, grad) -> (s1, failed, nugget_points) and
+    sums2(beta, grad) -> s2 over the ordered positions [t0, t1) (libkriging_gb300.VecchiaShard on a GPU).  Two
+    exchanges of partial sums: [A (p x p), b (p), sum log v, failed] before the GLS beta, [Q, dQ_k, sum dv_k / v]
+    after it.  Returns (vll, grad or None, beta, sigma2), identical on every rank."""
+    import torch.distributed as dist
+    from . import _lib
+    from .kriging import vecchia_finish, vecchia_gls_beta
+    rank, world = dist.get_rank(group), dist.get_world_size(group)
+    lo, hi = shard_range(n, rank, world)
+    shard = make_shard(lo, hi)
+    s1, failed, _ = shard.sums1(theta, return_grad)
+    tot1 = allreduce_sums(np.concatenate([s1, [float(failed)]]), group)
+    if tot1[-1] > 0:
+        raise _lib.LibKrigingError("[ERROR] Exceed max numerical nugget added to force chol matrix (%d points)"
+                                   % int(tot1[-1]))
+    s1 = tot1[:-1]
+    beta = vecchia_gls_beta(p, s1)
+    s2 = allreduce_sums(shard.sums2(beta, return_grad), group)
+    vll, sigma2, grad = vecchia_finish(n, d, s1[p * p + p], s2, return_grad)
+    return vll, grad, beta, sigma2

@@ -28,6 +28,28 @@ def test_sets_match_oracle(gpu_lib, n, d, m):
         assert np.sum(nbr[t] >= 0) == min(m, t)
 
 
+@pytest.mark.parametrize("case", ["uniform3", "duplicates", "flat_dim", "d8", "clustered"])
+def test_grid_sets_match_oracle_beyond_the_brute_force_range(gpu_lib, case):
+    """The grid-accelerated order and neighbour sets (positions above 2048 search a grid over a prefix of the order)
+    equal the oracle's O(n^2) restatement exactly, including ties between duplicated points, a degenerate
+    dimension, d = 8 and clustered inputs; neighbours in (squared distance, index) order."""
+    rng = np.random.default_rng(11)
+    n, d, m = 9000, 3, 30
+    if case == "d8":
+        n, d, m = 5000, 8, 16
+    X = rng.uniform(size=(n, d))
+    if case == "duplicates":
+        X[rng.choice(n, 300, replace=False)] = X[rng.choice(n, 300, replace=False)]
+    elif case == "flat_dim":
+        X[:, 1] = 0.5
+    elif case == "clustered":
+        X = np.concatenate([0.01 * rng.standard_normal((n // 2, d)) + 0.3, rng.uniform(size=(n - n // 2, d))])
+    order, nbr = gpu_lib.vecchia_sets(X, m)
+    o_order, o_nbr = O.vecchia_sets(X, m)
+    assert np.array_equal(order, o_order)
+    assert np.array_equal(nbr, o_nbr)
+
+
 @pytest.mark.parametrize("kernel", ["gauss", "matern5_2", "matern3_2", "exp"])
 def test_vll_and_gradient_vs_oracle(gpu_lib, kernel):
     X, y = _data(400, 3, 7)
@@ -140,3 +162,24 @@ def test_light_fit_predict_routes_to_predict_vecchia(gpu_lib):
     assert np.array_equal(m1, m2) and np.array_equal(s1, s2)
     with pytest.raises(Exception, match="light Vecchia fit"):
         k.predict(Xn, True, True, False)
+
+
+def test_vecchia_shards_sum_to_the_single_evaluation(gpu_lib):
+    """The sharded form's device half: two VecchiaShard ranges [0, n/2), [n/2, n) of the model's sets, their partial
+    sums added on the host (what the ranks' all-reduce does), give the single evaluation's VLL and gradient."""
+    from libkriging_gb300.kriging import VecchiaShard, vecchia_finish, vecchia_gls_beta
+    X, y = _data(700, 3, 21)
+    k = gpu_lib.Kriging("matern5_2")
+    k.fit(y, X, "constant", False, "none", "LLVecchia(12)", {"theta": np.full((1, 3), 0.3)})
+    order, nbr = k.vecchia_sets()
+    th = np.array([0.25, 0.3, 0.35])
+    v_ref, g_ref = k.logLikelihoodVecchiaFun(th, True)
+    n, d, p = 700, 3, 1
+    F = np.ones((n, 1))
+    shards = [VecchiaShard("matern5_2", X, y, F, order, nbr, a, b) for a, b in ((0, 350), (350, 700))]
+    s1 = sum(s.sums1(th, True)[0] for s in shards)
+    beta = vecchia_gls_beta(p, s1)
+    s2 = sum(s.sums2(beta, True) for s in shards)
+    vll, sigma2, grad = vecchia_finish(n, d, s1[p * p + p], s2, True)
+    assert rel_err(vll, v_ref) <= 1e-12
+    assert rel_err(grad, g_ref) <= 1e-10
