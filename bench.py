@@ -104,11 +104,10 @@ class ClockSampler:
 
 
 def _digits_note(lib, slices):
-    """Operand precision of the mixed path for `slices` (the engine runs the inverse two slices lower)."""
+    """Operand precision of the mixed path for `slices`: 7-bit digits, slices + 1 (6..8) for the Cholesky and
+    max(5, slices - 2) for the inverse and W^T W."""
     inv = max(4, slices - 2)
-    if lib.lkg_get_tensor_path() == 3:  # 7-bit digits: slices + 1 (6..8) for the Cholesky, slices (5..8) inverse
-        return "Cholesky %d 7-bit digits, inverse %d" % (min(8, max(6, slices + 1)), min(8, max(5, inv)))
-    return "Cholesky %d 8-bit slices, inverse %d" % (slices, inv)
+    return "Cholesky %d 7-bit digits, inverse %d" % (min(8, max(6, slices + 1)), min(8, max(5, inv)))
 
 
 def kernel_stats(lib):
@@ -277,11 +276,15 @@ def run_gpu(args):
         dist.init_process_group("nccl")
     import libkriging_gb300 as lk
     lib = lk.load()
-    if args.tensor_path is not None:
-        lib.lkg_set_tensor_path(args.tensor_path)
+    if args.digit_tile:
+        if lib.lkg_set_digit_tile(args.digit_tile) != args.digit_tile:
+            raise RuntimeError(lk._lib.last_error())
     peak_fp64 = ctypes.c_double()
     if lib.lkg_probe_fp64_peak(ctypes.byref(peak_fp64)) != 0:
         raise RuntimeError("FP64 peak probe failed: " + lk._lib.last_error())
+    peak_dmma = ctypes.c_double()
+    if lib.lkg_probe_dmma_peak(ctypes.byref(peak_dmma)) != 0:
+        raise RuntimeError("DMMA peak probe failed: " + lk._lib.last_error())
     X, y, theta, alpha = make_inputs(args.n)
     gamma = np.concatenate([theta, [alpha]])
     k = lk.Kriging("matern5_2", "nugget")
@@ -331,7 +334,9 @@ def run_gpu(args):
                 config=dict(workload="dense LL+grad, n=%d, d=8, matern5_2, nugget 1e-6" % args.n,
                             precision="mixed: O(n^3) products on bf16 tensor cores by error-free digit splitting "
                                       "(%s), FP64 panels and reductions" % _digits_note(lib, used),
-                            digit_products="tcgen05" if lib.lkg_get_tensor_path() else "mma.sync",
+                            digit_products="tcgen05, 7-bit digits, 128x%d tiles, %s" % (
+                                lib.lkg_get_digit_tile(), "two TMEM accumulator sets" if lib.lkg_get_digit_tile() == 32
+                                else "one TMEM accumulator set"),
                             parallelism="replicas" if world > 1 else "single GPU",
                             l2="inputs larger than L2 (R, L^-1, R^-1: 3 x %.2f GB)" % (8.0 * args.n * args.n / 1e9)),
                 e2e=dict(value=world / e2e_s, unit=UNIT, h2d_bytes_per_step=8 * gamma.size,
@@ -347,7 +352,7 @@ def run_gpu(args):
                 wall_s_timed_region=wall_value,
                 measured_peaks={k2: v for k2, v in peaks.items() if k2 in ("hbm_gbs", "bf16_tflops",
                                                                            "bf16_tflops_sustained")},
-                fp64_peak_tflops=peak_fp64.value,
+                fp64_peak_tflops=peak_fp64.value, fp64_dmma_tflops=peak_dmma.value,
                 stage_ms={kk: round(v, 3) for kk, v in stage.items()}, kernels=_kern(stats),
                 kernel_stats_steps=stats_steps)
     if rank == 0 and world == 1 and not args.no_batched:
@@ -652,12 +657,11 @@ def main():
     ap.add_argument("--nested-n", type=int, default=1_000_000, help="points of the nested workload")
     ap.add_argument("--nested-q", type=int, default=100_000, help="gPoE prediction points of the nested workload")
     ap.add_argument("--no-batched", action="store_true", help="omit the batched multistart sub-record")
+    ap.add_argument("--digit-tile", type=int, default=0, choices=[0, 32, 64],
+                    help="output tile width of the digit products (0: the library's default)")
     ap.add_argument("--batched-steps", type=int, default=2, help="timed BFGS64 fits of the batched sub-record")
     ap.add_argument("--ref-budget-s", type=float, default=300.0,
                     help="reference arm: stop timing full CPU evaluations once the next would pass this many s")
-    ap.add_argument("--tensor-path", type=int, default=None, choices=[0, 1, 2, 3],
-                    help="digit-product kernels of the mixed path: 0 mma.sync, 1 tcgen05 (W^T W on mma.sync), 2 "
-                         "tcgen05, 3 tcgen05 on 7-bit digits in 256-wide k blocks (default: the library's)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -108,6 +108,23 @@ int lkg_kriging_last_slices(void* ptr);
  * batched launch, so rounds < evaluations there).  Either pointer may be NULL. */
 int lkg_kriging_eval_counts(void* ptr, long long* evaluations, long long* rounds);
 
+/* No counterpart in the reference: the project's autotuner.  lkg_kriging_autotune_precision picks the fastest
+ * precision of this model's objective -- 0 (FP64) or 5..7 slices of the mixed path -- whose LL and gradient at gamma
+ * stay within tol_ll / tol_grad (relative, with a 10x margin) of the FP64 path's, by timing each candidate on the
+ * GPU; it sets that precision and returns it (-1 on error).  Choices are tabled per problem shape and tolerance
+ * (and persisted to $LKG_TUNE_FILE when set); LKG_AUTOTUNE=0 or lkg_autotune_enable(0) turns measuring off.
+ * lkg_autotune_record tables a choice from given costs (lowest finite cost, ties to the earlier candidate) and
+ * returns it; lkg_autotune_lookup returns a tabled choice or `fallback`; lkg_autotune_report writes
+ * "key<TAB>choice<TAB>cost<LF>" lines and returns the size needed; save / load / clear manage the table. */
+int lkg_kriging_autotune_precision(void* ptr, const double* gamma, int gamma_n, double tol_ll, double tol_grad);
+void lkg_autotune_enable(int on);
+int lkg_autotune_record(const char* key, const int* candidates, const double* costs, int n);
+int lkg_autotune_lookup(const char* key, int fallback);
+int lkg_autotune_report(char* out, int cap);
+int lkg_autotune_save(const char* path);
+int lkg_autotune_load(const char* path);
+void lkg_autotune_clear(void);
+
 /* Vecchia approximation (objective "LLVecchia" / "LLVecchia(m)" of lkg_kriging_fit[_params]).  The reference
  * exposes these through its C++ Kriging class only (Kriging.hpp:145-173; no lk_* counterpart):
  *   logLikelihoodVecchiaFun(theta, return_grad) -> (vll, grad)  Kriging.hpp:145-150, Kriging.cpp:926-941
@@ -218,6 +235,9 @@ const char* lkg_device_name(void);
 /* No counterpart in the reference: measured FP64 FMA throughput (TFLOP/s) of this GPU, the roofline denominator of
  * the FP64 kernels (the DFMA pipe; FP64 mma.sync is slower on GB300). */
 int lkg_probe_fp64_peak(double* tflops_out);
+/* No counterpart in the reference: measured FP64 tensor-core (DMMA, mma.sync m8n8k4 f64) throughput in TFLOP/s --
+ * the comparison that decides whether the FP64 tiles use DFMA or DMMA on this part. */
+int lkg_probe_dmma_peak(double* tflops_out);
 /* No counterpart in the reference (it times stages with Bench::tic/toc, src/lib/Bench.cpp): per-kernel launch
  * counts, and with timing enabled CUDA-event durations on each launch's own stream plus the launch's algorithmic
  * flops and bytes.  lkg_stats_report writes "name<TAB>launches<TAB>timed<TAB>ms<TAB>flops<TAB>bytes<LF>" lines and
@@ -226,17 +246,19 @@ void lkg_stats_enable(int on);
 void lkg_stats_reset(void);
 int lkg_stats_report(char* out, int cap);
 /* No counterpart in the reference: C = A B^T (A M x K, B N x K, C M x N, column-major host buffers) through the
- * split-bf16 tensor-core GEMM with `slices` digits -- the check hook of the mixed path's emulated products.  On
- * tensor path 3, as in the engine, `slices` 8-bit slices become min(8, max(6, slices + 1)) 7-bit digits. */
+ * split-bf16 tensor-core GEMM -- the check hook of the mixed path's emulated products.  As in the engine, the
+ * precision's `slices` become min(8, max(5, slices + 1)) 7-bit digits. */
 int lkg_ozaki_gemm_check(int M, int N, int K, const double* A, const double* B, int slices, double* C);
-/* No counterpart in the reference: the kernels of the mixed path's digit products -- 0 = mma.sync (warp-level),
- * 1 = tcgen05 (TMEM accumulators) for the Cholesky and triangular-inverse updates with W^T W on mma.sync, 2 =
- * tcgen05 for all three, 3 = tcgen05 on 7-bit digits with one exponent per 256-wide k block and two-level (256 / 64)
- * blocked Cholesky and triangular inverse, one digit more than the precision's slice count (the default: the
- * fastest on this part).  Returns the path now in effect; the environment variable LK_OZAKI_TC sets the initial
- * value. */
+/* No counterpart in the reference: the kernels of the mixed path's digit products.  One family remains: 3 =
+ * tcgen05 on 7-bit digits with one exponent per 256-wide k block and two-level (256 / 64) blocked Cholesky and
+ * triangular inverse.  lkg_set_tensor_path returns 3, or -1 for any other value. */
 int lkg_set_tensor_path(int tc);
 int lkg_get_tensor_path(void);
+/* No counterpart in the reference: output tile width of the digit products, 32 (two TMEM accumulator sets, so the
+ * fold of one tile overlaps the products of the next; the default) or 64 (one set; every A digit image serves
+ * twice the columns).  Returns the width set, or -1 for another value. */
+int lkg_set_digit_tile(int tn);
+int lkg_get_digit_tile(void);
 /* No counterpart in the reference: one product of the 7-bit digit kernel on host data, S digits (5..8):
  * mode 0: C (M x N) = A B^T (A M x K, B N x K); mode 1: C = A A^T lower (M x M); mode 2: C = W^T W lower with
  * W = A (M x M, lower).  Returns 0, -1 (error text in lkg_get_last_error) or -2 when a wait of the kernel expired

@@ -89,6 +89,7 @@ _SIGS = {
     "lkg_optim_set_max_restart": (None, [_i]),
     "lkg_device_name": (_cp, []),
     "lkg_probe_fp64_peak": (_i, [_dp]),
+    "lkg_probe_dmma_peak": (_i, [_dp]),
     "lkg_stats_enable": (None, [_i]),
     "lkg_stats_reset": (None, []),
     "lkg_stats_report": (_i, [ctypes.c_char_p, _i]),
@@ -96,6 +97,14 @@ _SIGS = {
     "lkg_kriging_get_precision": (_i, [_vp]),
     "lkg_kriging_last_slices": (_i, [_vp]),
     "lkg_kriging_eval_counts": (_i, [_vp, _vp, _vp]),
+    "lkg_kriging_autotune_precision": (_i, [_vp, _dp, _i, _d, _d]),
+    "lkg_autotune_enable": (None, [_i]),
+    "lkg_autotune_record": (_i, [_cp, _ip, _dp, _i]),
+    "lkg_autotune_lookup": (_i, [_cp, _i]),
+    "lkg_autotune_report": (_i, [ctypes.c_char_p, _i]),
+    "lkg_autotune_save": (_i, [_cp]),
+    "lkg_autotune_load": (_i, [_cp]),
+    "lkg_autotune_clear": (None, []),
     "lkg_ozaki_gemm_check": (_i, [_i, _i, _i, _dp, _dp, _i, _dp]),
     "lkg_kriging_log_likelihood_vecchia_fun": (_i, [_vp, _dp, _i, _i, _dp, _dp]),
     "lkg_kriging_set_vecchia_exact_commit": (_i, [_vp, _i]),
@@ -106,6 +115,8 @@ _SIGS = {
     "lkg_kriging_predict_vecchia": (_i, [_vp, _dp, _i, _i, _i, _i, _dp, _dp]),
     "lkg_set_tensor_path": (_i, [_i]),
     "lkg_get_tensor_path": (_i, []),
+    "lkg_set_digit_tile": (_i, [_i]),
+    "lkg_get_digit_tile": (_i, []),
     "lkg_vecchia_sets_noalloc": (_i, [_i, _i, _vp, _i, _vp, _vp, _vp]),
     "lkg_vecchia_shard_new": (_vp, [_cp, _i, _i, _i, _dp, _dp, _dp, _ip, _ip, _i, _i, _i]),
     "lkg_vecchia_shard_delete": (None, [_vp]),

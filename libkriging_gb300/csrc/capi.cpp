@@ -522,6 +522,12 @@ int lkg_kriging_last_slices(void* ptr) {
   });
 }
 
+int lkg_kriging_autotune_precision(void* ptr, const double* gamma, int gamma_n, double tol_ll, double tol_grad) {
+  return run_entry<int>(-1, [&]() -> int {
+    return K(ptr)->autotune_precision(std::vector<double>(gamma, gamma + gamma_n), tol_ll, tol_grad);
+  });
+}
+
 int lkg_kriging_eval_counts(void* ptr, long long* evaluations, long long* rounds) {
   return run_entry<int>(-1, [&]() -> int {
     const Kriging* k = K(ptr);

@@ -47,15 +47,15 @@ void copy_dinv_block(const double* Dinv, int64_t dinv_bstride, int blk, double* 
                      int k0, int nb, int batch, cudaStream_t st);
 
 // Mixed-precision variants (trailing updates, trtri updates and W^T W on the bf16 tensor cores by error-free
-// splitting into `slices` digit planes, see ozaki.cuh); diagonal blocks, panels and small products stay FP64.
+// splitting into 7-bit digit planes, see ozaki7.cuh); the diagonal blocks stay FP64.
 struct MixedWorkspace {
   int slices = 7;      // digit slices of the Cholesky's trailing updates
   int slices_inv = 6;  // digit slices of the triangular inverse and W^T W (gradient only)
-  void* panel = nullptr;  // bf16 planes, split_plane_elems(n, 64, slices) per batch entry
+  void* panel = nullptr;  // bf16 planes, oz7_plane_elems(n, 256, 8) per batch entry
   int* panel_exp = nullptr;
   void* rowblk = nullptr;  // bf16 planes, same size
   int* rowblk_exp = nullptr;
-  void* wfull = nullptr;  // bf16 planes, split_plane_elems(n, n, slices) per batch entry
+  void* wfull = nullptr;  // bf16 planes, oz7_plane_elems(n, n, digits) per batch entry
   int* wfull_exp = nullptr;
   int n = 0;
 };

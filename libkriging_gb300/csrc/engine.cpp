@@ -17,7 +17,6 @@
 #include "common.cuh"
 #include "dense_fp64.cuh"
 #include "lik_kernels.cuh"
-#include "ozaki.cuh"
 #include "ozaki7.cuh"
 
 namespace lkg {
@@ -178,10 +177,9 @@ void Engine::ensure_mixed_buffers(bool with_grad) {
       }
     mixed_alloc_slices_ = slices_;
   }
-  // sized for both forms of the digit products: 8-bit digits in 64-wide chunks, or up to 8 7-bit digits in
-  // 256-wide blocks (ozaki7.cuh)
-  const size_t pe = std::max(split_plane_elems(n_, NB, slices_), oz7_plane_elems(n_, OZ7_KB, 8)) * cap_;
-  const size_t ee = std::max(split_exp_elems(n_, NB), oz7_exp_elems(n_, OZ7_KB, OZ7_KB)) * cap_;
+  // up to 8 7-bit digits of a 256-wide panel per batch entry (ozaki7.cuh)
+  const size_t pe = oz7_plane_elems(n_, OZ7_KB, 8) * cap_;
+  const size_t ee = oz7_exp_elems(n_, OZ7_KB, OZ7_KB) * cap_;
   if (!dpanel_) {
     LKG_CUDA(cudaMalloc(&dpanel_, pe * 2));
     LKG_CUDA(cudaMalloc(&drowblk_, pe * 2));
@@ -189,8 +187,8 @@ void Engine::ensure_mixed_buffers(bool with_grad) {
     dalloc(&drowblk_exp_, ee);
   }
   if (with_grad && !dwfull_) {
-    LKG_CUDA(cudaMalloc(&dwfull_, std::max(split_plane_elems(n_, n_, slices_), oz7_plane_elems(n_, n_, std::min(8, slices_ + 1))) * cap_ * 2));
-    dalloc(&dwfull_exp_, std::max(split_exp_elems(n_, n_), oz7_exp_elems(n_, n_, OZ7_KB)) * cap_);
+    LKG_CUDA(cudaMalloc(&dwfull_, oz7_plane_elems(n_, n_, std::min(8, slices_ + 1)) * cap_ * 2));
+    dalloc(&dwfull_exp_, oz7_exp_elems(n_, n_, OZ7_KB) * cap_);
   }
 }
 
@@ -549,9 +547,7 @@ void Engine::evaluate(int batch, const double* thetas, const double* factors, bo
     LKG_CUDA(cudaMemcpyAsync(adj.data(), dadj_, sizeof(double) * adj.size(), cudaMemcpyDeviceToHost, st_));
   }
   LKG_CUDA(cudaStreamSynchronize(st_));
-  if (slices_ > 0 && ozaki_tensor_path() && ozaki_tc_error_and_reset())
-    throw std::runtime_error("mixed path: a tensor-core digit product did not complete (timed out)");
-  if (slices_ > 0 && ozaki_tensor_path() == 3 && oz7_error_and_reset())
+  if (slices_ > 0 && oz7_error_and_reset())
     throw std::runtime_error("mixed path: a tensor-core digit product did not complete (timed out)");
   for (int b = 0; b < batch; ++b) {
     EvalOut& o = out[b];

@@ -10,6 +10,8 @@
 // batcher into ONE batched GPU evaluation per round (the reference runs the starts one after another).
 #include "kriging.hpp"
 
+#include "autotune.hpp"
+
 #include <algorithm>
 #include <cmath>
 #include <condition_variable>
@@ -273,6 +275,44 @@ std::tuple<double, std::vector<double>> Kriging::logLikelihoodFun(const std::vec
   std::vector<double> grad;
   const double ll = loglik_from(out[0], extra, return_grad ? &grad : nullptr, (int)gamma.size());
   return {ll, grad};
+}
+
+int Kriging::autotune_precision(const std::vector<double>& gamma, double tol_ll, double tol_grad) {
+  if (!(tol_ll > 0.0) || !(tol_grad > 0.0)) throw std::invalid_argument("autotune_precision: tolerances must be > 0");
+  const int saved = m_slices;
+  std::ostringstream key;
+  key.precision(3);
+  key << "precision:k=" << m_kernel << ":nm=" << (m_noise_model == NoiseModel::Nugget ? 1 : 0) << ":n=" << m_n
+      << ":d=" << m_d << ":tol=" << tol_ll << "," << tol_grad;
+  // the FP64 reference values, then each candidate timed (the second of two evaluations) and checked
+  set_precision(0);
+  auto [ll64, g64] = logLikelihoodFun(gamma, true, false);
+  double gnorm = 0.0;
+  for (double v : g64) gnorm += v * v;
+  gnorm = std::sqrt(gnorm);
+  auto cost = [&](int slices) -> double {
+    set_precision(slices);
+    double ms = 0.0;
+    std::vector<double> g;
+    double ll = 0.0;
+    for (int rep = 0; rep < 2; ++rep) {
+      auto r = logLikelihoodFun(gamma, true, true);
+      ll = std::get<0>(r);
+      g = std::get<1>(r);
+      ms = 0.0;
+      for (const auto& kv : m_bench) ms += kv.second;
+    }
+    if (slices == 0) return ms;
+    if (m_last_slices != slices) return std::numeric_limits<double>::infinity();  // retreated to FP64
+    double dg = 0.0;
+    for (size_t i = 0; i < g.size(); ++i) dg += (g[i] - g64[i]) * (g[i] - g64[i]);
+    const double e_ll = std::fabs(ll - ll64) / std::max(std::fabs(ll64), 1e-300);
+    const double e_g = std::sqrt(dg) / std::max(gnorm, 1e-300);
+    return (e_ll * 10.0 <= tol_ll && e_g * 10.0 <= tol_grad) ? ms : std::numeric_limits<double>::infinity();
+  };
+  const int choice = Autotuner::instance().choose(key.str(), {0, 5, 6, 7}, saved, cost);
+  set_precision(choice);
+  return choice;
 }
 
 void Kriging::logLikelihoodFunBatch(const Mat& gammas, bool return_grad, std::vector<double>& ll,

@@ -159,6 +159,10 @@ class Kriging {
   int precision() const { return m_slices; }
   // mixed-path bookkeeping of the last logLikelihoodFun: slices used (0 = FP64, also after a retreat)
   int last_slices() const { return m_last_slices; }
+  // The fastest precision (0 = FP64, or 5..7 slices of the mixed path) whose logLikelihoodFun(gamma, grad) stays
+  // within tol_ll / tol_grad (relative) of the FP64 path's, measured on this model (CUDA-event timings, errors with a
+  // 10x margin); tabled by the autotuner under the problem's shape and the tolerances, then set as the precision.
+  int autotune_precision(const std::vector<double>& gamma, double tol_ll, double tol_grad);
   // route the fit's objective evaluations through a shared service (design = this model's index there); nullptr
   // restores the model's own engine
   void attach_service(DenseService* s, int design) {

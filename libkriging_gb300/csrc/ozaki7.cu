@@ -7,8 +7,9 @@
 // so a digit product is below 2^12 in magnitude and the sum over i + j = g of up to S products over the 256 columns
 // of a block stays below S * 256 * 2^12 <= 2^23: every FP32 tensor-core accumulator is an exact integer.  Products
 // with i + j <= S + 1 are formed (S (S + 1) / 2 bf16 GEMMs per block), one accumulator per diagonal g, and the S
-// diagonals are folded into FP64 once per block: Horner in base 128 over g = 2..5 and g = 6..S+1 (int64), one
-// 128-bit integer, one correctly rounded conversion.  S = 8 gives 56-bit operands (FP64-level products); S = 5
+// diagonals are folded into FP64 once per block: adjacent diagonals paired in int32, the exact sum split into two
+// integers below 2^46 that are exact doubles, one correctly rounded FP64 addition.  S = 8 gives 56-bit operands
+// (FP64-level products); S = 5
 // (35 bits) serves the triangular inverse and W^T W, which feed only the gradient.
 //
 // Data layout: the split writes each (digit, 64-wide k sub-chunk, 128-row tile) as the 16 KB shared-memory image of
@@ -21,9 +22,10 @@
 //   warp 1        TMEM allocation (512 columns = S diagonals x 64 columns); one thread issues tcgen05.mma
 //                 (M 128, N 64 k, K 16): A digit i against up to 4 adjacent B digits at once, and releases each A
 //                 stage and B buffer with tcgen05.commit
-//   warps 2..17   epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 (rows) and 16 columns, 4 at a time:
-//                 Horner-folds the S diagonals, converts to FP64 and updates C, then releases TMEM to the next
-//                 block (18 warps leave 96 registers a thread: a sub-partition holds 5 warps of its 16K registers)
+//   warps 2..17   epilogue: warp w reads TMEM lanes 32 (w % 4) .. +31 (rows) and 8 columns, 4 at a time:
+//                 folds the S diagonals exactly (int32 pairs, two exact doubles, one rounded FP64 addition) and
+//                 updates C, then releases its accumulator set to the next block (18 warps leave 96 registers a
+//                 thread: a sub-partition holds 5 warps of its 16K registers)
 // All mbarrier waits are bounded; on expiry the CTA records an error (oz7_error_and_reset), drains what it issued and
 // returns.
 #include "ozaki7.cuh"
@@ -36,19 +38,25 @@ void set_last_error(const char* msg);
 
 namespace {
 
-constexpr int TM = 128, TN = 32;
+constexpr int TM = 128;
 constexpr int NA_MAX = 10;                     // A ring stages at most
 constexpr uint32_t A_BYTES = TM * 128;         // one digit of a 128-row tile, one 64-wide sub-chunk: 16 KB
-constexpr uint32_t B_BYTES = TN * 128;         // 32-row tile: 4 KB
 constexpr uint64_t kWaitNs = 200000000ull;     // an mbarrier wait gives up after 200 ms
-constexpr uint32_t TMEM_SET = 256;             // two accumulator sets of S x 32 columns (S <= 8) in 512 columns
 
-// A ring depth for S digits: what 227 KB of shared memory holds beside the two B buffers (10 for S = 8); a deep ring
-// keeps enough digit images in flight to cover the L2 latency at the rate the MMAs consume them
-template <int S>
+// Output tiles are 128 x TN.  TN = 32: two accumulator sets of S x 32 TMEM columns, so the fold of one tile overlaps
+// the products of the next; TN = 64: one set of S x 64 columns (each A digit image serves twice the columns, the fold
+// waits for the products).  The tile width is chosen per launch (oz7_set_tile).
+template <int TN>
+constexpr uint32_t b_bytes() { return TN * 128; }  // one digit of a TN-row B tile, one 64-wide sub-chunk
+template <int S, int TN>
+constexpr int nsets() { return 2 * S * TN <= 512 ? 2 : 1; }
+
+// A ring depth: what 227 KB of shared memory holds beside the two B buffers (10 for TN = 32, 6 for TN = 64 at
+// S = 8); a deep ring keeps enough digit images in flight to cover the L2 latency at the rate the MMAs consume them
+template <int S, int TN>
 constexpr int ring_depth() {
-  return (int)((227u * 1024u - 1024u - 2u * S * B_BYTES) / A_BYTES) < NA_MAX
-             ? (int)((227u * 1024u - 1024u - 2u * S * B_BYTES) / A_BYTES)
+  return (int)((227u * 1024u - 1024u - 2u * S * b_bytes<TN>()) / A_BYTES) < NA_MAX
+             ? (int)((227u * 1024u - 1024u - 2u * S * b_bytes<TN>()) / A_BYTES)
              : NA_MAX;
 }
 constexpr int NTHREADS = 576;                  // 18 warps
@@ -56,8 +64,8 @@ constexpr int NTHREADS = 576;                  // 18 warps
 __device__ int g_oz7_error;
 __device__ int g_oz7_where[8];  // first expired wait: role, tile, k block, sub-chunk, digit, and the role's counters
 
-// instruction descriptor of tcgen05.mma kind::f16: D FP32, A and B bf16, both K-major, M = 128, N = 32 k (the B
-// digits 1 .. k side by side, up to N = 256)
+// instruction descriptor of tcgen05.mma kind::f16: D FP32, A and B bf16, both K-major, M = 128, N = TN k (k B
+// digits side by side, up to N = 256)
 __host__ __device__ constexpr uint32_t idesc_n(int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
 }
@@ -139,34 +147,39 @@ __device__ __forceinline__ void mma_commit(uint32_t mbar) {
                : "memory");
 }
 
-// exact value of the signed 128-bit integer H times 2^E, rounded to nearest (ties to even)
-__device__ __forceinline__ double i128_to_double(__int128 H, int E) {
-  if (H == 0) return 0.0;
-  const bool neg = H < 0;
-  const unsigned __int128 u = neg ? (unsigned __int128)(-H) : (unsigned __int128)H;
-  const unsigned long long hi = (unsigned long long)(u >> 64), lo = (unsigned long long)u;
-  const int p = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)lo);  // top bit
-  unsigned long long mant;
-  int e = p;
-  if (p <= 52) {
-    mant = lo << (52 - p);
-  } else {
-    const int sh = p - 52;
-    mant = (unsigned long long)(u >> sh);
-    const unsigned __int128 rem = u & (((unsigned __int128)1 << sh) - 1);
-    const unsigned __int128 half = (unsigned __int128)1 << (sh - 1);
-    if (rem > half || (rem == half && (mant & 1ull))) {
-      ++mant;
-      if (mant >> 53) {
-        mant >>= 1;
-        ++e;
-      }
-    }
-  }
-  const int fld = e + E + 1023;
-  if (fld <= 0 || fld >= 2047) return ldexp(neg ? -(double)u : (double)u, E);
+// x 2^e for an integer |x| < 2^53, built from its bits with integer instructions (FP64 issue is scarce on this
+// part): exact whenever the result is a normal number; the rare out-of-range case goes through ldexp
+__device__ __forceinline__ double exact_scaled(long long x, int e) {
+  if (x == 0) return 0.0;
+  const unsigned long long sgn = (unsigned long long)x & 0x8000000000000000ull;
+  const unsigned long long u = x < 0 ? (unsigned long long)(-x) : (unsigned long long)x;
+  const int p = 63 - __clzll((long long)u);  // top bit (<= 52)
+  const int fld = p + e + 1023;
+  if (fld <= 0 || fld >= 2047) return ldexp((double)x, e);
   return __longlong_as_double(
-      (long long)((neg ? 0x8000000000000000ull : 0ull) | ((unsigned long long)fld << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+      (long long)(sgn | ((unsigned long long)fld << 52) | ((u << (52 - p)) & 0xFFFFFFFFFFFFFull)));
+}
+
+// The block's exact product H = sum_g v_g 128^(S + 1 - g) (v_g the FP32 diagonal sums, g = 2 .. S + 1, exact
+// integers with |v_g| <= (g - 1) 2^20) times 2^E, correctly rounded: adjacent diagonals first combine in int32
+// (v_g 128 + v_(g+1) < 2^31), then H = hi 2^28 + lo with lo the last four diagonals and hi the first S - 4, both
+// below 2^46 and so exact as doubles; one FP64 addition rounds their sum once (ties to even).
+template <int S>
+__device__ __forceinline__ double fold_diagonals(const uint32_t (&v)[S][4], int q, int E) {
+  int iv[S];
+#pragma unroll
+  for (int j = 0; j < S; ++j) iv[j] = __float2int_rn(__uint_as_float(v[j][q]));
+  const long long lo = ((long long)(iv[S - 4] * 128 + iv[S - 3]) << 14) + (iv[S - 2] * 128 + iv[S - 1]);
+  long long hi;
+  if constexpr (S == 8)
+    hi = ((long long)(iv[0] * 128 + iv[1]) << 14) + (iv[2] * 128 + iv[3]);
+  else if constexpr (S == 7)
+    hi = ((long long)iv[0] << 14) + (iv[1] * 128 + iv[2]);
+  else if constexpr (S == 6)
+    hi = iv[0] * 128 + iv[1];
+  else
+    hi = iv[0];
+  return exact_scaled(hi, E + 28) + exact_scaled(lo, E);
 }
 
 // ---------------------------------------------------------------------------------------------------------------
@@ -266,14 +279,16 @@ struct Tile {
   int m0, n0, kb0, kb1;
 };
 
+template <int TN>
 __device__ __forceinline__ bool tile_of(const Oz7Args& g, long long t, Tile& T) {
-  if (g.lower || g.wtw) {  // lower tiles in row-major order: row block I holds the 32-wide column blocks 0 .. 4 I + 3
-    // I = max { I : 2 I (I + 1) <= t } from an FP32 estimate and integer corrections (FP64 is scarce here)
-    int I = (int)((sqrtf(2.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
-    while (2ll * (I + 1) * (I + 2) <= t) ++I;
-    while (I > 0 && 2ll * I * (I + 1) > t) --I;
+  constexpr long long CPB = TM / TN;  // column tiles per 128 columns
+  if (g.lower || g.wtw) {  // lower tiles in row-major order: row block I holds the column tiles 0 .. CPB (I + 1) - 1
+    // I = max { I : CPB I (I + 1) / 2 <= t } from an FP32 estimate and integer corrections (FP64 is scarce here)
+    int I = (int)((sqrtf(8.0f * (float)t / (float)CPB + 1.0f) - 1.0f) * 0.5f);
+    while (CPB * (I + 1) * (I + 2) / 2 <= t) ++I;
+    while (I > 0 && CPB * I * (I + 1) / 2 > t) --I;
     T.m0 = I * TM;
-    T.n0 = (int)(t - 2ll * I * (I + 1)) * TN;
+    T.n0 = (int)(t - CPB * I * (I + 1) / 2) * TN;
   } else {
     const int tx = (g.M + TM - 1) / TM;
     T.m0 = (int)(t % tx) * TM;
@@ -295,12 +310,16 @@ struct Bars {
   uint64_t a_full[NA_MAX], a_empty[NA_MAX], b_full[2], b_empty[2], acc_full[2], acc_empty[2], drain;
 };
 
-template <int S>
+template <int S, int TN>
 __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long ntiles) {
   static_assert(S >= 5 && S <= 8, "digit count");
-  constexpr int NA = ring_depth<S>();
+  static_assert(TN == 32 || TN == 64, "tile width");
+  constexpr int NA = ring_depth<S, TN>();
   static_assert(NA >= 2 && NA <= NA_MAX, "A ring depth");
+  constexpr uint32_t B_BYTES = b_bytes<TN>();
   constexpr uint32_t B_BUF = S * B_BYTES;
+  constexpr int NSET = nsets<S, TN>();
+  constexpr uint32_t TMEM_SET = S * TN;  // columns of one accumulator set
   extern __shared__ unsigned char oz7_raw[];
   __shared__ Bars bars;
   __shared__ uint32_t tslot;
@@ -352,7 +371,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
       last_fill_b[0] = last_fill_b[1] = -1;
       for (long long ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
         Tile T;
-        if (!tile_of(g, ti, T)) continue;
+        if (!tile_of<TN>(g, ti, T)) continue;
         const int tA = T.m0 / TM, tB = T.n0 / TM, hB = T.n0 % TM;
         for (int kb = T.kb0; kb < T.kb1 && ok; ++kb) {
           const int s1 = min((kb + 1) * spb, g.SA.nsub);
@@ -401,12 +420,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
       bool issued = false;
       for (long long ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
         Tile T;
-        if (!tile_of(g, ti, T)) continue;
+        if (!tile_of<TN>(g, ti, T)) continue;
         for (int kb = T.kb0; kb < T.kb1 && ok; ++kb) {
-          // accumulator set uacc & 1: the epilogue releases set s after folding the block that used it, so the
-          // products of this block overlap the fold of the previous one
-          const int set = uacc & 1;
-          if (!mbar_wait(bar(bars.acc_empty[set]), ((uacc >> 1) & 1) ^ 1)) {
+          // accumulator set uacc % NSET: the epilogue releases a set after folding the block that used it (with two
+          // sets the products of this block overlap the fold of the previous one)
+          const int set = NSET == 2 ? (int)(uacc & 1) : 0;
+          const uint32_t use = NSET == 2 ? (uacc >> 1) : uacc;  // uses of this set before this one
+          if (!mbar_wait(bar(bars.acc_empty[set]), (use & 1) ^ 1)) {
             record_expiry(3, ti, kb, -1, -1, ua, ub, uacc);
             ok = false;
             break;
@@ -436,14 +456,20 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
               }
               asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
               const uint64_t adesc0 = sdesc(sA + st * A_BYTES);
-              // A digit i meets B digits 1 .. S + 1 - i: adjacent 32-row blocks of one K-major operand, whose
-              // diagonals i + 1 .. S + 1 are adjacent 32-column blocks of TMEM -- one MMA of N = 32 (S + 1 - i)
-              const uint32_t d = tset + (uint32_t)((i - 1) * TN);
-              const uint32_t idesc = idesc_n(TN * (S + 1 - i));
+              // A digit i meets B digits 1 .. S + 1 - i: adjacent TN-row blocks of one K-major operand, whose
+              // diagonals i + 1 .. S + 1 are adjacent TN-column blocks of TMEM -- MMAs of up to N = 256 (256 / TN
+              // digits each: one MMA for TN = 32)
 #pragma unroll
-              for (int kk = 0; kk < 4; ++kk)
-                mma_issue(d, adesc0 + (uint64_t)(2 * kk), bdesc0 + (uint64_t)(2 * kk), idesc,
-                          (!first_sub || i > 1 || kk > 0) ? 1u : 0u);
+              for (int j0 = 1; j0 <= S + 1 - i; j0 += 256 / TN) {
+                const int k = (S + 2 - i - j0) < 256 / TN ? (S + 2 - i - j0) : 256 / TN;
+                const uint32_t d = tset + (uint32_t)((i + j0 - 2) * TN);
+                const uint64_t bdesc = bdesc0 + (uint64_t)((j0 - 1) * (B_BYTES >> 4));
+                const uint32_t idesc = idesc_n(TN * k);
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk)
+                  mma_issue(d, adesc0 + (uint64_t)(2 * kk), bdesc + (uint64_t)(2 * kk), idesc,
+                            (!first_sub || i > 1 || kk > 0) ? 1u : 0u);
+              }
               mma_commit(bar(bars.a_empty[st]));
               issued = true;
               ++ua;
@@ -466,7 +492,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
   } else {
     // ------------------------------- epilogue -------------------------------
     // 16 warps: warp w owns TMEM lanes 32 (w % 4) .. +31 (rows) and the 8 columns 8 cg .. +7, taken 4 at a time:
-    // the S diagonals of 4 columns are loaded together, Horner-folded, converted and added into C.
+    // the S diagonals of 4 columns are loaded together, folded exactly, rounded once and added into C.
     constexpr int CPW = TN / 4;  // columns per epilogue warp
     const int quarter = w & 3, cg = (w - 2) >> 2;
     const uint32_t tl0 = tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(cg * CPW);
@@ -475,10 +501,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
     uint32_t uacc = 0;
     for (long long ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
       Tile T;
-      if (!tile_of(g, ti, T)) continue;
+      if (!tile_of<TN>(g, ti, T)) continue;
       const int row = T.m0 + 32 * quarter + lane, col0 = T.n0 + cg * CPW;
       for (int kb = T.kb0; kb < T.kb1 && ok; ++kb) {
-        const int set = uacc & 1;
+        const int set = NSET == 2 ? (int)(uacc & 1) : 0;
+        const uint32_t use = NSET == 2 ? (uacc >> 1) : uacc;
         const uint32_t tl = tl0 + (uint32_t)set * TMEM_SET;
         const bool first = (kb == T.kb0);
         const bool need_c = !(first && g.beta == 0.0);
@@ -497,7 +524,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
         // C = beta C + alpha P in one FP64 operation where the coefficients allow it
         const int upd = !need_c ? (g.alpha == 1.0 ? 0 : 1)
                                 : ((!first || g.beta == 1.0) ? (g.alpha == -1.0 ? 2 : (g.alpha == 1.0 ? 3 : 4)) : 5);
-        const bool got = mbar_wait(bar(bars.acc_full[set]), (uacc >> 1) & 1);
+        const bool got = mbar_wait(bar(bars.acc_full[set]), use & 1);
         if (!__all_sync(0xffffffffu, got)) {
           if (lane == 0) record_expiry(6 + 16 * w, ti, kb, -1, -1, 0, 0, uacc);
           ok = false;
@@ -531,20 +558,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
           asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
-            long long h1 = 0, h2 = 0;
-#pragma unroll
-            for (int dg = 2; dg <= S + 1; ++dg) {
-              const long long iv = (long long)__float2int_rn(__uint_as_float(v[dg - 2][q]));
-              if (dg <= 5)
-                h1 = h1 * 128 + iv;
-              else
-                h2 = h2 * 128 + iv;
-            }
             const int col = col0 + q0 + q;
             if (row < g.M && col < g.N && (!tri || row >= col)) {
-              // H = h1 128^(S-4) + h2: the block's exact product in units 2^(er + ec - 7 (S + 1))
-              const __int128 H = ((__int128)h1 << (7 * (S - 4))) + (__int128)h2;
-              const double val = i128_to_double(H, er + ec[q] - 7 * (S + 1));
+              // the block's exact product, in units 2^(er + ec - 7 (S + 1)), rounded once
+              const double val = fold_diagonals<S>(v, q, er + ec[q] - 7 * (S + 1));
               double out;
               switch (upd) {
                 case 0: out = val; break;
@@ -571,12 +588,12 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
   if (w == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;\n" ::"r"(tmem));
 }
 
-template <int S>
+template <int S, int TN>
 void launch_oz7(const Oz7Args& a, long long ntiles, int batch, cudaStream_t st) {
-  const size_t smem = (size_t)ring_depth<S>() * A_BYTES + 2 * S * B_BYTES + 1024;
+  const size_t smem = (size_t)ring_depth<S, TN>() * A_BYTES + 2 * S * b_bytes<TN>() + 1024;
   static bool attr = false;
   if (!attr) {
-    LKG_CUDA(cudaFuncSetAttribute(k_oz7_gemm<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    LKG_CUDA(cudaFuncSetAttribute(k_oz7_gemm<S, TN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = true;
   }
   static int nsm = 0;
@@ -586,18 +603,35 @@ void launch_oz7(const Oz7Args& a, long long ntiles, int batch, cudaStream_t st) 
     LKG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   }
   const long long gx = std::min<long long>(ntiles, std::max(1, nsm / std::max(1, batch)));
-  k_oz7_gemm<S><<<dim3((unsigned)gx, 1, batch), NTHREADS, smem, st>>>(a, ntiles);
+  k_oz7_gemm<S, TN><<<dim3((unsigned)gx, 1, batch), NTHREADS, smem, st>>>(a, ntiles);
   LKG_LAUNCH("k_oz7_gemm");
 }
 
-void dispatch(int S, const Oz7Args& a, long long ntiles, int batch, cudaStream_t st) {
+int g_tile_n = 32;  // the tile width of the next launches (oz7_set_tile)
+
+template <int TN>
+void dispatch_tn(int S, const Oz7Args& a, long long ntiles, int batch, cudaStream_t st) {
   switch (S) {
-    case 5: launch_oz7<5>(a, ntiles, batch, st); break;
-    case 6: launch_oz7<6>(a, ntiles, batch, st); break;
-    case 7: launch_oz7<7>(a, ntiles, batch, st); break;
-    case 8: launch_oz7<8>(a, ntiles, batch, st); break;
+    case 5: launch_oz7<5, TN>(a, ntiles, batch, st); break;
+    case 6: launch_oz7<6, TN>(a, ntiles, batch, st); break;
+    case 7: launch_oz7<7, TN>(a, ntiles, batch, st); break;
+    case 8: launch_oz7<8, TN>(a, ntiles, batch, st); break;
     default: throw std::invalid_argument("ozaki7: number of digits must be 5 .. 8");
   }
+}
+
+// number of tiles of a launch for the tile width tn: lower / W^T W products enumerate the tiles on or below the
+// diagonal (row block I holds (128 / tn) (I + 1) column tiles)
+long long tile_count(const Oz7Args& a, int tn) {
+  const long long tx = ceil_div(a.M, TM), ty = ceil_div(a.N, tn);
+  return (a.lower || a.wtw) ? (long long)(TM / tn) * tx * (tx + 1) / 2 : tx * ty;
+}
+
+void dispatch(int S, const Oz7Args& a, int batch, cudaStream_t st) {
+  if (g_tile_n == 64)
+    dispatch_tn<64>(S, a, tile_count(a, 64), batch, st);
+  else
+    dispatch_tn<32>(S, a, tile_count(a, 32), batch, st);
 }
 
 }  // namespace
@@ -648,31 +682,33 @@ void oz7_gemm(int M, int N, int kb0, int kb1, double alpha, const Split7& SA, co
   if (M <= 0 || N <= 0 || kb1 <= kb0) return;
   if (SA.S != SB.S || SA.sub_per_blk != SB.sub_per_blk || SA.nsub != SB.nsub)
     throw std::invalid_argument("oz7_gemm: operands split differently");
-  if (SA.rows_pad < ceil_div(M, TM) * TM || SB.rows_pad < ceil_div(N, TN) * TN)
+  // split operands are padded to whole 128-row images, which cover any 32- or 64-wide column tile
+  if (SA.rows_pad < ceil_div(M, TM) * TM || SB.rows_pad < ceil_div(N, TM) * TM)
     throw std::logic_error("oz7_gemm: operand rows do not cover C");
+  if (lower && M != N) throw std::invalid_argument("oz7_gemm: lower products are square");
   Oz7Args a{M, N, kb0, kb1, alpha, beta, SA, SB, C, ldc, c_batch, lower ? 1 : 0, 0};
-  const long long tx = ceil_div(M, TM), ty = ceil_div(N, TN);
-  long long ntiles = tx * ty;
-  if (lower) {
-    if (M != N) throw std::invalid_argument("oz7_gemm: lower products are square");
-    ntiles = 2 * tx * (tx + 1);  // row block I holds 4 I + 4 column blocks of 32
-  }
   const double K = std::min<double>((double)(kb1 - kb0) * SA.sub_per_blk * OZ7_SUB,
                                     (double)(SA.nsub - kb0 * SA.sub_per_blk) * OZ7_SUB);
   const double fl = lower ? K * M * (M + 1.0) : 2.0 * M * N * K;
   LaunchTimer lt("k_oz7_gemm", st, fl * batch * SA.S * (SA.S + 1) / 2.0,
                  8.0 * ((beta == 0.0) ? 1.0 : 2.0) * M * N * batch);
-  dispatch(SA.S, a, ntiles, batch, st);
+  dispatch(SA.S, a, batch, st);
 }
 
 void oz7_wtw(int n, const Split7& SW, double* C, int64_t ldc, int64_t cstride, int batch, cudaStream_t st) {
-  const long long I = ceil_div(n, TM);
   Oz7Args a{n, n, 0, SW.nblk, 1.0, 0.0, SW, SW, C, ldc, cstride, 0, 1};
   // executed work: tile (I, J) sums the k blocks from the one holding row 128 I
   LaunchTimer lt("k_oz7_wtw", st, (double)n * (n + 1.0) * (n + 2.0) / 3.0 * batch * SW.S * (SW.S + 1) / 2.0,
                  8.0 * n * (n + 1.0) * batch);
-  dispatch(SW.S, a, 2 * I * (I + 1), batch, st);
+  dispatch(SW.S, a, batch, st);
 }
+
+void oz7_set_tile(int tn) {
+  if (tn != 32 && tn != 64) throw std::invalid_argument("oz7_set_tile: tile width must be 32 or 64");
+  g_tile_n = tn;
+}
+
+int oz7_tile() { return g_tile_n; }
 
 int oz7_error_and_reset(int* where) {
   int e = 0, z = 0;

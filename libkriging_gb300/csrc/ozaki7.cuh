@@ -42,6 +42,9 @@ void oz7_gemm(int M, int N, int kb0, int kb1, double alpha, const Split7& SA, co
               int64_t ldc, int64_t c_batch, int batch, bool lower, cudaStream_t st);
 // C = W^T W (lower) with W split by columns (rows of SW = columns of W, k = rows of W)
 void oz7_wtw(int n, const Split7& SW, double* C, int64_t ldc, int64_t cstride, int batch, cudaStream_t st);
+// output tile width of the digit products: 32 (two TMEM accumulator sets, the default) or 64 (one set)
+void oz7_set_tile(int tn);
+int oz7_tile();
 // 1 if a CTA gave up waiting since the last call (then reset); synchronous.  where (8 ints, optional): the first
 // expired wait -- role (1, 2 producer B / A; 3, 4, 5 MMA TMEM / B / A; 6 + 16 warp epilogue), tile, k block,
 // sub-chunk, digit and the role's counters

@@ -288,6 +288,15 @@ class Kriging:
     def last_slices(self):
         return _lib.load().lkg_kriging_last_slices(self._h)
 
+    def autotune_precision(self, gamma, tol_ll=1e-8, tol_grad=1e-6):
+        """Pick and set the fastest precision (0 = FP64, 5..7 mixed slices) whose LL / gradient at gamma stay within
+        the tolerances of the FP64 path's (see lkg_kriging_autotune_precision); returns it."""
+        g = np.ascontiguousarray(gamma, dtype=np.float64)
+        r = _lib.load().lkg_kriging_autotune_precision(self._h, ptr(g), g.size, float(tol_ll), float(tol_grad))
+        if r < 0:
+            raise _lib.LibKrigingError(_lib.last_error())
+        return r
+
     def eval_counts(self):
         """(objective evaluations, GPU evaluation launches) since this model was created."""
         ev, ro = ctypes.c_longlong(), ctypes.c_longlong()

@@ -1,6 +1,5 @@
-"""The tcgen05 kernels of the mixed path's digit products (ozaki_tc.cu) against FP64 and against the mma.sync
-kernels: the same exact digit arithmetic, so the results agree to the last rounding of the per-chunk folds (bit for
-bit where both fold alike)."""
+"""The mixed path's digit-product kernel (ozaki7.cu: tcgen05 on 7-bit digits, 128 x 32 tiles, two TMEM accumulator
+sets) against FP64 products, and the mixed likelihood it drives against the FP64 path."""
 import ctypes
 
 import numpy as np
@@ -23,38 +22,16 @@ def _emulated(lk, A, B, S):
     return C
 
 
-@pytest.fixture
-def tensor_path(gpu_lib):
+def test_tensor_path_is_the_7bit_kernel(gpu_lib):
     lib = gpu_lib.load()
-    old = lib.lkg_get_tensor_path()
-    yield lib
-    lib.lkg_set_tensor_path(old)
-
-
-@pytest.mark.parametrize("S", [4, 6, 7, 8])
-@pytest.mark.parametrize("shape", [(64, 64, 64), (200, 130, 257), (129, 300, 64), (384, 256, 512)])
-def test_tc_gemm_matches_fp64_and_mma_sync(gpu_lib, tensor_path, S, shape):
-    M, N, K = shape
-    rng = np.random.default_rng(M + N + K + S)
-    A = rng.standard_normal((M, K)) * np.exp(rng.uniform(-5, 5, size=(M, 1)))
-    B = rng.standard_normal((N, K))
-    assert tensor_path.lkg_set_tensor_path(0) == 0
-    C_sync = _emulated(gpu_lib, A, B, S)
-    assert tensor_path.lkg_set_tensor_path(1) == 1
-    C_tc = _emulated(gpu_lib, A, B, S)
-    scale = np.abs(A) @ np.abs(B).T
-    if K <= 64 and S == 8:  # the single-stage kernel folds exactly as the mma.sync kernel does
-        assert np.array_equal(C_tc, C_sync)
-    else:  # the pipelined kernel rounds the chunk's exact value once instead of twice
-        assert np.max(np.abs(C_tc - C_sync) / scale) < 1e-15
-    if S >= 7:
-        err = np.max(np.abs(C_tc - A @ B.T) / scale)
-        assert err < (4e-15 if S == 7 else 2e-15), err
+    assert lib.lkg_get_tensor_path() == 3
+    assert lib.lkg_set_tensor_path(3) == 3
+    assert lib.lkg_set_tensor_path(1) == -1
 
 
 @pytest.mark.parametrize("S", [4, 6, 7])
 @pytest.mark.parametrize("shape", [(64, 64, 64), (200, 130, 257), (129, 300, 64), (384, 256, 512), (300, 70, 1000)])
-def test_oz7_gemm_matches_fp64(gpu_lib, tensor_path, S, shape):
+def test_oz7_gemm_matches_fp64(gpu_lib, S, shape):
     """Tensor path 3: 7-bit digits with one exponent per 256-wide k block; several k blocks are summed in FP64.
     S = 7 slices -> 8 digits (56-bit operands) reaches FP64-level products, S = 6 -> 7 digits (49 bits), S = 4 -> 5
     digits (35 bits) the precision of the triangular inverse and W^T W."""
@@ -62,7 +39,6 @@ def test_oz7_gemm_matches_fp64(gpu_lib, tensor_path, S, shape):
     rng = np.random.default_rng(M + N + K + S)
     A = rng.standard_normal((M, K)) * np.exp(rng.uniform(-5, 5, size=(M, 1)))
     B = rng.standard_normal((N, K))
-    assert tensor_path.lkg_set_tensor_path(3) == 3
     C = _emulated(gpu_lib, A, B, S)
     scale = np.abs(A) @ np.abs(B).T
     err = np.max(np.abs(C - A @ B.T) / scale)
@@ -77,9 +53,8 @@ def _config2_like(n, d=8, seed=123):
     return X, y, theta
 
 
-@pytest.mark.parametrize("path", [1, 2, 3])
 @pytest.mark.parametrize("n", [640, 2048, 1000])
-def test_tc_mixed_loglik(gpu_lib, tensor_path, n, path):
+def test_mixed_loglik_matches_fp64(gpu_lib, n):
     X, y, theta = _config2_like(n)
     alpha = 1.0 / (1.0 + 1e-6)
     k = gpu_lib.Kriging("matern5_2", "nugget")
@@ -88,12 +63,40 @@ def test_tc_mixed_loglik(gpu_lib, tensor_path, n, path):
     k.set_precision(0)
     ll64, g64, _ = k.logLikelihoodFun(g, True)
     k.set_precision(7)
-    tensor_path.lkg_set_tensor_path(0)
-    ll_s, g_s, _ = k.logLikelihoodFun(g, True)
-    tensor_path.lkg_set_tensor_path(path)
     ll_t, g_t, _ = k.logLikelihoodFun(g, True)
+    assert k.last_slices() == 7
     assert abs(ll_t - ll64) / abs(ll64) < 1e-8
     assert rel_err(g_t, g64) < 1e-6
-    if path < 3:  # the same digits as the mma.sync kernels
-        assert abs(ll_t - ll_s) / abs(ll_s) < 1e-12
-        assert rel_err(g_t, g_s) < 1e-10
+
+
+@pytest.mark.parametrize("tn", [32, 64])
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_both_tile_widths_give_identical_products(gpu_lib, tn, mode):
+    """The 128 x 32 tiles (two accumulator sets) and the 128 x 64 tiles (one set) compute every output from the same
+    exact diagonal sums with the same single rounding, so the products agree bit for bit -- for the rectangular,
+    the lower (A A^T) and the W^T W forms, over several k blocks."""
+    lib = gpu_lib.load()
+    rng = np.random.default_rng(5 + mode)
+    M, N, K = 300, 200, 700
+    A = rng.standard_normal((M, K))
+    if mode == 2:
+        A = np.tril(rng.standard_normal((M, M)))
+    B = rng.standard_normal((N, K))
+    dp = ctypes.POINTER(ctypes.c_double)
+    ip = ctypes.POINTER(ctypes.c_int)
+    out = {}
+    old = lib.lkg_get_digit_tile()
+    try:
+        for t in (32, 64):
+            assert lib.lkg_set_digit_tile(t) == t
+            n_out = M if mode else N
+            C = np.zeros((M, n_out), order="F")
+            where = np.zeros(8, dtype=np.int32)
+            Af, Bf = np.asfortranarray(A), np.asfortranarray(B)
+            rc = lib.lkg_oz7_mode_check(mode, M, N, K, Af.ctypes.data_as(dp), Bf.ctypes.data_as(dp), 8,
+                                        C.ctypes.data_as(dp), where.ctypes.data_as(ip))
+            assert rc == 0, (rc, where)
+            out[t] = C
+    finally:
+        lib.lkg_set_digit_tile(old)
+    assert np.array_equal(out[32], out[64])

@@ -24,18 +24,10 @@ def _emulated(lk, A, B, S):
     return C
 
 
-@pytest.fixture
-def tensor_path(gpu_lib):
-    lib = gpu_lib.load()
-    old = lib.lkg_get_tensor_path()
-    yield lib
-    lib.lkg_set_tensor_path(old)
-
-
 @pytest.mark.parametrize("S", [7, 8])
 @pytest.mark.parametrize("shape", [(64, 64, 64), (200, 130, 257), (129, 300, 64)])
 def test_emulated_gemm_is_fp64_accurate(gpu_lib, S, shape):
-    """The default tensor path (7-bit digits, 8 of them for S >= 7: 56-bit operands) and the 8-bit-slice paths."""
+    """7-bit digits, 8 of them for S >= 7: 56-bit operands."""
     M, N, K = shape
     rng = np.random.default_rng(M + N + K)
     A = rng.standard_normal((M, K)) * np.exp(rng.uniform(-5, 5, size=(M, 1)))
@@ -45,13 +37,11 @@ def test_emulated_gemm_is_fp64_accurate(gpu_lib, S, shape):
     # error bound relative to |A||B|^T (the natural scale of an FP64 product)
     scale = np.abs(A) @ np.abs(B).T
     err = np.max(np.abs(C - ref) / scale)
-    seven_bit = gpu_lib.load().lkg_get_tensor_path() == 3
-    assert err < (4e-15 if (S == 7 or seven_bit) else 2e-15), err
+    assert err < 4e-15, err
 
 
-def test_emulated_gemm_fewer_slices_degrades_gracefully(gpu_lib, tensor_path):
-    """8-bit slices (tensor path 1): every slice dropped costs accuracy."""
-    tensor_path.lkg_set_tensor_path(1)
+def test_emulated_gemm_fewer_slices_degrades_gracefully(gpu_lib):
+    """Every 7-bit digit dropped costs accuracy: slices 4 .. 7 -> 5 .. 8 digits (35 .. 56-bit operands)."""
     rng = np.random.default_rng(1)
     A, B = rng.standard_normal((64, 128)), rng.standard_normal((64, 128))
     ref = A @ B.T
