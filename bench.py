@@ -483,11 +483,19 @@ def make_vecchia_inputs(n=1 << 20, d=3, seed=123):
 
 
 def run_gpu_vecchia(args):
+    """One step = one Vecchia LL + gradient evaluation (VLL(30)) of the fitted n = 2^20 model, sets resident on the
+    device.  The line also times the GPU construction of the sets (maxmin order + neighbours) and the whole fit."""
     import libkriging_gb300 as lk
     lib = lk.load()
+    peak_fp64 = ctypes.c_double()
+    if lib.lkg_probe_fp64_peak(ctypes.byref(peak_fp64)) != 0:
+        raise RuntimeError("FP64 peak probe failed: " + lk._lib.last_error())
     n = args.n if args.n != 16384 else (1 << 20)
     X, y = make_vecchia_inputs(n)
     lk.set_num_nugget(1e-6)
+    t0 = time.perf_counter()
+    lk.vecchia_sets(X, 30)
+    sets_s = time.perf_counter() - t0
     k = lk.Kriging("gauss")
     k.set_vecchia_exact_commit(False)
     lib.lkg_stats_reset()
@@ -497,13 +505,9 @@ def run_gpu_vecchia(args):
     fit_s = time.perf_counter() - t0
     lib.lkg_stats_enable(0)
     fit_stats = kernel_stats(lib)
-    print("vecchia: n=%d fit %.2f s; %s" % (n, fit_s, {kk: round(v["ms"], 1) for kk, v in fit_stats.items()}),
-          file=sys.stderr, flush=True)
     th = k.theta()
     for _ in range(args.warmup):
         k.logLikelihoodVecchiaFun(th, True)
-    lib.lkg_stats_reset()
-    lib.lkg_stats_enable(1)
     clocks = ClockSampler(0)
     clocks.start()
     t0 = time.perf_counter()
@@ -511,19 +515,25 @@ def run_gpu_vecchia(args):
         vll, g = k.logLikelihoodVecchiaFun(th, True)
     wall = time.perf_counter() - t0
     clk = clocks.stop()
+    lib.lkg_stats_reset()
+    lib.lkg_stats_enable(1)
+    for _ in range(min(args.steps, 3)):
+        k.logLikelihoodVecchiaFun(th, True)
     lib.lkg_stats_enable(0)
     stats = kernel_stats(lib)
-    pts = stats.get("k_vecchia_points", {"ms": wall * 1e3})
     line = dict(metric="VLL(30)+grad evals/s at n=2^20, d=3 (gauss, num_nugget 1e-6)", value=args.steps / wall,
                 unit="evals/s", n_gpus=1, steps=args.steps, warmup=args.warmup, ms_per_step=1000 * wall / args.steps,
                 higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f64",
                 data="synthetic (seeded PCG64, seed 123)",
-                config=dict(workload="Vecchia LLVecchia(30), n=%d, d=3, gauss, light commit" % n),
-                fit_s_including_sets=fit_s, theta=th.tolist(), vll=vll, clocks=clk,
+                config=dict(workload="Vecchia LLVecchia(30), n=%d, d=3, gauss, light commit" % n,
+                            l2="inputs larger than L2 (n x 30 neighbour table + per-point terms)"),
+                e2e=dict(value=args.steps / wall, unit="evals/s", h2d_bytes_per_step=8 * 3,
+                         d2h_bytes_per_step=8 * 4,
+                         note="logLikelihoodVecchiaFun through the C ABI: theta in, (VLL, gradient) out"),
+                sets_s=sets_s, fit_s_including_sets=fit_s, theta=th.tolist(), vll=vll, clocks=clk,
                 fit_kernels={kk: dict(launches=v["launches"], ms=round(v["ms"], 3)) for kk, v in fit_stats.items()},
-                gpu_launches=int(sum(v["launches"] for v in stats.values())),
-                point_kernel_ms=pts["ms"] / max(1, args.steps),
-                kernels={kk: dict(launches=v["launches"], ms=round(v["ms"], 3)) for kk, v in stats.items()})
+                gpu_launches=int(sum(v["launches"] for v in stats.values()) / max(1, min(args.steps, 3))),
+                roofline=_roof(stats, peak_fp64.value, None), kernels=_kern(stats))
     if not args.no_cpu_baseline:
         from oracle import oracle as O
         O.build()
@@ -538,8 +548,21 @@ def run_gpu_vecchia(args):
                                           nbr.shape[1], 1e-6, 0, cnt)
         s = (time.perf_counter() - t1) * n / cnt
         line["cpu_baseline"] = dict(value=1.0 / s, unit="evals/s", cores=1, kind="port",
-                                    sample="serial per-point loop of _logLikelihoodVecchia with gradient on the "
-                                           "first %d of %d ordered points, scaled by n" % (cnt, n))
+                                    sample="serial per-point loop of _logLikelihoodVecchia with gradient (the "
+                                           "reference's loop is serial) on the first %d of %d ordered points, "
+                                           "scaled by n" % (cnt, n))
+        # the reference-style O(n^2) set construction on a bounded size, against the GPU grid construction
+        ns = 16384
+        Xs = X[:ns]
+        t1 = time.perf_counter()
+        O.vecchia_sets(Xs, 30)
+        cpu_sets = time.perf_counter() - t1
+        t1 = time.perf_counter()
+        lk.vecchia_sets(Xs, 30)
+        gpu_sets = time.perf_counter() - t1
+        line["sets_cpu_baseline"] = dict(n=ns, cpu_s=cpu_sets, gpu_s=gpu_sets, cores=1, kind="port",
+                                         sample="make_vecchia_sets restated (O(n^2) maxmin + neighbour selection) "
+                                                "on the first %d points" % ns)
     print(json.dumps(line), flush=True)
 
 

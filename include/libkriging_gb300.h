@@ -259,6 +259,12 @@ int lkg_get_tensor_path(void);
  * twice the columns).  Returns the width set, or -1 for another value. */
 int lkg_set_digit_tile(int tn);
 int lkg_get_digit_tile(void);
+/* No counterpart in the reference: the mixed Cholesky's look-ahead (n >= 1024, single-matrix evaluations): the next
+ * 256-wide panel is factored on a second stream on `ctas` SMs while the rest of the trailing update runs on the
+ * others; 0 turns it off (default 8, or LKG_LOOKAHEAD_CTAS).  The factor is the same bit for bit either way.
+ * Returns the value set, or -1 outside 0 .. 64. */
+int lkg_set_lookahead(int ctas);
+int lkg_get_lookahead(void);
 /* No counterpart in the reference: one product of the 7-bit digit kernel on host data, S digits (5..8):
  * mode 0: C (M x N) = A B^T (A M x K, B N x K); mode 1: C = A A^T lower (M x M); mode 2: C = W^T W lower with
  * W = A (M x M, lower).  Returns 0, -1 (error text in lkg_get_last_error) or -2 when a wait of the kernel expired

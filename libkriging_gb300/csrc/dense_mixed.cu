@@ -17,39 +17,84 @@ int oz7_inv_digits(int slices_inv) { return std::min(8, std::max(5, slices_inv))
 // Two-level blocked Cholesky: 256-wide panels factored in 64-wide steps (FP64 diagonal block; panel solve and the update
 // of the panel's remaining columns as 64-deep digit products), then one rank-256 trailing update per panel.  Every
 // product reads split copies of its operands, so the in-place ones (the panel solve) are safe.
-void potrf_blocked_mixed7(double* A, int64_t lda, int64_t mstride, int n, double* Dinv, int* info, int batch,
-                          const MixedWorkspace& ws, cudaStream_t st) {
+//
+// Look-ahead (single matrix, ws.side_stream set): the trailing update of panel p is cut into the strip of panel p + 1's
+// columns and the rest.  After the strip, panel p + 1 is factored on the side stream -- its diagonal blocks, splits
+// and small products on ws.side_ctas SMs -- while the rest of the update runs on the other SMs; the main stream
+// waits for the panel before splitting it.  Every entry receives the same operations either way, so the factor is
+// bit-identical with and without the look-ahead.
+void factor_panel7(double* A, int64_t lda, int64_t mstride, int n, int K0, double* Dinv, int* info, int batch,
+                   Split7& SA, Split7& SD, int max_ctas, cudaStream_t st) {
   const int nblk = ceil_div(n, NB);
   const int64_t dstride = (int64_t)nblk * NB * NB;
+  const int W = std::min(OZ7_KB, n - K0);
+  for (int k0 = K0; k0 < K0 + W; k0 += NB) {
+    const int nb = std::min(NB, n - k0), k = k0 / NB;
+    potrf_diag(A, lda, mstride, k0, nb, Dinv, dstride, k, info, batch, st);
+    const int M = n - k0 - nb;
+    if (M <= 0) continue;
+    double* A21 = A + (k0 + nb) + (int64_t)k0 * lda;
+    // L21 = A21 Dinv_k^T: B rows are the rows of Dinv_k
+    oz7_split(M, nb, A21, 1, lda, mstride, batch, SA, st);
+    oz7_split(nb, nb, Dinv + (int64_t)k * NB * NB, 1, NB, dstride, batch, SD, st);
+    oz7_gemm_ex(M, nb, 0, 1, 1.0, SA, 0, SD, 0, 0.0, A21, lda, mstride, batch, false, max_ctas, st);
+    const int wr = K0 + W - (k0 + nb);  // panel columns right of this block
+    if (wr > 0) {  // A(k0+nb:, k0+nb:K0+W) -= L21 L21(0:wr, :)^T (the strict upper part written is never read)
+      oz7_split(M, nb, A21, 1, lda, mstride, batch, SA, st);
+      oz7_gemm_ex(M, wr, 0, 1, -1.0, SA, 0, SA, 0, 1.0, A21 + (int64_t)nb * lda, lda, mstride, batch, false,
+                  max_ctas, st);
+    }
+  }
+}
+
+void potrf_blocked_mixed7(double* A, int64_t lda, int64_t mstride, int n, double* Dinv, int* info, int batch,
+                          const MixedWorkspace& ws, cudaStream_t st) {
   LKG_CUDA(cudaMemsetAsync(info, 0, sizeof(int) * batch, st));
   const int S = oz7_digits(ws.slices);
   Split7 P = oz7_buffer(ws.panel, ws.panel_exp, S, ws.n, OZ7_KB, OZ7_KB);
   Split7 SA = oz7_buffer(ws.panel, ws.panel_exp, S, ws.n, NB, NB);
   Split7 SD = oz7_buffer(ws.rowblk, ws.rowblk_exp, S, ws.n, NB, NB);
+  const bool ahead = ws.side_stream && batch == 1;
+  if (!ahead) {
+    for (int K0 = 0; K0 < n; K0 += OZ7_KB) {
+      const int W = std::min(OZ7_KB, n - K0);
+      factor_panel7(A, lda, mstride, n, K0, Dinv, info, batch, SA, SD, 0, st);
+      const int M2 = n - K0 - W;
+      if (M2 <= 0) continue;
+      // A22 -= P2 P2^T, P2 = L(K0+W:, K0:K0+W), one 256-wide k block
+      double* P2 = A + (K0 + W) + (int64_t)K0 * lda;
+      oz7_split(M2, W, P2, 1, lda, mstride, batch, P, st);
+      oz7_gemm(M2, M2, 0, 1, -1.0, P, P, 1.0, P2 + (int64_t)W * lda, lda, mstride, batch, true, st);
+    }
+    return;
+  }
+  // the side stream's panel splits have their own buffer: the main stream's trailing update still reads P (the
+  // Dinv splits in rowblk are used by one stream at a time)
+  Split7 SAs = oz7_buffer(ws.side, ws.side_exp, S, ws.n, NB, NB);
+  const int rest_ctas = std::max(1, oz7_sm_count() - ws.side_ctas);
+  factor_panel7(A, lda, mstride, n, 0, Dinv, info, batch, SA, SD, 0, st);
   for (int K0 = 0; K0 < n; K0 += OZ7_KB) {
     const int W = std::min(OZ7_KB, n - K0);
-    for (int k0 = K0; k0 < K0 + W; k0 += NB) {
-      const int nb = std::min(NB, n - k0), k = k0 / NB;
-      potrf_diag(A, lda, mstride, k0, nb, Dinv, dstride, k, info, batch, st);
-      const int M = n - k0 - nb;
-      if (M <= 0) continue;
-      double* A21 = A + (k0 + nb) + (int64_t)k0 * lda;
-      // L21 = A21 Dinv_k^T: B rows are the rows of Dinv_k
-      oz7_split(M, nb, A21, 1, lda, mstride, batch, SA, st);
-      oz7_split(nb, nb, Dinv + (int64_t)k * NB * NB, 1, NB, dstride, batch, SD, st);
-      oz7_gemm(M, nb, 0, 1, 1.0, SA, SD, 0.0, A21, lda, mstride, batch, false, st);
-      const int wr = K0 + W - (k0 + nb);  // panel columns right of this block
-      if (wr > 0) {  // A(k0+nb:, k0+nb:K0+W) -= L21 L21(0:wr, :)^T (the strict upper part written is never read)
-        oz7_split(M, nb, A21, 1, lda, mstride, batch, SA, st);
-        oz7_gemm(M, wr, 0, 1, -1.0, SA, SA, 1.0, A21 + (int64_t)nb * lda, lda, mstride, batch, false, st);
-      }
-    }
     const int M2 = n - K0 - W;
-    if (M2 <= 0) continue;
-    // A22 -= P2 P2^T, P2 = L(K0+W:, K0:K0+W), one 256-wide k block
+    if (M2 <= 0) break;
     double* P2 = A + (K0 + W) + (int64_t)K0 * lda;
     oz7_split(M2, W, P2, 1, lda, mstride, batch, P, st);
-    oz7_gemm(M2, M2, 0, 1, -1.0, P, P, 1.0, P2 + (int64_t)W * lda, lda, mstride, batch, true, st);
+    const int W1 = std::min(OZ7_KB, M2);  // the next panel's width
+    // the strip of the next panel's columns: A(K0+W:, K0+W:K0+W+W1) -= P2 P2(0:W1, :)^T
+    oz7_gemm_ex(M2, W1, 0, 1, -1.0, P, 0, P, 0, 1.0, P2 + (int64_t)W * lda, lda, mstride, batch, false, 0, st);
+    const int M3 = M2 - W1;
+    if (M3 <= 0) {  // the last panel: nothing left to overlap with
+      factor_panel7(A, lda, mstride, n, K0 + W, Dinv, info, batch, SA, SD, 0, st);
+      continue;
+    }
+    LKG_CUDA(cudaEventRecord(ws.ev_strip, st));
+    LKG_CUDA(cudaStreamWaitEvent(ws.side_stream, ws.ev_strip, 0));
+    factor_panel7(A, lda, mstride, n, K0 + W, Dinv, info, batch, SAs, SD, ws.side_ctas, ws.side_stream);
+    LKG_CUDA(cudaEventRecord(ws.ev_panel, ws.side_stream));
+    // the rest of the update, lower: A(K0+W+W1:, K0+W+W1:) -= P2(W1:, :) P2(W1:, :)^T
+    oz7_gemm_ex(M3, M3, 0, 1, -1.0, P, W1, P, W1, 1.0, P2 + W1 + (int64_t)(W + W1) * lda, lda, mstride, batch, true,
+                rest_ctas, st);
+    LKG_CUDA(cudaStreamWaitEvent(st, ws.ev_panel, 0));
   }
 }
 

@@ -112,6 +112,7 @@ int lkg_probe_dmma_peak(double* tflops_out) {
 }  // extern "C"
 
 // ---- emulated-GEMM check entry point (host buffers) ----
+#include "engine.hpp"
 #include "ozaki7.cuh"
 
 namespace lkg {
@@ -140,6 +141,18 @@ extern "C" int lkg_set_digit_tile(int tn) {
 }
 
 extern "C" int lkg_get_digit_tile(void) { return lkg::oz7_tile(); }
+
+extern "C" int lkg_set_lookahead(int ctas) {
+  try {
+    lkg::set_lookahead_ctas(ctas);
+  } catch (const std::exception& e) {
+    lkg::set_last_error(e.what());
+    return -1;
+  }
+  return ctas;
+}
+
+extern "C" int lkg_get_lookahead(void) { return lkg::lookahead_ctas_setting(); }
 
 extern "C" int lkg_ozaki_gemm_check(int M, int N, int K, const double* A, const double* B, int slices, double* C) {
   // C = A * B^T with A (M x K) and B (N x K) column-major, computed by the split-bf16 tensor-core path

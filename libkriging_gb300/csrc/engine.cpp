@@ -10,6 +10,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <atomic>
 #include <cstdlib>
 #include <cstring>
 #include <string>
@@ -151,10 +152,13 @@ Engine::~Engine() {
   if (dgls_info_) cudaFree(dgls_info_);
   if (dXe_) cudaFree(dXe_);
   if (dnv_) cudaFree(dnv_);
-  for (void* p : {dpanel_, drowblk_, dwfull_})
+  for (void* p : {dpanel_, drowblk_, dwfull_, dside_})
     if (p) cudaFree(p);
-  for (int* p : {dpanel_exp_, drowblk_exp_, dwfull_exp_})
+  for (int* p : {dpanel_exp_, drowblk_exp_, dwfull_exp_, dside_exp_})
     if (p) cudaFree(p);
+  if (ev_strip_) cudaEventDestroy(ev_strip_);
+  if (ev_panel_) cudaEventDestroy(ev_panel_);
+  if (side_st_) cudaStreamDestroy(side_st_);
   if (st_) cudaStreamDestroy(st_);
 }
 
@@ -163,14 +167,35 @@ void Engine::set_slices(int s) {
   slices_ = s;
 }
 
+// SMs kept for the mixed Cholesky's look-ahead panel work (0: no look-ahead); the initial value comes from
+// LKG_LOOKAHEAD_CTAS (default 8), lkg_set_lookahead changes it
+namespace {
+std::atomic<int> g_lookahead_ctas{[] {
+  const char* v = std::getenv("LKG_LOOKAHEAD_CTAS");
+  const int x = v ? std::atoi(v) : 8;
+  return x >= 0 && x <= 64 ? x : 8;
+}()};
+}  // namespace
+
+void set_lookahead_ctas(int c) {
+  if (c < 0 || c > 64) throw std::invalid_argument("look-ahead: SMs for the panel work must be 0 .. 64");
+  g_lookahead_ctas = c;
+}
+int lookahead_ctas_setting() { return g_lookahead_ctas; }
+
+// the look-ahead pays when the matrix has several 256-wide panels
+bool Engine::lookahead_enabled() const { return g_lookahead_ctas > 0 && n_ >= 4 * OZ7_KB; }
+
+int Engine::lookahead_ctas() const { return g_lookahead_ctas; }
+
 void Engine::ensure_mixed_buffers(bool with_grad) {
   if (mixed_alloc_slices_ != slices_) {
-    for (void** p : {&dpanel_, &drowblk_, &dwfull_})
+    for (void** p : {&dpanel_, &drowblk_, &dwfull_, &dside_})
       if (*p) {
         cudaFree(*p);
         *p = nullptr;
       }
-    for (int** p : {&dpanel_exp_, &drowblk_exp_, &dwfull_exp_})
+    for (int** p : {&dpanel_exp_, &drowblk_exp_, &dwfull_exp_, &dside_exp_})
       if (*p) {
         cudaFree(*p);
         *p = nullptr;
@@ -185,6 +210,17 @@ void Engine::ensure_mixed_buffers(bool with_grad) {
     LKG_CUDA(cudaMalloc(&drowblk_, pe * 2));
     dalloc(&dpanel_exp_, ee);
     dalloc(&drowblk_exp_, ee);
+  }
+  // the look-ahead's own panel splits (single-matrix evaluations of a size where it pays)
+  if (lookahead_enabled() && !dside_) {
+    const size_t pe1 = oz7_plane_elems(n_, OZ7_KB, 8), ee1 = oz7_exp_elems(n_, OZ7_KB, OZ7_KB);
+    LKG_CUDA(cudaMalloc(&dside_, pe1 * 2));
+    dalloc(&dside_exp_, ee1);
+    if (!side_st_) {
+      LKG_CUDA(cudaStreamCreateWithFlags(&side_st_, cudaStreamNonBlocking));
+      LKG_CUDA(cudaEventCreateWithFlags(&ev_strip_, cudaEventDisableTiming));
+      LKG_CUDA(cudaEventCreateWithFlags(&ev_panel_, cudaEventDisableTiming));
+    }
   }
   if (with_grad && !dwfull_) {
     LKG_CUDA(cudaMalloc(&dwfull_, oz7_plane_elems(n_, n_, std::min(8, slices_ + 1)) * cap_ * 2));
@@ -385,6 +421,14 @@ void Engine::evaluate(int batch, const double* thetas, const double* factors, bo
     mw.rowblk_exp = drowblk_exp_;
     mw.wfull = dwfull_;
     mw.wfull_exp = dwfull_exp_;
+    if (batch == 1 && dside_ && lookahead_enabled()) {
+      mw.side_stream = side_st_;
+      mw.ev_strip = ev_strip_;
+      mw.ev_panel = ev_panel_;
+      mw.side = dside_;
+      mw.side_exp = dside_exp_;
+      mw.side_ctas = lookahead_ctas();
+    }
   }
   bool retreated = false;
   bool w_valid = false;  // W = L^-1 of the accepted factor is already in dW_

@@ -36,6 +36,10 @@ struct LooOut {
   std::vector<double> s2;      // sigma2LOO = 1 / diag(B)
 };
 
+// SMs kept for the panel work of the mixed Cholesky's look-ahead (0 turns it off); process-wide
+void set_lookahead_ctas(int c);
+int lookahead_ctas_setting();
+
 class Engine {
  public:
   // X: n x d column-major, y: n, F: n x p column-major (all host, copied to HBM).  batch_cap: max thetas per call.
@@ -107,6 +111,8 @@ class Engine {
   }
   // 0 selects the FP64 path; 4..8 the mixed path with that many bf16 digit slices (7 ~ FP64-level products)
   void set_slices(int s);
+  bool lookahead_enabled() const;
+  int lookahead_ctas() const;
   int slices() const { return slices_; }
   cudaStream_t stream() const { return st_; }
 
@@ -147,8 +153,10 @@ class Engine {
   double* dXe_ = nullptr;                 // per-entry copy of its design's X (several designs only)
   int* dnv_ = nullptr;                    // per-entry valid sizes on the device (several designs only)
   int slices_ = 0;
-  void *dpanel_ = nullptr, *drowblk_ = nullptr, *dwfull_ = nullptr;
-  int *dpanel_exp_ = nullptr, *drowblk_exp_ = nullptr, *dwfull_exp_ = nullptr;
+  void *dpanel_ = nullptr, *drowblk_ = nullptr, *dwfull_ = nullptr, *dside_ = nullptr;
+  int *dpanel_exp_ = nullptr, *drowblk_exp_ = nullptr, *dwfull_exp_ = nullptr, *dside_exp_ = nullptr;
+  cudaStream_t side_st_ = nullptr;  // look-ahead stream of the mixed Cholesky (single-matrix evaluations)
+  cudaEvent_t ev_strip_ = nullptr, ev_panel_ = nullptr;
   int mixed_alloc_slices_ = 0;
   int64_t lda_, mstride_, dstride_, fystride_;
   cudaStream_t st_ = nullptr;

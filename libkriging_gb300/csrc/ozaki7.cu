@@ -372,7 +372,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
       for (long long ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
         Tile T;
         if (!tile_of<TN>(g, ti, T)) continue;
-        const int tA = T.m0 / TM, tB = T.n0 / TM, hB = T.n0 % TM;
+        const int tA = (T.m0 + g.a_row0) / TM, tB = (T.n0 + g.b_row0) / TM, hB = (T.n0 + g.b_row0) % TM;
         for (int kb = T.kb0; kb < T.kb1 && ok; ++kb) {
           const int s1 = min((kb + 1) * spb, g.SA.nsub);
           for (int s = kb * spb; s < s1 && ok; ++s) {
@@ -511,8 +511,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
         const bool need_c = !(first && g.beta == 0.0);
         // operands of the update, loaded while the block's products run: the column exponents and the first four
         // C values (each group then prefetches the next group's C)
-        const int er = ea[(int64_t)kb * g.SA.rows_pad + row];
-        const int* ebk = eb + (int64_t)kb * g.SB.rows_pad;
+        const int er = ea[(int64_t)kb * g.SA.rows_pad + g.a_row0 + row];
+        const int* ebk = eb + (int64_t)kb * g.SB.rows_pad + g.b_row0;
         double cnext[4];
         int enext[4];
 #pragma unroll
@@ -589,7 +589,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) k_oz7_gemm(Oz7Args g, long long n
 }
 
 template <int S, int TN>
-void launch_oz7(const Oz7Args& a, long long ntiles, int batch, cudaStream_t st) {
+void launch_oz7(const Oz7Args& a, long long ntiles, int batch, int max_ctas, cudaStream_t st) {
   const size_t smem = (size_t)ring_depth<S, TN>() * A_BYTES + 2 * S * b_bytes<TN>() + 1024;
   static bool attr = false;
   if (!attr) {
@@ -602,7 +602,8 @@ void launch_oz7(const Oz7Args& a, long long ntiles, int batch, cudaStream_t st) 
     LKG_CUDA(cudaGetDevice(&dev));
     LKG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   }
-  const long long gx = std::min<long long>(ntiles, std::max(1, nsm / std::max(1, batch)));
+  long long gx = std::min<long long>(ntiles, std::max(1, nsm / std::max(1, batch)));
+  if (max_ctas > 0) gx = std::min<long long>(gx, max_ctas);
   k_oz7_gemm<S, TN><<<dim3((unsigned)gx, 1, batch), NTHREADS, smem, st>>>(a, ntiles);
   LKG_LAUNCH("k_oz7_gemm");
 }
@@ -610,12 +611,12 @@ void launch_oz7(const Oz7Args& a, long long ntiles, int batch, cudaStream_t st) 
 int g_tile_n = 32;  // the tile width of the next launches (oz7_set_tile)
 
 template <int TN>
-void dispatch_tn(int S, const Oz7Args& a, long long ntiles, int batch, cudaStream_t st) {
+void dispatch_tn(int S, const Oz7Args& a, long long ntiles, int batch, int max_ctas, cudaStream_t st) {
   switch (S) {
-    case 5: launch_oz7<5, TN>(a, ntiles, batch, st); break;
-    case 6: launch_oz7<6, TN>(a, ntiles, batch, st); break;
-    case 7: launch_oz7<7, TN>(a, ntiles, batch, st); break;
-    case 8: launch_oz7<8, TN>(a, ntiles, batch, st); break;
+    case 5: launch_oz7<5, TN>(a, ntiles, batch, max_ctas, st); break;
+    case 6: launch_oz7<6, TN>(a, ntiles, batch, max_ctas, st); break;
+    case 7: launch_oz7<7, TN>(a, ntiles, batch, max_ctas, st); break;
+    case 8: launch_oz7<8, TN>(a, ntiles, batch, max_ctas, st); break;
     default: throw std::invalid_argument("ozaki7: number of digits must be 5 .. 8");
   }
 }
@@ -627,11 +628,11 @@ long long tile_count(const Oz7Args& a, int tn) {
   return (a.lower || a.wtw) ? (long long)(TM / tn) * tx * (tx + 1) / 2 : tx * ty;
 }
 
-void dispatch(int S, const Oz7Args& a, int batch, cudaStream_t st) {
+void dispatch(int S, const Oz7Args& a, int batch, cudaStream_t st, int max_ctas = 0) {
   if (g_tile_n == 64)
-    dispatch_tn<64>(S, a, tile_count(a, 64), batch, st);
+    dispatch_tn<64>(S, a, tile_count(a, 64), batch, max_ctas, st);
   else
-    dispatch_tn<32>(S, a, tile_count(a, 32), batch, st);
+    dispatch_tn<32>(S, a, tile_count(a, 32), batch, max_ctas, st);
 }
 
 }  // namespace
@@ -679,24 +680,42 @@ void oz7_split(int rows, int K, const double* p, int64_t s_r, int64_t s_k, int64
 
 void oz7_gemm(int M, int N, int kb0, int kb1, double alpha, const Split7& SA, const Split7& SB, double beta, double* C,
               int64_t ldc, int64_t c_batch, int batch, bool lower, cudaStream_t st) {
+  oz7_gemm_ex(M, N, kb0, kb1, alpha, SA, 0, SB, 0, beta, C, ldc, c_batch, batch, lower, 0, st);
+}
+
+int oz7_sm_count() {
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    LKG_CUDA(cudaGetDevice(&dev));
+    LKG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  }
+  return nsm;
+}
+
+void oz7_gemm_ex(int M, int N, int kb0, int kb1, double alpha, const Split7& SA, int a_row0, const Split7& SB,
+                 int b_row0, double beta, double* C, int64_t ldc, int64_t c_batch, int batch, bool lower, int max_ctas,
+                 cudaStream_t st) {
   if (M <= 0 || N <= 0 || kb1 <= kb0) return;
   if (SA.S != SB.S || SA.sub_per_blk != SB.sub_per_blk || SA.nsub != SB.nsub)
     throw std::invalid_argument("oz7_gemm: operands split differently");
+  if (a_row0 < 0 || b_row0 < 0 || a_row0 % TM || b_row0 % TM)
+    throw std::invalid_argument("oz7_gemm: operand row offsets must be multiples of 128");
   // split operands are padded to whole 128-row images, which cover any 32- or 64-wide column tile
-  if (SA.rows_pad < ceil_div(M, TM) * TM || SB.rows_pad < ceil_div(N, TM) * TM)
+  if (SA.rows_pad < a_row0 + ceil_div(M, TM) * TM || SB.rows_pad < b_row0 + ceil_div(N, TM) * TM)
     throw std::logic_error("oz7_gemm: operand rows do not cover C");
   if (lower && M != N) throw std::invalid_argument("oz7_gemm: lower products are square");
-  Oz7Args a{M, N, kb0, kb1, alpha, beta, SA, SB, C, ldc, c_batch, lower ? 1 : 0, 0};
+  Oz7Args a{M, N, kb0, kb1, alpha, beta, SA, SB, C, ldc, c_batch, lower ? 1 : 0, 0, a_row0, b_row0};
   const double K = std::min<double>((double)(kb1 - kb0) * SA.sub_per_blk * OZ7_SUB,
                                     (double)(SA.nsub - kb0 * SA.sub_per_blk) * OZ7_SUB);
   const double fl = lower ? K * M * (M + 1.0) : 2.0 * M * N * K;
   LaunchTimer lt("k_oz7_gemm", st, fl * batch * SA.S * (SA.S + 1) / 2.0,
                  8.0 * ((beta == 0.0) ? 1.0 : 2.0) * M * N * batch);
-  dispatch(SA.S, a, batch, st);
+  dispatch(SA.S, a, batch, st, max_ctas);
 }
 
 void oz7_wtw(int n, const Split7& SW, double* C, int64_t ldc, int64_t cstride, int batch, cudaStream_t st) {
-  Oz7Args a{n, n, 0, SW.nblk, 1.0, 0.0, SW, SW, C, ldc, cstride, 0, 1};
+  Oz7Args a{n, n, 0, SW.nblk, 1.0, 0.0, SW, SW, C, ldc, cstride, 0, 1, 0, 0};
   // executed work: tile (I, J) sums the k blocks from the one holding row 128 I
   LaunchTimer lt("k_oz7_wtw", st, (double)n * (n + 1.0) * (n + 2.0) / 3.0 * batch * SW.S * (SW.S + 1) / 2.0,
                  8.0 * n * (n + 1.0) * batch);

@@ -27,6 +27,7 @@ struct Oz7Args {
   int64_t ldc, c_batch;
   int lower;  // square lower product: tiles on or below the diagonal, entries r >= c
   int wtw;    // R^-1 = W^T W (lower): tile (I, J) sums the k blocks from the one holding row 128 I
+  int a_row0, b_row0;  // first operand rows of A and B in their splits (multiples of 128)
 };
 
 size_t oz7_plane_elems(int rows, int K, int S);     // bf16 elements per batch entry
@@ -40,6 +41,12 @@ void oz7_split(int rows, int K, const double* p, int64_t s_r, int64_t s_k, int64
 // C(M x N) = beta C + alpha A B^T over the k blocks [kb0, kb1) (A rows from SA, B rows from SB)
 void oz7_gemm(int M, int N, int kb0, int kb1, double alpha, const Split7& SA, const Split7& SB, double beta, double* C,
               int64_t ldc, int64_t c_batch, int batch, bool lower, cudaStream_t st);
+// the same with the operands' rows starting at a_row0 / b_row0 of their splits (multiples of 128) and at most
+// max_ctas persistent CTAs per batch entry (0: one per SM), so that work on another stream keeps some SMs
+void oz7_gemm_ex(int M, int N, int kb0, int kb1, double alpha, const Split7& SA, int a_row0, const Split7& SB,
+                 int b_row0, double beta, double* C, int64_t ldc, int64_t c_batch, int batch, bool lower, int max_ctas,
+                 cudaStream_t st);
+int oz7_sm_count();
 // C = W^T W (lower) with W split by columns (rows of SW = columns of W, k = rows of W)
 void oz7_wtw(int n, const Split7& SW, double* C, int64_t ldc, int64_t cstride, int batch, cudaStream_t st);
 // output tile width of the digit products: 32 (two TMEM accumulator sets, the default) or 64 (one set)

@@ -663,7 +663,11 @@ int VecchiaEngine::partial_sums1(const double* theta, bool with_grad, std::vecto
                ddW_, dstatus_};
   const double cnt = t1_ - t0_;
   {
-    LaunchTimer lt("k_vecchia_points", st_, cnt * m_ * (m_ + 1) / 2.0, 8.0 * cnt * (1.0 + d) * m_);
+    // per point: the (m + 1)^3 / 3 Cholesky-and-solve work of the conditional and the d (4 m^2) derivative terms
+    const double mm = m_;
+    LaunchTimer lt("k_vecchia_points", st_,
+                   cnt * ((mm + 1) * (mm + 1) * (mm + 1) / 3.0 + (with_grad ? d * 4.0 * mm * mm : 0.0)),
+                   8.0 * cnt * (1.0 + d) * m_);
     launch_points(kernel_, a, st_);
   }
   int* dcount = dstatus_ + n;

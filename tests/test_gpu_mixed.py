@@ -89,3 +89,27 @@ def test_mixed_batch_matches_single(gpu_lib):
         ll, g, _ = k.logLikelihoodFun(thetas[i], True)
         assert ll == ll_b[i]
         assert np.array_equal(g, g_b[i])
+
+
+@pytest.mark.parametrize("n,ctas", [(1100, 8), (2048, 4), (3000, 16)])
+def test_lookahead_factor_is_bit_identical(gpu_lib, n, ctas):
+    """The look-ahead Cholesky (next panel factored on a second stream while the rest of the trailing update runs)
+    performs the same operations per entry: LL and gradient equal, bit for bit, those without it."""
+    lib = gpu_lib.load()
+    X, y, theta = _config2_like(n)
+    g = np.concatenate([theta, [1.0 / (1.0 + 1e-6)]])
+    k = gpu_lib.Kriging("matern5_2", "nugget")
+    k.fit(y, X, "constant", False, "none", "LL", {"theta": theta.reshape(1, -1), "sigma2": 1.0, "nugget": 1e-6})
+    k.set_precision(7)
+    old = lib.lkg_get_lookahead()
+    try:
+        assert lib.lkg_set_lookahead(0) == 0
+        ll0, g0, _ = k.logLikelihoodFun(g, True)
+        assert lib.lkg_set_lookahead(ctas) == ctas
+        ll1, g1, _ = k.logLikelihoodFun(g, True)
+        ll2, g2, _ = k.logLikelihoodFun(g, True)
+    finally:
+        lib.lkg_set_lookahead(old)
+    assert k.last_slices() == 7
+    assert ll1 == ll0 and ll2 == ll0
+    assert np.array_equal(g1, g0) and np.array_equal(g2, g0)
