@@ -306,6 +306,8 @@ def run_gpu(args):
     barrier()
     # ---- mixed path (headline) ----
     k.set_precision(args.slices)
+    # the autotuner picks the SMs kept for the Cholesky look-ahead at this size (timed evaluations, tabled)
+    lookahead_tuned = k.autotune_lookahead(gamma)
     for _ in range(args.warmup):
         k.logLikelihoodFun(gamma, True, False, bench=True)
     barrier()
@@ -338,6 +340,8 @@ def run_gpu(args):
                                 lib.lkg_get_digit_tile(), "two TMEM accumulator sets" if lib.lkg_get_digit_tile() == 32
                                 else "one TMEM accumulator set"),
                             parallelism="replicas" if world > 1 else "single GPU",
+                            cholesky_lookahead_sms=dict(autotuned=lookahead_tuned,
+                                                        setting=lib.lkg_get_lookahead()),
                             l2="inputs larger than L2 (R, L^-1, R^-1: 3 x %.2f GB)" % (8.0 * args.n * args.n / 1e9)),
                 e2e=dict(value=world / e2e_s, unit=UNIT, h2d_bytes_per_step=8 * gamma.size,
                          d2h_bytes_per_step=8 * (1 + gamma.size)),

@@ -117,6 +117,10 @@ int lkg_kriging_eval_counts(void* ptr, long long* evaluations, long long* rounds
  * returns it; lkg_autotune_lookup returns a tabled choice or `fallback`; lkg_autotune_report writes
  * "key<TAB>choice<TAB>cost<LF>" lines and returns the size needed; save / load / clear manage the table. */
 int lkg_kriging_autotune_precision(void* ptr, const double* gamma, int gamma_n, double tol_ll, double tol_grad);
+/* No counterpart in the reference: times logLikelihoodFun(gamma, grad) of this (mixed-precision) model with 0, 12,
+ * 16, 24 and 32 SMs kept for the Cholesky look-ahead's panel work and tables the fastest for the model's size; later
+ * evaluations of that size use it unless lkg_set_lookahead fixed a value.  Returns the choice, -1 on error. */
+int lkg_kriging_autotune_lookahead(void* ptr, const double* gamma, int gamma_n);
 void lkg_autotune_enable(int on);
 int lkg_autotune_record(const char* key, const int* candidates, const double* costs, int n);
 int lkg_autotune_lookup(const char* key, int fallback);
@@ -261,8 +265,9 @@ int lkg_set_digit_tile(int tn);
 int lkg_get_digit_tile(void);
 /* No counterpart in the reference: the mixed Cholesky's look-ahead (n >= 1024, single-matrix evaluations): the next
  * 256-wide panel is factored on a second stream on `ctas` SMs while the rest of the trailing update runs on the
- * others; 0 turns it off (default 8, or LKG_LOOKAHEAD_CTAS).  The factor is the same bit for bit either way.
- * Returns the value set, or -1 outside 0 .. 64. */
+ * others.  0 turns it off; -1 (the default, unless LKG_LOOKAHEAD_CTAS is set) uses the autotuned choice for the
+ * matrix size (lkg_kriging_autotune_lookahead), else 16.  The factor is the same bit for bit either way.  Returns
+ * the value set, or -2 on an argument outside -1 .. 64 (lkg_get_lookahead returns the setting). */
 int lkg_set_lookahead(int ctas);
 int lkg_get_lookahead(void);
 /* No counterpart in the reference: one product of the 7-bit digit kernel on host data, S digits (5..8):

@@ -98,6 +98,7 @@ _SIGS = {
     "lkg_kriging_last_slices": (_i, [_vp]),
     "lkg_kriging_eval_counts": (_i, [_vp, _vp, _vp]),
     "lkg_kriging_autotune_precision": (_i, [_vp, _dp, _i, _d, _d]),
+    "lkg_kriging_autotune_lookahead": (_i, [_vp, _dp, _i]),
     "lkg_autotune_enable": (None, [_i]),
     "lkg_autotune_record": (_i, [_cp, _ip, _dp, _i]),
     "lkg_autotune_lookup": (_i, [_cp, _i]),

@@ -79,6 +79,11 @@ void Autotuner::clear() {
   table_.clear();
 }
 
+void Autotuner::clear_key(const std::string& key) {
+  std::lock_guard<std::mutex> lk(mu_);
+  table_.erase(key);
+}
+
 bool Autotuner::save_file(const std::string& path) const {
   std::ostringstream o;
   o.precision(17);

@@ -34,6 +34,7 @@ class Autotuner {
   bool load_file(const std::string& path);
   bool save_file(const std::string& path) const;
   void clear();
+  void clear_key(const std::string& key);
 
  private:
   Autotuner();

@@ -528,6 +528,12 @@ int lkg_kriging_autotune_precision(void* ptr, const double* gamma, int gamma_n, 
   });
 }
 
+int lkg_kriging_autotune_lookahead(void* ptr, const double* gamma, int gamma_n) {
+  return run_entry<int>(-1, [&]() -> int {
+    return K(ptr)->autotune_lookahead(std::vector<double>(gamma, gamma + gamma_n));
+  });
+}
+
 int lkg_kriging_eval_counts(void* ptr, long long* evaluations, long long* rounds) {
   return run_entry<int>(-1, [&]() -> int {
     const Kriging* k = K(ptr);

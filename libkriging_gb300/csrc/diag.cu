@@ -147,7 +147,7 @@ extern "C" int lkg_set_lookahead(int ctas) {
     lkg::set_lookahead_ctas(ctas);
   } catch (const std::exception& e) {
     lkg::set_last_error(e.what());
-    return -1;
+    return -2;
   }
   return ctas;
 }

@@ -8,6 +8,8 @@
 // with x = L' \ E* and R^-1 = (L^-1)' L^-1.
 #include "engine.hpp"
 
+#include "autotune.hpp"
+
 #include <algorithm>
 #include <cmath>
 #include <atomic>
@@ -167,26 +169,37 @@ void Engine::set_slices(int s) {
   slices_ = s;
 }
 
-// SMs kept for the mixed Cholesky's look-ahead panel work (0: no look-ahead); the initial value comes from
-// LKG_LOOKAHEAD_CTAS (default 8), lkg_set_lookahead changes it
+// SMs kept for the mixed Cholesky's look-ahead panel work (0: no look-ahead).  An explicit setting
+// (LKG_LOOKAHEAD_CTAS, lkg_set_lookahead) applies to every size; otherwise (-1) the autotuner's choice for the matrix
+// size is used ("lookahead:n=<n>", see Kriging::autotune_lookahead), else kLookaheadDefault.
 namespace {
+constexpr int kLookaheadDefault = 16;
 std::atomic<int> g_lookahead_ctas{[] {
   const char* v = std::getenv("LKG_LOOKAHEAD_CTAS");
-  const int x = v ? std::atoi(v) : 8;
-  return x >= 0 && x <= 64 ? x : 8;
+  if (!v) return -1;
+  const int x = std::atoi(v);
+  return x >= 0 && x <= 64 ? x : -1;
 }()};
 }  // namespace
 
 void set_lookahead_ctas(int c) {
-  if (c < 0 || c > 64) throw std::invalid_argument("look-ahead: SMs for the panel work must be 0 .. 64");
+  if (c < -1 || c > 64) throw std::invalid_argument("look-ahead: SMs for the panel work must be -1 .. 64");
   g_lookahead_ctas = c;
 }
 int lookahead_ctas_setting() { return g_lookahead_ctas; }
 
-// the look-ahead pays when the matrix has several 256-wide panels
-bool Engine::lookahead_enabled() const { return g_lookahead_ctas > 0 && n_ >= 4 * OZ7_KB; }
+std::string lookahead_tune_key(int n) { return "lookahead:n=" + std::to_string(n); }
 
-int Engine::lookahead_ctas() const { return g_lookahead_ctas; }
+int lookahead_ctas_for(int n) {
+  const int c = g_lookahead_ctas;
+  if (c >= 0) return c;
+  return Autotuner::instance().lookup(lookahead_tune_key(n), kLookaheadDefault);
+}
+
+// the look-ahead pays when the matrix has several 256-wide panels
+bool Engine::lookahead_enabled() const { return n_ >= 4 * OZ7_KB && lookahead_ctas_for(n_) > 0; }
+
+int Engine::lookahead_ctas() const { return lookahead_ctas_for(n_); }
 
 void Engine::ensure_mixed_buffers(bool with_grad) {
   if (mixed_alloc_slices_ != slices_) {

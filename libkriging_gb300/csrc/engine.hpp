@@ -36,9 +36,12 @@ struct LooOut {
   std::vector<double> s2;      // sigma2LOO = 1 / diag(B)
 };
 
-// SMs kept for the panel work of the mixed Cholesky's look-ahead (0 turns it off); process-wide
+// SMs kept for the panel work of the mixed Cholesky's look-ahead (0 turns it off, -1 = the autotuned or default
+// choice per matrix size); process-wide
 void set_lookahead_ctas(int c);
 int lookahead_ctas_setting();
+std::string lookahead_tune_key(int n);
+int lookahead_ctas_for(int n);
 
 class Engine {
  public:

@@ -11,6 +11,7 @@
 #include "kriging.hpp"
 
 #include "autotune.hpp"
+#include "engine.hpp"
 
 #include <algorithm>
 #include <cmath>
@@ -312,6 +313,34 @@ int Kriging::autotune_precision(const std::vector<double>& gamma, double tol_ll,
   };
   const int choice = Autotuner::instance().choose(key.str(), {0, 5, 6, 7}, saved, cost);
   set_precision(choice);
+  return choice;
+}
+
+int Kriging::autotune_lookahead(const std::vector<double>& gamma) {
+  if (m_slices == 0) throw std::invalid_argument("autotune_lookahead: the look-ahead belongs to the mixed path");
+  const int saved = lookahead_ctas_setting();
+  auto cost = [&](int ctas) -> double {
+    set_lookahead_ctas(ctas);
+    double ms = 0.0;
+    for (int rep = 0; rep < 2; ++rep) {  // the second of two evaluations (the first allocates)
+      logLikelihoodFun(gamma, true, true);
+      ms = 0.0;
+      for (const auto& kv : m_bench) ms += kv.second;
+    }
+    return ms;
+  };
+  int choice = 16;
+  try {
+    const std::string key = lookahead_tune_key(m_n);
+    if (Autotuner::instance().enabled()) {
+      Autotuner::instance().clear_key(key);
+      choice = Autotuner::instance().choose(key, {0, 12, 16, 24, 32}, 16, cost);
+    }
+  } catch (...) {
+    set_lookahead_ctas(saved);
+    throw;
+  }
+  set_lookahead_ctas(saved);
   return choice;
 }
 

@@ -163,6 +163,10 @@ class Kriging {
   // within tol_ll / tol_grad (relative) of the FP64 path's, measured on this model (CUDA-event timings, errors with a
   // 10x margin); tabled by the autotuner under the problem's shape and the tolerances, then set as the precision.
   int autotune_precision(const std::vector<double>& gamma, double tol_ll, double tol_grad);
+  // The SMs kept for the mixed Cholesky's look-ahead at this model's size (0 = none, 12, 16, 24, 32), chosen by timing
+  // logLikelihoodFun(gamma, grad) on the mixed path for each (the factor is identical for all); tabled by the
+  // autotuner under the matrix size and used by every later evaluation of that size.  Returns the choice.
+  int autotune_lookahead(const std::vector<double>& gamma);
   // route the fit's objective evaluations through a shared service (design = this model's index there); nullptr
   // restores the model's own engine
   void attach_service(DenseService* s, int design) {

@@ -297,6 +297,15 @@ class Kriging:
             raise _lib.LibKrigingError(_lib.last_error())
         return r
 
+    def autotune_lookahead(self, gamma):
+        """Time the mixed Cholesky's look-ahead with 0 / 12 / 16 / 24 / 32 SMs for the panel work on this model and table
+        the fastest for its size (see lkg_kriging_autotune_lookahead); returns it."""
+        g = np.ascontiguousarray(gamma, dtype=np.float64)
+        r = _lib.load().lkg_kriging_autotune_lookahead(self._h, ptr(g), g.size)
+        if r < 0:
+            raise _lib.LibKrigingError(_lib.last_error())
+        return r
+
     def eval_counts(self):
         """(objective evaluations, GPU evaluation launches) since this model was created."""
         ev, ro = ctypes.c_longlong(), ctypes.c_longlong()
