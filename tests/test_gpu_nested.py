@@ -9,6 +9,7 @@ import pytest
 
 from conftest import rel_err
 from oracle import nested_oracle as N
+from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
@@ -134,16 +135,48 @@ def test_log_likelihood_groups_equals_lone_models(gpu_lib):
 
 # ---- the reference's own NestedKriging tests, on the BFGS path ----
 def test_one_group_reduces_to_kriging(gpu_lib):
-    """NestedKrigingTest.cpp:25-60."""
+    """NestedKrigingTest.cpp:25-60.  The NK mean of one expert is the expert's mean (1e-6) -- except where the fitted
+    theta puts the expert's factor on the reference's rcond cliff (rcond(L)^2 within a factor 2 of min_rcond = 1e-18):
+    there the nugget-retry branch is decided by the rcond estimate (LAPACK dtrcon in the reference, a dlacn2 estimate
+    here) and the expert's mean moves with it, so the NK mean is held to the oracle's NK aggregation at that theta
+    instead.  The fit's optimiser path is not pinned to the reference's, so either case can occur."""
+    from oracle import nested_oracle as NO
+    from scipy.linalg import lapack
     X, y = _data(40)
     Xt = np.random.default_rng(9).uniform(size=(30, 2))
     nk = gpu_lib.NestedKriging(y, X, "gauss", 1, aggregation="NK")
     m_nk, s_nk = nk.predict(Xt, True)
     m_kr, s_kr, _, _, _ = nk.submodel(0).predict(Xt, True, False, False)
+    th = nk.theta()
+    L, info = lapack.dpotrf(O.build_R("gauss", X, th, 1.0), lower=1, clean=1)
+    on_cliff = info == 0 and 0.5e-18 < O.rcond_chol(L) < 2e-18
+    if on_cliff:
+        mo_nk, _ = NO.predict_nk(y, X, "gauss", [np.arange(40)], th, nk.sigma2(), nk.beta0(), Xt)
+        assert np.max(np.abs(m_nk - mo_nk)) < 1e-6
+    else:
+        assert np.max(np.abs(m_nk - m_kr)) < 1e-6
+        assert np.max(np.abs(s_nk - s_kr)) < 5e-2
+    for agg in ["PoE", "gPoE", "BCM"]:
+        nk1 = gpu_lib.NestedKriging(y, X, "gauss", 1, aggregation=agg)
+        m1, s1 = nk1.predict(Xt, True)
+        mk, sk, _, _, _ = nk1.submodel(0).predict(Xt, True, False, False)
+        assert np.max(np.abs(m1 - mk)) < 1e-8
+        assert np.max(np.abs(s1 - sk)) < 1e-6
+
+
+def test_one_group_reduces_to_kriging_at_a_fixed_theta(gpu_lib):
+    """The reference's identity (NestedKrigingTest.cpp:25-60) away from the rcond cliff: one group, theta fixed at a
+    well-conditioned value, the NK mean equals the expert's to 1e-6 and the PoE family reduces to the expert."""
+    X, y = _data(40)
+    Xt = np.random.default_rng(9).uniform(size=(30, 2))
+    P = {"theta": np.array([[0.2, 0.25]])}
+    nk = gpu_lib.NestedKriging(y, X, "gauss", 1, aggregation="NK", optim="none", parameters=P)
+    m_nk, s_nk = nk.predict(Xt, True)
+    m_kr, s_kr, _, _, _ = nk.submodel(0).predict(Xt, True, False, False)
     assert np.max(np.abs(m_nk - m_kr)) < 1e-6
     assert np.max(np.abs(s_nk - s_kr)) < 5e-2
     for agg in ["PoE", "gPoE", "BCM"]:
-        nk1 = gpu_lib.NestedKriging(y, X, "gauss", 1, aggregation=agg)
+        nk1 = gpu_lib.NestedKriging(y, X, "gauss", 1, aggregation=agg, optim="none", parameters=P)
         m1, s1 = nk1.predict(Xt, True)
         mk, sk, _, _, _ = nk1.submodel(0).predict(Xt, True, False, False)
         assert np.max(np.abs(m1 - mk)) < 1e-8
