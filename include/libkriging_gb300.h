@@ -42,7 +42,8 @@ int lkg_kriging_fit_params(void* ptr, const double* y, int n, const double* X, i
                            int is_sigma2_estim, const double* theta, int theta_rows, int is_theta_estim,
                            const double* beta, int beta_n, int is_beta_estim, const double* nugget,
                            int is_nugget_estim);
-/* libkriging_c.h:58-69 lk_kriging_predict (return_deriv is rejected) */
+/* libkriging_c.h:58-69 lk_kriging_predict: mean (m), stdev (m), cov (m x m), and with return_deriv the derivatives of
+ * the mean and of the stdev with respect to the m points' coordinates (m x d each, column-major) */
 int lkg_kriging_predict(void* ptr, const double* X_n, int m, int d, int return_stdev, int return_cov,
                         int return_deriv, double* mean_out, double* stdev_out, double* cov_out, double* mean_deriv_out,
                         double* stdev_deriv_out);

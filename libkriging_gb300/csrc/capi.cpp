@@ -157,13 +157,13 @@ int lkg_kriging_predict(void* ptr, const double* X_n, int m, int d, int return_s
                         int return_deriv, double* mean_out, double* stdev_out, double* cov_out, double* mean_deriv_out,
                         double* stdev_deriv_out) {
   return run_entry<int>(-1, [&]() -> int {
-    (void)mean_deriv_out;
-    (void)stdev_deriv_out;
     auto [mean, sd, cov, md, sdd] = K(ptr)->predict(mat_of(X_n, m, d), return_stdev != 0, return_cov != 0,
                                                     return_deriv != 0);
     if (mean_out) std::memcpy(mean_out, mean.data(), sizeof(double) * mean.size());
     if (stdev_out && return_stdev) std::memcpy(stdev_out, sd.data(), sizeof(double) * sd.size());
     if (cov_out && return_cov) std::memcpy(cov_out, cov.v.data(), sizeof(double) * cov.v.size());
+    if (mean_deriv_out && return_deriv) std::memcpy(mean_deriv_out, md.v.data(), sizeof(double) * md.v.size());
+    if (stdev_deriv_out && return_deriv) std::memcpy(stdev_deriv_out, sdd.v.data(), sizeof(double) * sdd.v.size());
     return 0;
   });
 }

@@ -5,7 +5,7 @@
 //                      parse_method Optim.cpp:151-177, Random.cpp:13-49, make_fit_objective Kriging.cpp:1414-1470,
 //                      nugget reparametrisation Kriging.cpp:676-702)
 //   _logLikelihood     Kriging.cpp:214-341 (LL per noise model, gradient assembly, alpha-gradient)
-//   predict            Kriging.cpp:2240-2285 -> KrigingImpl.cpp:145-300 (mean, stdev, cov)
+//   predict            Kriging.cpp:2240-2285 -> KrigingImpl.cpp:145-300 (mean, stdev, cov, derivatives)
 // The multistart runs every start's L-BFGS-B in its own host thread; their objective calls are gathered by a
 // batcher into ONE batched GPU evaluation per round (the reference runs the starts one after another).
 #include "kriging.hpp"
@@ -75,6 +75,31 @@ std::vector<double> regression_matrix(RegressionModel r, const std::vector<doubl
   std::vector<double> F((size_t)n * cols.size());
   for (size_t q = 0; q < cols.size(); ++q) std::copy(cols[q].begin(), cols[q].end(), F.begin() + q * n);
   return F;
+}
+
+// Trend::regressionModelDerivative (src/lib/Trend.cpp:95-150): dF/dx at one point x (d values), d x p column-major,
+// DF(k, l) = d F_l / d x_k, columns in regression_matrix's order
+std::vector<double> regression_derivative(RegressionModel r, const double* x, int d, int p) {
+  std::vector<double> DF((size_t)d * p, 0.0);
+  auto at = [&](int k, int l) -> double& { return DF[k + (size_t)l * d]; };
+  int l = 1;
+  if (r == RegressionModel::Linear) {
+    for (int i = 0; i < d; ++i) at(i, l++) = 1.0;
+  } else if (r == RegressionModel::Interactive || r == RegressionModel::Quadratic) {
+    const bool sq = (r == RegressionModel::Quadratic);
+    for (int i = 0; i < d; ++i) {
+      at(i, l++) = 1.0;
+      for (int j = 0; j < (sq ? i + 1 : i); ++j, ++l) {
+        if (i == j) {
+          at(i, l) = 2.0 * x[i];
+        } else {
+          at(i, l) = x[j];
+          at(j, l) = x[i];
+        }
+      }
+    }
+  }
+  return DF;
 }
 
 // ---------------------------------------------------------------------------------------------------------------
@@ -1159,11 +1184,13 @@ std::tuple<std::vector<double>, std::vector<double>, Mat, Mat, Mat> Kriging::pre
   if (X_n.cols != m_d)
     throw std::runtime_error("Predict locations have wrong dimension: " + std::to_string(X_n.cols) + " instead of " +
                              std::to_string(m_d));
-  if (return_deriv) throw std::invalid_argument("predict: return_deriv is not supported by the GPU build");
   const int q = X_n.rows, d = m_d, n = m_n, p = m_p;
   const bool nug = (m_noise_model == NoiseModel::Nugget);
+  // Kriging.cpp:2262-2283: an LMP fit predicts with sigma2 (n - p) / (n - p - 2)
+  const double lmp_scale = (m_objective == "LMP") ? (n - p) / (n - p - 2.0) : 1.0;
+  const double sigma2 = m_sigma2 * lmp_scale;
   const double R_on_factor = nug ? m_alpha : 1.0;
-  const double var_scale = nug ? m_sigma2 / m_alpha : m_sigma2;
+  const double var_scale = nug ? sigma2 / m_alpha : sigma2;
   Mat Xnn;
   Xnn.rows = q;
   Xnn.cols = d;
@@ -1174,7 +1201,7 @@ std::tuple<std::vector<double>, std::vector<double>, Mat, Mat, Mat> Kriging::pre
   std::vector<double> Fn = regression_matrix(m_regmodel, Xnn.v, q, d, &pn);
   std::vector<double> zz = z();
   PredictOut po = predict_gpu(*m_model, Xnn.v.data(), q, m_theta.data(), R_on_factor, zz.data(), return_stdev || return_cov,
-                              return_cov, nug ? m_alpha : 1.0, nug);
+                              return_cov, nug ? m_alpha : 1.0, return_deriv);
   // yhat = F_n beta + Rstar_on' z
   std::vector<double> mean(q), sd;
   for (int i = 0; i < q; ++i) {
@@ -1183,11 +1210,11 @@ std::tuple<std::vector<double>, std::vector<double>, Mat, Mat, Mat> Kriging::pre
     mean[i] = m_centerY + m_scaleY * (fb + po.rz[i]);
   }
   Mat cov, md, sdd;
-  if (return_stdev || return_cov) {
+  std::vector<double> Rstar, Ec;
+  if (return_stdev || return_cov || return_deriv) {
     // Ecirc = (F_n - Rstar_on' M) * circ^-1   (rsolve_upper)
-    std::vector<double> Rstar;
     m_model->copy_model(0, nullptr, nullptr, nullptr, &Rstar, nullptr);
-    std::vector<double> Ec((size_t)q * p);
+    Ec.assign((size_t)q * p, 0.0);
     for (int i = 0; i < q; ++i) {
       for (int k = 0; k < p; ++k) {
         double e = Fn[i + (size_t)k * q] - po.rm[(size_t)i * p + k];
@@ -1215,6 +1242,51 @@ std::tuple<std::vector<double>, std::vector<double>, Mat, Mat, Mat> Kriging::pre
           for (int k = 0; k < p; ++k) e += Ec[i + (size_t)k * q] * Ec[j + (size_t)k * q];
           cov(i, j) = (cov(i, j) + e) * var_scale * m_scaleY * m_scaleY;
         }
+    }
+  }
+  if (return_deriv) {
+    // KrigingImpl.cpp:254-296, per point i with W_i = L^-1 DR_on_i (GPU) and DF_i = dF/dx at the point:
+    //   Dyhat(i, :)  = (DF_i beta + W_i' z)'
+    //   DEcirc_i     = circ'^-1 (DF_i - W_i' M)'                      (p x d)
+    //   Dysd2(i, :)  = -2 Rstar_on(:, i)' W_i + 2 Ecirc(i, :) DEcirc_i
+    // then the normalisation's chain rule and stdev_deriv = Dysd2 / (2 sqrt(ysd2)).
+    md.rows = sdd.rows = q;
+    md.cols = sdd.cols = d;
+    md.v.assign((size_t)q * d, 0.0);
+    sdd.v.assign((size_t)q * d, 0.0);
+    std::vector<double> xi(d), A((size_t)p * d), DE((size_t)p * d);
+    const double sd_scale = var_scale * m_scaleY * m_scaleY;
+    for (int i = 0; i < q; ++i) {
+      for (int k = 0; k < d; ++k) xi[k] = Xnn(i, k);
+      const std::vector<double> DF = regression_derivative(m_regmodel, xi.data(), d, p);
+      for (int k = 0; k < d; ++k) {
+        const size_t c = (size_t)i * d + k;
+        double fb = 0.0;
+        for (int l = 0; l < p; ++l) fb += DF[k + (size_t)l * d] * m_beta[l];
+        md.v[i + (size_t)k * q] = (fb + po.wz[c]) * m_scaleY / m_scaleX[k];
+      }
+      if (!return_stdev) continue;
+      for (int k = 0; k < d; ++k)
+        for (int l = 0; l < p; ++l)
+          A[l + (size_t)k * p] = DF[k + (size_t)l * d] - po.wm[((size_t)i * d + k) * p + l];
+      // forward substitution with circ' (lower): DE(l, k) = (A(l, k) - sum_{m<l} circ(m, l) DE(m, k)) / circ(l, l)
+      for (int k = 0; k < d; ++k)
+        for (int l = 0; l < p; ++l) {
+          double e = A[l + (size_t)k * p];
+          for (int m2 = 0; m2 < l; ++m2) e -= Rstar[m2 + (size_t)l * p] * DE[m2 + (size_t)k * p];
+          DE[l + (size_t)k * p] = e / Rstar[l + (size_t)l * p];
+        }
+      for (int k = 0; k < d; ++k) {
+        double ed = 0.0;
+        for (int l = 0; l < p; ++l) ed += Ec[i + (size_t)l * q] * DE[l + (size_t)k * p];
+        const double dysd2 = (-2.0 * po.wr[(size_t)i * d + k] + 2.0 * ed) * sd_scale / m_scaleX[k];
+        sdd.v[i + (size_t)k * q] = dysd2;
+      }
+    }
+    // the reference divides by 2 sqrt(ysd2) for every point, with ysd2 = 0 when the stdev is not requested
+    for (int i = 0; i < q; ++i) {
+      const double den = 2.0 * (return_stdev ? sd[i] : 0.0);
+      for (int k = 0; k < d; ++k) sdd.v[i + (size_t)k * q] /= den;
     }
   }
   return {mean, sd, cov, md, sdd};

@@ -7,6 +7,7 @@
 //                     alpha-gradient dot products of Kriging::_logLikelihood (src/lib/Kriging.cpp:307-326)
 //   gram/gls/residual KrigingImpl::populate_Model GLS block (src/lib/KrigingImpl.cpp:101-124)
 //   cov_cross         KrigingImpl::predict_impl R_on loop (src/lib/KrigingImpl.cpp:194-221)
+//   dcov_cross        KrigingImpl::predict_impl DR_on_i loop of the derivatives (src/lib/KrigingImpl.cpp:255-261)
 #include "lik_kernels.cuh"
 
 #include "stats.hpp"
@@ -120,6 +121,64 @@ __global__ void __launch_bounds__(256) k_cov_cross(int n_o, int q, int d, const 
       }
     }
     R[i + (int64_t)j * n_o] = (snap && coincident) ? 1.0 : cov_from_sum<K>(sum) * factor;
+  }
+}
+
+// d ln C / d x_k at dx = x_new - x_obs (Covariance.cpp:52-63, 90-100, 132-145, 181-196), the reference's operation
+// order: gauss -dx / theta^2; exp -sign(dx) / theta; matern3_2 -sqrt3 sign t / (1 + t) / theta;
+// matern5_2 -sqrt5 sign (a b) / (a + t b) / theta with t = s |dx / theta|, a = 1 + t, b = t / 3.
+template <int K>
+__device__ __forceinline__ double dlncov_dx(double dx, double th) {
+  const double sg = dx > 0.0 ? 1.0 : (dx < 0.0 ? -1.0 : 0.0);
+  if constexpr (K == KGAUSS) {
+    return -dx / (th * th);
+  } else if constexpr (K == KEXP) {
+    return -sg / th;
+  } else if constexpr (K == KMATERN32) {
+    const double t = sqrt(3.0) * fabs(dx / th);
+    return -sqrt(3.0) * sg * t / (1.0 + t) / th;
+  } else {
+    const double t = sqrt(5.0) * fabs(dx / th);
+    const double a = 1.0 + t, b = t / 3.0;
+    return -sqrt(5.0) * sg * (a * b) / (a + t * b) / th;
+  }
+}
+
+// DR(j, c * d + k) = R_on(j, c) d ln C / d x_k (Xn_c - Xo_j) for the q new points c (KrigingImpl.cpp:256-261), with
+// R_on(j, c) formed exactly as k_cov_cross forms it (coincident points give 1).  n_o x (q d), ld n_o.
+template <int K, int DM>
+__global__ void __launch_bounds__(256) k_dcov_cross(int n_o, int q, int d, const double* __restrict__ Xo,
+                                                    const double* __restrict__ Xn, const double* __restrict__ theta,
+                                                    double factor, double* __restrict__ DR) {
+  __shared__ double xo[DM][T], xn[DM][T], th[DM];
+  const int r0 = blockIdx.x * T, c0 = blockIdx.y * T, t = threadIdx.x;
+  for (int idx = t; idx < DM * T; idx += 256) {
+    const int k = idx / T, qq = idx % T;
+    xo[k][qq] = (k < d && r0 + qq < n_o) ? Xo[(r0 + qq) + (int64_t)k * n_o] : 0.0;
+    xn[k][qq] = (k < d && c0 + qq < q) ? Xn[(c0 + qq) + (int64_t)k * q] : 0.0;
+  }
+  if (t < DM) th[t] = (t < d) ? theta[t] : 1.0;
+  __syncthreads();
+  const int ri = t & 63, i = r0 + ri;
+  if (i >= n_o) return;
+  for (int s = 0; s < 16; ++s) {
+    const int cj = (t >> 6) + 4 * s, j = c0 + cj;
+    if (j >= q) continue;
+    double sum = 0.0;
+    bool coincident = true;
+#pragma unroll
+    for (int k = 0; k < DM; ++k) {
+      if (k < d) {
+        const double dx = xo[k][ri] - xn[k][cj];
+        coincident = coincident && (fabs(dx) <= 2.220446049250313e-16);
+        sum += cov_term<K>(dx, th[k]);
+      }
+    }
+    const double r = coincident ? 1.0 : cov_from_sum<K>(sum) * factor;
+    double* out = DR + i + (int64_t)j * d * n_o;
+#pragma unroll
+    for (int k = 0; k < DM; ++k)
+      if (k < d) out[(int64_t)k * n_o] = r * dlncov_dx<K>(xn[k][cj] - xo[k][ri], th[k]);
   }
 }
 
@@ -530,6 +589,17 @@ struct CovCrossLaunch {
 };
 
 template <int K, int DM>
+struct DCovCrossLaunch {
+  static void run(int n_o, int q, int d, const double* Xo, const double* Xn, const double* theta, double factor,
+                  double* DR, cudaStream_t st) {
+    LaunchTimer lt("k_dcov_cross", st, (double)n_o * q * (1.0 + d), 8.0 * n_o * q * d);
+    k_dcov_cross<K, DM><<<dim3(ceil_div(n_o, T), ceil_div(q, T), 1), 256, 0, st>>>(n_o, q, d, Xo, Xn, theta, factor,
+                                                                                    DR);
+    LKG_LAUNCH("k_dcov_cross");
+  }
+};
+
+template <int K, int DM>
 struct AdjointLaunch {
   static void run(int n, int d, const double* X, int64_t xb, const double* theta, const double* factor,
                   const double* xv, int64_t xvb, const double* Rinv, int64_t ldr, int64_t rstride, double* partials,
@@ -555,6 +625,12 @@ void cov_cross(int kernel, int n_o, int q, int d, const double* Xo, const double
                double factor, double* R, cudaStream_t st, bool snap_coincident) {
   if (n_o <= 0 || q <= 0) return;
   dispatch_kd<CovCrossLaunch>(kernel, d, n_o, q, d, Xo, Xn, theta, factor, R, snap_coincident, st);
+}
+
+void dcov_cross(int kernel, int n_o, int q, int d, const double* Xo, const double* Xn, const double* theta,
+                double factor, double* DR, cudaStream_t st) {
+  if (n_o <= 0 || q <= 0) return;
+  dispatch_kd<DCovCrossLaunch>(kernel, d, n_o, q, d, Xo, Xn, theta, factor, DR, st);
 }
 
 size_t adjoint_partials_size(int n, int d, int batch) {

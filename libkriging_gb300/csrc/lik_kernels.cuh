@@ -29,6 +29,11 @@ void cov_build_lower(int kernel, int n, int d, const double* X, int64_t x_bstrid
 void cov_cross(int kernel, int n_o, int q, int d, const double* Xo, const double* Xn, const double* theta,
                double factor, double* R, cudaStream_t st, bool snap_coincident = true);
 
+// Derivatives of R_on with respect to the new points: DR(j, c d + k) = R_on(j, c) dlnC/dx_k (Xn_c - Xo_j), n_o x (q d)
+// column-major (ld n_o), R_on as cov_cross forms it with snap_coincident.
+void dcov_cross(int kernel, int n_o, int q, int d, const double* Xo, const double* Xn, const double* theta,
+                double factor, double* DR, cudaStream_t st);
+
 // Adjoint partial sums over the strict lower triangle (+ diagonal terms), one partial per 64x64 tile,
 // then a deterministic fixed-order reduction into out[b * nacc + a].
 void adjoint_sums(int kernel, int n, int d, const double* X, int64_t x_bstride, const double* theta,

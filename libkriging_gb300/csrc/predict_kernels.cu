@@ -1,8 +1,9 @@
 // predict_kernels.cu -- GPU part of Kriging::predict.
 //
-// KrigingImpl::predict_impl (src/lib/KrigingImpl.cpp:145-251): R_on (:194-221), Rstar_on = L \ R_on (:223),
+// KrigingImpl::predict_impl (src/lib/KrigingImpl.cpp:145-300): R_on (:194-221), Rstar_on = L \ R_on (:223),
 // yhat = F_n beta + Rstar_on' z (:226), Fhat_n = Rstar_on' M (:232), sd2 = 1 - colsum(Rstar_on^2) + ... (:238),
-// Sigma_n = R_nn - Rstar_on' Rstar_on + Ecirc Ecirc' (:248).  The p-column trend algebra stays on the host.
+// Sigma_n = R_nn - Rstar_on' Rstar_on + Ecirc Ecirc' (:248); the derivatives' W_i = L \ DR_on_i and its products
+// with z, Rstar_on and M (:254-281).  The p-column trend algebra stays on the host.
 #include "predict_kernels.cuh"
 
 #include "stats.hpp"
@@ -27,29 +28,31 @@ __device__ double bsum(double v, double* red) {
   return s;
 }
 
-// per column j of Rs (n x q): rz[j] = Rs(:,j)'z, rr[j] = Rs(:,j)'Rs(:,j), rm[j*p + k] = Rs(:,j)'M(:,k)
-__global__ void k_predict_reduce(int n, int q, int p, const double* __restrict__ Rs, const double* __restrict__ z,
-                                 const double* __restrict__ M, double* __restrict__ rz, double* __restrict__ rr,
-                                 double* __restrict__ rm) {
+// per column c of W (n x ncols, ld n): oz[c] = W(:,c)'z, orr[c] = W(:,c)'R(:, c / rdiv) (ld n),
+// om[c * p + k] = W(:,c)'M(:,k); one CTA per (column, product), fixed-order sums
+__global__ void k_predict_reduce(int n, int ncols, int p, const double* __restrict__ W, const double* __restrict__ z,
+                                 const double* __restrict__ R, int rdiv, const double* __restrict__ M,
+                                 double* __restrict__ oz, double* __restrict__ orr, double* __restrict__ om) {
   const int j = blockIdx.x;
-  const int k = (int)blockIdx.y - 2;  // -2: rz, -1: rr, >= 0: rm column k
+  const int k = (int)blockIdx.y - 2;  // -2: z, -1: R, >= 0: M column k
   __shared__ double red[32];
-  const double* c = Rs + (size_t)j * n;
+  const double* c = W + (size_t)j * n;
+  const double* v = (k == -2) ? z : (k == -1) ? R + (size_t)(j / rdiv) * n : M + (size_t)k * n;
   double s = 0.0;
-  if (k == -2) {
-    for (int i = threadIdx.x; i < n; i += blockDim.x) s = fma(c[i], z[i], s);
-  } else if (k == -1) {
-    for (int i = threadIdx.x; i < n; i += blockDim.x) s = fma(c[i], c[i], s);
-  } else {
-    const double* m = M + (size_t)k * n;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) s = fma(c[i], m[i], s);
-  }
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s = fma(c[i], v[i], s);
   s = bsum<256>(s, red);
   if (threadIdx.x == 0) {
-    if (k == -2) rz[j] = s;
-    else if (k == -1) rr[j] = s;
-    else rm[(size_t)j * p + k] = s;
+    if (k == -2) oz[j] = s;
+    else if (k == -1) orr[j] = s;
+    else om[(size_t)j * p + k] = s;
   }
+}
+
+void predict_reduce(int n, int ncols, int p, const double* W, const double* z, const double* R, int rdiv,
+                    const double* M, double* oz, double* orr, double* om, cudaStream_t st) {
+  LaunchTimer lt("k_predict_reduce", st, 2.0 * n * ncols * (p + 2.0), 8.0 * n * ncols);
+  k_predict_reduce<<<dim3(ncols, 2 + p), 256, 0, st>>>(n, ncols, p, W, z, R, rdiv, M, oz, orr, om);
+  LKG_LAUNCH("k_predict_reduce");
 }
 
 struct DevBuf {
@@ -63,8 +66,7 @@ struct DevBuf {
 }  // namespace
 
 PredictOut predict_gpu(const Engine& model, const double* Xn, int q, const double* theta, double factor,
-                       const double* z, bool need_rr, bool need_cov, double nn_factor, bool nugget) {
-  (void)nugget;
+                       const double* z, bool need_rr, bool need_cov, double nn_factor, bool need_deriv) {
   const int n = model.n(), d = model.d(), p = model.p();
   cudaStream_t st = model.stream();
   PredictOut o;
@@ -75,9 +77,7 @@ PredictOut predict_gpu(const Engine& model, const double* Xn, int q, const doubl
   LKG_CUDA(cudaMemcpyAsync(dz.p, z, sizeof(double) * n, cudaMemcpyHostToDevice, st));
   cov_cross(model.kernel(), n, q, d, model.dX(), dXn.p, dth.p, factor, dRs.p, st);
   model.solve_lower_inplace(0, dRs.p, n, q);
-  LaunchTimer lt("k_predict_reduce", st, 2.0 * n * q * (p + 2.0), 8.0 * n * q);
-  k_predict_reduce<<<dim3(q, 2 + p), 256, 0, st>>>(n, q, p, dRs.p, dz.p, model.dFY(0), drz.p, drr.p, drm.p);
-  LKG_LAUNCH("k_predict_reduce");
+  predict_reduce(n, q, p, dRs.p, dz.p, dRs.p, 1, model.dFY(0), drz.p, drr.p, drm.p, st);
   o.rz.resize(q);
   o.rr.resize(q);
   o.rm.resize((size_t)q * p);
@@ -99,6 +99,35 @@ PredictOut predict_gpu(const Engine& model, const double* Xn, int q, const doubl
     LKG_CUDA(cudaStreamSynchronize(st));
     for (int j = 0; j < q; ++j)
       for (int i = 0; i < j; ++i) o.sigma[i + (size_t)j * q] = o.sigma[j + (size_t)i * q];
+  }
+  if (need_deriv) {
+    // W = L \ DR_on in chunks of points (n x qc d doubles at most 2^26), then its column products with z,
+    // Rstar_on(:, c) and M (KrigingImpl.cpp:254-281)
+    const int qc = (int)std::max<int64_t>(1, std::min<int64_t>(q, ((int64_t)1 << 26) / ((int64_t)n * d)));
+    DevBuf dW((size_t)n * qc * d), dwz((size_t)qc * d), dwr((size_t)qc * d), dwm((size_t)qc * d * std::max(p, 1));
+    o.wz.resize((size_t)q * d);
+    o.wr.resize((size_t)q * d);
+    o.wm.resize((size_t)q * d * p);
+    for (int c0 = 0; c0 < q; c0 += qc) {
+      const int nc = std::min(qc, q - c0), ncol = nc * d;
+      // the chunk's points are columns c0.. of the q x d column-major Xn: pass them with their own leading dimension
+      std::vector<double> xc((size_t)nc * d);
+      for (int k = 0; k < d; ++k)
+        for (int c = 0; c < nc; ++c) xc[c + (size_t)k * nc] = Xn[(c0 + c) + (size_t)k * q];
+      DevBuf dxc((size_t)nc * d);
+      LKG_CUDA(cudaMemcpyAsync(dxc.p, xc.data(), sizeof(double) * nc * d, cudaMemcpyHostToDevice, st));
+      dcov_cross(model.kernel(), n, nc, d, model.dX(), dxc.p, dth.p, factor, dW.p, st);
+      model.solve_lower_inplace(0, dW.p, n, ncol);
+      predict_reduce(n, ncol, p, dW.p, dz.p, dRs.p + (size_t)c0 * n, d, model.dFY(0), dwz.p, dwr.p, dwm.p, st);
+      LKG_CUDA(cudaMemcpyAsync(o.wz.data() + (size_t)c0 * d, dwz.p, sizeof(double) * ncol, cudaMemcpyDeviceToHost,
+                               st));
+      LKG_CUDA(cudaMemcpyAsync(o.wr.data() + (size_t)c0 * d, dwr.p, sizeof(double) * ncol, cudaMemcpyDeviceToHost,
+                               st));
+      if (p > 0)
+        LKG_CUDA(cudaMemcpyAsync(o.wm.data() + (size_t)c0 * d * p, dwm.p, sizeof(double) * ncol * p,
+                                 cudaMemcpyDeviceToHost, st));
+      LKG_CUDA(cudaStreamSynchronize(st));  // xc and dxc are released at the end of the iteration
+    }
   }
   LKG_CUDA(cudaStreamSynchronize(st));
   return o;

@@ -234,9 +234,12 @@ class Kriging:
         mean = np.zeros(m)
         sd = np.zeros(m) if return_stdev else None
         cov = np.zeros((m, m), order="F") if return_cov else None
+        md = np.zeros((m, d), order="F") if return_deriv else None
+        sdd = np.zeros((m, d), order="F") if return_deriv else None
         check(_lib.load().lkg_kriging_predict(self._h, ptr(X), m, d, int(bool(return_stdev)), int(bool(return_cov)),
-                                              int(bool(return_deriv)), ptr(mean), ptr(sd), ptr(cov), None, None))
-        return mean, sd, cov, None, None
+                                              int(bool(return_deriv)), ptr(mean), ptr(sd), ptr(cov), ptr(md),
+                                              ptr(sdd)))
+        return mean, sd, cov, md, sdd
 
     # ---- Vecchia (Kriging.hpp:145-173) ----
     def predictVecchia(self, X, return_stdev=True, m=0):

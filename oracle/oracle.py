@@ -158,6 +158,27 @@ def dlncov(kernel: str, dx, theta):
     return out
 
 
+def dlncov_dx(kernel: str, dx, theta):
+    """d ln Cov / d x at dx (Covariance.cpp:52-63 gauss, 90-100 exp, 132-145 matern3_2, 181-196 matern5_2), element by
+    element in the reference's operation order."""
+    out = np.empty(len(dx))
+    s3, s5 = math.sqrt(3.0), math.sqrt(5.0)
+    for i, (x, th) in enumerate(zip(dx, theta)):
+        sg = 1.0 if x > 0 else (-1.0 if x < 0 else 0.0)
+        if kernel == "gauss":
+            out[i] = -x / (th * th)
+        elif kernel == "exp":
+            out[i] = -sg / th
+        elif kernel == "matern3_2":
+            t = s3 * abs(x / th)
+            out[i] = -s3 * sg * t / (1.0 + t) / th
+        else:
+            t = s5 * abs(x / th)
+            a, b = 1.0 + t, t / 3.0
+            out[i] = -s5 * sg * (a * b) / (a + t * b) / th
+    return out
+
+
 def build_R(kernel: str, X, theta, factor: float = 1.0, diag=None):
     """cholCov's covariance build (LinearAlgebra.cpp:142-181): full symmetric n x n, column-major."""
     X = _colmajor(X)
@@ -326,6 +347,33 @@ def regression_matrix(regmodel: str, X):
     else:
         raise ValueError("Cannot convert '%s' as a regression model" % regmodel)
     return np.asfortranarray(np.stack(cols, axis=1))
+
+
+def regression_derivative(regmodel: str, x):
+    """Trend.cpp:95-150: dF/dx at one point, d x p with DF[k, l] = d F_l / d x_k."""
+    x = np.asarray(x, dtype=np.float64)
+    d = x.size
+    p = regression_matrix(regmodel, x.reshape(1, -1)).shape[1]
+    DF = np.zeros((d, p))
+    if regmodel in ("none", "constant"):
+        return DF
+    c = 1
+    if regmodel == "linear":
+        for i in range(d):
+            DF[i, c] = 1.0
+            c += 1
+        return DF
+    for i in range(d):
+        DF[i, c] = 1.0
+        c += 1
+        for j in range(i + 1 if regmodel == "quadratic" else i):
+            if i == j:
+                DF[i, c] = 2.0 * x[i]
+            else:
+                DF[i, c] = x[j]
+                DF[j, c] = x[i]
+            c += 1
+    return DF
 
 
 def theta_bounds(X, y, cfg: Config = CONFIG):
@@ -593,9 +641,12 @@ class OracleKriging:
                 grad[k] = (self.log_marg_post(ge, False)[0] - value) / 1e-6
         return value, grad
 
-    # KrigingImpl.cpp:145-251, Kriging.cpp:2240-2285 (mean and stdev)
-    def predict(self, Xn, theta, beta, sigma2, alpha=1.0, return_stdev=True, fixed_beta=False):
-        """fixed_beta: beta is a given trend (is_beta_estim = false), so z = L \\ (y - F beta) (KrigingImpl.cpp:116)."""
+    # KrigingImpl.cpp:145-300, Kriging.cpp:2240-2285 (mean, stdev and their derivatives)
+    def predict(self, Xn, theta, beta, sigma2, alpha=1.0, return_stdev=True, fixed_beta=False, return_deriv=False,
+                objective="LL"):
+        """fixed_beta: beta is a given trend (is_beta_estim = false), so z = L \\ (y - F beta) (KrigingImpl.cpp:116).
+        objective "LMP" scales sigma2 by (n - p) / (n - p - 2) (Kriging.cpp:2262).  With return_deriv the result is
+        (yhat, stdev, dyhat, dstdev), the derivatives q x d with respect to the prediction points."""
         Xn = np.atleast_2d(np.asarray(Xn, dtype=np.float64))
         Xn_n = (Xn - self.centerX) / self.scaleX
         Fn = regression_matrix(self.regmodel, Xn_n)
@@ -611,18 +662,46 @@ class OracleKriging:
                     R_on[i, j] = cov(self.kernel, dij, theta) * alpha
         z = m.ystar - m.Fstar @ np.asarray(beta, dtype=np.float64) if fixed_beta else m.Estar
         Rs = solve_lower(m.L, R_on)
+        beta = np.asarray(beta, dtype=np.float64)
         yhat = Fn @ beta + Rs.T @ z
         yhat = self.centerY + self.scaleY * yhat
-        if not return_stdev:
+        if not return_stdev and not return_deriv:
             return yhat, None
         E = Fn - Rs.T @ m.Fstar
         # rsolve_upper(circ, E): X * circ = E
         Ec = lapack.dtrtrs(m.Rstar, np.asfortranarray(E.T), lower=0, trans=1)[0].T if m.Rstar.size else E
-        sd2 = 1.0 - np.sum(Rs * Rs, axis=0) + np.sum(Ec * Ec, axis=1)
-        sd2 = np.where(np.isnan(sd2) | (sd2 < 0), 0.0, sd2)
+        if objective == "LMP":
+            p = self.F.shape[1]
+            sigma2 = sigma2 * (n_o - p) / (n_o - p - 2.0)
         var_scale = sigma2 / alpha if self.noise_model == "nugget" else sigma2
-        sd2 = sd2 * var_scale * self.scaleY * self.scaleY
-        return yhat, np.sqrt(sd2)
+        sd2 = np.zeros(q)
+        if return_stdev:
+            sd2 = 1.0 - np.sum(Rs * Rs, axis=0) + np.sum(Ec * Ec, axis=1)
+            sd2 = np.where(np.isnan(sd2) | (sd2 < 0), 0.0, sd2)
+            sd2 = sd2 * var_scale * self.scaleY * self.scaleY
+        if not return_deriv:
+            return yhat, np.sqrt(sd2)
+        # KrigingImpl.cpp:254-296
+        d = Xn_n.shape[1]
+        dy = np.zeros((q, d))
+        dsd2 = np.zeros((q, d))
+        for i in range(q):
+            DR = np.empty((n_o, d))
+            for j in range(n_o):
+                DR[j] = R_on[j, i] * dlncov_dx(self.kernel, Xn_n[i] - self.X[j], theta)
+            DF = regression_derivative(self.regmodel, Xn_n[i])
+            W = solve_lower(m.L, DR)
+            dy[i] = DF @ beta + W.T @ z
+            if return_stdev:
+                rhs = (DF - W.T @ m.Fstar).T
+                DE = lapack.dtrtrs(m.Rstar, np.asfortranarray(rhs), lower=0, trans=1)[0] if m.Rstar.size else rhs
+                dsd2[i] = -2.0 * Rs[:, i] @ W + 2.0 * Ec[i] @ DE
+        dy = dy * self.scaleY / self.scaleX
+        dsd2 = dsd2 * var_scale * self.scaleY * self.scaleY / self.scaleX
+        sd = np.sqrt(sd2)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            dsd = dsd2 / (2.0 * sd)[:, None]
+        return yhat, (sd if return_stdev else None), dy, dsd
 
 
     # Kriging.cpp:1717-2209 (BFGS[N], objective LL), with scipy's L-BFGS-B (Fortran/C port of Nocedal's 3.0 code)
