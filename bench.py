@@ -360,8 +360,21 @@ def run_gpu(args):
                 stage_ms={kk: round(v, 3) for kk, v in stage.items()}, kernels=_kern(stats),
                 kernel_stats_steps=stats_steps)
     if rank == 0 and world == 1 and not args.no_batched:
-        line["batched"] = batched_multistart(lk, lib, steps=args.batched_steps, warmup=1,
-                                             peak_fp64=peak_fp64.value, cpu=not args.no_cpu_baseline)
+        # the batched fits in FP64 (the record's value), and the same fits on the mixed path beside them: at this
+        # design's conditioning (cond(R) up to ~1e11) the mixed gradient can steer a fit to another local optimum,
+        # so the mixed fit is reported with its distance from the FP64 fit, not as the value
+        b64 = batched_multistart(lk, lib, steps=args.batched_steps, warmup=1, peak_fp64=peak_fp64.value,
+                                 cpu=not args.no_cpu_baseline)
+        bmx = batched_multistart(lk, lib, steps=1, warmup=1, peak_fp64=peak_fp64.value, cpu=False,
+                                 mixed_slices=args.slices)
+        b64["mixed"] = {kk: bmx[kk] for kk in ("value", "e2e", "device_ms_per_fit", "rounds_per_fit",
+                                               "evaluations_per_fit", "theta", "ll", "dtype", "roofline")}
+        b64["mixed"]["speedup_vs_fp64"] = dict(device=bmx["value"] / b64["value"],
+                                               e2e=bmx["e2e"]["value"] / b64["e2e"]["value"])
+        b64["mixed"]["rel_err_vs_fp64_fit"] = dict(
+            ll=abs(bmx["ll"] - b64["ll"]) / abs(b64["ll"]),
+            theta=float(np.linalg.norm(np.subtract(bmx["theta"], b64["theta"])) / np.linalg.norm(b64["theta"])))
+        line["batched"] = b64
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         rec, ll_o, g_o = cpu_baseline(X, y, theta, alpha)
         line["cpu_baseline"] = rec
@@ -651,6 +664,32 @@ def run_gpu_nested(args):
                 kernels={kk: dict(launches=v["launches"], ms=round(v["ms"], 3)) for kk, v in stats.items()},
                 dominant=dict(kernel=dom[0], ms=dom[1]["ms"], share=dom[1]["ms"] / max(1e-9, sum(
                     v["ms"] for v in stats.values()))))
+    if args.nested_nk:
+        # NK aggregation on one 128-point chunk: a model with the fitted common theta (optim "none", so every group
+        # keeps it), its NK factorisations, then one chunk of predictions; the pair cross-covariances are
+        # sum_{i<j} n_i n_j kernel evaluations and 2 x 128 x that many FP64 flops per chunk
+        nkm = lk.NestedKriging("matern3_2", aggregation="NK")
+        if args.mixed:
+            nkm.set_precision(args.slices)
+        t0 = time.perf_counter()
+        nkm.fit_groups(y, X, labels, "constant", "none", "LL", {"theta": np.asarray(nk.theta()).reshape(1, -1)})
+        nk_setup_s = time.perf_counter() - t0
+        s1 = float(np.sum(sizes.astype(np.float64)))
+        pair_evals = 0.5 * (s1 * s1 - float(np.sum(sizes.astype(np.float64) ** 2)))
+        lib.lkg_stats_reset()
+        lib.lkg_stats_enable(1)
+        t0 = time.perf_counter()
+        m_nk, s_nk = nkm.predict(Xp[:128], True)
+        nk_s = time.perf_counter() - t0
+        lib.lkg_stats_enable(0)
+        st_nk = kernel_stats(lib)
+        line["nk_chunk"] = dict(points=128, seconds=nk_s, setup_seconds=nk_setup_s, group_pairs=p * (p - 1) // 2,
+                                pair_kernel_evaluations=pair_evals, bilinear_flops=2.0 * 128 * pair_evals,
+                                kernels={kk: dict(launches=v["launches"], ms=round(v["ms"], 3))
+                                         for kk, v in st_nk.items()},
+                                mean_rel_diff_vs_gpoe=float(np.linalg.norm(m_nk - mean[:128]) /
+                                                            np.linalg.norm(mean[:128])))
+        del nkm
     print("nested (GPU part): " + json.dumps(line), file=sys.stderr, flush=True)
     if not args.no_cpu_baseline:
         from oracle import baseline as B
@@ -686,6 +725,8 @@ def main():
     ap.add_argument("--mixed", action="store_true", help="multistart / nested workloads on the mixed path")
     ap.add_argument("--nested-n", type=int, default=1_000_000, help="points of the nested workload")
     ap.add_argument("--nested-q", type=int, default=100_000, help="gPoE prediction points of the nested workload")
+    ap.add_argument("--nested-nk", action="store_true",
+                    help="nested workload: also time NK aggregation on one 128-point chunk")
     ap.add_argument("--no-batched", action="store_true", help="omit the batched multistart sub-record")
     ap.add_argument("--digit-tile", type=int, default=0, choices=[0, 32, 64],
                     help="output tile width of the digit products (0: the library's default)")

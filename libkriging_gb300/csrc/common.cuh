@@ -31,6 +31,23 @@ inline void check_cuda(cudaError_t e, const char* what, const char* file, int li
 #define LKG_CUDA(x) ::lkg::check_cuda((x), #x, __FILE__, __LINE__)
 #define LKG_LAUNCH(what) ::lkg::check_cuda(cudaGetLastError(), what, __FILE__, __LINE__)
 
+// 1 / sqrt(piv) by Newton's iteration y <- y (3 - piv y^2) / 2 from a single-precision seed: two steps take the
+// seed's 2^-23 relative error below FP64 rounding; outside the range where the seed is a normal float the square
+// root and the reciprocal are taken directly
+__device__ __forceinline__ void pivot_root(double piv, double& root, double& rroot) {
+  if (piv >= 1e-30 && piv <= 1e30) {
+    double y = (double)rsqrtf((float)piv);
+    const double h = -0.5 * piv;
+    y = y * fma(h, y * y, 1.5);
+    y = y * fma(h, y * y, 1.5);
+    rroot = y;
+    root = piv * y;
+  } else {
+    root = sqrt(piv);
+    rroot = 1.0 / root;
+  }
+}
+
 // ---------------------------------------------------------------------------------------------------------------
 // device covariance functions.  dx is X_j - X_i (sign irrelevant for Cov and DlnCovDtheta), inv_theta = 1/theta is
 // NOT used for the value so that the rounding matches the reference's dx/theta division.

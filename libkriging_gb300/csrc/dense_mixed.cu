@@ -35,8 +35,7 @@ void factor_panel7(double* A, int64_t lda, int64_t mstride, int n, int K0, doubl
     if (M <= 0) continue;
     double* A21 = A + (k0 + nb) + (int64_t)k0 * lda;
     // L21 = A21 Dinv_k^T: B rows are the rows of Dinv_k
-    oz7_split(M, nb, A21, 1, lda, mstride, batch, SA, st);
-    oz7_split(nb, nb, Dinv + (int64_t)k * NB * NB, 1, NB, dstride, batch, SD, st);
+    oz7_split2(M, nb, A21, 1, lda, mstride, SA, nb, nb, Dinv + (int64_t)k * NB * NB, 1, NB, dstride, SD, batch, st);
     oz7_gemm_ex(M, nb, 0, 1, 1.0, SA, 0, SD, 0, 0.0, A21, lda, mstride, batch, false, max_ctas, st);
     const int wr = K0 + W - (k0 + nb);  // panel columns right of this block
     if (wr > 0) {  // A(k0+nb:, k0+nb:K0+W) -= L21 L21(0:wr, :)^T (the strict upper part written is never read)
@@ -117,14 +116,14 @@ void trtri_blocked_mixed7(const double* L, int64_t lda, int64_t mstride, int n, 
       const int nb = std::min(NB, n - k0), k = k0 / NB;
       copy_dinv_block(Dinv, dstride, k, W, ldw, wstride, k0, nb, batch, st);
       if (k0 > 0) {  // W(k0:k0+nb, 0:k0) = -Dinv_k Acc(k0:k0+nb, 0:k0): B rows are the columns of Acc
-        oz7_split(nb, nb, Dinv + (int64_t)k * NB * NB, 1, NB, dstride, batch, SA, st);
-        oz7_split(k0, nb, W + k0, ldw, 1, wstride, batch, SB, st);
+        oz7_split2(nb, nb, Dinv + (int64_t)k * NB * NB, 1, NB, dstride, SA, k0, nb, W + k0, ldw, 1, wstride, SB,
+                   batch, st);
         oz7_gemm(nb, k0, 0, 1, -1.0, SA, SB, 0.0, W + k0, ldw, wstride, batch, false, st);
       }
       const int mr = K0 + Wd - (k0 + nb);  // rows of this 256-row block below the 64-row one
       if (mr > 0) {  // Acc(k0+nb:K0+Wd, 0:k0+nb) += L(k0+nb:K0+Wd, k0:k0+nb) W(k0:k0+nb, 0:k0+nb)
-        oz7_split(mr, nb, L + (k0 + nb) + (int64_t)k0 * lda, 1, lda, mstride, batch, SA, st);
-        oz7_split(k0 + nb, nb, W + k0, ldw, 1, wstride, batch, SB, st);
+        oz7_split2(mr, nb, L + (k0 + nb) + (int64_t)k0 * lda, 1, lda, mstride, SA, k0 + nb, nb, W + k0, ldw, 1,
+                   wstride, SB, batch, st);
         oz7_gemm(mr, k0 + nb, 0, 1, 1.0, SA, SB, 1.0, W + k0 + nb, ldw, wstride, batch, false, st);
       }
     }
@@ -132,8 +131,8 @@ void trtri_blocked_mixed7(const double* L, int64_t lda, int64_t mstride, int n, 
     if (M2 <= 0) continue;
     // Acc(K0+Wd:, 0:N) += L(K0+Wd:, K0:K0+Wd) W(K0:K0+Wd, 0:N), N = K0 + Wd
     const int N = K0 + Wd;
-    oz7_split(M2, Wd, L + (K0 + Wd) + (int64_t)K0 * lda, 1, lda, mstride, batch, SL, st);
-    oz7_split(N, Wd, W + K0, ldw, 1, wstride, batch, SR, st);
+    oz7_split2(M2, Wd, L + (K0 + Wd) + (int64_t)K0 * lda, 1, lda, mstride, SL, N, Wd, W + K0, ldw, 1, wstride, SR,
+               batch, st);
     oz7_gemm(M2, N, 0, 1, 1.0, SL, SR, 1.0, W + K0 + Wd, ldw, wstride, batch, false, st);
   }
 }

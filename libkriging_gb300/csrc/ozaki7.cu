@@ -190,14 +190,28 @@ __device__ __forceinline__ uint32_t bf16_bits_of_small(int d) {
   return (uint32_t)__float_as_int(f) >> 16;
 }
 
-// split: one warp per (row, k block); lane l holds the column pairs 2 l, 2 l + 1 of every 64-wide sub-chunk
+// one operand of a split launch: element (r, k) of batch entry b at p[b * bstride + r * s_r + k * s_k]
+struct SplitJob {
+  int rows, K;
+  const double* p;
+  int64_t s_r, s_k, bstride;
+  Split7 out;
+};
+
+// split: one warp per (row, k block); lane l holds the column pairs 2 l, 2 l + 1 of every 64-wide sub-chunk.  One
+// launch serves two operands: CTAs x < nx0 the first, the rest the second.
 template <int S>
-__global__ void __launch_bounds__(256) k_oz7_split(int rows, int K, const double* __restrict__ p, int64_t s_r,
-                                                   int64_t s_k, int64_t bstride, Split7 out) {
+__global__ void __launch_bounds__(256) k_oz7_split(SplitJob j0, SplitJob j1, int nx0) {
+  const bool second = (int)blockIdx.x >= nx0;
+  const int rows = second ? j1.rows : j0.rows, K = second ? j1.K : j0.K;
+  const double* __restrict__ p = second ? j1.p : j0.p;
+  const int64_t s_r = second ? j1.s_r : j0.s_r, s_k = second ? j1.s_k : j0.s_k;
+  const int64_t bstride = second ? j1.bstride : j0.bstride;
+  const Split7 out = second ? j1.out : j0.out;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int r = blockIdx.x * 8 + warp, kb = blockIdx.y;
+  const int r = ((int)blockIdx.x - (second ? nx0 : 0)) * 8 + warp, kb = blockIdx.y;
   const int64_t b = blockIdx.z;
-  if (r >= out.rows_pad) return;
+  if (r >= out.rows_pad || kb >= out.nblk) return;
   const int spb = out.sub_per_blk;
   double x[2 * OZ7_MAX_SPB];
 #pragma unroll
@@ -656,9 +670,10 @@ Split7 oz7_buffer(void* planes, int* exps, int S, int rows_cap, int K_cap, int k
   return s;
 }
 
-void oz7_split(int rows, int K, const double* p, int64_t s_r, int64_t s_k, int64_t bstride, int batch, Split7& out,
-               cudaStream_t st) {
-  if (rows <= 0 || K <= 0) return;
+namespace {
+
+// fills the descriptor's extents for a rows x K operand and checks them against its buffer
+void split_prepare(int rows, int K, Split7& out) {
   if (out.sub_per_blk < 1 || out.sub_per_blk > OZ7_MAX_SPB) throw std::invalid_argument("oz7_split: bad k block");
   if (out.S < 5 || out.S > 8) throw std::invalid_argument("oz7_split: digits must be 5 .. 8");
   out.rows_pad = ceil_div(rows, TM) * TM;
@@ -667,15 +682,45 @@ void oz7_split(int rows, int K, const double* p, int64_t s_r, int64_t s_k, int64
   if ((size_t)out.S * out.nsub * out.rows_pad * OZ7_SUB > (size_t)out.plane_bstride ||
       (size_t)out.nblk * out.rows_pad > (size_t)out.exp_bstride)
     throw std::logic_error("oz7_split: operand larger than its buffer");
-  dim3 grid(out.rows_pad / 8, out.nblk, batch);
-  LaunchTimer lt("k_oz7_split", st, 0.0, ((double)rows * K * (8.0 + 2.0 * out.S)) * batch);
-  switch (out.S) {
-    case 5: k_oz7_split<5><<<grid, 256, 0, st>>>(rows, K, p, s_r, s_k, bstride, out); break;
-    case 6: k_oz7_split<6><<<grid, 256, 0, st>>>(rows, K, p, s_r, s_k, bstride, out); break;
-    case 7: k_oz7_split<7><<<grid, 256, 0, st>>>(rows, K, p, s_r, s_k, bstride, out); break;
-    default: k_oz7_split<8><<<grid, 256, 0, st>>>(rows, K, p, s_r, s_k, bstride, out); break;
+}
+
+void split_launch(const SplitJob& j0, const SplitJob& j1, int batch, cudaStream_t st) {
+  const int nx0 = j0.rows > 0 ? j0.out.rows_pad / 8 : 0, nx1 = j1.rows > 0 ? j1.out.rows_pad / 8 : 0;
+  const int ny = std::max(j0.rows > 0 ? j0.out.nblk : 0, j1.rows > 0 ? j1.out.nblk : 0);
+  if (nx0 + nx1 == 0) return;
+  dim3 grid(nx0 + nx1, ny, batch);
+  LaunchTimer lt("k_oz7_split", st, 0.0,
+                 ((double)j0.rows * j0.K * (8.0 + 2.0 * j0.out.S) + (double)j1.rows * j1.K * (8.0 + 2.0 * j1.out.S)) *
+                     batch);
+  switch (j0.rows > 0 ? j0.out.S : j1.out.S) {
+    case 5: k_oz7_split<5><<<grid, 256, 0, st>>>(j0, j1, nx0); break;
+    case 6: k_oz7_split<6><<<grid, 256, 0, st>>>(j0, j1, nx0); break;
+    case 7: k_oz7_split<7><<<grid, 256, 0, st>>>(j0, j1, nx0); break;
+    default: k_oz7_split<8><<<grid, 256, 0, st>>>(j0, j1, nx0); break;
   }
   LKG_LAUNCH("k_oz7_split");
+}
+
+}  // namespace
+
+void oz7_split(int rows, int K, const double* p, int64_t s_r, int64_t s_k, int64_t bstride, int batch, Split7& out,
+               cudaStream_t st) {
+  if (rows <= 0 || K <= 0) return;
+  split_prepare(rows, K, out);
+  const SplitJob j0{rows, K, p, s_r, s_k, bstride, out}, none{0, 0, nullptr, 0, 0, 0, Split7{}};
+  split_launch(j0, none, batch, st);
+}
+
+void oz7_split2(int rows0, int K0, const double* p0, int64_t s_r0, int64_t s_k0, int64_t bstride0, Split7& out0,
+                int rows1, int K1, const double* p1, int64_t s_r1, int64_t s_k1, int64_t bstride1, Split7& out1,
+                int batch, cudaStream_t st) {
+  const bool a = rows0 > 0 && K0 > 0, c = rows1 > 0 && K1 > 0;
+  if (a) split_prepare(rows0, K0, out0);
+  if (c) split_prepare(rows1, K1, out1);
+  if (a && c && out0.S != out1.S) throw std::invalid_argument("oz7_split2: operands with different digit counts");
+  const SplitJob none{0, 0, nullptr, 0, 0, 0, Split7{}};
+  split_launch(a ? SplitJob{rows0, K0, p0, s_r0, s_k0, bstride0, out0} : none,
+               c ? SplitJob{rows1, K1, p1, s_r1, s_k1, bstride1, out1} : none, batch, st);
 }
 
 void oz7_gemm(int M, int N, int kb0, int kb1, double alpha, const Split7& SA, const Split7& SB, double beta, double* C,

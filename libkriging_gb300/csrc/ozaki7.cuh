@@ -38,6 +38,10 @@ Split7 oz7_buffer(void* planes, int* exps, int S, int rows_cap, int K_cap, int k
 // rows x K operand, element (r, k) at p[b*bstride + r*s_r + k*s_k], into out.S digit planes
 void oz7_split(int rows, int K, const double* p, int64_t s_r, int64_t s_k, int64_t bstride, int batch, Split7& out,
                cudaStream_t st);
+// two operands split by one launch (the same digit count); an operand with no rows is skipped
+void oz7_split2(int rows0, int K0, const double* p0, int64_t s_r0, int64_t s_k0, int64_t bstride0, Split7& out0,
+                int rows1, int K1, const double* p1, int64_t s_r1, int64_t s_k1, int64_t bstride1, Split7& out1,
+                int batch, cudaStream_t st);
 // C(M x N) = beta C + alpha A B^T over the k blocks [kb0, kb1) (A rows from SA, B rows from SB)
 void oz7_gemm(int M, int N, int kb0, int kb1, double alpha, const Split7& SA, const Split7& SB, double beta, double* C,
               int64_t ldc, int64_t c_batch, int batch, bool lower, cudaStream_t st);

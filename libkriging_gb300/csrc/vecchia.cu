@@ -76,14 +76,23 @@ __device__ double wsolve_upper_t(const double* L, double z, int mi, int lane) {
   return (lane < mi) ? val : 0.0;
 }
 
-// in-place lower Cholesky, lane i owns row i; returns false on a non-positive / NaN pivot (uniform over the warp)
+// (row, column) of entry e of a lower triangle enumerated row by row: e = r (r + 1) / 2 + c, c <= r
+__device__ __forceinline__ void tri_rc(int e, int& r, int& c) {
+  r = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
+  if ((r + 1) * (r + 2) / 2 <= e) ++r;
+  if (r * (r + 1) / 2 > e) --r;
+  c = e - r * (r + 1) / 2;
+}
+
+// in-place lower Cholesky, right-looking: column j scaled by 1 / L_jj, then the trailing lower triangle updated with
+// its (row, column) pairs spread over the lanes; returns false on a non-positive / NaN pivot (uniform over the warp)
 __device__ bool wchol(double* L, int mi, int lane) {
   for (int j = 0; j < mi; ++j) {
     __syncwarp();
     const double piv = L[j * LDP + j];
     if (!(piv > 0.0)) return false;
-    const double ljj = sqrt(piv);
-    const double rj = 1.0 / ljj;
+    double ljj, rj;
+    pivot_root(piv, ljj, rj);
     __syncwarp();
     if (lane == j) {
       L[j * LDP + j] = ljj;
@@ -91,9 +100,12 @@ __device__ bool wchol(double* L, int mi, int lane) {
     }
     if (lane > j && lane < mi) L[lane * LDP + j] *= rj;
     __syncwarp();
-    if (lane > j && lane < mi) {
-      const double lij = L[lane * LDP + j];
-      for (int c = j + 1; c <= lane; ++c) L[lane * LDP + c] -= lij * L[c * LDP + j];
+    const int m1 = mi - 1 - j, ne = m1 * (m1 + 1) / 2;
+    for (int e = lane; e < ne; e += 32) {
+      int rr, cc;
+      tri_rc(e, rr, cc);
+      const int r = j + 1 + rr, c = j + 1 + cc;
+      L[r * LDP + c] -= L[r * LDP + j] * L[c * LDP + j];
     }
   }
   __syncwarp();
@@ -198,20 +210,24 @@ __global__ void __launch_bounds__(WPB * 32) k_vecchia_points(VPointArgs a) {
     for (int k = 0; k < DM; ++k) xs[lane * DM + k] = (k < d) ? a.X[nbv + (int64_t)k * n] : 0.0;
   __syncwarp();
   double r = 0.0;
-  if (lane < mi) {
-    for (int b = 0; b < mi; ++b) {
-      double c;
-      if (b == lane) {
-        c = 1.0 + a.num_nugget;
-      } else {
-        double s = 0.0, pr = 1.0;
+  {  // RN: the strict lower triangle's pairs spread over the lanes and mirrored (C depends on |dx| or dx^2 only, so
+     // both orders give the same value)
+    const int np = mi * (mi - 1) / 2;
+    for (int e = lane; e < np; e += 32) {
+      int rr, cc;
+      tri_rc(e, rr, cc);
+      const int ra = rr + 1;
+      double s = 0.0, pr = 1.0;
 #pragma unroll
-        for (int k = 0; k < DM; ++k)
-          if (k < d) cov_fast_term<K>(xs[lane * DM + k] - xs[b * DM + k], ck[k], s, pr);
-        c = cov_fast_finish<K>(s, pr);
-      }
-      RN[lane * LDP + b] = c;
+      for (int k = 0; k < DM; ++k)
+        if (k < d) cov_fast_term<K>(xs[ra * DM + k] - xs[cc * DM + k], ck[k], s, pr);
+      const double c = cov_fast_finish<K>(s, pr);
+      RN[ra * LDP + cc] = c;
+      RN[cc * LDP + ra] = c;
     }
+  }
+  if (lane < mi) {
+    RN[lane * LDP + lane] = 1.0 + a.num_nugget;
     double s = 0.0, pr = 1.0;
 #pragma unroll
     for (int k = 0; k < DM; ++k)

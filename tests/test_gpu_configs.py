@@ -4,10 +4,10 @@
   quarter of its size; it runs the 256-wide two-level panels and many 256-wide k blocks of the mixed path): the
   FP64 path within 1e-10 (LL) / 1e-7 (gradient) of the oracle, the mixed path within 1e-8 / 1e-6.
 * Batched multistart, n = 2048, d = 6, gauss, Nugget mode with sigma2 and nugget fixed (alpha = 1 / (1 + 1e-8)):
-  LL and gradient at several starting points against the oracle, within a tolerance scaled by cond(R) (these
-  matrices reach cond(R) ~ 1e11, where any two backward-stable FP64 evaluations differ by ~cond * eps), and the
-  reference's multistart invariant (src/lib/Kriging.cpp:2086-2091): a BFGS16 fit equals, bit for bit, the best of
-  16 separate BFGS1 fits from the same starting points.
+  LL and gradient of the FP64 and mixed paths at several starting points against the oracle, within a tolerance
+  scaled by cond(R) (these matrices reach cond(R) ~ 1e11, where any two backward-stable FP64 evaluations differ by
+  ~cond * eps), and the reference's multistart invariant (src/lib/Kriging.cpp:2086-2091): a BFGS16 fit equals, bit
+  for bit, the best of 16 separate BFGS1 fits from the same starting points.
 
 The oracle side is ``oracle.baseline.eval_full``: the oracle's restatement with its pair loops spread over the host
 cores (equal to ``OracleKriging.log_likelihood`` up to the gradient's summation order; see tests/test_oracle.py).
@@ -67,8 +67,10 @@ def _cond_tol(X, theta, alpha, floor):
     return max(floor, 64.0 * EPS * w[-1] / w[0])
 
 
+@pytest.mark.parametrize("slices", [0, 7])
 @pytest.mark.parametrize("start", [2, 4, 0])
-def test_config3_loglik_vs_oracle(gpu_lib, start):
+def test_config3_loglik_vs_oracle(gpu_lib, start, slices):
+    """FP64 and mixed paths against the oracle within the same cond(R)-scaled tolerance."""
     X, y, thetas, s2, nu = _config3()
     alpha = s2 / (s2 + nu)
     th = thetas[start]
@@ -76,6 +78,7 @@ def test_config3_loglik_vs_oracle(gpu_lib, start):
     k.fit(y, X, "constant", False, "none", "LL",
           {"theta": th.reshape(1, -1), "sigma2": s2, "is_sigma2_estim": False, "nugget": nu,
            "is_nugget_estim": False})
+    k.set_precision(slices)
     ll, g, _ = k.logLikelihoodFun(th, True)
     ll_o, g_o, _, _ = B.eval_full(X, y, th, "gauss", alpha=alpha, fixed_var=(s2, nu))
     tol_ll = _cond_tol(X, th, alpha, 1e-10)
@@ -100,3 +103,4 @@ def test_config3_batched_equals_best_of_single_starts(gpu_lib):
             best = (ll1, k1.theta(), i)
     assert kb.logLikelihood() == best[0], (kb.logLikelihood(), best)
     assert np.array_equal(kb.theta(), best[1]), (kb.theta(), best[1], best[2])
+
