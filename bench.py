@@ -569,7 +569,7 @@ def run_gpu_vecchia(args):
                                            "reference's loop is serial) on the first %d of %d ordered points, "
                                            "scaled by n" % (cnt, n))
         # the reference-style O(n^2) set construction on a bounded size, against the GPU grid construction
-        ns = 16384
+        ns = min(n, args.vecchia_sets_cpu_n)
         Xs = X[:ns]
         t1 = time.perf_counter()
         O.vecchia_sets(Xs, 30)
@@ -725,6 +725,8 @@ def main():
     ap.add_argument("--mixed", action="store_true", help="multistart / nested workloads on the mixed path")
     ap.add_argument("--nested-n", type=int, default=1_000_000, help="points of the nested workload")
     ap.add_argument("--nested-q", type=int, default=100_000, help="gPoE prediction points of the nested workload")
+    ap.add_argument("--vecchia-sets-cpu-n", type=int, default=1 << 16,
+                    help="points of the O(n^2) CPU set construction timed beside the GPU one (vecchia workload)")
     ap.add_argument("--nested-nk", action="store_true",
                     help="nested workload: also time NK aggregation on one 128-point chunk")
     ap.add_argument("--no-batched", action="store_true", help="omit the batched multistart sub-record")
