@@ -16,9 +16,11 @@ against the oracle's full-size evaluation ("rel_err_vs_oracle").
   cpu_baseline  one full, unsampled reference-restated evaluation on the host cores (oracle/baseline.py)
   batched       the second half of the metric: BFGS64 fits of an n=2048, d=6 gauss design with sigma2 and nugget
                 fixed, every optimiser round one batched GPU evaluation of the 64 starts (its own value, e2e,
-                roofline and CPU baseline)
+                roofline and CPU baseline, all FP64); "batched.mixed" is the same fit on the mixed path with its
+                speed-up and its distance from the FP64 fit
 Other workloads (--workload): "multistart" (the batched record alone), "vecchia" (Vecchia LL + gradient at n = 2^20,
-m = 30) and "nested" (NestedKriging, 10^6 points).  --impl reference times the reference-restated CPU path alone.
+m = 30) and "nested" (NestedKriging, 10^6 points; --nested-nk adds NK aggregation on one 128-point chunk, --mixed
+the mixed path with its difference from FP64).  --impl reference times the reference-restated CPU path alone.
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--n 16384] [--workload W]
 """
 from __future__ import annotations
@@ -634,14 +636,23 @@ def run_gpu_nested(args):
     thetas = rng.uniform(0.1, 0.6, size=(p, d))
     for _ in range(args.warmup):
         nk.logLikelihoodGroups(thetas, True)
-    lib.lkg_stats_reset()
-    lib.lkg_stats_enable(1)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         ll, g = nk.logLikelihoodGroups(thetas, True)
     wall = time.perf_counter() - t0
+    # per-kernel table from one more evaluation with per-launch CUDA events (kept out of the timed steps)
+    lib.lkg_stats_reset()
+    lib.lkg_stats_enable(1)
+    nk.logLikelihoodGroups(thetas, True)
     lib.lkg_stats_enable(0)
     stats = kernel_stats(lib)
+    mixed_err = None
+    if args.mixed:  # the same evaluation on the FP64 path
+        nk.set_precision(0)
+        ll64, g64 = nk.logLikelihoodGroups(thetas, True)
+        nk.set_precision(args.slices)
+        mixed_err = dict(ll_max=float(np.max(np.abs(ll - ll64) / np.abs(ll64))),
+                         grad_max=float(np.max(np.linalg.norm(g - g64, axis=1) / np.linalg.norm(g64, axis=1))))
     Xp = np.random.default_rng(124).uniform(size=(args.nested_q, d))
     t1 = time.perf_counter()
     mean, sd = nk.predict(Xp, True)
@@ -652,13 +663,15 @@ def run_gpu_nested(args):
     line = dict(metric="NestedKriging submodel LL+grad evals/s (all groups batched), N=%d, d=4, matern3_2" % n_total,
                 value=p * args.steps / wall, unit="evals/s", n_gpus=1, steps=args.steps, warmup=args.warmup,
                 ms_per_step=1000 * wall / args.steps, higher_is_better=True, scaling="weak", vs_baseline=None,
-                dtype="f64", data="synthetic (seeded PCG64, seed 123; lognormal group sizes, Z-order partition)",
+                dtype="bf16+f64" if args.mixed else "f64",
+                data="synthetic (seeded PCG64, seed 123; lognormal group sizes, Z-order partition)",
                 config=dict(workload="NestedKriging N=%d d=4 matern3_2, %d groups of %d..%d points (median %d)"
                             % (n_total, p, sizes.min(), sizes.max(), int(np.median(sizes))),
                             precision="mixed %d digits" % args.slices if args.mixed else "FP64",
                             l2="inputs larger than L2 (sum n_g^2 * 8 B = %.1f GB of covariance per step)"
                                % (8.0 * np.sum(sizes.astype(np.float64) ** 2) / 1e9)),
                 groups=p, sum_n_cubed=n3, fit_seconds=fit_s, submodel_fits_per_s=p / fit_s,
+                rel_err_vs_fp64=mixed_err,
                 predict_gpoe_points=args.nested_q, predict_seconds=pred_s, theta=nk.theta().tolist(),
                 sigma2=nk.sigma2(), clocks=clk, gpu_launches=int(sum(v["launches"] for v in stats.values())),
                 kernels={kk: dict(launches=v["launches"], ms=round(v["ms"], 3)) for kk, v in stats.items()},

@@ -86,12 +86,15 @@ __global__ void __launch_bounds__(256) k_nk_moments(int n, int qc, const double*
   }
 }
 
-// block = (pair of groups, 32 chunk points); thread (ty, tx): rows a0 + ty + 8m of group i, chunk point t0 + tx
+// block = (pair of groups, up to NKP chunk points); thread (ty, tx): rows a0 + ty + 8m of group i and chunk points
+// t0 + tx + 32u.  Each 32 x 32 tile of R_ij is formed once (division- and log1p-free covariance form) and applied to
+// every chunk point of the block: T(a, t) = sum_b R_ij(a, b) W_j(b, t), then cross(t) = sum_a W_i(a, t) T(a, t).
+constexpr int NKP = 128;
 template <int K, int DM>
 __global__ void __launch_bounds__(256) k_nk_cross(int p, int d, const NkGroup* __restrict__ G,
                                                   const double* __restrict__ theta, int qc,
                                                   double* __restrict__ cross) {
-  __shared__ double sxi[32][DM], sxj[32][DM], sR[32][33], sW[32][33], red[8][32];
+  __shared__ double sxi[32][DM], sxj[32][DM], sR[32][33], sW[32][NKP + 1];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   long long k = blockIdx.x;
   int i = 0;
@@ -101,28 +104,27 @@ __global__ void __launch_bounds__(256) k_nk_cross(int p, int d, const NkGroup* _
   }
   const int j = i + 1 + (int)k;
   const NkGroup gi = G[i], gj = G[j];
-  const int t0 = blockIdx.y * 32, t = t0 + tx;
-  double th[DM];
+  const int t0 = blockIdx.y * NKP, nt = min(NKP, qc - t0);
+  double ck[DM];
 #pragma unroll
-  for (int q = 0; q < DM; ++q) th[q] = (q < d) ? theta[q] : 1.0;
-  double cacc = 0.0;
+  for (int q = 0; q < DM; ++q) ck[q] = cov_scale<K>() / ((q < d) ? theta[q] : 1.0);
+  double cacc[4] = {0.0, 0.0, 0.0, 0.0};
   for (int a0 = 0; a0 < gi.n; a0 += 32) {
     __syncthreads();
     for (int idx = threadIdx.x; idx < 32 * DM; idx += 256) {
       const int a = idx % 32, q = idx / 32;
       sxi[a][q] = (q < d && a0 + a < gi.n) ? gi.X[(a0 + a) + (int64_t)q * gi.ldx] : 0.0;
     }
-    double T[4] = {0.0, 0.0, 0.0, 0.0};
+    double T[4][4] = {};
     for (int b0 = 0; b0 < gj.n; b0 += 32) {
       __syncthreads();
       for (int idx = threadIdx.x; idx < 32 * DM; idx += 256) {
         const int b = idx % 32, q = idx / 32;
         sxj[b][q] = (q < d && b0 + b < gj.n) ? gj.X[(b0 + b) + (int64_t)q * gj.ldx] : 0.0;
       }
-#pragma unroll
-      for (int m = 0; m < 4; ++m) {  // coalesced over b: sW[b][tt] = W_j(b0 + b, t0 + tt)
-        const int tt = ty + 8 * m;
-        sW[tx][tt] = (b0 + tx < gj.n && t0 + tt < qc) ? gj.W[(b0 + tx) + (int64_t)(t0 + tt) * gj.ldw] : 0.0;
+      for (int idx = threadIdx.x; idx < 32 * NKP; idx += 256) {  // coalesced over b: sW[b][tt] = W_j(b0 + b, t0 + tt)
+        const int b = idx % 32, tt = idx / 32;
+        sW[b][tt] = (b0 + b < gj.n && tt < nt) ? gj.W[(b0 + b) + (int64_t)(t0 + tt) * gj.ldw] : 0.0;
       }
       __syncthreads();
 #pragma unroll
@@ -130,38 +132,52 @@ __global__ void __launch_bounds__(256) k_nk_cross(int p, int d, const NkGroup* _
         const int a = ty + 8 * m;
         double v = 0.0;
         if (a0 + a < gi.n && b0 + tx < gj.n) {
-          double s = 0.0;
+          double sum = 0.0, prod = 1.0;
 #pragma unroll
           for (int q = 0; q < DM; ++q)
-            if (q < d) s += cov_term<K>(sxi[a][q] - sxj[tx][q], th[q]);
-          v = cov_from_sum<K>(s);
+            if (q < d) cov_fast_term<K>(sxi[a][q] - sxj[tx][q], ck[q], sum, prod);
+          v = cov_fast_finish<K>(sum, prod);
         }
         sR[a][tx] = v;
       }
       __syncthreads();
+#pragma unroll 4
+      for (int bb = 0; bb < 32; ++bb) {
+        double w[4], r[4];
 #pragma unroll
-      for (int m = 0; m < 4; ++m) {
-        const int a = ty + 8 * m;
-        double acc = T[m];
-#pragma unroll 8
-        for (int bb = 0; bb < 32; ++bb) acc = fma(sR[a][bb], sW[bb][tx], acc);
-        T[m] = acc;
+        for (int u = 0; u < 4; ++u) w[u] = sW[bb][tx + 32 * u];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) r[m] = sR[ty + 8 * m][bb];
+#pragma unroll
+        for (int m = 0; m < 4; ++m)
+#pragma unroll
+          for (int u = 0; u < 4; ++u) T[m][u] = fma(r[m], w[u], T[m][u]);
       }
     }
-    if (t < qc) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int tt = tx + 32 * u;
+      if (tt >= nt) continue;
 #pragma unroll
       for (int m = 0; m < 4; ++m) {
         const int a = a0 + ty + 8 * m;
-        if (a < gi.n) cacc = fma(gi.W[a + (int64_t)t * gi.ldw], T[m], cacc);
+        if (a < gi.n) cacc[u] = fma(gi.W[a + (int64_t)(t0 + tt) * gi.ldw], T[m][u], cacc[u]);
       }
     }
   }
-  red[ty][tx] = cacc;
+  // fixed-order sum over the 8 row groups (sR reused: 8 x NKP partials)
   __syncthreads();
-  if (ty == 0 && t < qc) {
-    double s = red[0][tx];
-    for (int r = 1; r < 8; ++r) s += red[r][tx];
-    cross[(int64_t)blockIdx.x * qc + t] = s;
+  double* red = &sR[0][0];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) red[ty * NKP + tx + 32 * u] = cacc[u];
+  __syncthreads();
+  if (ty < 4) {
+    const int tt = tx + 32 * ty;
+    if (tt < nt) {
+      double s = red[tt];
+      for (int r = 1; r < 8; ++r) s += red[r * NKP + tt];
+      cross[(int64_t)blockIdx.x * qc + t0 + tt] = s;
+    }
   }
 }
 
@@ -182,7 +198,7 @@ struct NkCrossLaunch {
     if (npairs <= 0) return;
     if (npairs > 0x7fffffffLL) throw std::invalid_argument("NK aggregation: too many groups");
     LaunchTimer lt("k_nk_cross", st, 0.0, 0.0);
-    k_nk_cross<K, DM><<<dim3((unsigned)npairs, ceil_div(qc, 32), 1), 256, 0, st>>>(p, d, groups, theta, qc, cross);
+    k_nk_cross<K, DM><<<dim3((unsigned)npairs, ceil_div(qc, NKP), 1), 256, 0, st>>>(p, d, groups, theta, qc, cross);
     LKG_LAUNCH("k_nk_cross");
   }
 };

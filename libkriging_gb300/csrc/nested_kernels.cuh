@@ -32,8 +32,9 @@ struct NkGroup {
 };
 
 // cross[k * qc + t] = sum_{a,b} W_i(a,t) R_ij(a,b) W_j(b,t) for every pair k = (i < j) of the p groups, pairs
-// ranked i-major (k = 0 is (0,1), then (0,2), ...), R_ij recomputed from the points with the common theta.
-// groups: device array of p NkGroup.  One block per (pair, 32 chunk points); deterministic.
+// ranked i-major (k = 0 is (0,1), then (0,2), ...), R_ij recomputed from the points with the common theta (the
+// covariance's product form, equal to the reference's to a few ulps).  groups: device array of p NkGroup.  One block
+// per (pair, 128 chunk points), each tile of R_ij formed once per block; deterministic.
 void nk_cross(int kernel, int d, int p, const NkGroup* groups, const double* theta, int qc, double* cross,
               cudaStream_t st);
 

@@ -276,13 +276,25 @@ __global__ void __launch_bounds__(WPB * 32) k_vecchia_points(VPointArgs a) {
   for (int q = 0; q < p; ++q) cq[q] = wsolve_upper_t(LN, wsolve_lower(LN, fN[q], mi, lane), mi, lane);
   if (lane < 32) sa[lane] = av;
   __syncwarp();
+  // the factor is no longer needed: its buffer holds M_k(a, b) = RN(a, b) dlnC/dtheta_k(x_a - x_b) (a != b), formed
+  // once per pair (symmetric: |dx| or dx^2 only) with the pairs spread over the lanes, then s_a = sum_b M_k(a, b) a_b
+  const int npair = mi * (mi - 1) / 2;
   for (int k = 0; k < d; ++k) {
+    __syncwarp();
+    for (int e = lane; e < npair; e += 32) {
+      int rr, cc;
+      tri_rc(e, rr, cc);
+      const int ra = rr + 1;
+      const double mk = RN[ra * LDP + cc] * dlncov_fast<K>(xs[ra * DM + k] - xs[cc * DM + k], inv[k], ck[k]);
+      LN[ra * LDP + cc] = mk;
+      LN[cc * LDP + ra] = mk;
+    }
+    __syncwarp();
     double drk = 0.0, s = 0.0;
     if (lane < mi) {
       drk = r * dlncov_fast<K>(xs[lane * DM + k] - xo[k], inv[k], ck[k]);
       for (int b = 0; b < mi; ++b)
-        if (b != lane)
-          s += RN[lane * LDP + b] * dlncov_fast<K>(xs[lane * DM + k] - xs[b * DM + k], inv[k], ck[k]) * sa[b];
+        if (b != lane) s += LN[lane * LDP + b] * sa[b];
     }
     const double g = drk - s;
     const double adr = wsum(av * drk), as = wsum(av * s), gb = wsum(g * by);
