@@ -141,6 +141,11 @@ class NestedService : public DenseService {
     active_ = a;
   }
 
+  // precision of the batched evaluations from now on (0: FP64, 4..8: mixed)
+  void set_slices(int s) {
+    for (auto& c : classes_) c.eng->set_slices(s);
+  }
+
   void leave() {
     std::unique_lock<std::mutex> lk(mu_);
     active_--;
@@ -315,6 +320,7 @@ void NestedKriging::set_precision(int slices) {
   if (slices != 0 && (slices < 4 || slices > 8))
     throw std::invalid_argument("set_precision: slices must be 0 (FP64) or 4..8");
   m_slices = slices;
+  if (m_service) m_service->set_slices(slices);  // a fitted model's batched evaluations follow the setting
 }
 
 Kriging& NestedKriging::submodel(int i) {

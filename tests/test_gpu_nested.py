@@ -133,6 +133,29 @@ def test_log_likelihood_groups_equals_lone_models(gpu_lib):
         assert rel_err(grad[g], g1) < 1e-10
 
 
+def test_log_likelihood_groups_precision_switch(gpu_lib):
+    """set_precision on a fitted model switches its batched evaluations: the mixed path within 1e-8 (LL) / 1e-6
+    (gradient) of FP64, and back on FP64 the values of a model fitted in FP64, bit for bit."""
+    X, y = _data(1200, d=3)
+    rng = np.random.default_rng(12)
+    perm = rng.permutation(1200)
+    groups = [np.sort(perm[a:b]) for a, b in ((0, 300), (300, 700), (700, 1200))]
+    thetas = rng.uniform(0.2, 0.8, size=(3, 3))
+    nk64 = gpu_lib.NestedKriging("matern5_2", aggregation="PoE")
+    nk64.fit_groups(y, X, groups, optim="BFGS")
+    ll64, g64 = nk64.logLikelihoodGroups(thetas, True)
+    nk = gpu_lib.NestedKriging("matern5_2", aggregation="PoE")
+    nk.set_precision(7)
+    nk.fit_groups(y, X, groups, optim="BFGS")
+    llm, gm = nk.logLikelihoodGroups(thetas, True)
+    for g in range(3):
+        assert rel_err(llm[g], ll64[g]) < 1e-8
+        assert rel_err(gm[g], g64[g]) < 1e-6
+    nk.set_precision(0)
+    ll0, g0 = nk.logLikelihoodGroups(thetas, True)
+    assert np.array_equal(ll0, ll64) and np.array_equal(g0, g64)
+
+
 # ---- the reference's own NestedKriging tests, on the BFGS path ----
 def test_one_group_reduces_to_kriging(gpu_lib):
     """NestedKrigingTest.cpp:25-60.  The NK mean of one expert is the expert's mean (1e-6) -- except where the fitted
