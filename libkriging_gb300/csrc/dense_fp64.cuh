@@ -58,15 +58,12 @@ struct MixedWorkspace {
   void* wfull = nullptr;  // bf16 planes, oz7_plane_elems(n, n, digits) per batch entry
   int* wfull_exp = nullptr;
   int n = 0;
-  // look-ahead of the blocked Cholesky and of the triangular inverse (single matrix): the next panel / 256-row
-  // block is worked on side_stream, on side_ctas SMs kept free by the update of the remaining rows, with its splits
-  // in side (and side2 for the inverse's second operand), each the size of panel; off when null
+  // look-ahead of the blocked Cholesky (single matrix): the next panel is factored on side_stream, on side_ctas SMs
+  // kept free by the trailing update, with its splits in side / side_exp (the size of panel); off when null
   cudaStream_t side_stream = nullptr;
   cudaEvent_t ev_strip = nullptr, ev_panel = nullptr;
   void* side = nullptr;
   int* side_exp = nullptr;
-  void* side2 = nullptr;
-  int* side2_exp = nullptr;
   int side_ctas = 0;
 };
 void potrf_blocked_mixed(double* A, int64_t lda, int64_t mstride, int n, double* Dinv, int* info, int batch,

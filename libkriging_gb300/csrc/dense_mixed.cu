@@ -102,31 +102,28 @@ void potrf_blocked_mixed7(double* A, int64_t lda, int64_t mstride, int n, double
 // L(k0+nb:, k0:k0+nb) W(k0:k0+nb, 0:k0+nb).
 void trtri_block7(const double* L, int64_t lda, int64_t mstride, int n, int K0, int Wd, const double* Dinv,
                   int64_t dstride, double* W, int64_t ldw, int64_t wstride, int batch, Split7& SA, Split7& SB,
-                  int max_ctas, cudaStream_t st) {
+                  cudaStream_t st) {
   for (int k0 = K0; k0 < K0 + Wd; k0 += NB) {
     const int nb = std::min(NB, n - k0), k = k0 / NB;
     copy_dinv_block(Dinv, dstride, k, W, ldw, wstride, k0, nb, batch, st);
     if (k0 > 0) {  // W(k0:k0+nb, 0:k0) = -Dinv_k Acc(k0:k0+nb, 0:k0): B rows are the columns of Acc
       oz7_split2(nb, nb, Dinv + (int64_t)k * NB * NB, 1, NB, dstride, SA, k0, nb, W + k0, ldw, 1, wstride, SB,
                  batch, st);
-      oz7_gemm_ex(nb, k0, 0, 1, -1.0, SA, 0, SB, 0, 0.0, W + k0, ldw, wstride, batch, false, max_ctas, st);
+      oz7_gemm(nb, k0, 0, 1, -1.0, SA, SB, 0.0, W + k0, ldw, wstride, batch, false, st);
     }
     const int mr = K0 + Wd - (k0 + nb);  // rows of this 256-row block below the 64-row one
     if (mr > 0) {  // Acc(k0+nb:K0+Wd, 0:k0+nb) += L(k0+nb:K0+Wd, k0:k0+nb) W(k0:k0+nb, 0:k0+nb)
       oz7_split2(mr, nb, L + (k0 + nb) + (int64_t)k0 * lda, 1, lda, mstride, SA, k0 + nb, nb, W + k0, ldw, 1,
                  wstride, SB, batch, st);
-      oz7_gemm_ex(mr, k0 + nb, 0, 1, 1.0, SA, 0, SB, 0, 1.0, W + k0 + nb, ldw, wstride, batch, false, max_ctas, st);
+      oz7_gemm(mr, k0 + nb, 0, 1, 1.0, SA, SB, 1.0, W + k0 + nb, ldw, wstride, batch, false, st);
     }
   }
 }
 
 // Two-level triangular inverse: inside a 256-row block the 64-wide steps, below it one rank-256 update of the
-// accumulated rows; every product on the digit kernel.
-//
-// Look-ahead (single matrix, ws.side_stream and ws.side2 set): the update below block K0 is cut into the next
-// block's 256 rows and the rest; after that strip, the next block's 64-wide steps run on the side stream (splits in
-// side / side2, ws.side_ctas SMs) while the rest of the update runs on the other SMs.  Every entry receives the same
-// operations either way, so W is bit-identical with and without the look-ahead.
+// accumulated rows; every product on the digit kernel.  (A look-ahead like the Cholesky's -- the next block's 64-wide
+// steps on a side stream while the rest of the update runs -- measured 1.9 ms slower per n = 16384 evaluation: the
+// steps' wide products need most of the SMs, so it is not used here.)
 void trtri_blocked_mixed7(const double* L, int64_t lda, int64_t mstride, int n, const double* Dinv, double* W,
                           int64_t ldw, int64_t wstride, int batch, const MixedWorkspace& ws, cudaStream_t st) {
   const int nblk = ceil_div(n, NB);
@@ -138,48 +135,16 @@ void trtri_blocked_mixed7(const double* L, int64_t lda, int64_t mstride, int n, 
   Split7 SR = oz7_buffer(ws.rowblk, ws.rowblk_exp, S, ws.n, OZ7_KB, OZ7_KB);
   Split7 SA = oz7_buffer(ws.panel, ws.panel_exp, S, ws.n, NB, NB);
   Split7 SB = oz7_buffer(ws.rowblk, ws.rowblk_exp, S, ws.n, NB, NB);
-  const bool ahead = ws.side_stream && ws.side2 && batch == 1;
-  if (!ahead) {
-    for (int K0 = 0; K0 < n; K0 += OZ7_KB) {
-      const int Wd = std::min(OZ7_KB, n - K0);
-      trtri_block7(L, lda, mstride, n, K0, Wd, Dinv, dstride, W, ldw, wstride, batch, SA, SB, 0, st);
-      const int M2 = n - K0 - Wd;
-      if (M2 <= 0) continue;
-      // Acc(K0+Wd:, 0:N) += L(K0+Wd:, K0:K0+Wd) W(K0:K0+Wd, 0:N), N = K0 + Wd
-      const int N = K0 + Wd;
-      oz7_split2(M2, Wd, L + (K0 + Wd) + (int64_t)K0 * lda, 1, lda, mstride, SL, N, Wd, W + K0, ldw, 1, wstride, SR,
-                 batch, st);
-      oz7_gemm(M2, N, 0, 1, 1.0, SL, SR, 1.0, W + K0 + Wd, ldw, wstride, batch, false, st);
-    }
-    return;
-  }
-  Split7 SAs = oz7_buffer(ws.side, ws.side_exp, S, ws.n, NB, NB);
-  Split7 SBs = oz7_buffer(ws.side2, ws.side2_exp, S, ws.n, NB, NB);
-  const int rest_ctas = std::max(1, oz7_sm_count() - ws.side_ctas);
-  trtri_block7(L, lda, mstride, n, 0, std::min(OZ7_KB, n), Dinv, dstride, W, ldw, wstride, batch, SA, SB, 0, st);
   for (int K0 = 0; K0 < n; K0 += OZ7_KB) {
     const int Wd = std::min(OZ7_KB, n - K0);
+    trtri_block7(L, lda, mstride, n, K0, Wd, Dinv, dstride, W, ldw, wstride, batch, SA, SB, st);
     const int M2 = n - K0 - Wd;
-    if (M2 <= 0) break;
-    const int N = K0 + Wd, K1 = K0 + Wd;
-    oz7_split2(M2, Wd, L + K1 + (int64_t)K0 * lda, 1, lda, mstride, SL, N, Wd, W + K0, ldw, 1, wstride, SR, batch,
-               st);
-    const int W1 = std::min(OZ7_KB, M2);  // the next block's rows
-    // the strip: Acc(K1:K1+W1, 0:N) += L(K1:K1+W1, K0:K1) W(K0:K1, 0:N)
-    oz7_gemm_ex(W1, N, 0, 1, 1.0, SL, 0, SR, 0, 1.0, W + K1, ldw, wstride, batch, false, 0, st);
-    const int M3 = M2 - W1;
-    if (M3 <= 0) {  // the last block: nothing left to overlap with
-      trtri_block7(L, lda, mstride, n, K1, W1, Dinv, dstride, W, ldw, wstride, batch, SA, SB, 0, st);
-      continue;
-    }
-    LKG_CUDA(cudaEventRecord(ws.ev_strip, st));
-    LKG_CUDA(cudaStreamWaitEvent(ws.side_stream, ws.ev_strip, 0));
-    trtri_block7(L, lda, mstride, n, K1, W1, Dinv, dstride, W, ldw, wstride, batch, SAs, SBs, ws.side_ctas,
-                 ws.side_stream);
-    LKG_CUDA(cudaEventRecord(ws.ev_panel, ws.side_stream));
-    // the rest: Acc(K1+W1:, 0:N) += L(K1+W1:, K0:K1) W(K0:K1, 0:N), reading the strip's operands from row W1 on
-    oz7_gemm_ex(M3, N, 0, 1, 1.0, SL, W1, SR, 0, 1.0, W + K1 + W1, ldw, wstride, batch, false, rest_ctas, st);
-    LKG_CUDA(cudaStreamWaitEvent(st, ws.ev_panel, 0));
+    if (M2 <= 0) continue;
+    // Acc(K0+Wd:, 0:N) += L(K0+Wd:, K0:K0+Wd) W(K0:K0+Wd, 0:N), N = K0 + Wd
+    const int N = K0 + Wd;
+    oz7_split2(M2, Wd, L + (K0 + Wd) + (int64_t)K0 * lda, 1, lda, mstride, SL, N, Wd, W + K0, ldw, 1, wstride, SR,
+               batch, st);
+    oz7_gemm(M2, N, 0, 1, 1.0, SL, SR, 1.0, W + K0 + Wd, ldw, wstride, batch, false, st);
   }
 }
 

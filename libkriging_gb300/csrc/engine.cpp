@@ -154,9 +154,9 @@ Engine::~Engine() {
   if (dgls_info_) cudaFree(dgls_info_);
   if (dXe_) cudaFree(dXe_);
   if (dnv_) cudaFree(dnv_);
-  for (void* p : {dpanel_, drowblk_, dwfull_, dside_, dside2_})
+  for (void* p : {dpanel_, drowblk_, dwfull_, dside_})
     if (p) cudaFree(p);
-  for (int* p : {dpanel_exp_, drowblk_exp_, dwfull_exp_, dside_exp_, dside2_exp_})
+  for (int* p : {dpanel_exp_, drowblk_exp_, dwfull_exp_, dside_exp_})
     if (p) cudaFree(p);
   if (ev_strip_) cudaEventDestroy(ev_strip_);
   if (ev_panel_) cudaEventDestroy(ev_panel_);
@@ -203,12 +203,12 @@ int Engine::lookahead_ctas() const { return lookahead_ctas_for(n_); }
 
 void Engine::ensure_mixed_buffers(bool with_grad) {
   if (mixed_alloc_slices_ != slices_) {
-    for (void** p : {&dpanel_, &drowblk_, &dwfull_, &dside_, &dside2_})
+    for (void** p : {&dpanel_, &drowblk_, &dwfull_, &dside_})
       if (*p) {
         cudaFree(*p);
         *p = nullptr;
       }
-    for (int** p : {&dpanel_exp_, &drowblk_exp_, &dwfull_exp_, &dside_exp_, &dside2_exp_})
+    for (int** p : {&dpanel_exp_, &drowblk_exp_, &dwfull_exp_, &dside_exp_})
       if (*p) {
         cudaFree(*p);
         *p = nullptr;
@@ -224,14 +224,11 @@ void Engine::ensure_mixed_buffers(bool with_grad) {
     dalloc(&dpanel_exp_, ee);
     dalloc(&drowblk_exp_, ee);
   }
-  // the look-ahead's own operand splits (single-matrix evaluations of a size where it pays): the Cholesky's panel
-  // splits in side, the triangular inverse's two operands in side and side2
+  // the look-ahead's own panel splits (single-matrix evaluations of a size where it pays)
   if (lookahead_enabled() && !dside_) {
     const size_t pe1 = oz7_plane_elems(n_, OZ7_KB, 8), ee1 = oz7_exp_elems(n_, OZ7_KB, OZ7_KB);
     LKG_CUDA(cudaMalloc(&dside_, pe1 * 2));
-    LKG_CUDA(cudaMalloc(&dside2_, pe1 * 2));
     dalloc(&dside_exp_, ee1);
-    dalloc(&dside2_exp_, ee1);
     if (!side_st_) {
       LKG_CUDA(cudaStreamCreateWithFlags(&side_st_, cudaStreamNonBlocking));
       LKG_CUDA(cudaEventCreateWithFlags(&ev_strip_, cudaEventDisableTiming));
@@ -443,8 +440,6 @@ void Engine::evaluate(int batch, const double* thetas, const double* factors, bo
       mw.ev_panel = ev_panel_;
       mw.side = dside_;
       mw.side_exp = dside_exp_;
-      mw.side2 = dside2_;
-      mw.side2_exp = dside2_exp_;
       mw.side_ctas = lookahead_ctas();
     }
   }

@@ -156,9 +156,8 @@ class Engine {
   double* dXe_ = nullptr;                 // per-entry copy of its design's X (several designs only)
   int* dnv_ = nullptr;                    // per-entry valid sizes on the device (several designs only)
   int slices_ = 0;
-  void *dpanel_ = nullptr, *drowblk_ = nullptr, *dwfull_ = nullptr, *dside_ = nullptr, *dside2_ = nullptr;
-  int *dpanel_exp_ = nullptr, *drowblk_exp_ = nullptr, *dwfull_exp_ = nullptr, *dside_exp_ = nullptr,
-      *dside2_exp_ = nullptr;
+  void *dpanel_ = nullptr, *drowblk_ = nullptr, *dwfull_ = nullptr, *dside_ = nullptr;
+  int *dpanel_exp_ = nullptr, *drowblk_exp_ = nullptr, *dwfull_exp_ = nullptr, *dside_exp_ = nullptr;
   cudaStream_t side_st_ = nullptr;  // look-ahead stream of the mixed Cholesky (single-matrix evaluations)
   cudaEvent_t ev_strip_ = nullptr, ev_panel_ = nullptr;
   int mixed_alloc_slices_ = 0;

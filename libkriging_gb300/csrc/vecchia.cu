@@ -51,27 +51,26 @@ __device__ __forceinline__ int wargmax(double v, int lane, int mi) {
 }
 
 // The factor keeps 1 / L_jj in the spare last column of row j (index RCP = LDP - 1 = 32, never a matrix column since
-// m <= 32 fills 0 .. 31): the solves and the factorisation multiply instead of dividing (an FP64 division is a long
-// instruction sequence on this part).
+// m <= 32 fills 0 .. 31), and the unit lower factor U = L D^-1 (D = diag L) transposed in the strict upper part:
+// L[j][i] = L_ij / L_jj for i > j.  The solves then take one fused multiply-add per step and scale by 1 / L_jj once
+// (FP64 issue bounds these kernels: GB300 runs FP64 at 1/64 of the FP32 rate).
 constexpr int RCP = LDP - 1;
 
-// solve L z = b (lane i holds b_i); lanes >= mi return 0
+// solve L z = b (lane i holds b_i): U w = b by forward substitution, then z = D^-1 w; lanes >= mi return 0
 __device__ double wsolve_lower(const double* L, double b, int mi, int lane) {
   double val = (lane < mi) ? b : 0.0;
   for (int j = 0; j < mi; ++j) {
-    const double zj = __shfl_sync(FULL, val, j) * L[j * LDP + RCP];
-    if (lane == j) val = zj;
-    if (lane > j && lane < mi) val -= L[lane * LDP + j] * zj;
+    const double wj = __shfl_sync(FULL, val, j);
+    if (lane > j && lane < mi) val -= L[j * LDP + lane] * wj;
   }
-  return (lane < mi) ? val : 0.0;
+  return (lane < mi) ? val * L[lane * LDP + RCP] : 0.0;
 }
-// solve L' x = z
+// solve L' x = z: U' x = D^-1 z by back substitution
 __device__ double wsolve_upper_t(const double* L, double z, int mi, int lane) {
-  double val = (lane < mi) ? z : 0.0;
+  double val = (lane < mi) ? z * L[lane * LDP + RCP] : 0.0;
   for (int j = mi - 1; j >= 0; --j) {
-    const double xj = __shfl_sync(FULL, val, j) * L[j * LDP + RCP];
-    if (lane == j) val = xj;
-    if (lane < j) val -= L[j * LDP + lane] * xj;
+    const double xj = __shfl_sync(FULL, val, j);
+    if (lane < j) val -= L[lane * LDP + j] * xj;
   }
   return (lane < mi) ? val : 0.0;
 }
@@ -107,6 +106,15 @@ __device__ bool wchol(double* L, int mi, int lane) {
       const int r = j + 1 + rr, c = j + 1 + cc;
       L[r * LDP + c] -= L[r * LDP + j] * L[c * LDP + j];
     }
+  }
+  __syncwarp();
+  // the unit lower factor, transposed into the strict upper part: L[j][i] = L_ij / L_jj
+  const int np = mi * (mi - 1) / 2;
+  for (int e = lane; e < np; e += 32) {
+    int rr, cc;
+    tri_rc(e, rr, cc);
+    const int i = rr + 1;
+    L[cc * LDP + i] = L[i * LDP + cc] * L[cc * LDP + RCP];
   }
   __syncwarp();
   return true;
