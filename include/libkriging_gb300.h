@@ -271,6 +271,11 @@ int lkg_get_digit_tile(void);
  * the value set, or -2 on an argument outside -1 .. 64 (lkg_get_lookahead returns the setting). */
 int lkg_set_lookahead(int ctas);
 int lkg_get_lookahead(void);
+/* No counterpart in the reference: CUDA graphs for the two launch sequences of an evaluation (covariance build +
+ * factorisation; solves, GLS, R^-1 and adjoint sums), captured on the second run of a configuration and replayed
+ * afterwards; on by default unless LKG_GRAPHS=0, and off while per-launch timing (lkg_stats_enable) is on.  Results
+ * are the same bit for bit either way.  Returns the previous setting (1 on, 0 off). */
+int lkg_set_graphs(int on);
 /* No counterpart in the reference: one product of the 7-bit digit kernel on host data, S digits (5..8):
  * mode 0: C (M x N) = A B^T (A M x K, B N x K); mode 1: C = A A^T lower (M x M); mode 2: C = W^T W lower with
  * W = A (M x M, lower).  Returns 0, -1 (error text in lkg_get_last_error) or -2 when a wait of the kernel expired

@@ -120,6 +120,7 @@ _SIGS = {
     "lkg_get_digit_tile": (_i, []),
     "lkg_set_lookahead": (_i, [_i]),
     "lkg_get_lookahead": (_i, []),
+    "lkg_set_graphs": (_i, [_i]),
     "lkg_vecchia_sets_noalloc": (_i, [_i, _i, _vp, _i, _vp, _vp, _vp]),
     "lkg_vecchia_shard_new": (_vp, [_cp, _i, _i, _i, _dp, _dp, _dp, _ip, _ip, _i, _i, _i]),
     "lkg_vecchia_shard_delete": (None, [_vp]),

@@ -154,6 +154,12 @@ extern "C" int lkg_set_lookahead(int ctas) {
 
 extern "C" int lkg_get_lookahead(void) { return lkg::lookahead_ctas_setting(); }
 
+extern "C" int lkg_set_graphs(int on) {
+  const int old = lkg::graphs_enabled() ? 1 : 0;
+  lkg::set_graphs_enabled(on != 0);
+  return old;
+}
+
 extern "C" int lkg_ozaki_gemm_check(int M, int N, int K, const double* A, const double* B, int slices, double* C) {
   // C = A * B^T with A (M x K) and B (N x K) column-major, computed by the split-bf16 tensor-core path
   double *dA = nullptr, *dB = nullptr, *dC = nullptr;

@@ -21,6 +21,7 @@
 #include "dense_fp64.cuh"
 #include "lik_kernels.cuh"
 #include "ozaki7.cuh"
+#include "stats.hpp"
 
 namespace lkg {
 
@@ -147,6 +148,7 @@ Engine::Engine(int kernel, int n, int d, int p, int ndesign, const double* X, co
 }
 
 Engine::~Engine() {
+  clear_graphs();
   for (double* p : {dX_, dY_, dF_, dA_, dDinv_, dW_, dRinv_, dFY_, dEstar_, dxv_, dtheta_, dfactor_, ddiag_, dgram_,
                     dbeta_, drstar_, dsse_, dpart_, dadj_, dvec_, dcol_, dloo_m_, dloo_at_, dloo_vec_})
     if (p) cudaFree(p);
@@ -196,6 +198,83 @@ int lookahead_ctas_for(int n) {
   return Autotuner::instance().lookup(lookahead_tune_key(n), kLookaheadDefault);
 }
 
+namespace {
+std::atomic<bool> g_graphs{[] {
+  const char* v = std::getenv("LKG_GRAPHS");
+  return !(v && std::strcmp(v, "0") == 0);
+}()};
+}  // namespace
+
+void set_graphs_enabled(bool on) { g_graphs = on; }
+bool graphs_enabled() { return g_graphs; }
+
+void Engine::clear_graphs() {
+  for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+  graphs_.clear();
+  graph_launches_.clear();
+  graph_seen_.clear();
+  graph_refused_.clear();
+}
+
+void Engine::buffers_changed() {
+  ++buf_gen_;
+  clear_graphs();
+}
+
+void Engine::run_phase(const std::string& key, const std::function<void()>& launch, bool allow) {
+  if (!allow || !graphs_enabled() || stats_enabled() || graph_refused_.count(key)) {
+    launch();
+    return;
+  }
+  auto it = graphs_.find(key);
+  if (it != graphs_.end()) {
+    LKG_CUDA(cudaGraphLaunch(it->second, st_));
+    stats_add_launches(graph_launches_[key], +1);
+    return;
+  }
+  // the first run of a configuration goes direct: kernel attributes, module loading and lazily sized buffers are
+  // settled before anything is captured
+  if (graph_seen_.insert(key).second) {
+    launch();
+    return;
+  }
+  const auto before = stats_launch_counts();
+  auto delta = [&] {
+    std::map<std::string, long long> d;
+    for (auto& kv : stats_launch_counts()) {
+      const auto b = before.find(kv.first);
+      const long long c = kv.second - (b == before.end() ? 0 : b->second);
+      if (c) d[kv.first] = c;
+    }
+    return d;
+  };
+  LKG_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+  bool captured = true;
+  try {
+    launch();
+  } catch (...) {
+    captured = false;
+  }
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(st_, &g);
+  cudaGraphExec_t ex = nullptr;
+  if (captured && e == cudaSuccess && g) e = cudaGraphInstantiate(&ex, g, 0);
+  if (g) cudaGraphDestroy(g);
+  const auto d = delta();
+  if (!captured || e != cudaSuccess || !ex) {
+    // nothing ran: forget the capture's counts, keep this configuration on direct launches
+    (void)cudaGetLastError();
+    if (ex) cudaGraphExecDestroy(ex);
+    stats_add_launches(d, -1);
+    graph_refused_.insert(key);
+    launch();
+    return;
+  }
+  graphs_[key] = ex;
+  graph_launches_[key] = d;  // the capture counted this execution's launches already
+  LKG_CUDA(cudaGraphLaunch(ex, st_));
+}
+
 // the look-ahead pays when the matrix has several 256-wide panels
 bool Engine::lookahead_enabled() const { return n_ >= 4 * OZ7_KB && lookahead_ctas_for(n_) > 0; }
 
@@ -203,6 +282,7 @@ int Engine::lookahead_ctas() const { return lookahead_ctas_for(n_); }
 
 void Engine::ensure_mixed_buffers(bool with_grad) {
   if (mixed_alloc_slices_ != slices_) {
+    buffers_changed();
     for (void** p : {&dpanel_, &drowblk_, &dwfull_, &dside_})
       if (*p) {
         cudaFree(*p);
@@ -219,6 +299,7 @@ void Engine::ensure_mixed_buffers(bool with_grad) {
   const size_t pe = oz7_plane_elems(n_, OZ7_KB, 8) * cap_;
   const size_t ee = oz7_exp_elems(n_, OZ7_KB, OZ7_KB) * cap_;
   if (!dpanel_) {
+    buffers_changed();
     LKG_CUDA(cudaMalloc(&dpanel_, pe * 2));
     LKG_CUDA(cudaMalloc(&drowblk_, pe * 2));
     dalloc(&dpanel_exp_, ee);
@@ -226,6 +307,7 @@ void Engine::ensure_mixed_buffers(bool with_grad) {
   }
   // the look-ahead's own panel splits (single-matrix evaluations of a size where it pays)
   if (lookahead_enabled() && !dside_) {
+    buffers_changed();
     const size_t pe1 = oz7_plane_elems(n_, OZ7_KB, 8), ee1 = oz7_exp_elems(n_, OZ7_KB, OZ7_KB);
     LKG_CUDA(cudaMalloc(&dside_, pe1 * 2));
     dalloc(&dside_exp_, ee1);
@@ -236,6 +318,7 @@ void Engine::ensure_mixed_buffers(bool with_grad) {
     }
   }
   if (with_grad && !dwfull_) {
+    buffers_changed();
     LKG_CUDA(cudaMalloc(&dwfull_, oz7_plane_elems(n_, n_, std::min(8, slices_ + 1)) * cap_ * 2));
     dalloc(&dwfull_exp_, oz7_exp_elems(n_, n_, OZ7_KB) * cap_);
   }
@@ -243,6 +326,7 @@ void Engine::ensure_mixed_buffers(bool with_grad) {
 
 void Engine::ensure_grad_buffers() {
   if (dW_) return;
+  buffers_changed();
   dalloc(&dW_, (size_t)mstride_ * cap_);
   dalloc(&dRinv_, (size_t)mstride_ * cap_);
   part_size_ = adjoint_partials_size(n_, d_, cap_);
@@ -445,24 +529,37 @@ void Engine::evaluate(int batch, const double* thetas, const double* factors, bo
   }
   bool retreated = false;
   bool w_valid = false;  // W = L^-1 of the accepted factor is already in dW_
+  // the covariance build and the factorisation as one launch sequence (a CUDA graph after its first run): its
+  // inputs -- theta, factor, diagonal -- are read from device memory
+  const bool graphs_ok = (bench == nullptr);
+  auto factor_phase = [&](bool mixed) {
+    const std::string key = "factor:b=" + std::to_string(batch) + ":m=" + std::to_string(mixed ? slices_ : 0) +
+                            ":xe=" + std::to_string(dXb == dXe_) + ":la=" +
+                            std::to_string(mixed && mw.side_stream ? mw.side_ctas : 0) + ":t=" +
+                            std::to_string(oz7_tile()) + ":g=" + std::to_string(buf_gen_);
+    run_phase(key, [&] {
+      cov_build_lower(kernel_, n, d, dXb, xbs, dtheta_, dfactor_, ddiag_, dA_, lda_, mstride_, batch, st_, mixed,
+                      dnv);
+      if (mixed)
+        potrf_blocked_mixed(dA_, lda_, mstride_, n, dDinv_, dinfo_, batch, mw, st_);
+      else
+        potrf_blocked(dA_, lda_, mstride_, n, dDinv_, dinfo_, batch, st_);
+    }, graphs_ok);
+  };
   for (int attempt = 0;; ++attempt) {
     LKG_CUDA(cudaMemcpyAsync(ddiag_, diag.data(), sizeof(double) * batch, cudaMemcpyHostToDevice, st_));
-    cov_build_lower(kernel_, n, d, dXb, xbs, dtheta_, dfactor_, ddiag_, dA_, lda_, mstride_, batch, st_,
-                    slices_ > 0 && !retreated, dnv);
     if (slices_ > 0 && !retreated) {
-      potrf_blocked_mixed(dA_, lda_, mstride_, n, dDinv_, dinfo_, batch, mw, st_);
+      factor_phase(true);
       LKG_CUDA(cudaMemcpyAsync(info.data(), dinfo_, sizeof(int) * batch, cudaMemcpyDeviceToHost, st_));
       LKG_CUDA(cudaStreamSynchronize(st_));
       bool any_fail = false;
       for (int b = 0; b < batch; ++b) any_fail = any_fail || (info[b] != 0 && !dead[b]);
       if (any_fail) {  // retreat: redo this factorisation on the FP64 path before the nugget-retry rules apply
         retreated = true;
-        cov_build_lower(kernel_, n, d, dXb, xbs, dtheta_, dfactor_, ddiag_, dA_, lda_, mstride_, batch, st_, false,
-                        dnv);
-        potrf_blocked(dA_, lda_, mstride_, n, dDinv_, dinfo_, batch, st_);
+        factor_phase(false);
       }
     } else {
-      potrf_blocked(dA_, lda_, mstride_, n, dDinv_, dinfo_, batch, st_);
+      factor_phase(false);
     }
     LKG_CUDA(cudaMemcpyAsync(info.data(), dinfo_, sizeof(int) * batch, cudaMemcpyDeviceToHost, st_));
     LKG_CUDA(cudaStreamSynchronize(st_));
@@ -541,7 +638,15 @@ void Engine::evaluate(int batch, const double* thetas, const double* factors, bo
   }
   tm.lap("R = _Cov(dX) & L = Chol(R)");
 
-  // ---- [F* y*] = L \ [F y], GLS, E*, SSE ----
+  // ---- [F* y*] = L \ [F y], GLS, E*, SSE, and the gradient's R^-1 and adjoint sums: one launch sequence (a CUDA
+  // graph after its first run) ----
+  if (with_grad) ensure_grad_buffers();
+  const bool mixed_post = slices_ > 0 && !retreated;
+  const std::string post_key = "post:b=" + std::to_string(batch) + ":m=" + std::to_string(mixed_post ? slices_ : 0) +
+                               ":gr=" + std::to_string(with_grad) + ":w=" + std::to_string(w_valid) + ":sa=" +
+                               std::to_string(skip_adjoint_) + ":xe=" + std::to_string(dXb == dXe_) + ":t=" +
+                               std::to_string(oz7_tile()) + ":g=" + std::to_string(buf_gen_);
+  // [F y] of every entry's design (outside the sequence: the entries' designs change between evaluations)
   for (int b = 0; b < batch; ++b) {
     double* fy = dFY_ + (size_t)b * fystride_;
     const size_t e = entry_design_[b];
@@ -549,42 +654,43 @@ void Engine::evaluate(int batch, const double* thetas, const double* factors, bo
       LKG_CUDA(cudaMemcpyAsync(fy, dF_ + e * n * p, sizeof(double) * n * p, cudaMemcpyDeviceToDevice, st_));
     LKG_CUDA(cudaMemcpyAsync(fy + (size_t)n * p, dY_ + e * n, sizeof(double) * n, cudaMemcpyDeviceToDevice, st_));
   }
-  trsm_lower_left(dA_, lda_, mstride_, n, dDinv_, dFY_, n, fystride_, p + 1, batch, st_);
-  tm.lap("F* = L \\ F, y* = L \\ y");
-  gram_and_logdet(n, p + 1, dFY_, n, fystride_, dA_, lda_, mstride_, dgram_, gram_stride_, batch, st_);
-  if (p > 0) {
-    gls_solve(p, dgram_, gram_stride_, dbeta_, p, drstar_, p * p, dgls_info_, batch, st_);
-  } else {
-    LKG_CUDA(cudaMemsetAsync(dgls_info_, 0, sizeof(int) * batch, st_));
-  }
-  tm.lap("^b = R*^-1 R*'^-1 F*'y*");
-  residual_sse(n, p, dFY_, n, fystride_, dbeta_, std::max(p, 1), dEstar_, n, dsse_, 1, batch, st_);
-  tm.lap("z = L \\ (y - F*b), SSE = z'z");
-
-  if (with_grad) {
-    ensure_grad_buffers();
-    LKG_CUDA(cudaMemcpyAsync(dxv_, dEstar_, sizeof(double) * n * batch, cudaMemcpyDeviceToDevice, st_));
-    trsm_lower_left_t(dA_, lda_, mstride_, n, dDinv_, dxv_, n, n, 1, batch, st_);
-    tm.lap("x = tL \\ z");
-    if (slices_ > 0 && !retreated) {
-      if (!w_valid) trtri_blocked_mixed(dA_, lda_, mstride_, n, dDinv_, dW_, lda_, mstride_, batch, mw, st_);
-      wtw_lower_mixed(dW_, lda_, mstride_, n, dRinv_, lda_, mstride_, batch, mw, st_);
+  run_phase(post_key, [&] {
+    trsm_lower_left(dA_, lda_, mstride_, n, dDinv_, dFY_, n, fystride_, p + 1, batch, st_);
+    tm.lap("F* = L \\ F, y* = L \\ y");
+    gram_and_logdet(n, p + 1, dFY_, n, fystride_, dA_, lda_, mstride_, dgram_, gram_stride_, batch, st_);
+    if (p > 0) {
+      gls_solve(p, dgram_, gram_stride_, dbeta_, p, drstar_, p * p, dgls_info_, batch, st_);
     } else {
-      if (!w_valid) trtri_blocked(dA_, lda_, mstride_, n, dDinv_, dW_, lda_, mstride_, batch, st_);
-      wtw_lower(dW_, lda_, mstride_, n, dRinv_, lda_, mstride_, batch, st_);
+      LKG_CUDA(cudaMemsetAsync(dgls_info_, 0, sizeof(int) * batch, st_));
     }
-    tm.lap("R^-1 = L^-T * L^-1");
-    if (lmp_mode_ && p > 0) {  // B = R^-1 - A'A in the lower triangle of R^-1
-      build_At(batch);
-      sub_aat_lower(n, p, dloo_at_, (int64_t)n * p, dRinv_, lda_, mstride_, batch, st_);
-      tm.lap("B = R^-1 - RiF (F'RiF)^-1 F'Ri");
+    tm.lap("^b = R*^-1 R*'^-1 F*'y*");
+    residual_sse(n, p, dFY_, n, fystride_, dbeta_, std::max(p, 1), dEstar_, n, dsse_, 1, batch, st_);
+    tm.lap("z = L \\ (y - F*b), SSE = z'z");
+
+    if (with_grad) {
+      LKG_CUDA(cudaMemcpyAsync(dxv_, dEstar_, sizeof(double) * n * batch, cudaMemcpyDeviceToDevice, st_));
+      trsm_lower_left_t(dA_, lda_, mstride_, n, dDinv_, dxv_, n, n, 1, batch, st_);
+      tm.lap("x = tL \\ z");
+      if (slices_ > 0 && !retreated) {
+        if (!w_valid) trtri_blocked_mixed(dA_, lda_, mstride_, n, dDinv_, dW_, lda_, mstride_, batch, mw, st_);
+        wtw_lower_mixed(dW_, lda_, mstride_, n, dRinv_, lda_, mstride_, batch, mw, st_);
+      } else {
+        if (!w_valid) trtri_blocked(dA_, lda_, mstride_, n, dDinv_, dW_, lda_, mstride_, batch, st_);
+        wtw_lower(dW_, lda_, mstride_, n, dRinv_, lda_, mstride_, batch, st_);
+      }
+      tm.lap("R^-1 = L^-T * L^-1");
+      if (lmp_mode_ && p > 0) {  // B = R^-1 - A'A in the lower triangle of R^-1
+        build_At(batch);
+        sub_aat_lower(n, p, dloo_at_, (int64_t)n * p, dRinv_, lda_, mstride_, batch, st_);
+        tm.lap("B = R^-1 - RiF (F'RiF)^-1 F'Ri");
+      }
+      if (!skip_adjoint_) {
+        adjoint_sums(kernel_, n, d, dXb, xbs, dtheta_, dfactor_, dxv_, n, dRinv_, lda_, mstride_, dpart_, dadj_, batch,
+                     st_);
+        tm.lap("gradR computation [optimized]");
+      }
     }
-    if (!skip_adjoint_) {
-      adjoint_sums(kernel_, n, d, dXb, xbs, dtheta_, dfactor_, dxv_, n, dRinv_, lda_, mstride_, dpart_, dadj_, batch,
-                   st_);
-      tm.lap("gradR computation [optimized]");
-    }
-  }
+  }, graphs_ok && !lmp_mode_);
 
   // ---- results to host ----
   std::vector<double> gram((size_t)gram_stride_ * batch), sse(batch), beta((size_t)std::max(p, 1) * batch);
@@ -625,8 +731,12 @@ void Engine::evaluate(int batch, const double* thetas, const double* factors, bo
 }
 
 void Engine::ensure_loo_buffers(bool with_product) {
-  if (!dloo_at_) dalloc(&dloo_at_, (size_t)cap_ * n_ * std::max(p_, 1));
+  if (!dloo_at_) {
+    buffers_changed();
+    dalloc(&dloo_at_, (size_t)cap_ * n_ * std::max(p_, 1));
+  }
   if (with_product && !dloo_m_) {
+    buffers_changed();
     dalloc(&dloo_m_, (size_t)mstride_);
     dalloc(&dloo_vec_, (size_t)n_ * (2 * d_ + 2));
   }

@@ -6,7 +6,9 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <functional>
 #include <map>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -40,6 +42,9 @@ struct LooOut {
 // choice per matrix size); process-wide
 void set_lookahead_ctas(int c);
 int lookahead_ctas_setting();
+// CUDA graphs for the launch sequences of Engine::evaluate (on by default; LKG_GRAPHS=0 turns them off)
+void set_graphs_enabled(bool on);
+bool graphs_enabled();
 std::string lookahead_tune_key(int n);
 int lookahead_ctas_for(int n);
 
@@ -143,8 +148,19 @@ class Engine {
   void rcond_core(int batch, std::vector<double>& rc2, const std::vector<int>& nvb, const double* A, int64_t lda,
                   int64_t mstride, int n, const double* Dinv);
 
+  // Runs launch(): directly the first time a key is seen, then captured once into a CUDA graph and replayed on the
+  // engine's stream (the key names everything the launch sequence depends on besides device memory contents).
+  // Off when allow is false, when graphs are disabled, and while per-launch timing is on.
+  void run_phase(const std::string& key, const std::function<void()>& launch, bool allow);
+  void clear_graphs();
+  void buffers_changed();  // a device buffer was (re)allocated: every captured graph may hold a stale address
+
   int kernel_, n_, d_, p_, cap_;
   int ndesign_ = 1;
+  std::map<std::string, cudaGraphExec_t> graphs_;
+  std::map<std::string, std::map<std::string, long long>> graph_launches_;
+  std::set<std::string> graph_seen_, graph_refused_;
+  long long buf_gen_ = 0;
   bool skip_adjoint_ = false;                      // leave_one_out needs R^-1 but not the adjoint sums
   bool lmp_mode_ = false;                          // evaluate_lmp: adjoint sums against B
   double *dloo_m_ = nullptr, *dloo_at_ = nullptr;  // leave-one-out scratch: n x n product, A' (n x p per entry)

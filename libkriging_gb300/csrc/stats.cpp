@@ -87,6 +87,21 @@ long long stats_total_launches() {
   return reg().total;
 }
 
+std::map<std::string, long long> stats_launch_counts() {
+  std::lock_guard<std::mutex> lk(reg().mu);
+  std::map<std::string, long long> m;
+  for (auto& kv : reg().acc) m[kv.first] = kv.second.launches;
+  return m;
+}
+
+void stats_add_launches(const std::map<std::string, long long>& counts, int sign) {
+  std::lock_guard<std::mutex> lk(reg().mu);
+  for (auto& kv : counts) {
+    reg().acc[kv.first].launches += sign * kv.second;
+    reg().total += sign * kv.second;
+  }
+}
+
 std::string stats_report() {
   std::lock_guard<std::mutex> lk(reg().mu);
   reg().drain();
