@@ -238,10 +238,10 @@ void Engine::run_phase(const std::string& key, const std::function<void()>& laun
     launch();
     return;
   }
-  const auto before = stats_launch_counts();
+  const auto before = stats_thread_launch_counts();
   auto delta = [&] {
     std::map<std::string, long long> d;
-    for (auto& kv : stats_launch_counts()) {
+    for (auto& kv : stats_thread_launch_counts()) {
       const auto b = before.find(kv.first);
       const long long c = kv.second - (b == before.end() ? 0 : b->second);
       if (c) d[kv.first] = c;

@@ -87,12 +87,11 @@ long long stats_total_launches() {
   return reg().total;
 }
 
-std::map<std::string, long long> stats_launch_counts() {
-  std::lock_guard<std::mutex> lk(reg().mu);
-  std::map<std::string, long long> m;
-  for (auto& kv : reg().acc) m[kv.first] = kv.second.launches;
-  return m;
-}
+namespace {
+thread_local std::map<std::string, long long> t_launches;  // this thread's launches per kernel name
+}  // namespace
+
+std::map<std::string, long long> stats_thread_launch_counts() { return t_launches; }
 
 void stats_add_launches(const std::map<std::string, long long>& counts, int sign) {
   std::lock_guard<std::mutex> lk(reg().mu);
@@ -115,6 +114,7 @@ std::string stats_report() {
 
 LaunchTimer::LaunchTimer(const char* kernel, cudaStream_t st, double flops, double bytes)
     : name_(kernel), st_(st), flops_(flops), bytes_(bytes) {
+  t_launches[name_]++;
   Registry& r = reg();
   std::lock_guard<std::mutex> lk(r.mu);
   r.acc[name_].launches++;

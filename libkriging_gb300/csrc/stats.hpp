@@ -17,9 +17,9 @@ void stats_reset();
 // "name\tlaunches\ttimed_launches\tms\tflops\tbytes\n" per kernel (synchronises pending events)
 std::string stats_report();
 long long stats_total_launches();
-// launch count per kernel name, and adding (sign +1) or removing (-1) such counts: a replayed CUDA graph adds the
-// launches it was captured with
-std::map<std::string, long long> stats_launch_counts();
+// launch count per kernel name of the calling thread's launches, and adding (sign +1) or removing (-1) such counts:
+// a replayed CUDA graph adds the launches it was captured with
+std::map<std::string, long long> stats_thread_launch_counts();
 void stats_add_launches(const std::map<std::string, long long>& counts, int sign);
 
 class LaunchTimer {
