@@ -717,6 +717,20 @@ def run_gpu_nested(args):
             t_s += s
             n3s += float(len(idx)) ** 3
         per_step = t_s * n3 / n3s
+        # the gPoE prediction on the CPU: the sample groups' full predictions of qs points, scaled to every group
+        # and the q points by sum n_g^2 q (the triangular solves dominate)
+        qs = min(2000, args.nested_q)
+        t_p, n2s = 0.0, 0.0
+        for gi in pick[:4]:
+            idx = np.flatnonzero(labels == gi)
+            _, _, s = B.predict_group_full(X[idx], y[idx], nk.theta(), "matern3_2", nk.beta0(), Xp[:qs])
+            t_p += s
+            n2s += float(len(idx)) ** 2 * qs
+        n2q = float(np.sum(sizes.astype(np.float64) ** 2)) * args.nested_q
+        line["predict_cpu_baseline"] = dict(
+            seconds=t_p * n2q / n2s, points=args.nested_q, gpu_seconds=pred_s, cores=int(det["threads"]), kind="port",
+            sample="4 groups' predictions of %d points timed in full (covariances, factor, triangular solves), "
+                   "scaled to all %d groups and %d points by sum n_g^2 q" % (qs, p, args.nested_q))
         line["cpu_baseline"] = dict(value=p / per_step, unit="evals/s", cores=int(det["threads"]), kind="port",
                                     sample="reference-restated LL+grad of %d groups (%s points) each timed in full, "
                                            "scaled to all %d groups by sum n_g^3 (the reference fits its groups one "
