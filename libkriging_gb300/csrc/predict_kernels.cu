@@ -6,6 +6,9 @@
 // with z, Rstar_on and M (:254-281).  The p-column trend algebra stays on the host.
 #include "predict_kernels.cuh"
 
+#include <cstdint>
+#include <mutex>
+
 #include "stats.hpp"
 
 #include "common.cuh"
@@ -55,12 +58,32 @@ void predict_reduce(int n, int ncols, int p, const double* W, const double* z, c
   LKG_LAUNCH("k_predict_reduce");
 }
 
+// Device scratch from the stream-ordered pool: allocation and release are queued on the stream (no device-wide
+// synchronisation when many submodels predict concurrently), and the pool keeps released memory for reuse.
+void keep_pool_memory() {
+  static std::once_flag once;
+  std::call_once(once, [] {
+    int dev = 0;
+    LKG_CUDA(cudaGetDevice(&dev));
+    cudaMemPool_t pool;
+    LKG_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+    uint64_t keep = UINT64_MAX;
+    LKG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+  });
+}
+
 struct DevBuf {
   double* p = nullptr;
-  explicit DevBuf(size_t n) { LKG_CUDA(cudaMalloc(&p, sizeof(double) * std::max<size_t>(n, 1))); }
-  ~DevBuf() {
-    if (p) cudaFree(p);
+  cudaStream_t st;
+  DevBuf(size_t n, cudaStream_t s) : st(s) {
+    keep_pool_memory();
+    LKG_CUDA(cudaMallocAsync((void**)&p, sizeof(double) * std::max<size_t>(n, 1), st));
   }
+  ~DevBuf() {
+    if (p) cudaFreeAsync(p, st);
+  }
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
 };
 
 }  // namespace
@@ -71,13 +94,33 @@ PredictOut predict_gpu(const Engine& model, const double* Xn, int q, const doubl
   cudaStream_t st = model.stream();
   PredictOut o;
   if (q <= 0) return o;
-  DevBuf dXn((size_t)q * d), dth(d), dz(n), dRs((size_t)n * q), drz(q), drr(q), drm((size_t)q * std::max(p, 1));
+  // the covariance and the derivatives need Rstar_on for all points at once; otherwise the points go in chunks of
+  // at most 2^25 / n (Rstar_on of a chunk below 256 MB)
+  const bool whole = need_cov || need_deriv;
+  const int qc = whole ? q : (int)std::max<int64_t>(1, std::min<int64_t>(q, ((int64_t)1 << 25) / n));
+  DevBuf dXn((size_t)q * d, st), dth(d, st), dz(n, st), dRs((size_t)n * qc, st), drz(q, st), drr(q, st),
+      drm((size_t)q * std::max(p, 1), st);
   LKG_CUDA(cudaMemcpyAsync(dXn.p, Xn, sizeof(double) * q * d, cudaMemcpyHostToDevice, st));
   LKG_CUDA(cudaMemcpyAsync(dth.p, theta, sizeof(double) * d, cudaMemcpyHostToDevice, st));
   LKG_CUDA(cudaMemcpyAsync(dz.p, z, sizeof(double) * n, cudaMemcpyHostToDevice, st));
-  cov_cross(model.kernel(), n, q, d, model.dX(), dXn.p, dth.p, factor, dRs.p, st);
-  model.solve_lower_inplace(0, dRs.p, n, q);
-  predict_reduce(n, q, p, dRs.p, dz.p, dRs.p, 1, model.dFY(0), drz.p, drr.p, drm.p, st);
+  if (whole) {
+    cov_cross(model.kernel(), n, q, d, model.dX(), dXn.p, dth.p, factor, dRs.p, st);
+    model.solve_lower_inplace(0, dRs.p, n, q);
+    predict_reduce(n, q, p, dRs.p, dz.p, dRs.p, 1, model.dFY(0), drz.p, drr.p, drm.p, st);
+  } else {
+    // the chunk's points as their own q x d column-major block
+    DevBuf dXc((size_t)qc * d, st);
+    for (int c0 = 0; c0 < q; c0 += qc) {
+      const int nc = std::min(qc, q - c0);
+      for (int k = 0; k < d; ++k)
+        LKG_CUDA(cudaMemcpyAsync(dXc.p + (size_t)k * nc, dXn.p + (size_t)k * q + c0, sizeof(double) * nc,
+                                 cudaMemcpyDeviceToDevice, st));
+      cov_cross(model.kernel(), n, nc, d, model.dX(), dXc.p, dth.p, factor, dRs.p, st);
+      model.solve_lower_inplace(0, dRs.p, n, nc);
+      predict_reduce(n, nc, p, dRs.p, dz.p, dRs.p, 1, model.dFY(0), drz.p + c0, drr.p + c0,
+                     drm.p + (size_t)c0 * p, st);
+    }
+  }
   o.rz.resize(q);
   o.rr.resize(q);
   o.rm.resize((size_t)q * p);
@@ -86,7 +129,7 @@ PredictOut predict_gpu(const Engine& model, const double* Xn, int q, const doubl
   if (p > 0) LKG_CUDA(cudaMemcpyAsync(o.rm.data(), drm.p, sizeof(double) * q * p, cudaMemcpyDeviceToHost, st));
   if (need_cov) {
     // R_nn (lower, diag 1) then Sigma = R_nn - Rs' Rs (lower), mirrored on the host
-    DevBuf dRnn((size_t)q * q), dfac(1), ddiag(1);
+    DevBuf dRnn((size_t)q * q, st), dfac(1, st), ddiag(1, st);
     LKG_CUDA(cudaMemcpyAsync(dfac.p, &nn_factor, sizeof(double), cudaMemcpyHostToDevice, st));
     const double one = 1.0;
     LKG_CUDA(cudaMemcpyAsync(ddiag.p, &one, sizeof(double), cudaMemcpyHostToDevice, st));
@@ -101,20 +144,21 @@ PredictOut predict_gpu(const Engine& model, const double* Xn, int q, const doubl
       for (int i = 0; i < j; ++i) o.sigma[i + (size_t)j * q] = o.sigma[j + (size_t)i * q];
   }
   if (need_deriv) {
-    // W = L \ DR_on in chunks of points (n x qc d doubles at most 2^26), then its column products with z,
+    // W = L \ DR_on in chunks of points (n x qd d doubles at most 2^26), then its column products with z,
     // Rstar_on(:, c) and M (KrigingImpl.cpp:254-281)
-    const int qc = (int)std::max<int64_t>(1, std::min<int64_t>(q, ((int64_t)1 << 26) / ((int64_t)n * d)));
-    DevBuf dW((size_t)n * qc * d), dwz((size_t)qc * d), dwr((size_t)qc * d), dwm((size_t)qc * d * std::max(p, 1));
+    const int qd = (int)std::max<int64_t>(1, std::min<int64_t>(q, ((int64_t)1 << 26) / ((int64_t)n * d)));
+    DevBuf dW((size_t)n * qd * d, st), dwz((size_t)qd * d, st), dwr((size_t)qd * d, st),
+        dwm((size_t)qd * d * std::max(p, 1), st);
     o.wz.resize((size_t)q * d);
     o.wr.resize((size_t)q * d);
     o.wm.resize((size_t)q * d * p);
-    for (int c0 = 0; c0 < q; c0 += qc) {
-      const int nc = std::min(qc, q - c0), ncol = nc * d;
+    for (int c0 = 0; c0 < q; c0 += qd) {
+      const int nc = std::min(qd, q - c0), ncol = nc * d;
       // the chunk's points are columns c0.. of the q x d column-major Xn: pass them with their own leading dimension
       std::vector<double> xc((size_t)nc * d);
       for (int k = 0; k < d; ++k)
         for (int c = 0; c < nc; ++c) xc[c + (size_t)k * nc] = Xn[(c0 + c) + (size_t)k * q];
-      DevBuf dxc((size_t)nc * d);
+      DevBuf dxc((size_t)nc * d, st);
       LKG_CUDA(cudaMemcpyAsync(dxc.p, xc.data(), sizeof(double) * nc * d, cudaMemcpyHostToDevice, st));
       dcov_cross(model.kernel(), n, nc, d, model.dX(), dxc.p, dth.p, factor, dW.p, st);
       model.solve_lower_inplace(0, dW.p, n, ncol);

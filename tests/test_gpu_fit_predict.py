@@ -128,3 +128,19 @@ def test_nugget_fit(gpu_lib):
     ll_o, g_o = ora.log_likelihood(g)
     assert rel_err(ll, ll_o) < 1e-10
     assert rel_err(grad, g_o) < 1e-7
+
+
+def test_predict_in_point_chunks(gpu_lib):
+    """q = 10000 points at n = 4096 run in two chunks (Rstar_on of a chunk below 256 MB); each point's mean and
+    stdev equal those of the same point predicted within a smaller set (per-column solves, the same operations)."""
+    rng = np.random.default_rng(9)
+    X = rng.uniform(size=(4096, 3))
+    y = np.sin(2 * np.pi * X).sum(axis=1)
+    k = gpu_lib.Kriging("matern5_2")
+    k.fit(y, X, "constant", False, "none", "LL", {"theta": np.full((1, 3), 0.4)})
+    Xn = rng.uniform(size=(10000, 3))
+    mean, sd, _, _, _ = k.predict(Xn, True, False, False)
+    for a, b in ((0, 40), (8170, 8230), (9950, 10000)):
+        m1, s1, _, _, _ = k.predict(Xn[a:b], True, False, False)
+        assert rel_err(mean[a:b], m1) < 1e-13
+        assert rel_err(sd[a:b], s1) < 1e-12
