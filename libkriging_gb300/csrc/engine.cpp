@@ -150,7 +150,7 @@ Engine::Engine(int kernel, int n, int d, int p, int ndesign, const double* X, co
 Engine::~Engine() {
   clear_graphs();
   for (double* p : {dX_, dY_, dF_, dA_, dDinv_, dW_, dRinv_, dFY_, dEstar_, dxv_, dtheta_, dfactor_, ddiag_, dgram_,
-                    dbeta_, drstar_, dsse_, dpart_, dadj_, dvec_, dcol_, dloo_m_, dloo_at_, dloo_vec_})
+                    dbeta_, drstar_, dsse_, dpart_, dadj_, dvec_, dcol_, dloo_m_, dloo_at_, dloo_vec_, dWp_})
     if (p) cudaFree(p);
   if (dinfo_) cudaFree(dinfo_);
   if (dgls_info_) cudaFree(dgls_info_);
@@ -333,6 +333,18 @@ void Engine::ensure_grad_buffers() {
   dalloc(&dpart_, part_size_);
 }
 
+const double* Engine::factor_inverse() {
+  if (!dWp_) {
+    buffers_changed();
+    dalloc(&dWp_, (size_t)mstride_);
+  }
+  if (!wp_valid_) {
+    trtri_blocked(dA_, lda_, mstride_, n_, dDinv_, dWp_, lda_, mstride_, 1, st_);
+    wp_valid_ = true;
+  }
+  return dWp_;
+}
+
 void Engine::solve_lower_inplace(int b, double* dB, int64_t ldb, int r) const {
   trsm_lower_left(dA_ + (size_t)b * mstride_, lda_, mstride_, n_, dDinv_ + (size_t)b * dstride_, dB, ldb, 0, r, 1,
                   st_);
@@ -469,6 +481,7 @@ void Engine::rcond_core(int batch, std::vector<double>& rc2, const std::vector<i
 void Engine::evaluate(int batch, const double* thetas, const double* factors, bool with_grad,
                       std::vector<EvalOut>& out, std::map<std::string, double>* bench, const int* designs) {
   if (batch < 1 || batch > cap_) throw std::invalid_argument("Engine::evaluate: batch out of range");
+  wp_valid_ = false;
   if (ndesign_ > 1 && !designs) throw std::invalid_argument("Engine::evaluate: design of each entry required");
   const Config& cfg = config();
   const int n = n_, d = d_, p = p_;
@@ -844,6 +857,7 @@ void Engine::leave_one_out(int batch, const double* thetas, const double* factor
 }
 
 void Engine::evaluate_update(const Engine& old, const double* theta, double factor, EvalOut& out) {
+  wp_valid_ = false;
   const int n = n_, d = d_, p = p_, no = old.n(), nu = n_ - old.n();
   if (ndesign_ != 1 || old.ndesign() != 1 || nu < 1 || old.d() != d || old.p() != p || old.kernel() != kernel_)
     throw std::invalid_argument("Engine::evaluate_update: the new design must extend the old one");
@@ -954,6 +968,7 @@ void Engine::evaluate_update(const Engine& old, const double* theta, double fact
 void Engine::adopt_model(const double* L, const double* Fstar, const double* ystar, const double* Rstar,
                          const double* Estar) {
   if (ndesign_ != 1) throw std::invalid_argument("Engine::adopt_model: one design only");
+  wp_valid_ = false;
   const int n = n_, p = p_;
   LKG_CUDA(cudaMemcpy2DAsync(dA_, sizeof(double) * lda_, L, sizeof(double) * n, sizeof(double) * n, n,
                              cudaMemcpyHostToDevice, st_));

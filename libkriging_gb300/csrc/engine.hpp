@@ -135,6 +135,9 @@ class Engine {
   const double* dEstar(int b = 0) const { return dEstar_ + (size_t)b * n_; }
   // solve L Z = B in place for entry b (B device, n x r, ldb)
   void solve_lower_inplace(int b, double* dB, int64_t ldb, int r) const;
+  // W = L^-1 of the (single-matrix) factor, formed once per factor on the FP64 path and kept for predictions whose
+  // solves run as digit products (W R_on)
+  const double* factor_inverse();
 
  private:
   void ensure_grad_buffers();
@@ -157,6 +160,8 @@ class Engine {
 
   int kernel_, n_, d_, p_, cap_;
   int ndesign_ = 1;
+  double* dWp_ = nullptr;  // factor_inverse()
+  bool wp_valid_ = false;
   std::map<std::string, cudaGraphExec_t> graphs_;
   std::map<std::string, std::map<std::string, long long>> graph_launches_;
   std::set<std::string> graph_seen_, graph_refused_;

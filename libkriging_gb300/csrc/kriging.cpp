@@ -1200,8 +1200,10 @@ std::tuple<std::vector<double>, std::vector<double>, Mat, Mat, Mat> Kriging::pre
   int pn = 0;
   std::vector<double> Fn = regression_matrix(m_regmodel, Xnn.v, q, d, &pn);
   std::vector<double> zz = z();
+  // on a mixed-precision model the solves of large predictions run as digit products with L^-1 (FP64-level)
+  const bool digits = m_slices > 0 && n >= 512 && q >= 256;
   PredictOut po = predict_gpu(*m_model, Xnn.v.data(), q, m_theta.data(), R_on_factor, zz.data(), return_stdev || return_cov,
-                              return_cov, nug ? m_alpha : 1.0, return_deriv);
+                              return_cov, nug ? m_alpha : 1.0, return_deriv, digits);
   // yhat = F_n beta + Rstar_on' z
   std::vector<double> mean(q), sd;
   for (int i = 0; i < q; ++i) {

@@ -14,6 +14,7 @@
 #include "common.cuh"
 #include "dense_fp64.cuh"
 #include "lik_kernels.cuh"
+#include "ozaki7.cuh"
 
 namespace lkg {
 
@@ -88,8 +89,8 @@ struct DevBuf {
 
 }  // namespace
 
-PredictOut predict_gpu(const Engine& model, const double* Xn, int q, const double* theta, double factor,
-                       const double* z, bool need_rr, bool need_cov, double nn_factor, bool need_deriv) {
+PredictOut predict_gpu(Engine& model, const double* Xn, int q, const double* theta, double factor, const double* z,
+                       bool need_rr, bool need_cov, double nn_factor, bool need_deriv, bool digits) {
   const int n = model.n(), d = model.d(), p = model.p();
   cudaStream_t st = model.stream();
   PredictOut o;
@@ -110,16 +111,35 @@ PredictOut predict_gpu(const Engine& model, const double* Xn, int q, const doubl
   } else {
     // the chunk's points as their own q x d column-major block
     DevBuf dXc((size_t)qc * d, st);
+    // digit products: L^-1 split once (rows of W, k = its columns), each chunk's R_on split by points (rows = points,
+    // k = observations), Rstar_on = W R_on written over R_on (the product reads the split copies)
+    constexpr int S = 8;
+    const double* W = digits ? model.factor_inverse() : nullptr;
+    DevBuf dWs(digits ? oz7_plane_elems(n, n, S) / 4 + 1 : 1, st), dRsp(digits ? oz7_plane_elems(qc, n, S) / 4 + 1 : 1, st);
+    DevBuf dWe(digits ? oz7_exp_elems(n, n, OZ7_KB) / 2 + 1 : 1, st), dRse(digits ? oz7_exp_elems(qc, n, OZ7_KB) / 2 + 1 : 1, st);
+    Split7 SW, SR;
+    if (digits) {
+      SW = oz7_buffer(dWs.p, reinterpret_cast<int*>(dWe.p), S, n, n, OZ7_KB);
+      SR = oz7_buffer(dRsp.p, reinterpret_cast<int*>(dRse.p), S, qc, n, OZ7_KB);
+      oz7_split(n, n, W, 1, model.lda(), 0, 1, SW, st);
+    }
     for (int c0 = 0; c0 < q; c0 += qc) {
       const int nc = std::min(qc, q - c0);
       for (int k = 0; k < d; ++k)
         LKG_CUDA(cudaMemcpyAsync(dXc.p + (size_t)k * nc, dXn.p + (size_t)k * q + c0, sizeof(double) * nc,
                                  cudaMemcpyDeviceToDevice, st));
       cov_cross(model.kernel(), n, nc, d, model.dX(), dXc.p, dth.p, factor, dRs.p, st);
-      model.solve_lower_inplace(0, dRs.p, n, nc);
+      if (digits) {
+        oz7_split(nc, n, dRs.p, n, 1, 0, 1, SR, st);
+        oz7_gemm(n, nc, 0, SW.nblk, 1.0, SW, SR, 0.0, dRs.p, n, 0, 1, false, st);
+      } else {
+        model.solve_lower_inplace(0, dRs.p, n, nc);
+      }
       predict_reduce(n, nc, p, dRs.p, dz.p, dRs.p, 1, model.dFY(0), drz.p + c0, drr.p + c0,
                      drm.p + (size_t)c0 * p, st);
     }
+    if (digits && oz7_error_and_reset())
+      throw std::runtime_error("predict: a tensor-core digit product did not complete (timed out)");
   }
   o.rz.resize(q);
   o.rr.resize(q);

@@ -18,8 +18,10 @@ struct PredictOut {
 };
 
 // Xn: q x d column-major, already normalised.  R_on = factor * C(X_o - X_n) (coincident points -> 1),
-// Rstar_on = L \ R_on with the committed factor of `model`.
-PredictOut predict_gpu(const Engine& model, const double* Xn, int q, const double* theta, double factor,
-                       const double* z, bool need_rr, bool need_cov, double nn_factor, bool need_deriv = false);
+// Rstar_on = L \ R_on with the committed factor of `model`.  digits: Rstar_on as the product L^-1 R_on on the
+// tensor cores (8 seven-bit digits, FP64-level products; L^-1 formed once per factor) instead of the FP64
+// triangular solve -- used for the mean and stdev of large predictions on a mixed-precision model.
+PredictOut predict_gpu(Engine& model, const double* Xn, int q, const double* theta, double factor, const double* z,
+                       bool need_rr, bool need_cov, double nn_factor, bool need_deriv = false, bool digits = false);
 
 }  // namespace lkg

@@ -144,3 +144,27 @@ def test_predict_in_point_chunks(gpu_lib):
         m1, s1, _, _, _ = k.predict(Xn[a:b], True, False, False)
         assert rel_err(mean[a:b], m1) < 1e-13
         assert rel_err(sd[a:b], s1) < 1e-12
+
+
+def test_predict_digit_solves_on_mixed_model(gpu_lib):
+    """A mixed-precision model runs the solves of large predictions as digit products with L^-1 (8 seven-bit digits):
+    the same means and stdevs as the FP64 triangular solve to FP64 rounding, and the oracle's."""
+    rng = np.random.default_rng(10)
+    X = rng.uniform(size=(2048, 3))
+    y = np.sin(2 * np.pi * X).sum(axis=1) + 0.5 * X[:, 0] * X[:, 1]
+    th = np.array([0.4, 0.5, 0.6])
+    k64 = gpu_lib.Kriging("matern5_2")
+    k64.fit(y, X, "constant", False, "none", "LL", {"theta": th.reshape(1, -1)})
+    km = gpu_lib.Kriging("matern5_2")
+    km.set_precision(7)
+    km.fit(y, X, "constant", False, "none", "LL", {"theta": th.reshape(1, -1)})
+    Xn = rng.uniform(size=(3000, 3))
+    m64, s64, _, _, _ = k64.predict(Xn, True, False, False)
+    mm, sm, _, _, _ = km.predict(Xn, True, False, False)
+    assert rel_err(mm, m64) < 1e-11
+    assert rel_err(sm, s64) < 1e-9
+    ora = O.OracleKriging(y, X, "matern5_2")
+    m = O.populate_model("matern5_2", ora.X, ora.y, ora.F, th, 1.0, None, False)
+    mo, so = ora.predict(Xn[:300], th, m.betahat, m.SSEstar / 2048)
+    assert rel_err(mm[:300], mo) < 1e-9
+    assert rel_err(sm[:300], so) < 1e-7
