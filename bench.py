@@ -534,6 +534,12 @@ def run_gpu_vecchia(args):
         vll, g = k.logLikelihoodVecchiaFun(th, True)
     wall = time.perf_counter() - t0
     clk = clocks.stop()
+    # predictVecchia at scale: 10^4 new points, each kriged on its 30 nearest observations
+    Xq = np.random.default_rng(124).uniform(size=(10000, 3))
+    k.predictVecchia(Xq[:100], True, 30)
+    t0 = time.perf_counter()
+    pmean, psd = k.predictVecchia(Xq, True, 30)
+    pv_s = time.perf_counter() - t0
     lib.lkg_stats_reset()
     lib.lkg_stats_enable(1)
     for _ in range(min(args.steps, 3)):
@@ -550,6 +556,7 @@ def run_gpu_vecchia(args):
                          d2h_bytes_per_step=8 * 4,
                          note="logLikelihoodVecchiaFun through the C ABI: theta in, (VLL, gradient) out"),
                 sets_s=sets_s, fit_s_including_sets=fit_s, theta=th.tolist(), vll=vll, clocks=clk,
+                predict_vecchia=dict(points=int(Xq.shape[0]), m=30, seconds=pv_s),
                 fit_kernels={kk: dict(launches=v["launches"], ms=round(v["ms"], 3)) for kk, v in fit_stats.items()},
                 gpu_launches=int(sum(v["launches"] for v in stats.values()) / max(1, min(args.steps, 3))),
                 roofline=_roof(stats, peak_fp64.value, None), kernels=_kern(stats))
@@ -579,6 +586,17 @@ def run_gpu_vecchia(args):
         t1 = time.perf_counter()
         lk.vecchia_sets(Xs, 30)
         gpu_sets = time.perf_counter() - t1
+        # predictVecchia on the CPU: the reference's per-point work on a sample of the points, all host threads
+        from oracle import baseline as Bv
+        resid = (y - (k.beta()[0] if len(k.beta()) else 0.0))
+        qs = 256
+        pm_c, _, pv_cpu = Bv.predict_vecchia_sample("gauss", X, resid, th, k.sigma2(), Xq[:qs], 30)
+        line["predict_vecchia"]["cpu_baseline"] = dict(
+            seconds=pv_cpu * Xq.shape[0] / qs, cores=Bv.host_threads(), kind="port",
+            mean_rel_diff=float(np.linalg.norm(pm_c - (pmean[:qs] - (k.beta()[0] if len(k.beta()) else 0.0)))
+                                / np.linalg.norm(pm_c)),
+            sample="%d of the %d points' predictions timed in full (distances to all %d observations, partial "
+                   "selection, local kriging) on all host threads, scaled by the point count" % (qs, Xq.shape[0], n))
         line["sets_cpu_baseline"] = dict(n=ns, cpu_s=cpu_sets, gpu_s=gpu_sets, cores=1, kind="port",
                                          sample="make_vecchia_sets restated (O(n^2) maxmin + neighbour selection) "
                                                 "on the first %d points" % ns)

@@ -157,3 +157,33 @@ def predict_group_full(X, y, theta, kernel, beta0, Xq):
     mean = beta0 + Rs.T @ z
     var = 1.0 - np.sum(Rs * Rs, axis=0)
     return mean, var, time.perf_counter() - t
+
+
+def predict_vecchia_sample(kernel, X, resid, theta, sigma2, Xq, m=30, threads=None):
+    """Kriging::predictVecchia's per-point work as the reference runs it (Kriging.cpp:950-1022): squared distances to
+    every observation, a partial selection of the m nearest (std::nth_element there, numpy's argpartition here), the
+    m x m local kriging system through the oracle's safe_chol_lower, mean and stdev; the points spread over `threads`
+    host threads (the reference's OpenMP loop over points).  Returns (mean, stdev, seconds)."""
+    from concurrent.futures import ThreadPoolExecutor
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    Xq = np.atleast_2d(np.asarray(Xq, dtype=np.float64))
+    theta = np.asarray(theta, dtype=np.float64)
+    threads = threads or host_threads()
+    q = Xq.shape[0]
+    mean, sd = np.empty(q), np.empty(q)
+
+    def one(t):
+        s = ((X - Xq[t]) ** 2).sum(axis=1)
+        nb = np.argpartition(s, m)[:m]
+        RN = O.cov_cross(kernel, X[nb], X[nb], theta)
+        RN[np.diag_indices(m)] = 1.0 + O.CONFIG.num_nugget
+        r = O.cov_cross(kernel, X[nb], Xq[t:t + 1], theta)[:, 0]
+        LN, _ = O.safe_chol_lower(RN)
+        a = O.solve_upper_t(LN, O.solve_lower(LN, r.reshape(-1, 1)))[:, 0]
+        mean[t] = a @ resid[nb]
+        sd[t] = math.sqrt(sigma2 * max(0.0, 1.0 - r @ a))
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(one, range(q)))
+    return mean, sd, time.perf_counter() - t0
