@@ -590,7 +590,8 @@ def run_gpu_vecchia(args):
         from oracle import baseline as Bv
         resid = (y - (k.beta()[0] if len(k.beta()) else 0.0))
         qs = 256
-        pm_c, _, pv_cpu = Bv.predict_vecchia_sample("gauss", X, resid, th, k.sigma2(), Xq[:qs], 30)
+        pm_c, _, pv_cpu = Bv.predict_vecchia_sample("gauss", X, resid, th, k.sigma2(), Xq[:qs], 30,
+                                                     num_nugget=lk.get_num_nugget())
         line["predict_vecchia"]["cpu_baseline"] = dict(
             seconds=pv_cpu * Xq.shape[0] / qs, cores=Bv.host_threads(), kind="port",
             mean_rel_diff=float(np.linalg.norm(pm_c - (pmean[:qs] - (k.beta()[0] if len(k.beta()) else 0.0)))

@@ -159,11 +159,14 @@ def predict_group_full(X, y, theta, kernel, beta0, Xq):
     return mean, var, time.perf_counter() - t
 
 
-def predict_vecchia_sample(kernel, X, resid, theta, sigma2, Xq, m=30, threads=None):
+def predict_vecchia_sample(kernel, X, resid, theta, sigma2, Xq, m=30, threads=None, num_nugget=None):
     """Kriging::predictVecchia's per-point work as the reference runs it (Kriging.cpp:950-1022): squared distances to
     every observation, a partial selection of the m nearest (std::nth_element there, numpy's argpartition here), the
     m x m local kriging system through the oracle's safe_chol_lower, mean and stdev; the points spread over `threads`
-    host threads (the reference's OpenMP loop over points).  Returns (mean, stdev, seconds)."""
+    host threads (the reference's OpenMP loop over points).  num_nugget: the jitter of the local systems (the
+    numerical nugget of LinearAlgebra::set_num_nugget; the oracle's configuration when None).  Returns (mean without
+    the trend, stdev, seconds)."""
+    import dataclasses
     from concurrent.futures import ThreadPoolExecutor
     X = np.ascontiguousarray(X, dtype=np.float64)
     Xq = np.atleast_2d(np.asarray(Xq, dtype=np.float64))
@@ -171,14 +174,15 @@ def predict_vecchia_sample(kernel, X, resid, theta, sigma2, Xq, m=30, threads=No
     threads = threads or host_threads()
     q = Xq.shape[0]
     mean, sd = np.empty(q), np.empty(q)
+    cfg = O.CONFIG if num_nugget is None else dataclasses.replace(O.CONFIG, num_nugget=float(num_nugget))
 
     def one(t):
         s = ((X - Xq[t]) ** 2).sum(axis=1)
         nb = np.argpartition(s, m)[:m]
         RN = O.cov_cross(kernel, X[nb], X[nb], theta)
-        RN[np.diag_indices(m)] = 1.0 + O.CONFIG.num_nugget
+        RN[np.diag_indices(m)] = 1.0 + cfg.num_nugget
         r = O.cov_cross(kernel, X[nb], Xq[t:t + 1], theta)[:, 0]
-        LN, _ = O.safe_chol_lower(RN)
+        LN, _ = O.safe_chol_lower(RN, cfg)
         a = O.solve_upper_t(LN, O.solve_lower(LN, r.reshape(-1, 1)))[:, 0]
         mean[t] = a @ resid[nb]
         sd[t] = math.sqrt(sigma2 * max(0.0, 1.0 - r @ a))
