@@ -60,7 +60,8 @@ void predict_reduce(int n, int ncols, int p, const double* W, const double* z, c
 }
 
 // Device scratch from the stream-ordered pool: allocation and release are queued on the stream (no device-wide
-// synchronisation when many submodels predict concurrently), and the pool keeps released memory for reuse.
+// synchronisation when many submodels predict concurrently), and the device's default pool keeps up to 8 GiB of
+// released memory for reuse (raised from its default of none, never lowered).
 void keep_pool_memory() {
   static std::once_flag once;
   std::call_once(once, [] {
@@ -68,8 +69,10 @@ void keep_pool_memory() {
     LKG_CUDA(cudaGetDevice(&dev));
     cudaMemPool_t pool;
     LKG_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
-    uint64_t keep = UINT64_MAX;
-    LKG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    uint64_t keep = 0;
+    LKG_CUDA(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    const uint64_t want = (uint64_t)8 << 30;
+    if (keep < want) LKG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, (void*)&want));
   });
 }
 
